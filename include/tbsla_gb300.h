@@ -1,0 +1,232 @@
+/*
+ * tbsla_gb300 — C ABI of the GB300-native TBSLA SpMV / PageRank / CG path.
+ *
+ * This is the drop-in boundary.  It replaces the reference's per-format C
+ * interface C_CPP_Matrix<FMT>_* (src/cpp/interface/c/include/tbsla/cpp/
+ * MatrixCSR.h:13-21, which no longer compiles against the reference's own
+ * headers) with one working interface over an opaque matrix handle, and it
+ * is what the C++ classes tbsla::cpp::Matrix* of this library are built on.
+ *
+ * Conventions
+ *  - Every entry point returns an int status: TBSLA_OK (0) or a negative
+ *    TBSLA_ERR_* code; tbsla_status_string() names it.  Nothing throws across
+ *    the ABI.  Bad input (out-of-range index, non-monotone row pointer,
+ *    truncated file, size mismatch) is rejected on the host before any
+ *    kernel runs.
+ *  - A handle keeps the reference's host layout (the arrays a reference
+ *    Matrix object owns) plus a device copy built on first use (or by
+ *    tbsla_matrix_upload); any host-side mutation drops the device copy.
+ *  - Entry points with host pointers (tbsla_Ax, tbsla_spmv, ...) copy the
+ *    input vector to the GPU, run the kernels and copy the result back
+ *    before returning.  *_device entry points take device pointers and a
+ *    cudaStream_t (passed as void*, NULL = the handle's own stream) and do
+ *    not synchronise.
+ *  - Handles are not thread-safe; one stream per handle, as the reference's
+ *    objects are used from one thread.
+ *  - No CPU fallback: with no usable GPU every compute entry point returns
+ *    TBSLA_ERR_NO_DEVICE.
+ */
+#ifndef TBSLA_GB300_H
+#define TBSLA_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define TBSLA_OK 0
+#define TBSLA_ERR_INVALID_ARG (-1)   /* bad argument (null handle, wrong format, size) */
+#define TBSLA_ERR_BAD_MATRIX (-2)    /* matrix arrays fail validation */
+#define TBSLA_ERR_ALLOC (-3)         /* host or device allocation failed */
+#define TBSLA_ERR_CUDA (-4)          /* a CUDA call failed */
+#define TBSLA_ERR_IO (-5)            /* file missing, short or malformed */
+#define TBSLA_ERR_NOT_CONVERGED (-6) /* iteration limit reached (results still written) */
+#define TBSLA_ERR_TIMEOUT (-7)       /* a bounded device wait gave up */
+#define TBSLA_ERR_UNSUPPORTED (-8)   /* operation not defined for this format */
+#define TBSLA_ERR_NO_DEVICE (-9)     /* no CUDA device usable */
+
+/* ---- formats and value precisions ----------------------------------------- */
+#define TBSLA_COO 0
+#define TBSLA_SCOO 1
+#define TBSLA_CSR 2
+#define TBSLA_ELL 3
+#define TBSLA_DENSE 4
+
+#define TBSLA_F64 0  /* values stored as double on the device (default) */
+#define TBSLA_F32 1  /* values stored as float, products and sums in double */
+#define TBSLA_BF16 2 /* values stored as bfloat16, products and sums in double */
+
+typedef struct tbsla_matrix tbsla_matrix;
+
+/* Distribution metadata of a block, as in tbsla::cpp::Matrix
+ * (src/cpp/include/tbsla/cpp/Matrix.hpp:54-55), plus ELL's max_col
+ * (MatrixELL.hpp:43). */
+typedef struct tbsla_info {
+  int n_row, n_col, ln_row, ln_col, f_row, f_col;
+  long nnz;
+  int pr, pc, NR, NC;
+  int max_col;
+} tbsla_info;
+
+const char* tbsla_status_string(int status);
+/* Library version string. */
+const char* tbsla_version(void);
+/* Selects the CUDA device used by handles created afterwards (default 0). */
+int tbsla_device_init(int device);
+/* Pinned host buffers, for callers that want full-speed host<->device copies. */
+int tbsla_host_alloc(void** ptr, size_t bytes);
+int tbsla_host_free(void* ptr);
+
+/* ---- handle lifecycle: C_CPP_Matrix<FMT>_create/_destroy
+ *      (interface/c/include/tbsla/cpp/MatrixCSR.h:13-14) ------------------- */
+int tbsla_matrix_create(tbsla_matrix** m, int format);
+int tbsla_matrix_destroy(tbsla_matrix* m);
+int tbsla_matrix_format(const tbsla_matrix* m, int* format);
+int tbsla_matrix_info(const tbsla_matrix* m, tbsla_info* info);
+
+/* Copies caller arrays into the handle (the caller keeps ownership).  Array
+ * lengths follow the reference layouts: COO/SCOO values/row/col[nnz]; CSR
+ * values[nnz], rowptr[ln_row+1], colidx[nnz]; ELL values/columns
+ * [ln_row*max_col] row-major; DENSE values[ln_row*ln_col] row-major. */
+int tbsla_matrix_set_coo(tbsla_matrix* m, const tbsla_info* info, const double* values,
+                         const int* row, const int* col);
+int tbsla_matrix_set_csr(tbsla_matrix* m, const tbsla_info* info, const double* values,
+                         const int* rowptr, const int* colidx);
+int tbsla_matrix_set_ell(tbsla_matrix* m, const tbsla_info* info, const double* values,
+                         const int* columns);
+int tbsla_matrix_set_dense(tbsla_matrix* m, const tbsla_info* info, const double* values);
+/* Borrowed pointers to the handle's host arrays (valid until the next
+ * mutation).  idx0/idx1: COO/SCOO row/col, CSR rowptr/colidx, ELL columns/NULL,
+ * DENSE NULL/NULL. */
+int tbsla_matrix_arrays(const tbsla_matrix* m, const double** values, const int** idx0,
+                        const int** idx1);
+
+/* ---- generators: tbsla::cpp::Matrix::fill_* (Matrix.hpp:40-42) -------------- */
+int tbsla_matrix_fill_cdiag(tbsla_matrix* m, int n_row, int n_col, int cdiag, int pr, int pc,
+                            int NR, int NC);
+int tbsla_matrix_fill_cqmat(tbsla_matrix* m, int n_row, int n_col, int c, double q,
+                            unsigned int seed_mult, int pr, int pc, int NR, int NC);
+int tbsla_matrix_fill_random(tbsla_matrix* m, int n_row, int n_col, double nnz_ratio,
+                             unsigned int seed_mult, int pr, int pc, int NR, int NC);
+
+/* Synthetic workload generators (no counterpart in the reference; the
+ * reference's generators only emit all-ones values).  All are
+ * deterministic functions of their arguments, independent of thread count.
+ *  - uniform_rows: square n x n; row i holds column i plus k-1 further
+ *    distinct columns uniform in [0,n), sorted; values U[-1,1).
+ *  - powerlaw: square n x n; row lengths Zipf(zipf_s) on [1,max_len]
+ *    rescaled to mean `mean_len`, rounded, clipped to [1,max_len]; each
+ *    column is uniform on [0,n) with probability 1-local_frac, else uniform
+ *    within +-band of the diagonal; distinct and sorted per row; values
+ *    U[-1,1).
+ *  - dense_uniform: n_row x n_col DENSE with values U[-1,1).
+ *  - pa_graph: PageRank graph, CSR of the transposed adjacency (A[i][j] = 1
+ *    for an edge j -> i) of a directed graph on n nodes with out-degrees
+ *    Zipf(zipf_s) rescaled to mean `mean_deg`, a fraction `dangling_frac`
+ *    of nodes with out-degree 0, targets by preferential attachment
+ *    (probability proportional to in-degree + 1).
+ *  - diffusion7: SPD 7-point finite-volume diffusion matrix on an n^3 grid
+ *    with Dirichlet boundaries and face coefficients exp(g), g a Gaussian
+ *    random field with standard deviation sigma and correlation length
+ *    corr_len cells. */
+int tbsla_matrix_fill_uniform_rows(tbsla_matrix* m, int n, int k, unsigned long long seed);
+int tbsla_matrix_fill_powerlaw(tbsla_matrix* m, int n, double mean_len, double zipf_s,
+                               int max_len, double local_frac, int band,
+                               unsigned long long seed);
+int tbsla_matrix_fill_dense_uniform(tbsla_matrix* m, int n_row, int n_col,
+                                    unsigned long long seed);
+int tbsla_matrix_fill_pa_graph(tbsla_matrix* m, int n, double mean_deg, double zipf_s,
+                               int max_deg, double dangling_frac, unsigned long long seed);
+int tbsla_matrix_fill_diffusion7(tbsla_matrix* m, int n, double sigma, double corr_len,
+                                 unsigned long long seed);
+/* Deterministic vector fills: U[lo,hi) per index from (seed, i). */
+int tbsla_fill_uniform(double* out, long n, double lo, double hi, unsigned long long seed);
+
+/* ---- conversions: MatrixCSR/ELL/SCOO/DENSE(const MatrixCOO&)
+ *      (MatrixCSR.cpp:49-96, MatrixELL.cpp:25-79, MatrixSCOO.cpp:75-101,
+ *      MatrixDENSE.cpp:15-37) --------------------------------------------- */
+int tbsla_matrix_convert(tbsla_matrix** out, const tbsla_matrix* coo, int format);
+
+/* ---- binary I/O: write/read (e.g. MatrixCSR.cpp:236-295), the reference's
+ *      wire format byte for byte --------------------------------------------- */
+int tbsla_matrix_write(const tbsla_matrix* m, const char* path, int append);
+int tbsla_matrix_read(tbsla_matrix* m, const char* path, long offset);
+
+/* ---- device copy ------------------------------------------------------------- */
+/* Value storage precision of the device copy (TBSLA_F64 default). */
+int tbsla_matrix_set_precision(tbsla_matrix* m, int precision);
+/* Builds the device copy now (otherwise built by the first compute call). */
+int tbsla_matrix_upload(tbsla_matrix* m);
+/* Device bytes held by the handle's matrix copy. */
+int tbsla_matrix_device_bytes(const tbsla_matrix* m, size_t* bytes);
+/* CSR: block budget of the row-block partition (nnz per block, multiple of
+ * 256, default 2048); changing it rebuilds the partition. */
+int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
+
+/* ---- SpMV: Matrix::Ax / Matrix::spmv (Matrix.hpp:14-15) ----------------------- */
+/* r <- A v (CSR, ELL: overwrite; returns without touching r when nnz == 0)
+ * r += A v (COO, SCOO, DENSE: accumulate into the caller's r).
+ * vect_incr shifts output rows for COO/SCOO (MatrixCOO.cpp:140,
+ * MatrixSCOO.cpp:162); other formats ignore it, as in the reference.
+ * Lengths: v has n_col (COO) or ln_col entries; r has n_row (COO) or ln_row. */
+int tbsla_Ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr);
+/* r <- A v into a zero-filled r (the reference returns a new[] array). */
+int tbsla_spmv(const tbsla_matrix* m, double* r, const double* v, int vect_incr);
+int tbsla_Ax_device(const tbsla_matrix* m, double* r, const double* v, int vect_incr,
+                    void* stream);
+int tbsla_spmv_device(const tbsla_matrix* m, double* r, const double* v, int vect_incr,
+                      void* stream);
+
+/* ---- composite ops: Matrix.cpp:5-31 ------------------------------------------ */
+/* r <- A(Av + v) (a_axpx_, returns a new array in the reference). */
+int tbsla_a_axpx_(const tbsla_matrix* m, double* r, const double* v, int vect_incr);
+/* buffer <- Av; buffer += v; r <- A buffer (Ax semantics of the format). */
+int tbsla_AAxpAx(const tbsla_matrix* m, double* r, const double* v, double* buffer,
+                 int vect_incr);
+/* AAxpAx, then r += v. */
+int tbsla_AAxpAxpx(const tbsla_matrix* m, double* r, const double* v, double* buffer,
+                   int vect_incr);
+
+/* ---- column-stochastic preparation: get_col_sums / normalize_cols /
+ *      make_stochastic (MatrixCSR.cpp:1192-1232, Matrix.cpp:33-38) ----------- */
+/* s[j - f_col] += sum_i a_ij over the handle's values (s has ln_col entries). */
+int tbsla_get_col_sums(tbsla_matrix* m, double* s);
+/* a_ij /= s[j - f_col] where that is > 0; updates host and device values. */
+int tbsla_normalize_cols(tbsla_matrix* m, const double* s);
+/* s <- column sums (zeroed first), then normalize_cols(s). */
+int tbsla_make_stochastic(tbsla_matrix* m, double* s);
+
+/* ---- PageRank (src/mpi/matrix/Matrix.cpp:540-602, 641-790), CSR only --------
+ * A column-stochastic (zero columns = dangling nodes).  x_0 = 1/n and
+ *   x_{k+1} = beta*A x_k + (beta*D_k + (1-beta)*S_k) * t
+ * with S_k = sum x_k, D_k = sum of x_k over dangling nodes, t = 1/n.  Stops
+ * when sum|x_{k+1}-x_k| < epsilon or after max_iterations; the result is
+ * divided by its sum.  *iterations receives the count, *error the last L1
+ * change.  Returns TBSLA_ERR_NOT_CONVERGED (result still written) when the
+ * limit is hit first. */
+int tbsla_page_rank(tbsla_matrix* m, double beta, double epsilon, int max_iterations,
+                    double* result, int* iterations, double* error);
+/* Personalised PageRank for nvec teleport vectors at once (one SpMM-style
+ * matrix pass per iteration).  teleport and result are n x nvec row-major;
+ * each teleport column must sum to 1.  Runs until every column's L1 change
+ * is < epsilon or max_iterations.  nvec <= 32. */
+int tbsla_page_rank_batched(tbsla_matrix* m, int nvec, const double* teleport, double beta,
+                            double epsilon, int max_iterations, double* result,
+                            int* iterations);
+
+/* ---- CG (src/mpi/matrix/CG.cpp:32-73) ------------------------------------------
+ * Solves A x = b for SPD CSR A from the start vector in x, stopping at
+ * ||b - A x|| <= rel_tol * ||b||.  precond: 0 none, 1 Jacobi.  The SpMV runs
+ * on the handle's value precision; with TBSLA_F32/TBSLA_BF16 storage the
+ * residual is recomputed in FP64 from FP64 values every `refresh` iterations
+ * (0 = never).  rel_residual receives the FP64 true residual at exit. */
+int tbsla_cg(tbsla_matrix* m, const double* b, double* x, int max_iterations, double rel_tol,
+             int precond, int refresh, int* iterations, double* rel_residual);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TBSLA_GB300_H */

@@ -1,0 +1,706 @@
+// Device copy of a matrix handle and the orchestration of the path's kernels.
+//
+// HBM layout per format (built once by dev_upload, dropped on host mutation):
+//   CSR   rowptr int32[ln_row+1], colidx int32[nnz], values V[nnz],
+//         row-block partition int32[nblocks+1]
+//   ELL   columns int32[max_col*ln_row] and values V[max_col*ln_row],
+//         slot-major (transposed from the reference's row-major)
+//   COO/  rows, cols int32[nnz] and values V[nnz], stably sorted by row
+//   SCOO
+//   DENSE values V[ln_row*ln_col], row-major
+// V is the storage precision (double / float / bfloat16); products and sums
+// are always FP64.  Vectors are FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "device.hpp"
+#include "kernels/kernels.hpp"
+
+namespace tbsla_impl {
+
+using namespace tbsla_gpu;
+
+namespace {
+
+int g_device = 0;
+
+#define TRY(call)                                   \
+  do {                                              \
+    cudaError_t e_ = (call);                        \
+    if (e_ != cudaSuccess) return status_of(e_);    \
+  } while (0)
+
+int status_of(cudaError_t e) {
+  if (e == cudaSuccess) return TBSLA_OK;
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return TBSLA_ERR_ALLOC;
+  }
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return TBSLA_ERR_NO_DEVICE;
+  return TBSLA_ERR_CUDA;
+}
+
+int check_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return TBSLA_ERR_NO_DEVICE;
+  }
+  return TBSLA_OK;
+}
+
+size_t prec_size(int prec) { return prec == TBSLA_F64 ? 8 : prec == TBSLA_F32 ? 4 : 2; }
+
+template <class T>
+int dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) return TBSLA_OK;
+  cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return TBSLA_ERR_ALLOC;
+  }
+  return TBSLA_OK;
+}
+
+}  // namespace
+
+struct DeviceMatrix {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int prec = TBSLA_F64;
+  size_t bytes = 0;
+  void* vals = nullptr;
+  int* idx0 = nullptr;
+  int* idx1 = nullptr;
+  int* blocks = nullptr;
+  int nblocks = 0;
+  int items = 8;
+  long nnz = 0;  // entries on the device
+  int min_row = 0, max_row = -1;
+  double* x = nullptr;
+  size_t x_len = 0;
+  double* y = nullptr;
+  size_t y_len = 0;
+  double* t = nullptr;
+  size_t t_len = 0;
+  // persistent-kernel control and reduction scratch
+  unsigned* counter = nullptr;
+  double* partials = nullptr;
+  size_t partials_len = 0;
+  double* result = nullptr;
+
+  ~DeviceMatrix() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t,
+                    (void*)counter, (void*)partials, (void*)result})
+      if (p) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  int vec(double** p, size_t* len, size_t need) {
+    if (*len >= need && *p) return TBSLA_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *len = 0;
+    int st = dalloc(p, std::max<size_t>(need, 1));
+    if (st == TBSLA_OK) *len = need;
+    return st;
+  }
+  int ctl(size_t nred_per_cta, int grid) {
+    if (!counter) {
+      int st = dalloc(&counter, 4);
+      if (st) return st;
+      TRY(cudaMemsetAsync(counter, 0, 4 * sizeof(unsigned), stream));
+      st = dalloc(&result, 256);
+      if (st) return st;
+    }
+    size_t need = std::max<size_t>(nred_per_cta * grid, (size_t)kSumBlocks * 32);
+    return vec(&partials, &partials_len, need);
+  }
+};
+
+void device_release(DeviceMatrix* d) { delete d; }
+
+int dev_select(int device) {
+  int st = check_device();
+  if (st) return st;
+  int n = 0;
+  cudaGetDeviceCount(&n);
+  if (device < 0 || device >= n) return TBSLA_ERR_INVALID_ARG;
+  g_device = device;
+  return status_of(cudaSetDevice(device));
+}
+
+int dev_host_alloc(void** p, size_t bytes) {
+  int st = check_device();
+  if (st) return st;
+  cudaError_t e = cudaHostAlloc(p, bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return TBSLA_ERR_ALLOC;
+  }
+  return TBSLA_OK;
+}
+
+int dev_host_free(void* p) { return status_of(cudaFreeHost(p)); }
+
+namespace {
+
+// Stable counting sort of COO/SCOO triplets by row (device copy order).
+void sort_by_row(const tbsla_matrix* m, long nnz, int rmin, int rmax, std::vector<int>& rows,
+                 std::vector<int>& cols, std::vector<double>& vals) {
+  const int* r = m->idx0.data();
+  const int* c = m->idx1.data();
+  const double* v = m->values.data();
+  size_t span = (size_t)(rmax - rmin) + 1;
+  std::vector<long> pos(span + 1, 0);
+  for (long k = 0; k < nnz; k++) pos[r[k] - rmin + 1]++;
+  for (size_t i = 0; i < span; i++) pos[i + 1] += pos[i];
+  rows.resize(nnz);
+  cols.resize(nnz);
+  vals.resize(nnz);
+  for (long k = 0; k < nnz; k++) {
+    long p = pos[r[k] - rmin]++;
+    rows[p] = r[k];
+    cols[p] = c[k];
+    vals[p] = v[k];
+  }
+}
+
+// FP64 host values -> device storage precision.
+int upload_values(DeviceMatrix* d, const double* host, size_t n) {
+  if (n == 0) return TBSLA_OK;
+  void* dst = nullptr;
+  cudaError_t e = cudaMalloc(&dst, n * prec_size(d->prec));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return TBSLA_ERR_ALLOC;
+  }
+  d->vals = dst;
+  d->bytes += n * prec_size(d->prec);
+  if (d->prec == TBSLA_F64) return status_of(cudaMemcpyAsync(dst, host, n * 8, cudaMemcpyHostToDevice, d->stream));
+  double* tmp = nullptr;
+  int st = dalloc(&tmp, n);
+  if (st) return st;
+  TRY(cudaMemcpyAsync(tmp, host, n * 8, cudaMemcpyHostToDevice, d->stream));
+  TRY(convert_values(tmp, dst, d->prec, (long)n, d->stream));
+  TRY(cudaStreamSynchronize(d->stream));
+  cudaFree(tmp);
+  return TBSLA_OK;
+}
+
+int upload_ints(DeviceMatrix* d, int** dst, const int* host, size_t n) {
+  int st = dalloc(dst, n);
+  if (st) return st;
+  d->bytes += n * 4;
+  if (n == 0) return TBSLA_OK;
+  return status_of(cudaMemcpyAsync(*dst, host, n * 4, cudaMemcpyHostToDevice, d->stream));
+}
+
+int build(const tbsla_matrix* m, DeviceMatrix* d) {
+  const tbsla_info& I = m->info;
+  TRY(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+  switch (m->format) {
+    case TBSLA_CSR: {
+      if (I.nnz == 0) return TBSLA_OK;
+      const int* rp = m->idx0.data();
+      long end = rp[I.ln_row];
+      d->nnz = end;
+      int st = upload_ints(d, &d->idx0, rp, (size_t)I.ln_row + 1);
+      if (!st) st = upload_ints(d, &d->idx1, m->idx1.data(), (size_t)end);
+      if (!st) st = upload_values(d, m->values.data(), (size_t)end);
+      if (st) return st;
+      int tile = std::max(256, std::min(4096, m->csr_tile));
+      d->items = tile <= 1024 ? 4 : tile <= 2048 ? 8 : 16;
+      int* blocks = nullptr;
+      csr_partition(rp, I.ln_row, 256 * d->items, &blocks, &d->nblocks);
+      st = upload_ints(d, &d->blocks, blocks, (size_t)d->nblocks + 1);
+      if (!st) st = status_of(cudaStreamSynchronize(d->stream));
+      delete[] blocks;
+      return st;
+    }
+    case TBSLA_ELL: {
+      if (I.nnz == 0 || I.max_col == 0) return TBSLA_OK;
+      size_t n = (size_t)I.ln_row * I.max_col;
+      double* tv = nullptr;
+      int* tc = nullptr;
+      int st = dalloc(&tv, n);
+      if (!st) st = dalloc(&tc, n);
+      if (!st) st = dalloc(&d->idx0, n);
+      if (st) return st;
+      void* vcm = nullptr;
+      if (cudaMalloc(&vcm, n * prec_size(d->prec)) != cudaSuccess) {
+        cudaGetLastError();
+        return TBSLA_ERR_ALLOC;
+      }
+      d->vals = vcm;
+      d->bytes += n * (4 + prec_size(d->prec));
+      TRY(cudaMemcpyAsync(tv, m->values.data(), n * 8, cudaMemcpyHostToDevice, d->stream));
+      TRY(cudaMemcpyAsync(tc, m->idx0.data(), n * 4, cudaMemcpyHostToDevice, d->stream));
+      TRY(ell_transpose(tv, tc, vcm, d->prec, d->idx0, I.ln_row, I.max_col, d->stream));
+      TRY(cudaStreamSynchronize(d->stream));
+      cudaFree(tv);
+      cudaFree(tc);
+      return TBSLA_OK;
+    }
+    case TBSLA_COO:
+    case TBSLA_SCOO: {
+      long nnz = I.nnz;
+      d->nnz = nnz;
+      if (nnz == 0) return TBSLA_OK;
+      const int* r = m->idx0.data();
+      int rmin = r[0], rmax = r[0];
+      for (long k = 1; k < nnz; k++) {
+        rmin = std::min(rmin, r[k]);
+        rmax = std::max(rmax, r[k]);
+      }
+      d->min_row = rmin;
+      d->max_row = rmax;
+      std::vector<int> rows, cols;
+      std::vector<double> vals;
+      sort_by_row(m, nnz, rmin, rmax, rows, cols, vals);
+      int st = upload_ints(d, &d->idx0, rows.data(), nnz);
+      if (!st) st = upload_ints(d, &d->idx1, cols.data(), nnz);
+      if (!st) st = upload_values(d, vals.data(), nnz);
+      if (!st) st = status_of(cudaStreamSynchronize(d->stream));
+      return st;
+    }
+    case TBSLA_DENSE: {
+      if (I.nnz == 0) return TBSLA_OK;
+      int st = upload_values(d, m->values.data(), (size_t)I.ln_row * I.ln_col);
+      if (!st) st = status_of(cudaStreamSynchronize(d->stream));
+      return st;
+    }
+  }
+  return TBSLA_ERR_INVALID_ARG;
+}
+
+size_t in_len(const tbsla_matrix* m) {
+  return m->format == TBSLA_COO ? (size_t)m->info.n_col : (size_t)m->info.ln_col;
+}
+size_t out_len(const tbsla_matrix* m) {
+  return m->format == TBSLA_COO ? (size_t)m->info.n_row : (size_t)m->info.ln_row;
+}
+bool accumulates(int format) {
+  return format == TBSLA_COO || format == TBSLA_SCOO || format == TBSLA_DENSE;
+}
+// CSR / ELL / DENSE return without touching r when empty (MatrixCSR.cpp:210,
+// MatrixELL.cpp:182, MatrixDENSE.cpp:78).
+bool skips_empty(const tbsla_matrix* m) {
+  const tbsla_info& I = m->info;
+  switch (m->format) {
+    case TBSLA_CSR: return I.nnz == 0;
+    case TBSLA_ELL: return I.nnz == 0 || I.max_col == 0;
+    case TBSLA_DENSE: return I.nnz == 0;
+    case TBSLA_SCOO: return I.nnz == 0;
+  }
+  return false;
+}
+
+DeviceMatrix* ensure(const tbsla_matrix* m, int* st) {
+  *st = TBSLA_OK;
+  if (m->dev) {
+    cudaSetDevice(m->dev->device);
+    return m->dev;
+  }
+  *st = validate(m);  // bad arrays are reported before any device work
+  if (*st) return nullptr;
+  *st = check_device();
+  if (*st) return nullptr;
+  cudaSetDevice(g_device);
+  auto* d = new DeviceMatrix();
+  d->device = g_device;
+  d->prec = m->precision;
+  *st = build(m, d);
+  if (*st) {
+    delete d;
+    return nullptr;
+  }
+  m->dev = d;
+  return d;
+}
+
+CsrArgs csr_args(const tbsla_matrix* m, DeviceMatrix* d) {
+  CsrArgs a;
+  a.vals = d->vals;
+  a.prec = d->prec;
+  a.rowptr = d->idx0;
+  a.colidx = d->idx1;
+  a.blocks = d->blocks;
+  a.nblocks = d->nblocks;
+  a.f_col = m->info.f_col;
+  a.items = d->items;
+  return a;
+}
+
+// r (device) op= A v (device) on stream s, following the format's Ax semantics.
+int ax_device(const tbsla_matrix* m, DeviceMatrix* d, double* r, const double* v, int vect_incr,
+              cudaStream_t s) {
+  const tbsla_info& I = m->info;
+  if (skips_empty(m)) return TBSLA_OK;
+  switch (m->format) {
+    case TBSLA_CSR:
+      return status_of(csr_spmv(csr_args(m, d), v, r, s));
+    case TBSLA_ELL:
+      return status_of(ell_spmv(d->vals, d->prec, d->idx0, I.ln_row, I.max_col, I.f_col, v, r, s));
+    case TBSLA_COO:
+    case TBSLA_SCOO: {
+      if (d->nnz == 0) return TBSLA_OK;
+      bool scoo = m->format == TBSLA_SCOO;
+      long off = (long)vect_incr - (scoo ? I.f_row : 0);
+      long len = scoo ? I.ln_row : I.n_row;
+      if (d->min_row + off < 0 || d->max_row + off >= len) return TBSLA_ERR_INVALID_ARG;
+      return status_of(coo_spmv(d->vals, d->prec, d->idx0, d->idx1, d->nnz, (int)off,
+                                scoo ? -I.f_col : 0, v, r, s));
+    }
+    case TBSLA_DENSE:
+      return status_of(dense_gemv(d->vals, d->prec, I.ln_row, I.ln_col, v, r, s));
+  }
+  return TBSLA_ERR_INVALID_ARG;
+}
+
+}  // namespace
+
+int dev_upload(const tbsla_matrix* m) {
+  int st;
+  ensure(m, &st);
+  return st;
+}
+
+int dev_bytes(const tbsla_matrix* m, size_t* bytes) {
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  *bytes = d->bytes;
+  return TBSLA_OK;
+}
+
+int dev_ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr, bool zero_first,
+           bool host, void* stream) {
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  if (!host) {
+    cudaStream_t s = stream ? (cudaStream_t)stream : d->stream;
+    if (zero_first) TRY(cudaMemsetAsync(r, 0, out_len(m) * sizeof(double), s));
+    return ax_device(m, d, r, v, vect_incr, s);
+  }
+  if (!zero_first && skips_empty(m)) return TBSLA_OK;
+  size_t nx = in_len(m), ny = out_len(m);
+  if ((st = d->vec(&d->x, &d->x_len, nx)) || (st = d->vec(&d->y, &d->y_len, ny))) return st;
+  cudaStream_t s = d->stream;
+  if (nx) TRY(cudaMemcpyAsync(d->x, v, nx * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (zero_first) TRY(cudaMemsetAsync(d->y, 0, ny * sizeof(double), s));
+  else if (accumulates(m->format) && ny) TRY(cudaMemcpyAsync(d->y, r, ny * sizeof(double), cudaMemcpyHostToDevice, s));
+  st = ax_device(m, d, d->y, d->x, vect_incr, s);
+  if (st) return st;
+  if (ny) TRY(cudaMemcpyAsync(r, d->y, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
+  return status_of(cudaStreamSynchronize(s));
+}
+
+int dev_a_axpx(const tbsla_matrix* m, double* r, const double* v, int vect_incr) {
+  // Matrix::a_axpx_, Matrix.cpp:5-14: r = spmv(v); r += v; return spmv(r).
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  size_t nx = in_len(m), ny = out_len(m);
+  if (nx != ny) return TBSLA_ERR_INVALID_ARG;
+  if ((st = d->vec(&d->x, &d->x_len, nx)) || (st = d->vec(&d->y, &d->y_len, ny)) ||
+      (st = d->vec(&d->t, &d->t_len, ny)))
+    return st;
+  cudaStream_t s = d->stream;
+  TRY(cudaMemcpyAsync(d->x, v, nx * 8, cudaMemcpyHostToDevice, s));
+  TRY(cudaMemsetAsync(d->t, 0, ny * 8, s));
+  if ((st = ax_device(m, d, d->t, d->x, vect_incr, s))) return st;
+  TRY(vec_add(d->t, d->x, (long)nx, s));
+  TRY(cudaMemsetAsync(d->y, 0, ny * 8, s));
+  if ((st = ax_device(m, d, d->y, d->t, vect_incr, s))) return st;
+  TRY(cudaMemcpyAsync(r, d->y, ny * 8, cudaMemcpyDeviceToHost, s));
+  return status_of(cudaStreamSynchronize(s));
+}
+
+int dev_aaxpax(const tbsla_matrix* m, double* r, const double* v, double* buffer, int vect_incr,
+               bool plus_x) {
+  // Matrix::AAxpAx / AAxpAxpx, Matrix.cpp:16-31: Ax(buffer, v); buffer += v;
+  // Ax(r, buffer) [; r += v].  Buffer and r keep the format's Ax semantics.
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  size_t nx = in_len(m), ny = out_len(m);
+  if (nx != ny) return TBSLA_ERR_INVALID_ARG;
+  if ((st = d->vec(&d->x, &d->x_len, nx)) || (st = d->vec(&d->y, &d->y_len, ny)) ||
+      (st = d->vec(&d->t, &d->t_len, ny)))
+    return st;
+  cudaStream_t s = d->stream;
+  TRY(cudaMemcpyAsync(d->x, v, nx * 8, cudaMemcpyHostToDevice, s));
+  TRY(cudaMemcpyAsync(d->t, buffer, ny * 8, cudaMemcpyHostToDevice, s));
+  TRY(cudaMemcpyAsync(d->y, r, ny * 8, cudaMemcpyHostToDevice, s));
+  if ((st = ax_device(m, d, d->t, d->x, vect_incr, s))) return st;
+  TRY(vec_add(d->t, d->x, (long)nx, s));
+  if ((st = ax_device(m, d, d->y, d->t, vect_incr, s))) return st;
+  if (plus_x) TRY(vec_add(d->y, d->x, (long)nx, s));
+  TRY(cudaMemcpyAsync(buffer, d->t, ny * 8, cudaMemcpyDeviceToHost, s));
+  TRY(cudaMemcpyAsync(r, d->y, ny * 8, cudaMemcpyDeviceToHost, s));
+  return status_of(cudaStreamSynchronize(s));
+}
+
+// ---- column-stochastic preparation -----------------------------------------------
+
+namespace {
+// FP64 device copy of the CSR values (the device storage may be narrower).
+int values64(const tbsla_matrix* m, DeviceMatrix* d, double** out, bool* owned) {
+  long n = d->nnz;
+  if (d->prec == TBSLA_F64) {
+    *out = (double*)d->vals;
+    *owned = false;
+    return TBSLA_OK;
+  }
+  int st = dalloc(out, (size_t)n);
+  if (st) return st;
+  *owned = true;
+  return status_of(cudaMemcpyAsync(*out, m->values.data(), n * 8, cudaMemcpyHostToDevice, d->stream));
+}
+}  // namespace
+
+int dev_col_sums(tbsla_matrix* m, double* s, bool zero_first) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const tbsla_info& I = m->info;
+  if (I.nnz == 0) {  // MatrixCSR.cpp:1194-1197: nothing to add
+    if (zero_first) std::memset(s, 0, sizeof(double) * I.ln_col);
+    return TBSLA_OK;
+  }
+  size_t nc = I.ln_col;
+  if ((st = d->vec(&d->t, &d->t_len, nc))) return st;
+  cudaStream_t str = d->stream;
+  if (zero_first) TRY(cudaMemsetAsync(d->t, 0, nc * 8, str));
+  else TRY(cudaMemcpyAsync(d->t, s, nc * 8, cudaMemcpyHostToDevice, str));
+  double* v64;
+  bool owned;
+  if ((st = values64(m, d, &v64, &owned))) return st;
+  TRY(csr_col_sums(v64, d->idx0, d->idx1, I.ln_row, I.f_col, d->t, str));
+  TRY(cudaMemcpyAsync(s, d->t, nc * 8, cudaMemcpyDeviceToHost, str));
+  TRY(cudaStreamSynchronize(str));
+  if (owned) cudaFree(v64);
+  return TBSLA_OK;
+}
+
+int dev_normalize_cols(tbsla_matrix* m, const double* s) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const tbsla_info& I = m->info;
+  if (I.nnz == 0) return TBSLA_OK;
+  size_t nc = I.ln_col;
+  if ((st = d->vec(&d->t, &d->t_len, nc))) return st;
+  cudaStream_t str = d->stream;
+  TRY(cudaMemcpyAsync(d->t, s, nc * 8, cudaMemcpyHostToDevice, str));
+  double* v64;
+  bool owned;
+  if ((st = values64(m, d, &v64, &owned))) return st;
+  TRY(csr_normalize_cols(v64, d->idx0, d->idx1, I.ln_row, I.f_col, d->t, str));
+  // keep the host arrays (the reference layout) in step with the device
+  TRY(cudaMemcpyAsync(m->values.data(), v64, d->nnz * 8, cudaMemcpyDeviceToHost, str));
+  if (owned) TRY(convert_values(v64, d->vals, d->prec, d->nnz, str));
+  TRY(cudaStreamSynchronize(str));
+  if (owned) cudaFree(v64);
+  return TBSLA_OK;
+}
+
+int dev_make_stochastic(tbsla_matrix* m, double* s) {
+  int st = dev_col_sums(m, s, true);
+  if (st) return st;
+  return dev_normalize_cols(m, s);
+}
+
+// ---- PageRank ------------------------------------------------------------------------
+
+namespace {
+int dangling_flags(const tbsla_matrix* m, DeviceMatrix* d, unsigned char** flags) {
+  int n = m->info.ln_row;
+  if (cudaMalloc((void**)flags, (size_t)n) != cudaSuccess) {
+    cudaGetLastError();
+    return TBSLA_ERR_ALLOC;
+  }
+  return status_of(csr_dangling(d->idx0, d->idx1, m->info.ln_row, m->info.n_col, *flags, d->stream));
+}
+}  // namespace
+
+int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* result,
+                  int* iterations, double* error) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  const tbsla_info& I = m->info;
+  if (I.n_row != I.n_col || I.ln_row != I.n_row || I.f_col != 0 || max_it < 0)
+    return TBSLA_ERR_INVALID_ARG;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const int n = I.n_row;
+  cudaStream_t s = d->stream;
+  double *x0 = nullptr, *x1 = nullptr, *coef = nullptr;
+  int* flags = nullptr;  // [0] done, [1] iterations
+  unsigned char* dang = nullptr;
+  int grid = I.nnz > 0 ? csr_pagerank_grid(d->items, d->prec) : 1;
+  std::vector<unsigned char> hd(n);
+  auto cleanup = [&]() {
+    for (void* p : {(void*)x0, (void*)x1, (void*)coef, (void*)flags, (void*)dang})
+      if (p) cudaFree(p);
+  };
+  if ((st = dalloc(&x0, n)) || (st = dalloc(&x1, n)) || (st = dalloc(&coef, 2)) ||
+      (st = dalloc(&flags, 2)) || (st = d->ctl(3, grid)) || (st = dangling_flags(m, d, &dang))) {
+    cleanup();
+    return st;
+  }
+  // x_0 = 1/n; S_0 and D_0 summed in index order (the oracle's order).
+  const double x_init = 1.0 / n;
+  double S = 0, D = 0;
+  if (cudaMemcpyAsync(hd.data(), dang, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cleanup();
+    return TBSLA_ERR_CUDA;
+  }
+  for (int i = 0; i < n; i++) {
+    S += x_init;
+    if (hd[i]) D += x_init;
+  }
+  double c0 = beta * D + (1.0 - beta) * S;
+  vec_fill(x0, x_init, n, s);
+  cudaMemcpyAsync(coef, &c0, 8, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
+  CsrArgs a = csr_args(m, d);
+  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 1, flags, flags + 1};
+  Ctl ctl{d->counter, d->partials, d->result};
+  int launched = 0, hflags[2] = {0, 0};
+  const int chunk = 8;
+  while (launched < max_it && !hflags[0]) {
+    int k = std::min(chunk, max_it - launched);
+    for (int j = 0; j < k; j++, launched++) {
+      const bool even = (launched % 2) == 0;
+      p.coef_in = coef + (even ? 0 : 1);
+      p.coef_out = coef + (even ? 1 : 0);
+      cudaError_t e = I.nnz > 0 ? csr_pagerank_step(a, even ? x0 : x1, even ? x1 : x0, p, ctl, grid, s)
+                                : cudaErrorInvalidValue;
+      if (e != cudaSuccess) {
+        cleanup();
+        return I.nnz > 0 ? status_of(e) : TBSLA_ERR_BAD_MATRIX;
+      }
+    }
+    if (cudaMemcpyAsync(hflags, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      cleanup();
+      return TBSLA_ERR_CUDA;
+    }
+  }
+  const int iters = hflags[1];
+  double* fin = (iters % 2 == 1) ? x1 : x0;
+  // final normalisation x /= sum(x) (Matrix.cpp:149-171)
+  double* sum = d->result + 8;
+  st = status_of(mat_colsum(fin, n, 1, d->partials, sum, s));
+  if (!st) st = status_of(mat_scale_cols(fin, n, 1, sum, s));
+  if (!st) st = status_of(cudaMemcpyAsync(result, fin, (size_t)n * 8, cudaMemcpyDeviceToHost, s));
+  double herr = 0;
+  if (!st) st = status_of(cudaMemcpyAsync(&herr, d->result, 8, cudaMemcpyDeviceToHost, s));
+  if (!st) st = status_of(cudaStreamSynchronize(s));
+  cleanup();
+  if (st) return st;
+  if (iterations) *iterations = iters;
+  if (error) *error = herr;
+  return hflags[0] ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
+}
+
+int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double beta, double eps,
+                          int max_it, double* result, int* iterations) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  const tbsla_info& I = m->info;
+  if (I.n_row != I.n_col || I.ln_row != I.n_row || I.f_col != 0 || nvec < 1 || nvec > 32 ||
+      max_it < 0 || I.nnz == 0)
+    return TBSLA_ERR_INVALID_ARG;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const int n = I.n_row;
+  const size_t nn = (size_t)n * nvec;
+  cudaStream_t s = d->stream;
+  double *X0 = nullptr, *X1 = nullptr, *T = nullptr, *coef = nullptr;
+  int* flags = nullptr;
+  unsigned char* dang = nullptr;
+  int grid = csr_pagerank_batched_grid(d->prec);
+  auto cleanup = [&]() {
+    for (void* p : {(void*)X0, (void*)X1, (void*)T, (void*)coef, (void*)flags, (void*)dang})
+      if (p) cudaFree(p);
+  };
+  if ((st = dalloc(&X0, nn)) || (st = dalloc(&X1, nn)) || (st = dalloc(&T, nn)) ||
+      (st = dalloc(&coef, 64)) || (st = dalloc(&flags, 2)) || (st = d->ctl(96, grid)) ||
+      (st = dangling_flags(m, d, &dang))) {
+    cleanup();
+    return st;
+  }
+  std::vector<unsigned char> hd(n);
+  if (cudaMemcpyAsync(hd.data(), dang, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cleanup();
+    return TBSLA_ERR_CUDA;
+  }
+  const double x_init = 1.0 / n;
+  double S = 0, D = 0;
+  for (int i = 0; i < n; i++) {
+    S += x_init;
+    if (hd[i]) D += x_init;
+  }
+  std::vector<double> c0(nvec, beta * D + (1.0 - beta) * S);
+  vec_fill(X0, x_init, (long)nn, s);
+  cudaMemcpyAsync(T, tele, nn * 8, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(coef, c0.data(), nvec * 8, cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
+  CsrArgs a = csr_args(m, d);
+  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 32, flags, flags + 1};
+  Ctl ctl{d->counter, d->partials, d->result};
+  int launched = 0, hflags[2] = {0, 0};
+  while (launched < max_it && !hflags[0]) {
+    int k = std::min(8, max_it - launched);
+    for (int j = 0; j < k; j++, launched++) {
+      const bool even = (launched % 2) == 0;
+      p.coef_in = coef + (even ? 0 : 32);
+      p.coef_out = coef + (even ? 32 : 0);
+      cudaError_t e = csr_pagerank_batched_step(a, n, nvec, even ? X0 : X1, even ? X1 : X0, T, p, ctl, grid, s);
+      if (e != cudaSuccess) {
+        cleanup();
+        return status_of(e);
+      }
+    }
+    if (cudaMemcpyAsync(hflags, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess) {
+      cleanup();
+      return TBSLA_ERR_CUDA;
+    }
+  }
+  const int iters = hflags[1];
+  double* fin = (iters % 2 == 1) ? X1 : X0;
+  double* sums = d->result + 128;
+  st = status_of(mat_colsum(fin, n, nvec, d->partials, sums, s));
+  if (!st) st = status_of(mat_scale_cols(fin, n, nvec, sums, s));
+  if (!st) st = status_of(cudaMemcpyAsync(result, fin, nn * 8, cudaMemcpyDeviceToHost, s));
+  if (!st) st = status_of(cudaStreamSynchronize(s));
+  cleanup();
+  if (st) return st;
+  if (iterations) *iterations = iters;
+  return hflags[0] ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
+}
+
+int dev_cg(tbsla_matrix*, const double*, double*, int, double, int, int, int*, double*) {
+  return TBSLA_ERR_UNSUPPORTED;
+}
+
+}  // namespace tbsla_impl

@@ -1,0 +1,37 @@
+// Interface between the C ABI (capi.cpp, host compiler) and the CUDA side
+// (device.cu).  Plain pointers only.
+#pragma once
+
+#include <cstddef>
+
+#include "host/matrix.hpp"
+
+namespace tbsla_impl {
+
+int dev_select(int device);
+int dev_host_alloc(void** p, size_t bytes);
+int dev_host_free(void* p);
+
+int dev_upload(const tbsla_matrix* m);
+int dev_bytes(const tbsla_matrix* m, size_t* bytes);
+
+// Ax / spmv.  host = true: r and v are host pointers, copied in and out.
+int dev_ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr, bool zero_first,
+           bool host, void* stream);
+int dev_a_axpx(const tbsla_matrix* m, double* r, const double* v, int vect_incr);
+int dev_aaxpax(const tbsla_matrix* m, double* r, const double* v, double* buffer, int vect_incr,
+               bool plus_x);
+
+int dev_col_sums(tbsla_matrix* m, double* s, bool zero_first);
+int dev_normalize_cols(tbsla_matrix* m, const double* s);
+int dev_make_stochastic(tbsla_matrix* m, double* s);
+
+int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* result,
+                  int* iterations, double* error);
+int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double beta, double eps,
+                          int max_it, double* result, int* iterations);
+
+int dev_cg(tbsla_matrix* m, const double* b, double* x, int max_it, double rel_tol, int precond,
+           int refresh, int* iterations, double* rel_residual);
+
+}  // namespace tbsla_impl

@@ -1,0 +1,261 @@
+// DENSE GEMV and the small vector / preparation kernels of the path.
+//
+// dense_gemv replaces tbsla::cpp::MatrixDENSE::Ax
+// (src/cpp/matrix/MatrixDENSE.cpp:77-86): r_i += sum_j A_ij v_j on a
+// row-major ln_row x ln_col matrix.  One warp per row; lanes read the row with
+// 16-byte loads (pairs of doubles) where the row start is 16-byte aligned,
+// x comes through L1 (it is reused by every row), partial sums are combined
+// with a warp butterfly and added to r_i.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.hpp"
+
+namespace tbsla_gpu {
+
+namespace {
+
+constexpr int NT = 256;
+
+__device__ __forceinline__ double2 ld_stream2(const double* p, uint64_t pol) {
+  double2 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+               : "=d"(v.x), "=d"(v.y) : "l"(p), "l"(pol));
+  return v;
+}
+
+template <class V>
+__global__ void __launch_bounds__(NT) k_dense(const V* __restrict__ A, int ln_row, int ln_col,
+                                             const double* __restrict__ x, double* __restrict__ y) {
+  const int lane = threadIdx.x % kWarp;
+  const int gw = (blockIdx.x * NT + threadIdx.x) / kWarp;
+  const int nw = gridDim.x * NT / kWarp;
+  const uint64_t pol = policy_evict_first();
+  for (int row = gw; row < ln_row; row += nw) {
+    const V* a = A + (size_t)row * ln_col;
+    double acc = 0;
+    int j = lane;
+    for (; j + 3 * kWarp < ln_col; j += 4 * kWarp) {
+      double v0 = widen(ld_stream(a + j, pol)), v1 = widen(ld_stream(a + j + kWarp, pol));
+      double v2 = widen(ld_stream(a + j + 2 * kWarp, pol)), v3 = widen(ld_stream(a + j + 3 * kWarp, pol));
+      acc = add_rn(acc, mul_rn(v0, __ldg(x + j)));
+      acc = add_rn(acc, mul_rn(v1, __ldg(x + j + kWarp)));
+      acc = add_rn(acc, mul_rn(v2, __ldg(x + j + 2 * kWarp)));
+      acc = add_rn(acc, mul_rn(v3, __ldg(x + j + 3 * kWarp)));
+    }
+    for (; j < ln_col; j += kWarp) acc = add_rn(acc, mul_rn(widen(ld_stream(a + j, pol)), __ldg(x + j)));
+    acc = warp_sum(acc);
+    if (lane == 0) y[row] = add_rn(y[row], acc);
+  }
+}
+
+// FP64 rows with 16-byte aligned starts (ln_col even): 16-byte loads.
+__global__ void __launch_bounds__(NT) k_dense_f64x2(const double* __restrict__ A, int ln_row,
+                                                   int ln_col, const double* __restrict__ x,
+                                                   double* __restrict__ y) {
+  const int lane = threadIdx.x % kWarp;
+  const int gw = (blockIdx.x * NT + threadIdx.x) / kWarp;
+  const int nw = gridDim.x * NT / kWarp;
+  const uint64_t pol = policy_evict_first();
+  const int half = ln_col / 2;
+  const double2* x2 = reinterpret_cast<const double2*>(x);
+  for (int row = gw; row < ln_row; row += nw) {
+    const double* a = A + (size_t)row * ln_col;
+    double acc0 = 0, acc1 = 0;
+    int j = lane;
+    for (; j + 3 * kWarp < half; j += 4 * kWarp) {
+      double2 a0 = ld_stream2(a + 2 * j, pol), a1 = ld_stream2(a + 2 * (j + kWarp), pol);
+      double2 a2 = ld_stream2(a + 2 * (j + 2 * kWarp), pol), a3 = ld_stream2(a + 2 * (j + 3 * kWarp), pol);
+      double2 b0 = __ldg(x2 + j), b1 = __ldg(x2 + j + kWarp);
+      double2 b2 = __ldg(x2 + j + 2 * kWarp), b3 = __ldg(x2 + j + 3 * kWarp);
+      acc0 = add_rn(acc0, mul_rn(a0.x, b0.x)); acc1 = add_rn(acc1, mul_rn(a0.y, b0.y));
+      acc0 = add_rn(acc0, mul_rn(a1.x, b1.x)); acc1 = add_rn(acc1, mul_rn(a1.y, b1.y));
+      acc0 = add_rn(acc0, mul_rn(a2.x, b2.x)); acc1 = add_rn(acc1, mul_rn(a2.y, b2.y));
+      acc0 = add_rn(acc0, mul_rn(a3.x, b3.x)); acc1 = add_rn(acc1, mul_rn(a3.y, b3.y));
+    }
+    for (; j < half; j += kWarp) {
+      double2 a0 = ld_stream2(a + 2 * j, pol);
+      double2 b0 = __ldg(x2 + j);
+      acc0 = add_rn(acc0, mul_rn(a0.x, b0.x));
+      acc1 = add_rn(acc1, mul_rn(a0.y, b0.y));
+    }
+    double acc = warp_sum(add_rn(acc0, acc1));
+    if (lane == 0) y[row] = add_rn(y[row], acc);
+  }
+}
+
+__global__ void k_vec_add(double* __restrict__ y, const double* __restrict__ x, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = add_rn(y[i], x[i]);
+}
+
+__global__ void k_vec_fill(double* __restrict__ y, double v, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    y[i] = v;
+}
+
+// Warp per row; each entry's value added to its column's sum.
+__global__ void k_col_sums(const double* __restrict__ vals, const int* __restrict__ rowptr,
+                           const int* __restrict__ colidx, int n_row, int f_col, double* s) {
+  const int lane = threadIdx.x % kWarp;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int nw = gridDim.x * blockDim.x / kWarp;
+  for (int row = gw; row < n_row; row += nw)
+    for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += kWarp)
+      atomicAdd(s + (colidx[j] - f_col), vals[j]);
+}
+
+__global__ void k_normalize_cols(double* __restrict__ vals, const int* __restrict__ rowptr,
+                                 const int* __restrict__ colidx, int n_row, int f_col,
+                                 const double* __restrict__ s) {
+  const int lane = threadIdx.x % kWarp;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int nw = gridDim.x * blockDim.x / kWarp;
+  for (int row = gw; row < n_row; row += nw)
+    for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += kWarp) {
+      const double sv = s[colidx[j] - f_col];
+      if (sv > 0) vals[j] = __ddiv_rn(vals[j], sv);
+    }
+}
+
+__global__ void k_mark_cols(const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                            int n_row, unsigned char* has_entry) {
+  const int lane = threadIdx.x % kWarp;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
+  const int nw = gridDim.x * blockDim.x / kWarp;
+  for (int row = gw; row < n_row; row += nw)
+    for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += kWarp) has_entry[colidx[j]] = 0;
+}
+
+// Pass 1: CTA b sums rows b, b + grid, ... per column into partials[b][k].
+// With ncol == 1 all 256 threads stride over the vector.
+__global__ void __launch_bounds__(256) k_colsum_pass1(const double* __restrict__ x, long n, int ncol,
+                                                     double* __restrict__ partials) {
+  __shared__ double s[256];
+  double acc = 0;
+  if (ncol == 1) {
+    for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256) acc = add_rn(acc, x[i]);
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+      for (int i = 0; i < 256; i++) t = add_rn(t, s[i]);
+      partials[(size_t)blockIdx.x * 32] = t;
+    }
+    return;
+  }
+  const int lane = threadIdx.x % kWarp, warp = threadIdx.x / kWarp;
+  if (lane < ncol)
+    for (long i = (long)blockIdx.x * 8 + warp; i < n; i += (long)gridDim.x * 8) acc = add_rn(acc, x[i * ncol + lane]);
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x < ncol) {
+    double t = 0;
+    for (int w = 0; w < 8; w++) t = add_rn(t, s[w * kWarp + threadIdx.x]);
+    partials[(size_t)blockIdx.x * 32 + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_colsum_pass2(const double* __restrict__ partials, int nblk, int ncol, double* out) {
+  if ((int)threadIdx.x >= ncol) return;
+  double t = 0;
+  for (int b = 0; b < nblk; b++) t = add_rn(t, partials[(size_t)b * 32 + threadIdx.x]);
+  out[threadIdx.x] = t;
+}
+
+__global__ void k_scale_cols(double* __restrict__ x, long n, int ncol, const double* __restrict__ d) {
+  const long total = n * ncol;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x)
+    x[i] = __ddiv_rn(x[i], d[i % ncol]);
+}
+
+template <class V>
+__global__ void k_convert(const double* __restrict__ src, V* __restrict__ dst, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = narrow<V>(src[i]);
+}
+
+inline int grid_for(long n, int per = 256) {
+  return (int)std::max<long>(1, std::min<long>((n + per - 1) / per, 152L * 16));
+}
+
+}  // namespace
+
+cudaError_t dense_gemv(const void* vals, int prec, int ln_row, int ln_col, const double* x,
+                       double* y, cudaStream_t s) {
+  if (ln_row == 0 || ln_col == 0) return cudaSuccess;
+  const int grid = (int)std::min<long>(((long)ln_row + NT / kWarp - 1) / (NT / kWarp), 152L * 8);
+  switch (prec) {
+    case kF64:
+      if (ln_col % 2 == 0 && ((uintptr_t)vals % 16) == 0 && ((uintptr_t)x % 16) == 0)
+        k_dense_f64x2<<<grid, NT, 0, s>>>(static_cast<const double*>(vals), ln_row, ln_col, x, y);
+      else
+        k_dense<double><<<grid, NT, 0, s>>>(static_cast<const double*>(vals), ln_row, ln_col, x, y);
+      break;
+    case kF32: k_dense<float><<<grid, NT, 0, s>>>(static_cast<const float*>(vals), ln_row, ln_col, x, y); break;
+    case kBF16: k_dense<__nv_bfloat16><<<grid, NT, 0, s>>>(static_cast<const __nv_bfloat16*>(vals), ln_row, ln_col, x, y); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t vec_add(double* y, const double* x, long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_vec_add<<<grid_for(n), 256, 0, s>>>(y, x, n);
+  return cudaGetLastError();
+}
+
+cudaError_t vec_fill(double* y, double v, long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_vec_fill<<<grid_for(n), 256, 0, s>>>(y, v, n);
+  return cudaGetLastError();
+}
+
+cudaError_t mat_colsum(const double* x, long n, int ncol, double* partials, double* out,
+                       cudaStream_t s) {
+  if (ncol < 1 || ncol > kWarp) return cudaErrorInvalidValue;
+  k_colsum_pass1<<<kSumBlocks, 256, 0, s>>>(x, n, ncol, partials);
+  k_colsum_pass2<<<1, 32, 0, s>>>(partials, kSumBlocks, ncol, out);
+  return cudaGetLastError();
+}
+
+cudaError_t mat_scale_cols(double* x, long n, int ncol, const double* denom, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_scale_cols<<<grid_for(n * ncol), 256, 0, s>>>(x, n, ncol, denom);
+  return cudaGetLastError();
+}
+
+cudaError_t csr_col_sums(const double* vals, const int* rowptr, const int* colidx, int n_row,
+                         int f_col, double* s, cudaStream_t st) {
+  if (n_row <= 0) return cudaSuccess;
+  k_col_sums<<<grid_for((long)n_row * kWarp), 256, 0, st>>>(vals, rowptr, colidx, n_row, f_col, s);
+  return cudaGetLastError();
+}
+
+cudaError_t csr_normalize_cols(double* vals, const int* rowptr, const int* colidx, int n_row,
+                               int f_col, const double* s, cudaStream_t st) {
+  if (n_row <= 0) return cudaSuccess;
+  k_normalize_cols<<<grid_for((long)n_row * kWarp), 256, 0, st>>>(vals, rowptr, colidx, n_row, f_col, s);
+  return cudaGetLastError();
+}
+
+cudaError_t csr_dangling(const int* rowptr, const int* colidx, int n_row, int n_col,
+                         unsigned char* dangling, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(dangling, 1, (size_t)n_col, st);
+  if (e != cudaSuccess || n_row <= 0) return e;
+  k_mark_cols<<<grid_for((long)n_row * kWarp), 256, 0, st>>>(rowptr, colidx, n_row, dangling);
+  return cudaGetLastError();
+}
+
+cudaError_t convert_values(const double* src, void* dst, int prec, long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  switch (prec) {
+    case kF64: return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    case kF32: k_convert<float><<<grid_for(n), 256, 0, s>>>(src, (float*)dst, n); break;
+    case kBF16: k_convert<__nv_bfloat16><<<grid_for(n), 256, 0, s>>>(src, (__nv_bfloat16*)dst, n); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tbsla_gpu

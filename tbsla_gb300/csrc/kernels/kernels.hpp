@@ -1,0 +1,111 @@
+// Host-callable launchers of the SpMV-path kernels (one translation unit per
+// kernel family).  All take device pointers and a stream; none synchronise.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tbsla_gpu {
+
+enum Prec { kF64 = 0, kF32 = 1, kBF16 = 2 };
+
+// Control block of the persistent kernels: [0] next work item, [1] CTAs
+// finished; both return to 0 at the end of every launch (the last CTA
+// resets them).
+struct Ctl {
+  unsigned* counter;
+  double* partials;  // gridDim.x * nred doubles
+  double* result;    // nred doubles
+};
+
+// ---- CSR (row-block adaptive) ------------------------------------------------
+struct CsrArgs {
+  const void* vals;
+  int prec;
+  const int* rowptr;
+  const int* colidx;
+  const int* blocks;  // nblocks + 1 row boundaries
+  int nblocks;
+  int f_col;
+  int items;  // nnz budget per block / 256 (4, 8 or 16)
+};
+// y[row] = (A x)[row] for every row of the partition.
+cudaError_t csr_spmv(const CsrArgs& a, const double* x, double* y, cudaStream_t s);
+// Row-block partition of a CSR row pointer (host): blocks of consecutive
+// rows with at most `tile` entries and at most 256 rows each; a row longer
+// than `tile` forms a block on its own.  Returns the boundaries.
+void csr_partition(const int* rowptr, int n_row, int tile, int** out, int* nblocks);
+
+// PageRank step on CSR: y = beta*(A x) + c_i, with c_i = coef / n
+// (tele == nullptr) or coef * tele[i]; coef = beta*D + (1-beta)*S read from
+// coef_in[0] (device).  Reductions: result[0] = sum |y - x|, result[1] =
+// sum y, result[2] = sum over dangling rows of y; the last CTA also writes
+// coef_out[0] = beta*result[2] + (1-beta)*result[1] and sets *done when
+// result[0] < eps (a done flag already set makes the launch a no-op).
+struct PageRankArgs {
+  double beta;
+  double n_nodes;
+  double eps;
+  const double* tele;
+  const unsigned char* dangling;
+  const double* coef_in;
+  double* coef_out;
+  int* done;
+  int* iters;
+};
+cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
+                              const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s);
+// Batched personalised PageRank step: X, Y, T are n x nvec row-major
+// (nvec <= 32); per column k: Y = beta*A X + coef_k * T[:,k], with
+// coef_k = beta*D_k + (1-beta)*S_k from coef_in[k].  Reductions per column
+// k: result[k] = L1 change, result[nvec + k] = sum, result[2 nvec + k] =
+// dangling sum; the last CTA writes coef_out[k] and sets *done when every
+// column's change is < eps.
+cudaError_t csr_pagerank_batched_step(const CsrArgs& a, int n_row, int nvec, const double* X,
+                                      double* Y, const double* T, const PageRankArgs& p,
+                                      Ctl ctl, int grid, cudaStream_t s);
+
+// CTAs of the persistent PageRank kernels (resident capacity of the GPU).
+int csr_pagerank_grid(int items, int prec);
+int csr_pagerank_batched_grid(int prec);
+
+// ---- ELL (column-major device copy) -------------------------------------------
+cudaError_t ell_spmv(const void* vals, int prec, const int* cols, int ln_row, int max_col,
+                     int f_col, const double* x, double* y, cudaStream_t s);
+
+// ---- COO / SCOO (row-sorted device copy, reduce-by-key) ----------------------
+// y[row + row_off] += sum of vals * x[col + col_off] over entries of that row.
+cudaError_t coo_spmv(const void* vals, int prec, const int* rows, const int* cols, long nnz,
+                     int row_off, int col_off, const double* x, double* y, cudaStream_t s);
+
+// ---- DENSE (row-major GEMV, accumulating) -------------------------------------
+cudaError_t dense_gemv(const void* vals, int prec, int ln_row, int ln_col, const double* x,
+                       double* y, cudaStream_t s);
+
+// ---- vector / preparation kernels ---------------------------------------------
+cudaError_t vec_add(double* y, const double* x, long n, cudaStream_t s);  // y += x
+cudaError_t vec_fill(double* y, double v, long n, cudaStream_t s);
+// Column sums of a row-major n x ncol array (ncol <= 32) into out[ncol],
+// two passes in a fixed order (deterministic); `partials` holds
+// kSumBlocks * 32 doubles.
+constexpr int kSumBlocks = 512;
+cudaError_t mat_colsum(const double* x, long n, int ncol, double* partials, double* out,
+                       cudaStream_t s);
+// x[i*ncol + k] /= denom[k]
+cudaError_t mat_scale_cols(double* x, long n, int ncol, const double* denom, cudaStream_t s);
+// s[col - f_col] += value over all CSR entries (FP64 atomics).
+cudaError_t csr_col_sums(const double* vals, const int* rowptr, const int* colidx, int n_row,
+                         int f_col, double* s, cudaStream_t st);
+// value /= s[col - f_col] where that is > 0.
+cudaError_t csr_normalize_cols(double* vals, const int* rowptr, const int* colidx, int n_row,
+                               int f_col, const double* s, cudaStream_t st);
+// dangling[j] = (column j has no entry), j < n_col.
+cudaError_t csr_dangling(const int* rowptr, const int* colidx, int n_row, int n_col,
+                         unsigned char* dangling, cudaStream_t st);
+// Narrowing copy of FP64 values to the storage precision.
+cudaError_t convert_values(const double* src, void* dst, int prec, long n, cudaStream_t s);
+// Row-major -> column-major transpose of ELL arrays.
+cudaError_t ell_transpose(const double* vals_rm, const int* cols_rm, void* vals_cm, int prec,
+                          int* cols_cm, int ln_row, int max_col, cudaStream_t s);
+
+}  // namespace tbsla_gpu

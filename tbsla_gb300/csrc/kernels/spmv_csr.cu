@@ -1,0 +1,423 @@
+// CSR SpMV, row-block adaptive (the CSR-Stream / CSR-Vector scheme of
+// Greathouse & Daga, SC'14, built here for sm_103a), and the PageRank steps
+// that reuse its traversal with a fused epilogue.
+//
+// Replaces tbsla::cpp::MatrixCSR::Ax (src/cpp/matrix/MatrixCSR.cpp:209-233):
+// y_i = sum_j values_j * v[colidx_j - f_col], overwriting y.
+//
+// Layout: the reference CSR arrays as they are (int32 rowptr / colidx, values
+// in the storage precision) plus a row-block partition built once per
+// matrix (csr_partition).  A block is either
+//  - a run of <= 256 consecutive rows holding <= 256*ITEMS entries
+//    ("stream" block): the CTA reads the block's entries with coalesced
+//    loads, multiplies by the gathered x, stages the products in shared
+//    memory, then sums each row with a group of G lanes, G = the largest
+//    power of two with G * rows <= 256 (capped at 32).  With G == 1 a row is
+//    summed by one thread from 0 in entry order, with every product rounded
+//    before the add: the reference loop's rounding, bit for bit;
+//  - one row longer than 256*ITEMS ("vector" block): the whole CTA strides
+//    over it and reduces.
+// Matrix values, indices and row pointers are read once, through the
+// non-allocating read-only path with an L2 evict-first policy; x is gathered
+// through L1 so that it owns L2.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.hpp"
+
+namespace tbsla_gpu {
+
+namespace {
+
+constexpr int NT = 256;
+
+template <class V>
+__device__ __forceinline__ double row_dot_cta(const V* vals, const int* colidx, int s, int e,
+                                              const double* x, int f_col, uint64_t pol) {
+  double acc = 0;
+  int j = s + (int)threadIdx.x;
+  for (; j + 3 * NT < e; j += 4 * NT) {
+    int c0 = ld_stream(colidx + j, pol), c1 = ld_stream(colidx + j + NT, pol);
+    int c2 = ld_stream(colidx + j + 2 * NT, pol), c3 = ld_stream(colidx + j + 3 * NT, pol);
+    double v0 = widen(ld_stream(vals + j, pol)), v1 = widen(ld_stream(vals + j + NT, pol));
+    double v2 = widen(ld_stream(vals + j + 2 * NT, pol)), v3 = widen(ld_stream(vals + j + 3 * NT, pol));
+    double x0 = ld_gather(x + c0 - f_col), x1 = ld_gather(x + c1 - f_col);
+    double x2 = ld_gather(x + c2 - f_col), x3 = ld_gather(x + c3 - f_col);
+    acc = add_rn(acc, mul_rn(v0, x0));
+    acc = add_rn(acc, mul_rn(v1, x1));
+    acc = add_rn(acc, mul_rn(v2, x2));
+    acc = add_rn(acc, mul_rn(v3, x3));
+  }
+  for (; j < e; j += NT) acc = add_rn(acc, mul_rn(widen(ld_stream(vals + j, pol)), ld_gather(x + ld_stream(colidx + j, pol) - f_col)));
+  return acc;
+}
+
+struct Smem {
+  int rp[NT + 1];
+  double red[NT / kWarp];
+  int blk;
+  int flag;
+};
+
+// One block of the partition; epi.emit(row, sum, red) per row.
+template <class V, int ITEMS, class Epi>
+__device__ __forceinline__ void csr_block(const CsrArgs& a, int b, const double* x, const Epi& epi,
+                                          double* red, double* s_prod, Smem& sm, uint64_t pol) {
+  const V* vals = static_cast<const V*>(a.vals);
+  const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
+  const int nrows = r1 - r0;
+  const int tid = threadIdx.x;
+  if (nrows == 1) {
+    const int s = a.rowptr[r0], e = a.rowptr[r0 + 1];
+    double acc = row_dot_cta(vals, a.colidx, s, e, x, a.f_col, pol);
+    acc = block_sum<NT>(acc, sm.red);
+    if (tid == 0) epi.emit(r0, acc, red);
+    return;
+  }
+  for (int i = tid; i <= nrows; i += NT) sm.rp[i] = ld_stream(a.rowptr + r0 + i, pol);
+  __syncthreads();
+  const int s = sm.rp[0];
+  const int cnt = sm.rp[nrows] - s;
+  int cidx[ITEMS];
+  V vv[ITEMS];
+#pragma unroll
+  for (int k = 0; k < ITEMS; k++) {
+    const int i = k * NT + tid;
+    if (i < cnt) {
+      cidx[k] = ld_stream(a.colidx + s + i, pol);
+      vv[k] = ld_stream(vals + s + i, pol);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < ITEMS; k++) {
+    const int i = k * NT + tid;
+    if (i < cnt) s_prod[i] = mul_rn(widen(vv[k]), ld_gather(x + cidx[k] - a.f_col));
+  }
+  __syncthreads();
+  const int G = nrows <= 8 ? 32 : nrows <= 16 ? 16 : nrows <= 32 ? 8 : nrows <= 64 ? 4 : nrows <= 128 ? 2 : 1;
+  const int g = tid / G, lane = tid % G;
+  double acc = 0;
+  if (g < nrows) {
+    const int lo = sm.rp[g] - s, hi = sm.rp[g + 1] - s;
+    for (int j = lo + lane; j < hi; j += G) acc = add_rn(acc, s_prod[j]);
+  }
+  for (int o = G >> 1; o > 0; o >>= 1) acc = add_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+  if (g < nrows && lane == 0) epi.emit(r0 + g, acc, red);
+  __syncthreads();  // s_prod / rp reused by the next block
+}
+
+struct EpiStore {
+  static constexpr int kRed = 0;
+  double* y;
+  __device__ __forceinline__ void emit(int row, double s, double*) const { y[row] = s; }
+};
+
+template <class V, int ITEMS>
+__global__ void __launch_bounds__(NT) k_csr_spmv(CsrArgs a, const double* __restrict__ x,
+                                                double* __restrict__ y) {
+  __shared__ double s_prod[NT * ITEMS];
+  __shared__ Smem sm;
+  const uint64_t pol = policy_evict_first();
+  EpiStore epi{y};
+  csr_block<V, ITEMS>(a, blockIdx.x, x, epi, nullptr, s_prod, sm, pol);
+}
+
+// ---- persistent variant with reductions --------------------------------------
+
+__device__ __forceinline__ int next_block(Ctl ctl, Smem& sm) {
+  __syncthreads();
+  if (threadIdx.x == 0) sm.blk = (int)atomicAdd(ctl.counter, 1u);
+  __syncthreads();
+  return sm.blk;
+}
+
+// Per-CTA partials, then the last CTA to finish sums them in CTA order
+// (deterministic), calls epi.finalize(result) and resets the counters.
+template <int NRED, class Fin>
+__device__ __forceinline__ void reduce_and_finish(Ctl ctl, double* red, Smem& sm, Fin fin) {
+  for (int k = 0; k < NRED; k++) {
+    double v = block_sum<NT>(red[k], sm.red);
+    if (threadIdx.x == 0) ctl.partials[(size_t)blockIdx.x * NRED + k] = v;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = atomicAdd(ctl.counter + 1, 1u);
+    sm.flag = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!sm.flag) return;
+  __threadfence();
+  for (int k = 0; k < NRED; k++) {
+    double acc = 0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += NT)
+      acc = add_rn(acc, __ldcg(ctl.partials + (size_t)i * NRED + k));
+    acc = block_sum<NT>(acc, sm.red);
+    if (threadIdx.x == 0) ctl.result[k] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fin(ctl.result);
+    ctl.counter[0] = 0;
+    ctl.counter[1] = 0;
+    __threadfence();
+  }
+}
+
+struct EpiPageRank {
+  static constexpr int kRed = 3;
+  double* y;
+  const double* x;
+  const unsigned char* dangling;
+  const double* tele;
+  double beta, coef, coef_u;
+  __device__ __forceinline__ void emit(int row, double s, double* red) const {
+    const double t = tele ? mul_rn(coef, tele[row]) : coef_u;
+    const double yn = add_rn(mul_rn(beta, s), t);
+    red[0] = add_rn(red[0], fabs(yn - x[row]));
+    red[1] = add_rn(red[1], yn);
+    if (dangling[row]) red[2] = add_rn(red[2], yn);
+    y[row] = yn;
+  }
+};
+
+template <class V, int ITEMS>
+__global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __restrict__ x,
+                                                    double* __restrict__ y, PageRankArgs p,
+                                                    Ctl ctl) {
+  __shared__ double s_prod[NT * ITEMS];
+  __shared__ Smem sm;
+  if (*(volatile int*)p.done) return;  // converged in an earlier launch: no-op
+  const uint64_t pol = policy_evict_first();
+  const double coef = p.coef_in[0];
+  EpiPageRank epi{y, x, p.dangling, p.tele, p.beta, coef, coef / p.n_nodes};
+  double red[3] = {0, 0, 0};
+  for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm))
+    csr_block<V, ITEMS>(a, b, x, epi, red, s_prod, sm, pol);
+  const double beta = p.beta, eps = p.eps;
+  double* coef_out = p.coef_out;
+  int* done = p.done;
+  int* iters = p.iters;
+  reduce_and_finish<3>(ctl, red, sm, [=] __device__(double* r) {
+    coef_out[0] = add_rn(mul_rn(beta, r[2]), mul_rn(1.0 - beta, r[1]));
+    *iters += 1;
+    if (r[0] < eps) *done = 1;
+  });
+}
+
+// Batched personalised PageRank: lanes of a warp are the nvec vectors; the
+// warps of the CTA take the rows of a block in turn.  Each lane sums its
+// row's products in entry order.
+template <class V>
+__global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec,
+                                                            const double* __restrict__ X,
+                                                            double* __restrict__ Y,
+                                                            const double* __restrict__ T,
+                                                            PageRankArgs p, Ctl ctl) {
+  __shared__ Smem sm;
+  __shared__ double s_red[NT / kWarp][3 * kWarp];
+  if (*(volatile int*)p.done) return;
+  const uint64_t pol = policy_evict_first();
+  const V* vals = static_cast<const V*>(a.vals);
+  const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  const bool active = lane < nvec;
+  const double coef = active ? p.coef_in[lane] : 0.0;
+  double err = 0, sum = 0, dsum = 0;
+  for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm)) {
+    const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
+    for (int row = r0 + warp; row < r1; row += NT / kWarp) {
+      const int s = a.rowptr[row], e = a.rowptr[row + 1];
+      double acc = 0;
+      for (int base = s; base < e; base += kWarp) {
+        const int j = base + lane;
+        int c = 0;
+        double v = 0;
+        if (j < e) {
+          c = ld_stream(a.colidx + j, pol);
+          v = widen(ld_stream(vals + j, pol));
+        }
+        const int m = min(kWarp, e - base);
+        for (int t = 0; t < m; t++) {
+          const int ct = __shfl_sync(0xffffffffu, c, t);
+          const double vt = __shfl_sync(0xffffffffu, v, t);
+          if (active) acc = add_rn(acc, mul_rn(vt, ld_gather(X + (size_t)(ct - a.f_col) * nvec + lane)));
+        }
+      }
+      if (active) {
+        const size_t o = (size_t)row * nvec + lane;
+        const double yn = add_rn(mul_rn(p.beta, acc), mul_rn(coef, T[o]));
+        err = add_rn(err, fabs(yn - X[o]));
+        sum = add_rn(sum, yn);
+        if (p.dangling[row]) dsum = add_rn(dsum, yn);
+        Y[o] = yn;
+      }
+    }
+  }
+  // per-column CTA sums over warps, in warp order
+  s_red[warp][lane] = err;
+  s_red[warp][kWarp + lane] = sum;
+  s_red[warp][2 * kWarp + lane] = dsum;
+  __syncthreads();
+  if (threadIdx.x < 3 * kWarp) {
+    double acc = 0;
+    for (int w = 0; w < NT / kWarp; w++) acc = add_rn(acc, s_red[w][threadIdx.x]);
+    ctl.partials[(size_t)blockIdx.x * 3 * kWarp + threadIdx.x] = acc;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = atomicAdd(ctl.counter + 1, 1u);
+    sm.flag = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!sm.flag) return;
+  __threadfence();
+  if (threadIdx.x < 3 * kWarp) {
+    double acc = 0;
+#pragma unroll 8
+    for (int i = 0; i < (int)gridDim.x; i++)
+      acc = add_rn(acc, __ldcg(ctl.partials + (size_t)i * 3 * kWarp + threadIdx.x));
+    s_red[0][threadIdx.x] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int all = 1;
+    for (int k = 0; k < nvec; k++) {
+      const double e = s_red[0][k], sm_ = s_red[0][kWarp + k], d = s_red[0][2 * kWarp + k];
+      ctl.result[k] = e;
+      ctl.result[nvec + k] = sm_;
+      ctl.result[2 * nvec + k] = d;
+      p.coef_out[k] = add_rn(mul_rn(p.beta, d), mul_rn(1.0 - p.beta, sm_));
+      if (!(e < p.eps)) all = 0;
+    }
+    *p.iters += 1;
+    if (all) *p.done = 1;
+    ctl.counter[0] = 0;
+    ctl.counter[1] = 0;
+    __threadfence();
+  }
+}
+
+template <class V, int ITEMS>
+cudaError_t launch_spmv(const CsrArgs& a, const double* x, double* y, cudaStream_t s) {
+  k_csr_spmv<V, ITEMS><<<a.nblocks, NT, 0, s>>>(a, x, y);
+  return cudaGetLastError();
+}
+
+template <class V>
+cudaError_t spmv_items(const CsrArgs& a, const double* x, double* y, cudaStream_t s) {
+  switch (a.items) {
+    case 4: return launch_spmv<V, 4>(a, x, y, s);
+    case 8: return launch_spmv<V, 8>(a, x, y, s);
+    case 16: return launch_spmv<V, 16>(a, x, y, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+template <class V>
+cudaError_t pr_items(const CsrArgs& a, const double* x, double* y, const PageRankArgs& p, Ctl c,
+                     int grid, cudaStream_t s) {
+  switch (a.items) {
+    case 4: k_csr_pagerank<V, 4><<<grid, NT, 0, s>>>(a, x, y, p, c); break;
+    case 8: k_csr_pagerank<V, 8><<<grid, NT, 0, s>>>(a, x, y, p, c); break;
+    case 16: k_csr_pagerank<V, 16><<<grid, NT, 0, s>>>(a, x, y, p, c); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+void csr_partition(const int* rowptr, int n_row, int tile, int** out, int* nblocks) {
+  std::vector<int> b;
+  b.reserve((size_t)n_row / 64 + 16);
+  b.push_back(0);
+  int r = 0;
+  while (r < n_row) {
+    const long len = (long)rowptr[r + 1] - rowptr[r];
+    if (len > tile) {
+      r++;
+      b.push_back(r);
+      continue;
+    }
+    const int start = r;
+    const long base = rowptr[r];
+    while (r < n_row && r - start < NT && (long)rowptr[r + 1] - base <= tile) r++;
+    b.push_back(r);
+  }
+  *nblocks = (int)b.size() - 1;
+  *out = new int[b.size()];
+  std::copy(b.begin(), b.end(), *out);
+}
+
+namespace {
+template <class K>
+int resident_grid(K kernel) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, NT, 0);
+  return std::max(1, sms * std::max(1, per));
+}
+}  // namespace
+
+int csr_pagerank_grid(int items, int prec) {
+  switch (prec * 100 + items) {
+    case kF64 * 100 + 4: return resident_grid(k_csr_pagerank<double, 4>);
+    case kF64 * 100 + 8: return resident_grid(k_csr_pagerank<double, 8>);
+    case kF64 * 100 + 16: return resident_grid(k_csr_pagerank<double, 16>);
+    case kF32 * 100 + 4: return resident_grid(k_csr_pagerank<float, 4>);
+    case kF32 * 100 + 8: return resident_grid(k_csr_pagerank<float, 8>);
+    case kF32 * 100 + 16: return resident_grid(k_csr_pagerank<float, 16>);
+    case kBF16 * 100 + 4: return resident_grid(k_csr_pagerank<__nv_bfloat16, 4>);
+    case kBF16 * 100 + 8: return resident_grid(k_csr_pagerank<__nv_bfloat16, 8>);
+    case kBF16 * 100 + 16: return resident_grid(k_csr_pagerank<__nv_bfloat16, 16>);
+  }
+  return 152;
+}
+
+int csr_pagerank_batched_grid(int prec) {
+  switch (prec) {
+    case kF64: return resident_grid(k_csr_pagerank_batched<double>);
+    case kF32: return resident_grid(k_csr_pagerank_batched<float>);
+    case kBF16: return resident_grid(k_csr_pagerank_batched<__nv_bfloat16>);
+  }
+  return 152;
+}
+
+cudaError_t csr_spmv(const CsrArgs& a, const double* x, double* y, cudaStream_t s) {
+  if (a.nblocks == 0) return cudaSuccess;
+  switch (a.prec) {
+    case kF64: return spmv_items<double>(a, x, y, s);
+    case kF32: return spmv_items<float>(a, x, y, s);
+    case kBF16: return spmv_items<__nv_bfloat16>(a, x, y, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
+                              const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s) {
+  switch (a.prec) {
+    case kF64: return pr_items<double>(a, x, y, p, ctl, grid, s);
+    case kF32: return pr_items<float>(a, x, y, p, ctl, grid, s);
+    case kBF16: return pr_items<__nv_bfloat16>(a, x, y, p, ctl, grid, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t csr_pagerank_batched_step(const CsrArgs& a, int n_row, int nvec, const double* X,
+                                      double* Y, const double* T, const PageRankArgs& p,
+                                      Ctl ctl, int grid, cudaStream_t s) {
+  (void)n_row;
+  if (nvec < 1 || nvec > kWarp) return cudaErrorInvalidValue;
+  switch (a.prec) {
+    case kF64: k_csr_pagerank_batched<double><<<grid, NT, 0, s>>>(a, nvec, X, Y, T, p, ctl); break;
+    case kF32: k_csr_pagerank_batched<float><<<grid, NT, 0, s>>>(a, nvec, X, Y, T, p, ctl); break;
+    case kBF16: k_csr_pagerank_batched<__nv_bfloat16><<<grid, NT, 0, s>>>(a, nvec, X, Y, T, p, ctl); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tbsla_gpu

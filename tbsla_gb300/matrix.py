@@ -1,0 +1,344 @@
+"""Python mirror of the reference's ``tbsla::cpp::Matrix`` classes
+(src/cpp/include/tbsla/cpp/Matrix.hpp:11-57 and the five format classes) over
+the C ABI.  Method names, argument meaning and defaults follow the reference
+so that code written against the reference reads the same here:
+
+    m = MatrixCSR(); m.fill_cqmat(nr, nc, c, q, s)
+    r = m.spmv(v)                 # new array, zero-filled then Ax
+    m.Ax(r, v)                    # CSR/ELL overwrite r, COO/SCOO/DENSE add to r
+
+Vectors are float64 numpy arrays (host; copied to and from the GPU per
+call) or CUDA tensors (``Ax_device``; no copies, no synchronisation).  Every
+failure raises TbslaError carrying the C status code; there is no CPU
+fallback for any compute call.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import Info, TbslaError, check, lib
+
+
+def _ptr(a: np.ndarray):
+    return C.c_void_p(a.ctypes.data) if a is not None and a.size else None
+
+
+def _f64(a, name="vector") -> np.ndarray:
+    if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous:
+        raise TypeError(f"{name} must be a C-contiguous float64 numpy array")
+    return a
+
+
+class Matrix:
+    """Base of the five formats; owns one tbsla_matrix handle."""
+
+    FORMAT = -1
+
+    def __init__(self, coo: "MatrixCOO | None" = None, _handle=None):
+        h = C.c_void_p()
+        if _handle is not None:
+            h = _handle
+        elif coo is not None:
+            if not isinstance(coo, MatrixCOO):
+                raise TypeError("conversion constructors take a MatrixCOO")
+            check(lib.tbsla_matrix_convert(C.byref(h), coo._h, self.FORMAT), "convert")
+        else:
+            check(lib.tbsla_matrix_create(C.byref(h), self.FORMAT), "create")
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib.tbsla_matrix_destroy(h)
+            self._h = C.c_void_p()
+
+    # ---- metadata (Matrix.hpp:21-32) ----------------------------------------
+    def info(self) -> dict:
+        i = Info()
+        check(lib.tbsla_matrix_info(self._h, C.byref(i)))
+        return i.as_dict()
+
+    def get_n_row(self): return self.info()["n_row"]
+    def get_n_col(self): return self.info()["n_col"]
+    def get_f_row(self): return self.info()["f_row"]
+    def get_f_col(self): return self.info()["f_col"]
+    def get_ln_row(self): return self.info()["ln_row"]
+    def get_ln_col(self): return self.info()["ln_col"]
+    def get_pr(self): return self.info()["pr"]
+    def get_pc(self): return self.info()["pc"]
+    def get_NR(self): return self.info()["NR"]
+    def get_NC(self): return self.info()["NC"]
+    def get_nnz(self): return self.info()["nnz"]
+    def get_vectorization(self): return "CUDA sm_103a"
+
+    def _out_len(self):
+        i = self.info()
+        return i["n_row"] if self.FORMAT == L.COO else i["ln_row"]
+
+    def _in_len(self):
+        i = self.info()
+        return i["n_col"] if self.FORMAT == L.COO else i["ln_col"]
+
+    # ---- generators (Matrix.hpp:40-42) ------------------------------------------
+    def fill_cdiag(self, n_row, n_col, cdiag, pr=0, pc=0, NR=1, NC=1):
+        check(lib.tbsla_matrix_fill_cdiag(self._h, n_row, n_col, cdiag, pr, pc, NR, NC), "fill_cdiag")
+
+    def fill_cqmat(self, n_row, n_col, c, q, seed_mult=1, pr=0, pc=0, NR=1, NC=1):
+        check(lib.tbsla_matrix_fill_cqmat(self._h, n_row, n_col, c, float(q), seed_mult, pr, pc, NR, NC),
+              "fill_cqmat")
+
+    def fill_random(self, n_row, n_col, nnz_ratio, seed_mult=1, pr=0, pc=0, NR=1, NC=1):
+        check(lib.tbsla_matrix_fill_random(self._h, n_row, n_col, float(nnz_ratio), seed_mult, pr, pc,
+                                           NR, NC), "fill_random")
+
+    # ---- binary I/O (write / read) --------------------------------------------------
+    def write(self, path: str, append: bool = False):
+        check(lib.tbsla_matrix_write(self._h, str(path).encode(), int(append)), "write")
+
+    def read(self, path: str, pos: int = 0):
+        check(lib.tbsla_matrix_read(self._h, str(path).encode(), pos), "read")
+
+    # ---- device copy ------------------------------------------------------------------
+    def set_precision(self, prec: int):
+        check(lib.tbsla_matrix_set_precision(self._h, prec), "set_precision")
+
+    def upload(self):
+        check(lib.tbsla_matrix_upload(self._h), "upload")
+
+    def device_bytes(self) -> int:
+        b = C.c_size_t()
+        check(lib.tbsla_matrix_device_bytes(self._h, C.byref(b)), "device_bytes")
+        return b.value
+
+    # ---- SpMV (Matrix.hpp:14-15) --------------------------------------------------------
+    def Ax(self, r: np.ndarray, v: np.ndarray, vect_incr: int = 0):
+        _f64(r, "r"), _f64(v, "v")
+        if r.size < self._out_len() or v.size < self._in_len():
+            raise ValueError("vector too short for the matrix")
+        check(lib.tbsla_Ax(self._h, _ptr(r), _ptr(v), vect_incr), "Ax")
+
+    def spmv(self, v: np.ndarray, vect_incr: int = 0) -> np.ndarray:
+        _f64(v, "v")
+        if v.size < self._in_len():
+            raise ValueError("vector too short for the matrix")
+        r = np.empty(max(self._out_len(), 1))
+        check(lib.tbsla_spmv(self._h, _ptr(r), _ptr(v), vect_incr), "spmv")
+        return r[: self._out_len()]
+
+    def Ax_device(self, r, v, vect_incr: int = 0, stream=None):
+        """r, v: float64 CUDA tensors (device pointers); stream: a torch
+        stream or raw handle, None = the matrix's own stream."""
+        s = None if stream is None else C.c_void_p(getattr(stream, "cuda_stream", stream))
+        check(lib.tbsla_Ax_device(self._h, C.c_void_p(r.data_ptr()), C.c_void_p(v.data_ptr()),
+                                  vect_incr, s), "Ax_device")
+
+    def spmv_device(self, r, v, vect_incr: int = 0, stream=None):
+        s = None if stream is None else C.c_void_p(getattr(stream, "cuda_stream", stream))
+        check(lib.tbsla_spmv_device(self._h, C.c_void_p(r.data_ptr()), C.c_void_p(v.data_ptr()),
+                                    vect_incr, s), "spmv_device")
+
+    # ---- composite ops (Matrix.cpp:5-31) -------------------------------------------------
+    def a_axpx_(self, v: np.ndarray, vect_incr: int = 0) -> np.ndarray:
+        _f64(v, "v")
+        r = np.empty(self._out_len())
+        check(lib.tbsla_a_axpx_(self._h, _ptr(r), _ptr(v), vect_incr), "a_axpx_")
+        return r
+
+    def AAxpAx(self, r, v, buffer, vect_incr: int = 0):
+        check(lib.tbsla_AAxpAx(self._h, _ptr(_f64(r)), _ptr(_f64(v)), _ptr(_f64(buffer)), vect_incr),
+              "AAxpAx")
+
+    def AAxpAxpx(self, r, v, buffer, vect_incr: int = 0):
+        check(lib.tbsla_AAxpAxpx(self._h, _ptr(_f64(r)), _ptr(_f64(v)), _ptr(_f64(buffer)), vect_incr),
+              "AAxpAxpx")
+
+    # ---- column-stochastic preparation -----------------------------------------------------
+    def get_col_sums(self, s: np.ndarray):
+        check(lib.tbsla_get_col_sums(self._h, _ptr(_f64(s, "s"))), "get_col_sums")
+
+    def normalize_cols(self, s: np.ndarray):
+        check(lib.tbsla_normalize_cols(self._h, _ptr(_f64(s, "s"))), "normalize_cols")
+
+    def make_stochastic(self, s: np.ndarray):
+        check(lib.tbsla_make_stochastic(self._h, _ptr(_f64(s, "s"))), "make_stochastic")
+
+    # ---- host arrays (numpy copies of the reference-layout arrays) --------------------------
+    def arrays(self) -> dict:
+        i = self.info()
+        v, a, b = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        check(lib.tbsla_matrix_arrays(self._h, C.byref(v), C.byref(a), C.byref(b)))
+
+        def grab(p, n, ct, dt):
+            if n <= 0 or not p.value:
+                return np.zeros(0, dtype=dt)
+            return np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), shape=(n,)).copy()
+
+        f = self.FORMAT
+        nnz = i["nnz"]
+        if f in (L.COO, L.SCOO):
+            return {"values": grab(v, nnz, C.c_double, np.float64),
+                    "row": grab(a, nnz, C.c_int, np.int32), "col": grab(b, nnz, C.c_int, np.int32)}
+        if f == L.CSR:
+            rp = grab(a, i["ln_row"] + 1 if a.value else 0, C.c_int, np.int32)
+            return {"values": grab(v, nnz, C.c_double, np.float64), "rowptr": rp,
+                    "colidx": grab(b, nnz, C.c_int, np.int32)}
+        if f == L.ELL:
+            n = i["ln_row"] * i["max_col"]
+            return {"values": grab(v, n, C.c_double, np.float64), "columns": grab(a, n, C.c_int, np.int32)}
+        n = i["ln_row"] * i["ln_col"]
+        return {"values": grab(v, n, C.c_double, np.float64)}
+
+
+def _info(**kw) -> Info:
+    i = Info()
+    i.NR = i.NC = 1
+    for k, val in kw.items():
+        setattr(i, k, val)
+    return i
+
+
+class MatrixCOO(Matrix):
+    FORMAT = L.COO
+
+    @classmethod
+    def from_arrays(cls, n_row, n_col, row, col, values, fmt=None):
+        m = cls()
+        row = np.ascontiguousarray(row, np.int32)
+        col = np.ascontiguousarray(col, np.int32)
+        values = np.ascontiguousarray(values, np.float64)
+        i = _info(n_row=n_row, n_col=n_col, ln_row=n_row, ln_col=n_col, nnz=len(values))
+        check(lib.tbsla_matrix_set_coo(m._h, C.byref(i), _ptr(values), _ptr(row), _ptr(col)), "set_coo")
+        return m
+
+
+class MatrixSCOO(Matrix):
+    FORMAT = L.SCOO
+
+    @classmethod
+    def from_arrays(cls, info: dict, row, col, values):
+        m = cls()
+        row = np.ascontiguousarray(row, np.int32)
+        col = np.ascontiguousarray(col, np.int32)
+        values = np.ascontiguousarray(values, np.float64)
+        i = _info(**info)
+        check(lib.tbsla_matrix_set_coo(m._h, C.byref(i), _ptr(values), _ptr(row), _ptr(col)), "set_coo")
+        return m
+
+
+class MatrixCSR(Matrix):
+    FORMAT = L.CSR
+
+    @classmethod
+    def from_arrays(cls, n_row, n_col, rowptr, colidx, values, **info):
+        m = cls()
+        rowptr = np.ascontiguousarray(rowptr, np.int32)
+        colidx = np.ascontiguousarray(colidx, np.int32)
+        values = np.ascontiguousarray(values, np.float64)
+        kw = dict(n_row=n_row, n_col=n_col, ln_row=n_row, ln_col=n_col, nnz=len(values))
+        kw.update(info)
+        i = _info(**kw)
+        check(lib.tbsla_matrix_set_csr(m._h, C.byref(i), _ptr(values), _ptr(rowptr), _ptr(colidx)),
+              "set_csr")
+        return m
+
+    def set_tile(self, nnz_per_block: int):
+        check(lib.tbsla_matrix_set_csr_tile(self._h, nnz_per_block), "set_csr_tile")
+
+    # project generators
+    def fill_uniform_rows(self, n, k, seed):
+        check(lib.tbsla_matrix_fill_uniform_rows(self._h, n, k, seed), "fill_uniform_rows")
+
+    def fill_powerlaw(self, n, mean_len=16.0, zipf_s=2.0, max_len=4096, local_frac=0.3, band=1024,
+                      seed=1):
+        check(lib.tbsla_matrix_fill_powerlaw(self._h, n, mean_len, zipf_s, max_len, local_frac, band,
+                                             seed), "fill_powerlaw")
+
+    def fill_pa_graph(self, n, mean_deg=16.0, zipf_s=2.1, max_deg=4096, dangling_frac=0.05, seed=2):
+        check(lib.tbsla_matrix_fill_pa_graph(self._h, n, mean_deg, zipf_s, max_deg, dangling_frac, seed),
+              "fill_pa_graph")
+
+    def fill_diffusion7(self, n, sigma=1.0, corr_len=8.0, seed=3):
+        check(lib.tbsla_matrix_fill_diffusion7(self._h, n, sigma, corr_len, seed), "fill_diffusion7")
+
+    # PageRank / CG
+    def page_rank(self, beta=0.85, epsilon=1e-10, max_iterations=1000):
+        n = self.get_n_row()
+        x = np.empty(n)
+        it = C.c_int()
+        err = C.c_double()
+        st = lib.tbsla_page_rank(self._h, beta, epsilon, max_iterations, _ptr(x), C.byref(it), C.byref(err))
+        if st not in (L.OK, L.ERR_NOT_CONVERGED):
+            check(st, "page_rank")
+        return x, it.value, err.value, st == L.OK
+
+    def page_rank_batched(self, teleport: np.ndarray, beta=0.85, epsilon=1e-10, max_iterations=1000):
+        n, nvec = teleport.shape
+        t = np.ascontiguousarray(teleport, np.float64)
+        x = np.empty((n, nvec))
+        it = C.c_int()
+        st = lib.tbsla_page_rank_batched(self._h, nvec, _ptr(t), beta, epsilon, max_iterations, _ptr(x),
+                                         C.byref(it))
+        if st not in (L.OK, L.ERR_NOT_CONVERGED):
+            check(st, "page_rank_batched")
+        return x, it.value, st == L.OK
+
+    def CG(self, b: np.ndarray, x: np.ndarray | None = None, max_iterations=10000, rel_tol=1e-8,
+           precond=0, refresh=50):
+        b = _f64(b, "b")
+        x = np.zeros_like(b) if x is None else _f64(x, "x")
+        it = C.c_int()
+        rr = C.c_double()
+        st = lib.tbsla_cg(self._h, _ptr(b), _ptr(x), max_iterations, rel_tol, precond, refresh,
+                          C.byref(it), C.byref(rr))
+        if st not in (L.OK, L.ERR_NOT_CONVERGED):
+            check(st, "cg")
+        return x, it.value, rr.value, st == L.OK
+
+
+class MatrixELL(Matrix):
+    FORMAT = L.ELL
+
+    @classmethod
+    def from_arrays(cls, info: dict, columns, values):
+        m = cls()
+        columns = np.ascontiguousarray(columns, np.int32)
+        values = np.ascontiguousarray(values, np.float64)
+        i = _info(**info)
+        check(lib.tbsla_matrix_set_ell(m._h, C.byref(i), _ptr(values), _ptr(columns)), "set_ell")
+        return m
+
+
+class MatrixDENSE(Matrix):
+    FORMAT = L.DENSE
+
+    @classmethod
+    def from_arrays(cls, n_row, n_col, values):
+        m = cls()
+        values = np.ascontiguousarray(values, np.float64).reshape(-1)
+        i = _info(n_row=n_row, n_col=n_col, ln_row=n_row, ln_col=n_col, nnz=n_row * n_col)
+        check(lib.tbsla_matrix_set_dense(m._h, C.byref(i), _ptr(values)), "set_dense")
+        return m
+
+    def fill_dense_uniform(self, n_row, n_col, seed):
+        check(lib.tbsla_matrix_fill_dense_uniform(self._h, n_row, n_col, seed), "fill_dense_uniform")
+
+
+FORMATS = {L.COO: MatrixCOO, L.SCOO: MatrixSCOO, L.CSR: MatrixCSR, L.ELL: MatrixELL,
+           L.DENSE: MatrixDENSE}
+
+
+def fill_uniform(n: int, lo: float, hi: float, seed: int, out: np.ndarray | None = None) -> np.ndarray:
+    out = np.empty(n) if out is None else _f64(out, "out")
+    check(lib.tbsla_fill_uniform(_ptr(out), n, lo, hi, seed), "fill_uniform")
+    return out
+
+
+def device_init(device: int = 0):
+    check(lib.tbsla_device_init(device), "device_init")
+
+
+__all__ = ["Matrix", "MatrixCOO", "MatrixSCOO", "MatrixCSR", "MatrixELL", "MatrixDENSE", "FORMATS",
+           "fill_uniform", "device_init", "TbslaError"]
