@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of the TBSLA SpMV hot path on GB300.
+
+Workload (the large-SpMV configuration): square CSR matrix, n = 16,777,216
+rows, row lengths Zipf(2) on [1, 4096] rescaled to mean 16 (~268M entries),
+70% of the columns uniform over [0, n) and 30% within +-1024 of the diagonal,
+values U[-1,1) stored in FP64 (--prec selects FP32 / BF16 storage), x U[0,1),
+seed 1.  One step = one y = A x (tbsla::cpp::MatrixCSR::Ax).
+
+Metric: SpMV HBM GB/s of algorithmic bytes per step
+  B = nnz*(s_v + 4) + 4*(n+1) + 8*n (x, counted once) + 8*n (y)
+divided by the step's device time (CUDA events on the launching stream, L2
+flushed between steps).  `e2e` is the same metric through the C ABI's host
+entry point tbsla_Ax with pinned host x / y: the host->device copy of x and
+the device->host copy of y are inside the timed region.  The CPU baseline is
+the reference's CSR Ax loop (the reference core compiled from its sources
+where available, else the oracle's restatement of it) on all host cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (torchrun) every rank runs an independent replica (the path has
+no exchange step on one GPU); the value is the sum of bytes over the max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SpMV HBM GB/s (% peak); CG time-to-1e-8 residual: learned vs Jacobi PCG, 1 GB300"
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "csr_spmv_powerlaw_n16M_fp64.md")
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--n", type=int, default=1 << 24)
+    p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
+    p.add_argument("--tile", type=int, default=2048)
+    p.add_argument("--no-forms", action="store_true", help="skip the FP32 / BF16 side measurements")
+    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    a = p.parse_args()
+    a.warmup = max(a.warmup, 3)
+    return a
+
+
+def algorithmic_bytes(n: int, nnz: int, s_v: int) -> int:
+    return nnz * (s_v + 4) + 4 * (n + 1) + 8 * n + 8 * n
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per launch from the committed ncu summary, if present."""
+    try:
+        for line in open(PROFILE_SUMMARY):
+            if line.startswith("dram_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1].strip().split()[0]))
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [t.strip() for t in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_reference_time(arrays, x, n, nnz, seconds: float, reps_min: int = 2, reps_max: int = 50):
+    """Times the reference's CSR Ax loop on all host cores: the reference core
+    compiled from its own sources when it is available here, otherwise the
+    oracle's restatement of that loop (same loop, same OpenMP schedule)."""
+    import ctypes as C
+
+    import numpy as np
+
+    import oracle
+
+    rp, ci, va = arrays["rowptr"], arrays["colidx"], arrays["values"]
+    y = np.zeros(n)
+    kind = "port"
+    run = None
+    R = oracle.ref() if os.path.exists(oracle._build.REF_SO) else None
+    if R is not None:
+        try:
+            h = C.c_void_p(R.ref_new(2))
+            meta = np.array([n, n, n, n, 0, 0, 0, 0, 1, 1, 0], np.int32)
+            R.ref_adopt(h, C.c_void_p(meta.ctypes.data), C.c_long(nnz), C.c_void_p(va.ctypes.data),
+                        C.c_void_p(rp.ctypes.data), C.c_void_p(ci.ctypes.data))
+            kind = "reference"
+
+            def run():
+                R.ref_Ax(h, C.c_void_p(y.ctypes.data), C.c_void_p(x.ctypes.data), 0)
+        except OSError:
+            R = None
+    if run is None:
+        def run():
+            oracle.csr_ax(rp, ci, va, x, y, threads=True)
+    run()  # warm-up (first touch)
+    times = []
+    t_end = time.perf_counter() + seconds
+    while (len(times) < reps_min or time.perf_counter() < t_end) and len(times) < reps_max:
+        t0 = time.perf_counter()
+        run()
+        times.append(time.perf_counter() - t0)
+    return kind, times, y
+
+
+def run_ours(a):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import tbsla_gb300 as T
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    T.device_init(local)
+    if ws > 1:
+        import torch.distributed as td
+
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    n = a.n
+    t0 = time.time()
+    m = T.MatrixCSR()
+    m.fill_powerlaw(n, 16.0, 2.0, 4096, 0.3, 1024, 1)
+    nnz = m.get_nnz()
+    t_gen = time.time() - t0
+    m.set_tile(a.tile)
+    prec = {"f64": T.F64, "f32": T.F32, "bf16": T.BF16}[a.prec]
+    s_v = {"f64": 8, "f32": 4, "bf16": 2}[a.prec]
+    m.set_precision(prec)
+    t0 = time.time()
+    m.upload()
+    t_up = time.time() - t0
+    x = T.fill_uniform(n, 0.0, 1.0, 1)
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.empty(n, dtype=torch.float64, device="cuda")
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")  # 256 MB > L2
+    s = torch.cuda.Stream()
+    B = algorithmic_bytes(n, nnz, s_v)
+
+    def timed_steps(mat, k):
+        evs = []
+        with torch.cuda.stream(s):
+            for _ in range(k):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                mat.Ax_device(yt, xt, stream=s)
+                e1.record(s)
+                evs.append((e0, e1))
+        s.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in evs]
+
+    timed_steps(m, a.warmup)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    clk.start()
+    step_ms = timed_steps(m, a.steps)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    if ws > 1:
+        torch.distributed.barrier()
+    total_ms = sum(step_ms)
+    if ws > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / a.steps
+    value = ws * B * a.steps / (total_ms * 1e-3) / 1e9
+    kernel_gbs = B / (statistics.mean(step_ms) * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    # end to end through the C ABI's host entry point, pinned host buffers
+    hx, hy = C.c_void_p(), C.c_void_p()
+    T.check(T.lib.tbsla_host_alloc(C.byref(hx), n * 8))
+    T.check(T.lib.tbsla_host_alloc(C.byref(hy), n * 8))
+    xh = np.ctypeslib.as_array(C.cast(hx, C.POINTER(C.c_double)), shape=(n,))
+    yh = np.ctypeslib.as_array(C.cast(hy, C.POINTER(C.c_double)), shape=(n,))
+    xh[:] = x
+    for _ in range(a.warmup):
+        m.Ax(yh, xh)
+    e2e = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        T.check(T.lib.tbsla_Ax(m._h, hy, hx, 0))
+        e2e.append(time.perf_counter() - t0)
+    e2e_val = B / statistics.mean(e2e) / 1e9
+    y_dev = yt.cpu().numpy()
+    assert np.array_equal(y_dev, yh), "device-pointer and host entry points disagree"
+
+    extra = {"gflops": 2 * nnz / (ms_step * 1e-3) / 1e9, "gen_s": round(t_gen, 2), "upload_s": round(t_up, 2),
+             "step_ms_min": min(step_ms), "step_ms_max": max(step_ms),
+             "device_bytes": m.device_bytes()}
+    if not a.no_forms and a.prec == "f64":
+        for name, pv, sv in (("f32", T.F32, 4), ("bf16", T.BF16, 2)):
+            m.set_precision(pv)
+            m.upload()
+            timed_steps(m, a.warmup)
+            ms = statistics.mean(timed_steps(m, a.steps))
+            extra[f"{name}_values"] = {"ms_per_step": ms,
+                                       "GB/s": algorithmic_bytes(n, nnz, sv) / (ms * 1e-3) / 1e9,
+                                       "frac_of_peak": algorithmic_bytes(n, nnz, sv) / (ms * 1e-3) / 1e9 / peak}
+        m.set_precision(prec)
+
+    cpu = None
+    if rank == 0 and ws == 1:
+        arrays = m.arrays()
+        kind, times, y_cpu = cpu_reference_time(arrays, x, n, nnz, a.cpu_seconds)
+        import oracle
+
+        scale = oracle.csr_absrow(arrays["rowptr"], arrays["colidx"], arrays["values"], x)
+        if a.prec == "f64":
+            extra["max_err_vs_cpu_normalized"] = oracle.rel_err_normalized(y_dev, y_cpu, scale)
+        cpu = {"value": B / statistics.median(times) / 1e9, "unit": "GB/s", "cores": os.cpu_count(),
+               "kind": kind,
+               "sample": f"{len(times)} full Ax steps on the same matrix (median), OMP_NUM_THREADS="
+                         f"{os.environ.get('OMP_NUM_THREADS', 'all')}"}
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "GB/s",
+        "n_gpus": ws,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": a.prec,
+        "data": "synthetic: seeded generator (power-law rows, seed 1), no dataset",
+        "config": {"workload": f"csr_spmv_powerlaw_n{n}_mean16_zipf2_max4096_local30pct_{a.prec}",
+                   "format": "CSR", "n": n, "nnz": nnz, "value_dtype": a.prec, "x_y_dtype": "f64",
+                   "bytes_per_step": B, "block_budget_nnz": a.tile,
+                   "l2": "flushed (256 MB write) between steps; inputs 3.2+ GB > L2",
+                   "parallelism": f"replicas x{ws}"},
+        "roofline": {"bound": "hbm", "achieved": kernel_gbs, "peak": peak, "unit": "GB/s",
+                     "frac": kernel_gbs / peak, "peak_source": peak_kind, "traffic": profile_traffic(),
+                     "algorithmic_bytes": B},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
+                "ms_per_step": statistics.mean(e2e) * 1e3},
+        "gpu_launches": a.steps,
+        "clocks": clocks,
+        "extra": extra,
+    }
+    T.lib.tbsla_host_free(hx)
+    T.lib.tbsla_host_free(hy)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(a):
+    ws, rank, local = dist()
+    if rank != 0:
+        return
+    import numpy as np
+
+    import tbsla_gb300 as T
+
+    n = a.n
+    m = T.MatrixCSR()
+    m.fill_powerlaw(n, 16.0, 2.0, 4096, 0.3, 1024, 1)
+    nnz = m.get_nnz()
+    arrays = m.arrays()
+    del m
+    x = T.fill_uniform(n, 0.0, 1.0, 1)
+    B = algorithmic_bytes(n, nnz, 8)
+    kind, _, _ = cpu_reference_time(arrays, x, n, nnz, 0.0, reps_min=a.warmup, reps_max=a.warmup)
+    kind, times, _ = cpu_reference_time(arrays, x, n, nnz, 0.0, reps_min=a.steps, reps_max=a.steps)
+    sec = sum(times) / len(times)
+    val = B / sec / 1e9
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": val,
+        "unit": "GB/s",
+        "n_gpus": ws,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": sec * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic: seeded generator (power-law rows, seed 1), no dataset",
+        "config": {"workload": f"csr_spmv_powerlaw_n{n}_mean16_zipf2_max4096_local30pct_f64", "format": "CSR",
+                   "n": n, "nnz": nnz, "bytes_per_step": B, "parallelism": "host cores (OpenMP)"},
+        "cpu_baseline": {"value": val, "unit": "GB/s", "cores": os.cpu_count(), "kind": kind,
+                         "sample": f"{a.steps} full CSR Ax steps of the workload after {a.warmup} warm-up"},
+        "e2e": {"value": val, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)

@@ -117,7 +117,9 @@ int tbsla_matrix_fill_random(tbsla_matrix* m, int n_row, int n_col, double nnz_r
  *  - uniform_rows: square n x n; row i holds column i plus k-1 further
  *    distinct columns uniform in [0,n), sorted; values U[-1,1).
  *  - powerlaw: square n x n; row lengths Zipf(zipf_s) on [1,max_len]
- *    rescaled to mean `mean_len`, rounded, clipped to [1,max_len]; each
+ *    rescaled to mean `mean_len` (rounded stochastically, clipped to
+ *    [1,max_len], the scale chosen so that the expected length is exactly
+ *    mean_len); each
  *    column is uniform on [0,n) with probability 1-local_frac, else uniform
  *    within +-band of the diagonal; distinct and sorted per row; values
  *    U[-1,1).

@@ -552,6 +552,36 @@ struct Zipf {
   int draw(double u) const {
     return (int)(std::upper_bound(cdf.begin(), cdf.end(), u) - cdf.begin()) + 1;
   }
+  // Length of a draw k after rescaling: k * scale rounded stochastically
+  // (down, or up with probability equal to the fraction; u in [0,1) is the
+  // draw's own uniform), clipped to [lo, kmax].  Stochastic rounding keeps
+  // the expected length continuous in the scale, so the target mean is met
+  // exactly although 60% of the draws are k = 1.
+  static long rescale(int k, double scale, double u, long lo, long kmax) {
+    const double y = k * scale;
+    long r = (long)std::floor(y);
+    if (u < y - (double)r) r++;
+    return std::min<long>(std::max<long>(r, lo), kmax);
+  }
+  // Scale whose rescaled lengths have expectation `target` (bisection; the
+  // expectation sum_k p_k clamp(k*scale, lo, kmax) is monotone in the scale).
+  double scale_for(double target, long lo, long kmax) const {
+    auto mean_at = [&](double sc) {
+      double m = 0, prev = 0;
+      for (size_t k = 1; k <= cdf.size(); k++) {
+        m += (cdf[k - 1] - prev) * std::min<double>(std::max<double>(k * sc, (double)lo), (double)kmax);
+        prev = cdf[k - 1];
+      }
+      return m;
+    };
+    double a = 0, b = 2.0 * target / mean + 1.0;
+    while (mean_at(b) < target && b < 1e9) b *= 2;
+    for (int it = 0; it < 200; it++) {
+      double c = 0.5 * (a + b);
+      (mean_at(c) < target ? a : b) = c;
+    }
+    return b;
+  }
 };
 
 void finish_square_csr(tbsla_matrix* m, int n) {
@@ -603,14 +633,15 @@ int fill_powerlaw(tbsla_matrix* m, int n, double mean_len, double zipf_s, int ma
   if (n <= 0 || max_len <= 0 || max_len > n || band < 0) return TBSLA_ERR_INVALID_ARG;
   m->invalidate();
   Zipf z(zipf_s, max_len);
-  double scale = mean_len / z.mean;
+  // scale chosen so that the expected length after rounding and clipping is
+  // exactly mean_len
+  const double scale = z.scale_for(mean_len, 1, max_len);
   m->idx0.resize(n + 1);
   std::vector<int> len(n);
   parallel_for(n, [&](long b, long e) {
     for (long i = b; i < e; i++) {
       int k = z.draw(u01(hash3(seed, 1, (uint64_t)i)));
-      long l = std::lround(k * scale);
-      len[i] = (int)std::min<long>(std::max<long>(l, 1), max_len);
+      len[i] = (int)Zipf::rescale(k, scale, u01(hash3(seed, 12, (uint64_t)i)), 1, max_len);
     }
   });
   long acc = 0;
@@ -676,8 +707,9 @@ int fill_pa_graph(tbsla_matrix* m, int n, double mean_deg, double zipf_s, int ma
   if (n <= 1 || max_deg <= 0 || max_deg >= n) return TBSLA_ERR_INVALID_ARG;
   m->invalidate();
   Zipf z(zipf_s, max_deg);
-  // Rescale so that the mean over all nodes (dangling ones included) is mean_deg.
-  double scale = mean_deg / ((1.0 - dangling_frac) * z.mean);
+  // Rescale so that the expected out-degree over all nodes (dangling ones
+  // included) is mean_deg after rounding and clipping.
+  const double scale = z.scale_for(mean_deg / (1.0 - dangling_frac), 1, max_deg);
   std::vector<int> outdeg(n);
   parallel_for(n, [&](long b, long e) {
     for (long j = b; j < e; j++) {
@@ -686,8 +718,7 @@ int fill_pa_graph(tbsla_matrix* m, int n, double mean_deg, double zipf_s, int ma
         continue;
       }
       int k = z.draw(u01(hash3(seed, 7, (uint64_t)j)));
-      long d = std::lround(k * scale);
-      outdeg[j] = (int)std::min<long>(std::max<long>(d, 1), max_deg);
+      outdeg[j] = (int)Zipf::rescale(k, scale, u01(hash3(seed, 13, (uint64_t)j)), 1, max_deg);
     }
   });
   long E = 0;

@@ -1,0 +1,291 @@
+"""GPU parity of the SpMV path through the C ABI: every format against the
+golden vectors recorded from the reference and against the oracle on seeded
+inputs.
+
+Tolerance (FP64 forms): |y_gpu,i - y_ref,i| <= 1e-13 * sum_j |a_ij x_j| per
+entry (normalised by the absolute row sum so that cancellation cannot fail
+it).  Rows summed by one thread (CSR rows in blocks of > 128 rows, ELL rows)
+reproduce the reference's rounding and are additionally checked bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden_cases
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13
+
+
+def make(T, fmt, key, kind):
+    p = key.split("/")
+    m = T.FORMATS[fmt]()
+    if kind.startswith("cdiag"):
+        grid = tuple(int(t) for t in p[5].split("-")) if kind == "cdiag" else (0, 0, 1, 1)
+        src = m if kind == "cdiag" else T.MatrixCOO()
+        src.fill_cdiag(int(p[2]), int(p[3]), int(p[4]), *grid)
+    elif kind.startswith("cqmat"):
+        grid = tuple(int(t) for t in p[7].split("-")) if kind == "cqmat" else (0, 0, 1, 1)
+        src = m if kind == "cqmat" else T.MatrixCOO()
+        src.fill_cqmat(int(p[2]), int(p[3]), int(p[4]), float(p[5]), int(p[6]), *grid)
+    else:
+        grid = tuple(int(t) for t in p[6].split("-"))
+        src = m
+        src.fill_random(int(p[2]), int(p[3]), float(p[4]), int(p[5]), *grid)
+    if src is not m:
+        m = T.FORMATS[fmt](src)
+    return m
+
+
+@pytest.mark.parametrize("kind", ["cdiag", "cqmat", "random", "cdiag_conv", "cqmat_conv"])
+def test_golden_ax_every_format(gpu, golden, kind):
+    """Integer-valued reference test matrices (test_spmv_cdiag.cpp,
+    test_spmv_cqmat.cpp sweeps): the GPU result equals the reference's exactly,
+    including the overwrite (CSR, ELL) vs accumulate (COO, SCOO, DENSE) semantics
+    and the untouched output of empty CSR / ELL / DENSE matrices."""
+    T = gpu
+    n = 0
+    for key, case in golden_cases(golden["gen"], kind).items():
+        if "ax" not in case:
+            continue
+        fmt = int(key.split("/")[1])
+        m = make(T, fmt, key, kind)
+        i = m.info()
+        nr, nc = (i["n_row"], i["n_col"]) if fmt == 0 else (i["ln_row"], i["ln_col"])
+        r = np.full(max(nr, 1), 0.5)
+        v = np.arange(max(nc, 1), dtype=np.float64)
+        m.Ax(r, v)
+        assert np.array_equal(r, case["ax"]), key
+        n += 1
+    assert n >= 20
+
+
+def test_spmv_zero_fills(gpu):
+    T = gpu
+    for fmt in range(5):
+        m = T.FORMATS[fmt]()
+        m.fill_cdiag(20, 20, 3)
+        y = m.spmv(np.ones(20))
+        exp = np.array([(i - 3 >= 0) + (i + 3 < 20) for i in range(20)], float)
+        assert np.array_equal(y, exp), fmt
+
+
+def test_cfg1_uniform_matrix_all_formats(gpu, golden):
+    """n = 10^4, column i + 9 random columns per row, U[-1,1) values, x U[0,1),
+    seed 0: every format against the reference's own output."""
+    T = gpu
+    c1 = golden["cfg1"]
+    n = 10_000
+    csr = T.MatrixCSR()
+    csr.fill_uniform_rows(n, 10, 0)
+    a = csr.arrays()
+    x = T.fill_uniform(n, 0.0, 1.0, 0)
+    scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x)
+    rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(a["rowptr"]))
+    coo = T.MatrixCOO.from_arrays(n, n, rows, a["colidx"], a["values"])
+    mats = {0: coo, 1: T.MatrixSCOO(coo), 2: csr, 3: T.MatrixELL(coo)}
+    for fmt, m in mats.items():
+        y = np.zeros(n)
+        m.Ax(y, x)
+        assert oracle.rel_err_normalized(y, c1[f"y/{fmt}"], scale) <= TOL, fmt
+        if fmt in (2, 3):  # one thread per row, reference rounding
+            assert np.array_equal(y, c1[f"y/{fmt}"]), fmt
+    d = T.MatrixDENSE()
+    d.fill_dense_uniform(2000, 2000, 0)
+    xd = T.fill_uniform(2000, 0.0, 1.0, 0)
+    yd = np.zeros(2000)
+    d.Ax(yd, xd)
+    dscale = np.abs(d.arrays()["values"].reshape(2000, 2000) * xd).sum(1)
+    assert oracle.rel_err_normalized(yd, c1["y_dense"], dscale) <= TOL
+
+
+def test_vect_incr_and_blocks(gpu):
+    """vect_incr shifts COO/SCOO output rows (MatrixCOO.cpp:140,
+    MatrixSCOO.cpp:162); block matrices apply f_row / f_col offsets."""
+    T = gpu
+    coo = T.MatrixCOO()
+    coo.fill_cqmat(40, 40, 5, 0.5, 3)
+    a = coo.arrays()
+    keep = a["row"] < 30
+    small = T.MatrixCOO.from_arrays(40, 40, a["row"][keep], a["col"][keep], a["values"][keep] * 0.5)
+    v = np.linspace(-1, 1, 40)
+    for incr in (0, 5, 10):
+        r = np.full(40, 0.25)
+        small.Ax(r, v, incr)
+        exp = oracle.coo_ax(40, a["row"][keep], a["col"][keep], a["values"][keep] * 0.5, v,
+                            np.full(40, 0.25), incr)
+        assert np.allclose(r, exp, rtol=0, atol=1e-14)
+    with pytest.raises(T.TbslaError):
+        small.Ax(np.zeros(40), v, 11)  # row 29 + 11 is out of range
+    for fmt in (1, 2, 3, 4):
+        for grid in [(1, 0, 2, 1), (0, 1, 1, 2), (1, 2, 2, 3), (2, 1, 3, 2)]:
+            m = T.FORMATS[fmt]()
+            m.fill_cqmat(60, 45, 9, 0.5, 2, *grid)
+            i = m.info()
+            arr = m.arrays()
+            v = np.linspace(0.5, 2.0, i["ln_col"])
+            r = np.full(max(i["ln_row"], 1), 0.5)
+            m.Ax(r, v)
+            exp = np.full(max(i["ln_row"], 1), 0.5)
+            if fmt == 1 and i["nnz"]:
+                oracle.scoo_ax(i["ln_row"], i["f_row"], i["f_col"], arr["row"], arr["col"], arr["values"], v, exp)
+            elif fmt == 2 and i["nnz"]:
+                oracle.csr_ax(arr["rowptr"], arr["colidx"], arr["values"], v, exp, f_col=i["f_col"], nnz=i["nnz"])
+            elif fmt == 3:
+                oracle.ell_ax(arr["values"], arr["columns"], i["ln_row"], i["max_col"], v, exp, f_col=i["f_col"],
+                              nnz=i["nnz"])
+            elif fmt == 4:
+                oracle.dense_ax(arr["values"], i["ln_row"], i["ln_col"], v, exp, nnz=i["nnz"])
+            assert np.allclose(r, exp, rtol=0, atol=1e-12), (fmt, grid)
+
+
+def powerlaw(T, n, seed=5, **kw):
+    m = T.MatrixCSR()
+    m.fill_powerlaw(n, seed=seed, **kw)
+    return m
+
+
+@pytest.mark.parametrize("tile", [1024, 2048, 4096])
+def test_powerlaw_csr_fp64(gpu, tile):
+    """Zipf(2) rows (mean 16, up to 4096 entries, 30% near-diagonal) at
+    n = 2^18: every row within the FP64 tolerance of the oracle, for each
+    block budget of the row-block partition."""
+    T = gpu
+    n = 1 << 18
+    m = powerlaw(T, n)
+    m.set_tile(tile)
+    a = m.arrays()
+    x = T.fill_uniform(n, 0.0, 1.0, 1)
+    y = m.spmv(x)
+    ref = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x, threads=True)
+    scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x)
+    assert oracle.rel_err_normalized(y, ref, scale) <= TOL
+    # most rows are summed by one thread in entry order: bit-identical
+    assert np.mean(y == ref) > 0.5
+
+
+def test_long_and_empty_rows(gpu):
+    """Rows longer than the block budget (single-row blocks, several CTA
+    passes), empty rows between them, a one-row matrix."""
+    T = gpu
+    n = 3000
+    lens = np.zeros(n, np.int64)
+    lens[::7] = 1
+    lens[5] = 9000
+    lens[17] = 4097
+    lens[100:140] = 300
+    lens[2999] = 2048
+    rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    rng = np.random.default_rng(3)
+    nnz = int(rp[-1])
+    ci = rng.integers(0, n, nnz).astype(np.int32)
+    va = rng.uniform(-1, 1, nnz)
+    x = rng.uniform(0, 1, n)
+    m = T.MatrixCSR.from_arrays(n, n, rp, ci, va)
+    y = np.full(n, 7.0)
+    m.Ax(y, x)
+    ref = oracle.csr_ax(rp, ci, va, x)
+    scale = oracle.csr_absrow(rp, ci, va, x)
+    assert oracle.rel_err_normalized(y, ref, scale) <= TOL
+    assert (y[lens == 0] == 0).all()
+    one = T.MatrixCSR.from_arrays(1, 5, [0, 3], [0, 2, 4], [1.0, 2.0, 3.0])
+    assert np.array_equal(one.spmv(np.array([1.0, 1, 1, 1, 2])), [9.0])
+
+
+def test_empty_matrices_leave_output(gpu):
+    T = gpu
+    for fmt in range(5):
+        m = T.FORMATS[fmt]()
+        m.fill_cdiag(10, 5, 12)  # no entry falls inside the matrix
+        r = np.full(10, 3.0)
+        m.Ax(r, np.ones(5))
+        assert (r == 3.0).all(), fmt
+        assert (m.spmv(np.ones(5)) == 0).all(), fmt
+
+
+@pytest.mark.parametrize("prec", ["f32", "bf16"])
+def test_precision_forms(gpu, prec):
+    """FP32 / BF16 value storage, FP64 products and sums: equal (to FP64
+    rounding) to the oracle on the same rounded values; the error against
+    the FP64 oracle is that of the value rounding."""
+    T = gpu
+    n = 1 << 16
+    for fmt in (0, 1, 2, 3):
+        csr = powerlaw(T, n, seed=9, max_len=512)
+        a = csr.arrays()
+        if fmt == 2:
+            m = csr
+        else:
+            rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(a["rowptr"]))
+            coo = T.MatrixCOO.from_arrays(n, n, rows, a["colidx"], a["values"])
+            m = coo if fmt == 0 else T.FORMATS[fmt](coo)
+        m.set_precision(T.F32 if prec == "f32" else T.BF16)
+        x = T.fill_uniform(n, 0.0, 1.0, 4)
+        y = m.spmv(x)
+        rv = a["values"].astype(np.float32).astype(np.float64) if prec == "f32" else oracle.bf16_round(a["values"])
+        ref_r = oracle.csr_ax(a["rowptr"], a["colidx"], rv, x)
+        scale = oracle.csr_absrow(a["rowptr"], a["colidx"], rv, x)
+        assert oracle.rel_err_normalized(y, ref_r, scale) <= TOL, fmt
+        ref64 = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x)
+        err = oracle.rel_err_normalized(y, ref64, oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x))
+        bound = 2.0 ** -24 if prec == "f32" else 2.0 ** -8
+        assert err <= bound * 1.01, (fmt, err)
+
+
+def test_device_pointer_entry_points(gpu):
+    import torch
+
+    T = gpu
+    n = 50_000
+    m = powerlaw(T, n, seed=21)
+    a = m.arrays()
+    x = T.fill_uniform(n, -1.0, 1.0, 8)
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.full((n,), 2.0, dtype=torch.float64, device="cuda")
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        m.Ax_device(yt, xt, stream=s)
+    s.synchronize()
+    ref = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x)
+    scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x)
+    assert oracle.rel_err_normalized(yt.cpu().numpy(), ref, scale) <= TOL
+    zt = torch.full((n,), 2.0, dtype=torch.float64, device="cuda")
+    m.spmv_device(zt, xt)
+    torch.cuda.synchronize()
+    assert torch.equal(zt, yt)
+
+
+def test_composite_ops_match_reference(gpu, golden):
+    T = gpu
+    ops = golden["ops"]
+    for n in (10, 30):
+        for c in (0, 1, 3, 5, 9):
+            for fmt in range(5):
+                m = T.FORMATS[fmt]()
+                m.fill_cdiag(n, n, c)
+                v = 2 * np.arange(n, dtype=np.float64) + 1
+                assert np.array_equal(m.a_axpx_(v), ops[f"a_axpx/{fmt}/{n}/{c}"]), (fmt, n, c)
+                for name, fn in (("AAxpAx", m.AAxpAx), ("AAxpAxpx", m.AAxpAxpx)):
+                    r = np.full(n, 0.25)
+                    buf = np.full(n, 0.125)
+                    fn(r, v, buf)
+                    assert np.array_equal(r, ops[f"{name}/{fmt}/{n}/{c}/r"]), (name, fmt, n, c)
+                    assert np.array_equal(buf, ops[f"{name}/{fmt}/{n}/{c}/buffer"]), (name, fmt, n, c)
+
+
+def test_col_sums_normalize_match_reference(gpu, golden):
+    T = gpu
+    ops = golden["ops"]
+    for key in ("cqmat", "cdiag"):
+        m = T.MatrixCSR()
+        if key == "cqmat":
+            m.fill_cqmat(40, 40, 6, 0.4, 2)
+        else:
+            m.fill_cdiag(40, 40, 3)
+        s = np.zeros(40)
+        m.get_col_sums(s)
+        assert np.array_equal(s, ops[f"colsum/{key}/s"])  # integer-valued sums: exact
+        m.normalize_cols(s)
+        a = m.arrays()
+        end = int(a["rowptr"][-1])
+        assert np.array_equal(a["values"][:end], ops[f"colsum/{key}/values"][:end])
