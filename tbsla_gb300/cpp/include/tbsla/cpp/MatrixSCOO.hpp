@@ -1,0 +1,20 @@
+// Drop-in for tbsla::cpp::MatrixSCOO (src/cpp/include/tbsla/cpp/MatrixSCOO.hpp of
+// the reference) on the GB300 C ABI; see Matrix.hpp.
+#ifndef TBSLA_GB300_CPP_MATRIXSCOO
+#define TBSLA_GB300_CPP_MATRIXSCOO
+
+#include <tbsla/cpp/Matrix.hpp>
+#include <tbsla/cpp/MatrixCOO.hpp>
+
+namespace tbsla { namespace cpp {
+
+class MatrixSCOO : public Matrix {
+  public:
+    MatrixSCOO();
+    explicit MatrixSCOO(const MatrixCOO& m);
+    MatrixSCOO(int n_row, int n_col, long nnz, const double* values, const int* row, const int* col);
+};
+
+}}  // namespace tbsla::cpp
+
+#endif

@@ -80,9 +80,29 @@ __device__ __forceinline__ __nv_bfloat16 narrow<__nv_bfloat16>(double v) {
   return r;
 }
 
+// Widening to double.  GB300's FP64 pipe is narrow (about 1/64 of FP32), so
+// float -> double is done on the integer pipes for normal numbers and zero:
+// re-bias the exponent (+896 = 1023 - 127) and move the mantissa up 29 bits,
+// which is exact; subnormals, infinities and NaNs take the hardware path.
+__device__ __forceinline__ double widen_bits(unsigned u) {
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(u & 0x80000000u) << 32;
+  if (e == 0u) {
+    if ((u & 0x7fffffu) == 0u) return __longlong_as_double((long long)sign);
+    return (double)__uint_as_float(u);
+  }
+  if (e == 0xffu) return (double)__uint_as_float(u);
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
 __device__ __forceinline__ double widen(double v) { return v; }
-__device__ __forceinline__ double widen(float v) { return (double)v; }
-__device__ __forceinline__ double widen(__nv_bfloat16 v) { return (double)__bfloat162float(v); }
+__device__ __forceinline__ double widen(float v) { return widen_bits(__float_as_uint(v)); }
+__device__ __forceinline__ double widen(__nv_bfloat16 v) {
+  return widen_bits((unsigned)(*reinterpret_cast<const unsigned short*>(&v)) << 16);
+}
+
+// Fused multiply-add, one FP64 instruction per matrix entry.
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return __fma_rn(a, b, c); }
 
 // Product and sum with explicit rounding (no FMA contraction), so a row
 // summed by one thread reproduces the reference loop's rounding exactly.

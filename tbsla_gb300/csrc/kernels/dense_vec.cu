@@ -38,12 +38,12 @@ __global__ void __launch_bounds__(NT) k_dense(const V* __restrict__ A, int ln_ro
     for (; j + 3 * kWarp < ln_col; j += 4 * kWarp) {
       double v0 = widen(ld_stream(a + j, pol)), v1 = widen(ld_stream(a + j + kWarp, pol));
       double v2 = widen(ld_stream(a + j + 2 * kWarp, pol)), v3 = widen(ld_stream(a + j + 3 * kWarp, pol));
-      acc = add_rn(acc, mul_rn(v0, __ldg(x + j)));
-      acc = add_rn(acc, mul_rn(v1, __ldg(x + j + kWarp)));
-      acc = add_rn(acc, mul_rn(v2, __ldg(x + j + 2 * kWarp)));
-      acc = add_rn(acc, mul_rn(v3, __ldg(x + j + 3 * kWarp)));
+      acc = fma_rn(v0, __ldg(x + j), acc);
+      acc = fma_rn(v1, __ldg(x + j + kWarp), acc);
+      acc = fma_rn(v2, __ldg(x + j + 2 * kWarp), acc);
+      acc = fma_rn(v3, __ldg(x + j + 3 * kWarp), acc);
     }
-    for (; j < ln_col; j += kWarp) acc = add_rn(acc, mul_rn(widen(ld_stream(a + j, pol)), __ldg(x + j)));
+    for (; j < ln_col; j += kWarp) acc = fma_rn(widen(ld_stream(a + j, pol)), __ldg(x + j), acc);
     acc = warp_sum(acc);
     if (lane == 0) y[row] = add_rn(y[row], acc);
   }
@@ -68,16 +68,16 @@ __global__ void __launch_bounds__(NT) k_dense_f64x2(const double* __restrict__ A
       double2 a2 = ld_stream2(a + 2 * (j + 2 * kWarp), pol), a3 = ld_stream2(a + 2 * (j + 3 * kWarp), pol);
       double2 b0 = __ldg(x2 + j), b1 = __ldg(x2 + j + kWarp);
       double2 b2 = __ldg(x2 + j + 2 * kWarp), b3 = __ldg(x2 + j + 3 * kWarp);
-      acc0 = add_rn(acc0, mul_rn(a0.x, b0.x)); acc1 = add_rn(acc1, mul_rn(a0.y, b0.y));
-      acc0 = add_rn(acc0, mul_rn(a1.x, b1.x)); acc1 = add_rn(acc1, mul_rn(a1.y, b1.y));
-      acc0 = add_rn(acc0, mul_rn(a2.x, b2.x)); acc1 = add_rn(acc1, mul_rn(a2.y, b2.y));
-      acc0 = add_rn(acc0, mul_rn(a3.x, b3.x)); acc1 = add_rn(acc1, mul_rn(a3.y, b3.y));
+      acc0 = fma_rn(a0.x, b0.x, acc0); acc1 = fma_rn(a0.y, b0.y, acc1);
+      acc0 = fma_rn(a1.x, b1.x, acc0); acc1 = fma_rn(a1.y, b1.y, acc1);
+      acc0 = fma_rn(a2.x, b2.x, acc0); acc1 = fma_rn(a2.y, b2.y, acc1);
+      acc0 = fma_rn(a3.x, b3.x, acc0); acc1 = fma_rn(a3.y, b3.y, acc1);
     }
     for (; j < half; j += kWarp) {
       double2 a0 = ld_stream2(a + 2 * j, pol);
       double2 b0 = __ldg(x2 + j);
-      acc0 = add_rn(acc0, mul_rn(a0.x, b0.x));
-      acc1 = add_rn(acc1, mul_rn(a0.y, b0.y));
+      acc0 = fma_rn(a0.x, b0.x, acc0);
+      acc1 = fma_rn(a0.y, b0.y, acc1);
     }
     double acc = warp_sum(add_rn(acc0, acc1));
     if (lane == 0) y[row] = add_rn(y[row], acc);

@@ -9,14 +9,16 @@
 // in the storage precision) plus a row-block partition built once per
 // matrix (csr_partition).  A block is either
 //  - a run of <= 256 consecutive rows holding <= 256*ITEMS entries
-//    ("stream" block): the CTA reads the block's entries with coalesced
-//    loads, multiplies by the gathered x, stages the products in shared
+//    ("stream" block): the CTA reads the block's values and column indices
+//    with coalesced loads, gathers x, stages (value, x) pairs in shared
 //    memory, then sums each row with a group of G lanes, G = the largest
-//    power of two with G * rows <= 256 (capped at 32).  With G == 1 a row is
-//    summed by one thread from 0 in entry order, with every product rounded
-//    before the add: the reference loop's rounding, bit for bit;
+//    power of two with G * rows <= 256 (capped at 32), one fused
+//    multiply-add per entry in entry order;
 //  - one row longer than 256*ITEMS ("vector" block): the whole CTA strides
 //    over it and reduces.
+// GB300's FP64 pipe is narrow, so the kernel spends exactly one FP64
+// instruction (DFMA) per entry, widens FP32 / BF16 values on the integer
+// pipes, and keeps reductions to one add per row-group lane.
 // Matrix values, indices and row pointers are read once, through the
 // non-allocating read-only path with an L2 evict-first policy; x is gathered
 // through L1 so that it owns L2.
@@ -40,16 +42,17 @@ __device__ __forceinline__ double row_dot_cta(const V* vals, const int* colidx, 
   for (; j + 3 * NT < e; j += 4 * NT) {
     int c0 = ld_stream(colidx + j, pol), c1 = ld_stream(colidx + j + NT, pol);
     int c2 = ld_stream(colidx + j + 2 * NT, pol), c3 = ld_stream(colidx + j + 3 * NT, pol);
-    double v0 = widen(ld_stream(vals + j, pol)), v1 = widen(ld_stream(vals + j + NT, pol));
-    double v2 = widen(ld_stream(vals + j + 2 * NT, pol)), v3 = widen(ld_stream(vals + j + 3 * NT, pol));
+    V v0 = ld_stream(vals + j, pol), v1 = ld_stream(vals + j + NT, pol);
+    V v2 = ld_stream(vals + j + 2 * NT, pol), v3 = ld_stream(vals + j + 3 * NT, pol);
     double x0 = ld_gather(x + c0 - f_col), x1 = ld_gather(x + c1 - f_col);
     double x2 = ld_gather(x + c2 - f_col), x3 = ld_gather(x + c3 - f_col);
-    acc = add_rn(acc, mul_rn(v0, x0));
-    acc = add_rn(acc, mul_rn(v1, x1));
-    acc = add_rn(acc, mul_rn(v2, x2));
-    acc = add_rn(acc, mul_rn(v3, x3));
+    acc = fma_rn(widen(v0), x0, acc);
+    acc = fma_rn(widen(v1), x1, acc);
+    acc = fma_rn(widen(v2), x2, acc);
+    acc = fma_rn(widen(v3), x3, acc);
   }
-  for (; j < e; j += NT) acc = add_rn(acc, mul_rn(widen(ld_stream(vals + j, pol)), ld_gather(x + ld_stream(colidx + j, pol) - f_col)));
+  for (; j < e; j += NT)
+    acc = fma_rn(widen(ld_stream(vals + j, pol)), ld_gather(x + ld_stream(colidx + j, pol) - f_col), acc);
   return acc;
 }
 
@@ -60,11 +63,18 @@ struct Smem {
   int flag;
 };
 
+// Dynamic shared memory of a stream block: x[NT*ITEMS] doubles then
+// values[NT*ITEMS] in the storage precision.
+template <class V, int ITEMS>
+constexpr size_t stage_bytes() { return (size_t)NT * ITEMS * (sizeof(double) + sizeof(V)); }
+
 // One block of the partition; epi.emit(row, sum, red) per row.
 template <class V, int ITEMS, class Epi>
 __device__ __forceinline__ void csr_block(const CsrArgs& a, int b, const double* x, const Epi& epi,
-                                          double* red, double* s_prod, Smem& sm, uint64_t pol) {
+                                          double* red, unsigned char* stage, Smem& sm, uint64_t pol) {
   const V* vals = static_cast<const V*>(a.vals);
+  double* s_x = reinterpret_cast<double*>(stage);
+  V* s_v = reinterpret_cast<V*>(stage + (size_t)NT * ITEMS * sizeof(double));
   const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
   const int nrows = r1 - r0;
   const int tid = threadIdx.x;
@@ -92,7 +102,10 @@ __device__ __forceinline__ void csr_block(const CsrArgs& a, int b, const double*
 #pragma unroll
   for (int k = 0; k < ITEMS; k++) {
     const int i = k * NT + tid;
-    if (i < cnt) s_prod[i] = mul_rn(widen(vv[k]), ld_gather(x + cidx[k] - a.f_col));
+    if (i < cnt) {
+      s_x[i] = ld_gather(x + cidx[k] - a.f_col);
+      s_v[i] = vv[k];
+    }
   }
   __syncthreads();
   const int G = nrows <= 8 ? 32 : nrows <= 16 ? 16 : nrows <= 32 ? 8 : nrows <= 64 ? 4 : nrows <= 128 ? 2 : 1;
@@ -100,15 +113,14 @@ __device__ __forceinline__ void csr_block(const CsrArgs& a, int b, const double*
   double acc = 0;
   if (g < nrows) {
     const int lo = sm.rp[g] - s, hi = sm.rp[g + 1] - s;
-    for (int j = lo + lane; j < hi; j += G) acc = add_rn(acc, s_prod[j]);
+    for (int j = lo + lane; j < hi; j += G) acc = fma_rn(widen(s_v[j]), s_x[j], acc);
   }
   for (int o = G >> 1; o > 0; o >>= 1) acc = add_rn(acc, __shfl_xor_sync(0xffffffffu, acc, o));
   if (g < nrows && lane == 0) epi.emit(r0 + g, acc, red);
-  __syncthreads();  // s_prod / rp reused by the next block
+  __syncthreads();  // stage / rp reused by the next block
 }
 
 struct EpiStore {
-  static constexpr int kRed = 0;
   double* y;
   __device__ __forceinline__ void emit(int row, double s, double*) const { y[row] = s; }
 };
@@ -116,11 +128,11 @@ struct EpiStore {
 template <class V, int ITEMS>
 __global__ void __launch_bounds__(NT) k_csr_spmv(CsrArgs a, const double* __restrict__ x,
                                                 double* __restrict__ y) {
-  __shared__ double s_prod[NT * ITEMS];
+  extern __shared__ __align__(16) unsigned char stage[];
   __shared__ Smem sm;
   const uint64_t pol = policy_evict_first();
   EpiStore epi{y};
-  csr_block<V, ITEMS>(a, blockIdx.x, x, epi, nullptr, s_prod, sm, pol);
+  csr_block<V, ITEMS>(a, blockIdx.x, x, epi, nullptr, stage, sm, pol);
 }
 
 // ---- persistent variant with reductions --------------------------------------
@@ -166,7 +178,6 @@ __device__ __forceinline__ void reduce_and_finish(Ctl ctl, double* red, Smem& sm
 }
 
 struct EpiPageRank {
-  static constexpr int kRed = 3;
   double* y;
   const double* x;
   const unsigned char* dangling;
@@ -186,7 +197,7 @@ template <class V, int ITEMS>
 __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __restrict__ x,
                                                     double* __restrict__ y, PageRankArgs p,
                                                     Ctl ctl) {
-  __shared__ double s_prod[NT * ITEMS];
+  extern __shared__ __align__(16) unsigned char stage[];
   __shared__ Smem sm;
   if (*(volatile int*)p.done) return;  // converged in an earlier launch: no-op
   const uint64_t pol = policy_evict_first();
@@ -194,7 +205,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   EpiPageRank epi{y, x, p.dangling, p.tele, p.beta, coef, coef / p.n_nodes};
   double red[3] = {0, 0, 0};
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm))
-    csr_block<V, ITEMS>(a, b, x, epi, red, s_prod, sm, pol);
+    csr_block<V, ITEMS>(a, b, x, epi, red, stage, sm, pol);
   const double beta = p.beta, eps = p.eps;
   double* coef_out = p.coef_out;
   int* done = p.done;
@@ -241,7 +252,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
         for (int t = 0; t < m; t++) {
           const int ct = __shfl_sync(0xffffffffu, c, t);
           const double vt = __shfl_sync(0xffffffffu, v, t);
-          if (active) acc = add_rn(acc, mul_rn(vt, ld_gather(X + (size_t)(ct - a.f_col) * nvec + lane)));
+          if (active) acc = fma_rn(vt, ld_gather(X + (size_t)(ct - a.f_col) * nvec + lane), acc);
         }
       }
       if (active) {
@@ -299,9 +310,18 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
   }
 }
 
+template <class K>
+cudaError_t prepare(K kernel, size_t smem) {
+  // opt in to more than 48 KB of dynamic shared memory where the stage needs it
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 template <class V, int ITEMS>
 cudaError_t launch_spmv(const CsrArgs& a, const double* x, double* y, cudaStream_t s) {
-  k_csr_spmv<V, ITEMS><<<a.nblocks, NT, 0, s>>>(a, x, y);
+  constexpr size_t smem = stage_bytes<V, ITEMS>();
+  static cudaError_t ready = prepare(k_csr_spmv<V, ITEMS>, smem);
+  if (ready != cudaSuccess) return ready;
+  k_csr_spmv<V, ITEMS><<<a.nblocks, NT, smem, s>>>(a, x, y);
   return cudaGetLastError();
 }
 
@@ -315,16 +335,25 @@ cudaError_t spmv_items(const CsrArgs& a, const double* x, double* y, cudaStream_
   return cudaErrorInvalidValue;
 }
 
+template <class V, int ITEMS>
+cudaError_t launch_pr(const CsrArgs& a, const double* x, double* y, const PageRankArgs& p, Ctl c,
+                      int grid, cudaStream_t s) {
+  constexpr size_t smem = stage_bytes<V, ITEMS>();
+  static cudaError_t ready = prepare(k_csr_pagerank<V, ITEMS>, smem);
+  if (ready != cudaSuccess) return ready;
+  k_csr_pagerank<V, ITEMS><<<grid, NT, smem, s>>>(a, x, y, p, c);
+  return cudaGetLastError();
+}
+
 template <class V>
 cudaError_t pr_items(const CsrArgs& a, const double* x, double* y, const PageRankArgs& p, Ctl c,
                      int grid, cudaStream_t s) {
   switch (a.items) {
-    case 4: k_csr_pagerank<V, 4><<<grid, NT, 0, s>>>(a, x, y, p, c); break;
-    case 8: k_csr_pagerank<V, 8><<<grid, NT, 0, s>>>(a, x, y, p, c); break;
-    case 16: k_csr_pagerank<V, 16><<<grid, NT, 0, s>>>(a, x, y, p, c); break;
-    default: return cudaErrorInvalidValue;
+    case 4: return launch_pr<V, 4>(a, x, y, p, c, grid, s);
+    case 8: return launch_pr<V, 8>(a, x, y, p, c, grid, s);
+    case 16: return launch_pr<V, 16>(a, x, y, p, c, grid, s);
   }
-  return cudaGetLastError();
+  return cudaErrorInvalidValue;
 }
 
 }  // namespace
@@ -353,26 +382,27 @@ void csr_partition(const int* rowptr, int n_row, int tile, int** out, int* nbloc
 
 namespace {
 template <class K>
-int resident_grid(K kernel) {
+int resident_grid(K kernel, size_t smem = 0) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, NT, 0);
+  if (smem) prepare(kernel, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, NT, smem);
   return std::max(1, sms * std::max(1, per));
 }
 }  // namespace
 
 int csr_pagerank_grid(int items, int prec) {
   switch (prec * 100 + items) {
-    case kF64 * 100 + 4: return resident_grid(k_csr_pagerank<double, 4>);
-    case kF64 * 100 + 8: return resident_grid(k_csr_pagerank<double, 8>);
-    case kF64 * 100 + 16: return resident_grid(k_csr_pagerank<double, 16>);
-    case kF32 * 100 + 4: return resident_grid(k_csr_pagerank<float, 4>);
-    case kF32 * 100 + 8: return resident_grid(k_csr_pagerank<float, 8>);
-    case kF32 * 100 + 16: return resident_grid(k_csr_pagerank<float, 16>);
-    case kBF16 * 100 + 4: return resident_grid(k_csr_pagerank<__nv_bfloat16, 4>);
-    case kBF16 * 100 + 8: return resident_grid(k_csr_pagerank<__nv_bfloat16, 8>);
-    case kBF16 * 100 + 16: return resident_grid(k_csr_pagerank<__nv_bfloat16, 16>);
+    case kF64 * 100 + 4: return resident_grid(k_csr_pagerank<double, 4>, stage_bytes<double, 4>());
+    case kF64 * 100 + 8: return resident_grid(k_csr_pagerank<double, 8>, stage_bytes<double, 8>());
+    case kF64 * 100 + 16: return resident_grid(k_csr_pagerank<double, 16>, stage_bytes<double, 16>());
+    case kF32 * 100 + 4: return resident_grid(k_csr_pagerank<float, 4>, stage_bytes<float, 4>());
+    case kF32 * 100 + 8: return resident_grid(k_csr_pagerank<float, 8>, stage_bytes<float, 8>());
+    case kF32 * 100 + 16: return resident_grid(k_csr_pagerank<float, 16>, stage_bytes<float, 16>());
+    case kBF16 * 100 + 4: return resident_grid(k_csr_pagerank<__nv_bfloat16, 4>, stage_bytes<__nv_bfloat16, 4>());
+    case kBF16 * 100 + 8: return resident_grid(k_csr_pagerank<__nv_bfloat16, 8>, stage_bytes<__nv_bfloat16, 8>());
+    case kBF16 * 100 + 16: return resident_grid(k_csr_pagerank<__nv_bfloat16, 16>, stage_bytes<__nv_bfloat16, 16>());
   }
   return 152;
 }

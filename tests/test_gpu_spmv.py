@@ -4,8 +4,10 @@ inputs.
 
 Tolerance (FP64 forms): |y_gpu,i - y_ref,i| <= 1e-13 * sum_j |a_ij x_j| per
 entry (normalised by the absolute row sum so that cancellation cannot fail
-it).  Rows summed by one thread (CSR rows in blocks of > 128 rows, ELL rows)
-reproduce the reference's rounding and are additionally checked bit for bit.
+it).  ELL rows, summed by one thread with each product rounded before the
+add, reproduce the reference's rounding and are also checked bit for bit;
+CSR / DENSE use one fused multiply-add per entry (GB300's FP64 pipe is the
+scarce resource) and differ from the reference only in that rounding.
 """
 import numpy as np
 import pytest
@@ -88,7 +90,7 @@ def test_cfg1_uniform_matrix_all_formats(gpu, golden):
         y = np.zeros(n)
         m.Ax(y, x)
         assert oracle.rel_err_normalized(y, c1[f"y/{fmt}"], scale) <= TOL, fmt
-        if fmt in (2, 3):  # one thread per row, reference rounding
+        if fmt == 3:  # ELL: one thread per row, product rounded before the add
             assert np.array_equal(y, c1[f"y/{fmt}"]), fmt
     d = T.MatrixDENSE()
     d.fill_dense_uniform(2000, 2000, 0)
@@ -160,8 +162,6 @@ def test_powerlaw_csr_fp64(gpu, tile):
     ref = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x, threads=True)
     scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x)
     assert oracle.rel_err_normalized(y, ref, scale) <= TOL
-    # most rows are summed by one thread in entry order: bit-identical
-    assert np.mean(y == ref) > 0.5
 
 
 def test_long_and_empty_rows(gpu):
