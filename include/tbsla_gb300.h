@@ -166,6 +166,13 @@ int tbsla_matrix_device_bytes(const tbsla_matrix* m, size_t* bytes);
 /* CSR: block budget of the row-block partition (nnz per block, multiple of
  * 256, default 2048); changing it rebuilds the partition. */
 int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
+/* CSR SpMV kernel: TBSLA_CSR_MERGE (default; merge-path split, `items`
+ * row ends + entries per thread, 4/8/16) or TBSLA_CSR_ROWBLOCK (row-block
+ * adaptive; items ignored, see tbsla_matrix_set_csr_tile).  Changing it
+ * rebuilds the device copy. */
+#define TBSLA_CSR_MERGE 0
+#define TBSLA_CSR_ROWBLOCK 1
+int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items);
 
 /* ---- SpMV: Matrix::Ax / Matrix::spmv (Matrix.hpp:14-15) ----------------------- */
 /* r <- A v (CSR, ELL: overwrite; returns without touching r when nnz == 0)
@@ -226,6 +233,25 @@ int tbsla_page_rank_batched(tbsla_matrix* m, int nvec, const double* teleport, d
  * (0 = never).  rel_residual receives the FP64 true residual at exit. */
 int tbsla_cg(tbsla_matrix* m, const double* b, double* x, int max_iterations, double rel_tol,
              int precond, int refresh, int* iterations, double* rel_residual);
+
+/* ---- batched CG: many SPD systems of uneven size solved together ------------------
+ * (CG.cpp:32-73 per system).  tbsla_batch_create concatenates nsys square CSR
+ * handles (f_col 0) into one block-diagonal device matrix, values in
+ * `precision` plus an FP64 copy for the true residual, and the Jacobi
+ * diagonal.  tbsla_batch_cg solves all systems from the start vectors in x;
+ * rhs and x are the systems' vectors concatenated in order (offsets from
+ * tbsla_batch_rows).  Each system stops on its own when its FP64 true
+ * residual satisfies ||b - A x|| <= rel_tol ||b||; iterations[s] and
+ * rel_residual[s] receive its count and final true relative residual.
+ * graph_iters: iterations captured per CUDA graph replay (0: 10).  Returns
+ * TBSLA_ERR_NOT_CONVERGED if some system hit max_iterations. */
+typedef struct tbsla_batch tbsla_batch;
+int tbsla_batch_create(tbsla_batch** b, tbsla_matrix* const* systems, int nsys, int precision);
+int tbsla_batch_destroy(tbsla_batch* b);
+int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets);
+int tbsla_batch_cg(tbsla_batch* b, const double* rhs, double* x, int max_iterations, double rel_tol,
+                   int precond, int refresh, int graph_iters, int* iterations,
+                   double* rel_residual);
 
 #ifdef __cplusplus
 }

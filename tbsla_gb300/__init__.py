@@ -7,7 +7,7 @@ is its Python mirror.  Import fails if the library has not been built.
 """
 from . import _lib
 from ._lib import BF16, COO, CSR, DENSE, ELL, F32, F64, SCOO, TbslaError, check, lib
-from .matrix import (FORMATS, Matrix, MatrixCOO, MatrixCSR, MatrixDENSE, MatrixELL, MatrixSCOO,
+from .matrix import (FORMATS, Batch, Matrix, MatrixCOO, MatrixCSR, MatrixDENSE, MatrixELL, MatrixSCOO,
                      device_init, fill_uniform)
 
 __all__ = ["Matrix", "MatrixCOO", "MatrixSCOO", "MatrixCSR", "MatrixELL", "MatrixDENSE", "FORMATS",

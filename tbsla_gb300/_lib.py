@@ -93,6 +93,11 @@ _SIGS = {
     "tbsla_matrix_upload": (I, [P]),
     "tbsla_matrix_device_bytes": (I, [P, C.POINTER(C.c_size_t)]),
     "tbsla_matrix_set_csr_tile": (I, [P, I]),
+    "tbsla_matrix_set_csr_algorithm": (I, [P, I, I]),
+    "tbsla_batch_create": (I, [C.POINTER(P), C.POINTER(P), I, I]),
+    "tbsla_batch_destroy": (I, [P]),
+    "tbsla_batch_rows": (I, [P, IP, C.POINTER(L)]),
+    "tbsla_batch_cg": (I, [P, P, P, I, D, I, I, I, IP, DP]),
     "tbsla_Ax": (I, [P, P, P, I]),
     "tbsla_spmv": (I, [P, P, P, I]),
     "tbsla_Ax_device": (I, [P, P, P, I, P]),

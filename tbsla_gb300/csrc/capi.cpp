@@ -252,6 +252,18 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block) {
   return TBSLA_OK;
 }
 
+int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items) {
+  if (!m || (algorithm != TBSLA_CSR_MERGE && algorithm != TBSLA_CSR_ROWBLOCK) ||
+      (algorithm == TBSLA_CSR_MERGE && items != 4 && items != 8 && items != 16))
+    return TBSLA_ERR_INVALID_ARG;
+  if (m->csr_algo != algorithm || (algorithm == TBSLA_CSR_MERGE && m->merge_items != items)) {
+    m->invalidate();
+    m->csr_algo = algorithm;
+    if (algorithm == TBSLA_CSR_MERGE) m->merge_items = items;
+  }
+  return TBSLA_OK;
+}
+
 int tbsla_Ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr) {
   if (!m || !r || !v) return TBSLA_ERR_INVALID_ARG;
   return dev_ax(m, r, v, vect_incr, false, true, nullptr);

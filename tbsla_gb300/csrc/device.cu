@@ -79,9 +79,15 @@ struct DeviceMatrix {
   void* vals = nullptr;
   int* idx0 = nullptr;
   int* idx1 = nullptr;
-  int* blocks = nullptr;
+  int* blocks = nullptr;  // CSR row-block partition
   int nblocks = 0;
   int items = 8;
+  int algo = 0;            // CSR: 0 merge path, 1 row blocks
+  int* coord = nullptr;    // CSR merge path: first row of each tile
+  int* carry_row = nullptr;
+  double* carry_val = nullptr;
+  long ntiles = 0;
+  int merge_items = 8;
   long nnz = 0;  // entries on the device
   int min_row = 0, max_row = -1;
   double* x = nullptr;
@@ -100,7 +106,8 @@ struct DeviceMatrix {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t,
-                    (void*)counter, (void*)partials, (void*)result})
+                    (void*)counter, (void*)partials, (void*)result, (void*)coord, (void*)carry_row,
+                    (void*)carry_val})
       if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -224,9 +231,19 @@ int build(const tbsla_matrix* m, DeviceMatrix* d) {
       int* blocks = nullptr;
       csr_partition(rp, I.ln_row, 256 * d->items, &blocks, &d->nblocks);
       st = upload_ints(d, &d->blocks, blocks, (size_t)d->nblocks + 1);
-      if (!st) st = status_of(cudaStreamSynchronize(d->stream));
       delete[] blocks;
-      return st;
+      if (st) return st;
+      // merge-path tiles and their carry scratch
+      d->algo = m->csr_algo;
+      d->merge_items = m->merge_items;
+      const long enz = end - rp[0];
+      d->ntiles = merge_tiles(I.ln_row, enz, d->merge_items);
+      if ((st = dalloc(&d->coord, (size_t)d->ntiles + 1)) || (st = dalloc(&d->carry_row, (size_t)d->ntiles)) ||
+          (st = dalloc(&d->carry_val, (size_t)d->ntiles)))
+        return st;
+      d->bytes += (size_t)d->ntiles * 16 + 4;
+      TRY(csr_merge_setup(d->idx0, I.ln_row, enz, d->merge_items, d->coord, d->stream));
+      return status_of(cudaStreamSynchronize(d->stream));
     }
     case TBSLA_ELL: {
       if (I.nnz == 0 || I.max_col == 0) return TBSLA_OK;
@@ -349,7 +366,12 @@ int ax_device(const tbsla_matrix* m, DeviceMatrix* d, double* r, const double* v
   if (skips_empty(m)) return TBSLA_OK;
   switch (m->format) {
     case TBSLA_CSR:
-      return status_of(csr_spmv(csr_args(m, d), v, r, s));
+      if (d->algo == 1) return status_of(csr_spmv(csr_args(m, d), v, r, s));
+      {
+        MergeArgs a{d->vals, d->prec, d->idx0, d->idx1, I.ln_row, d->nnz - m->idx0[0], I.f_col,
+                    d->merge_items, d->coord, d->ntiles, d->carry_row, d->carry_val};
+        return status_of(csr_merge_spmv(a, v, r, s));
+      }
     case TBSLA_ELL:
       return status_of(ell_spmv(d->vals, d->prec, d->idx0, I.ln_row, I.max_col, I.f_col, v, r, s));
     case TBSLA_COO:
@@ -697,10 +719,6 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   if (st) return st;
   if (iterations) *iterations = iters;
   return hflags[0] ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
-}
-
-int dev_cg(tbsla_matrix*, const double*, double*, int, double, int, int, int*, double*) {
-  return TBSLA_ERR_UNSUPPORTED;
 }
 
 }  // namespace tbsla_impl

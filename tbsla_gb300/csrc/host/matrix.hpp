@@ -54,7 +54,9 @@ struct tbsla_matrix {
   tbsla_impl::Buf<double> values;
   tbsla_impl::Buf<int> idx0, idx1;
   int precision = TBSLA_F64;
-  int csr_tile = 2048;
+  int csr_tile = 2048;     // row-block budget (entries per block)
+  int csr_algo = 0;        // 0: merge path (default), 1: row blocks
+  int merge_items = 8;     // merge path: items per thread
   int device = 0;
   mutable tbsla_impl::DeviceMatrix* dev = nullptr;
 

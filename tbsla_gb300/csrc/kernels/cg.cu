@@ -1,0 +1,290 @@
+// Batched conjugate gradients on a block-diagonal concatenation of SPD CSR
+// systems of uneven sizes.
+//
+// Follows tbsla::mpi::Matrix::CG (src/mpi/matrix/CG.cpp:32-73) with its
+// vector helpers (:7-30), restated: the SpMV is q = A p (CG.cpp:61 passes
+// the arguments in the other order), alpha = r.z / p.q, beta = r_new.z_new /
+// r.z, optional Jacobi preconditioning z = D^-1 r, and a relative stop test
+// ||r|| <= tol ||b|| confirmed on the FP64 true residual b - A x.
+//
+// Every system keeps its own scalars; one iteration over the whole batch is
+// four launches (SpMV + p.q, update + r.z / r.r, scalars, direction) that
+// skip the rows of systems which are not ACTIVE, so systems of 16^3 and 96^3
+// rows run side by side and drop out as they converge.  The host captures a
+// number of iterations in a CUDA graph and replays it.  With FP32 / BF16
+// matrix storage the residual is recomputed in FP64 from the FP64 values
+// every `refresh` iterations (residual replacement) and on every apparent
+// convergence.
+#include "common.cuh"
+#include "csr_block.cuh"
+#include "kernels.hpp"
+
+namespace tbsla_gpu {
+
+namespace {
+
+using namespace csr;
+
+struct EpiDot {
+  double* q;
+  const double* p;
+  __device__ __forceinline__ void emit(int row, double s, double* red) const {
+    q[row] = s;
+    red[0] = fma_rn(p[row], s, red[0]);
+  }
+};
+
+struct EpiResidual {
+  const double* b;
+  double* r;
+  double* z;  // nullptr when unpreconditioned
+  const double* dinv;
+  __device__ __forceinline__ void emit(int row, double s, double* red) const {
+    const double ri = b[row] - s;
+    r[row] = ri;
+    const double zi = dinv ? dinv[row] * ri : ri;
+    if (dinv) z[row] = zi;
+    red[0] = fma_rn(ri, ri, red[0]);
+    red[1] = fma_rn(ri, zi, red[1]);
+  }
+};
+
+template <class V, int ITEMS>
+__global__ void __launch_bounds__(NT) k_cg_spmv_dot(CgBatch c) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  __shared__ Smem sm;
+  const int b = blockIdx.x;
+  const int sys = c.block_sys[b];
+  if (c.status[sys] != kActive) return;  // uniform over the CTA
+  const uint64_t pol = policy_evict_first();
+  CsrArgs a{c.vals, c.prec, c.rowptr, c.colidx, c.blocks, c.nblocks, 0, c.items};
+  EpiDot epi{c.q, c.p};
+  double red[1] = {0};
+  csr_block<V, ITEMS>(a, b, c.p, epi, red, stage, sm, pol);
+  const double v = block_sum<NT>(red[0], sm.red);
+  if (threadIdx.x == 0) atomicAdd(c.pq + sys, v);
+}
+
+template <int ITEMS>
+__global__ void __launch_bounds__(NT) k_cg_residual(CgBatch c, int mask) {
+  extern __shared__ __align__(16) unsigned char stage[];
+  __shared__ Smem sm;
+  const int b = blockIdx.x;
+  const int sys = c.block_sys[b];
+  if (!((mask >> c.status[sys]) & 1)) return;
+  const uint64_t pol = policy_evict_first();
+  CsrArgs a{c.vals64, kF64, c.rowptr, c.colidx, c.blocks, c.nblocks, 0, c.items};
+  EpiResidual epi{c.b, c.r, c.dinv ? c.z : nullptr, c.dinv};
+  double red[2] = {0, 0};
+  csr_block<double, ITEMS>(a, b, c.x, epi, red, stage, sm, pol);
+  const double rr = block_sum<NT>(red[0], sm.red);
+  const double rz = block_sum<NT>(red[1], sm.red);
+  if (threadIdx.x == 0) {
+    atomicAdd(c.rrt + sys, rr);
+    atomicAdd(c.rz + sys, rz);
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_cg_update(CgBatch c) {
+  __shared__ double red_s[NT / kWarp];
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  if (c.status[sys] != kActive) return;
+  const double pq = c.pq[sys];
+  const double alpha = pq != 0 ? c.rz[sys] / pq : 0.0;
+  const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  double rz = 0, rr = 0;
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+    const double pi = c.p[i], qi = c.q[i];
+    c.x[i] = fma_rn(alpha, pi, c.x[i]);
+    const double ri = fma_rn(-alpha, qi, c.r[i]);
+    c.r[i] = ri;
+    double zi = ri;
+    if (c.dinv) {
+      zi = c.dinv[i] * ri;
+      c.z[i] = zi;
+    }
+    rz = fma_rn(ri, zi, rz);
+    rr = fma_rn(ri, ri, rr);
+  }
+  rz = block_sum<NT>(rz, red_s);
+  rr = block_sum<NT>(rr, red_s);
+  if (threadIdx.x == 0) {
+    atomicAdd(c.rz_new + sys, rz);
+    atomicAdd(c.rr + sys, rr);
+  }
+}
+
+__global__ void k_cg_scalars(CgBatch c) {
+  for (int s = threadIdx.x; s < c.nsys; s += blockDim.x) {
+    if (c.status[s] != kActive) continue;
+    c.iters[s] += 1;
+    const double rzn = c.rz_new[s];
+    c.beta[s] = c.rz[s] != 0 ? rzn / c.rz[s] : 0.0;
+    c.rz[s] = rzn;
+    if (c.rr[s] <= c.tol2 * c.bb[s]) c.status[s] = kVerify;
+    else if (c.iters[s] >= c.max_it) c.status[s] = kStopped;
+    c.pq[s] = 0;
+    c.rz_new[s] = 0;
+    c.rr[s] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_cg_direction(CgBatch c) {
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  if (c.status[sys] != kActive) return;
+  const double beta = c.beta[sys];
+  const double* z = c.dinv ? c.z : c.r;
+  const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = fma_rn(beta, c.p[i], z[i]);
+}
+
+// Zero the true-residual accumulators of the masked systems.
+__global__ void k_cg_pre_residual(CgBatch c, int mask) {
+  for (int s = threadIdx.x; s < c.nsys; s += blockDim.x)
+    if ((mask >> c.status[s]) & 1) {
+      c.rrt[s] = 0;
+      c.rz[s] = 0;
+    }
+}
+
+__global__ void k_cg_post_residual(CgBatch c, int mask, int init) {
+  for (int s = threadIdx.x; s < c.nsys; s += blockDim.x) {
+    if (!((mask >> c.status[s]) & 1)) continue;
+    const bool ok = c.rrt[s] <= c.tol2 * c.bb[s];
+    if (init) {
+      c.iters[s] = 0;
+      c.pq[s] = c.rz_new[s] = c.rr[s] = 0;
+      c.status[s] = ok ? kDone : kRestart;
+    } else if (c.status[s] == kVerify) {
+      c.status[s] = ok ? kDone : (c.iters[s] >= c.max_it ? kStopped : kRestart);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_cg_restart(CgBatch c, int all) {
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  if (!all && c.status[sys] != kRestart) return;
+  const double* z = c.dinv ? c.z : c.r;
+  const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = z[i];
+}
+
+__global__ void k_cg_activate(CgBatch c) {
+  for (int s = threadIdx.x; s < c.nsys; s += blockDim.x)
+    if (c.status[s] == kRestart) c.status[s] = kActive;
+}
+
+__global__ void __launch_bounds__(NT) k_cg_norms(CgBatch c) {
+  __shared__ double red_s[NT / kWarp];
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  double bb = 0;
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) bb = fma_rn(c.b[i], c.b[i], bb);
+  bb = block_sum<NT>(bb, red_s);
+  if (threadIdx.x == 0) atomicAdd(c.bb + sys, bb);
+}
+
+__global__ void k_diag_inv(const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                           const double* __restrict__ vals, long n, double* __restrict__ dinv) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double d = 0;
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++)
+      if (colidx[j] == i) d += vals[j];
+    dinv[i] = d != 0 ? 1.0 / d : 1.0;
+  }
+}
+
+template <class K>
+cudaError_t prepare(K kernel, size_t smem) {
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+template <class V, int ITEMS>
+cudaError_t launch_dot(const CgBatch& c, cudaStream_t s) {
+  constexpr size_t smem = stage_bytes<V, ITEMS>();
+  static cudaError_t ready = prepare(k_cg_spmv_dot<V, ITEMS>, smem);
+  if (ready != cudaSuccess) return ready;
+  k_cg_spmv_dot<V, ITEMS><<<c.nblocks, NT, smem, s>>>(c);
+  return cudaGetLastError();
+}
+
+template <int ITEMS>
+cudaError_t launch_res(const CgBatch& c, int mask, cudaStream_t s) {
+  constexpr size_t smem = stage_bytes<double, ITEMS>();
+  static cudaError_t ready = prepare(k_cg_residual<ITEMS>, smem);
+  if (ready != cudaSuccess) return ready;
+  k_cg_residual<ITEMS><<<c.nblocks, NT, smem, s>>>(c, mask);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t cg_spmv_dot(const CgBatch& c, cudaStream_t s) {
+  if (c.nblocks == 0) return cudaSuccess;
+  const int key = c.prec * 100 + c.items;
+  switch (key) {
+    case kF64 * 100 + 4: return launch_dot<double, 4>(c, s);
+    case kF64 * 100 + 8: return launch_dot<double, 8>(c, s);
+    case kF32 * 100 + 4: return launch_dot<float, 4>(c, s);
+    case kF32 * 100 + 8: return launch_dot<float, 8>(c, s);
+    case kBF16 * 100 + 4: return launch_dot<__nv_bfloat16, 4>(c, s);
+    case kBF16 * 100 + 8: return launch_dot<__nv_bfloat16, 8>(c, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t cg_update(const CgBatch& c, cudaStream_t s) {
+  if (c.nchunks == 0) return cudaSuccess;
+  k_cg_update<<<c.nchunks, NT, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_scalars(const CgBatch& c, cudaStream_t s) {
+  k_cg_scalars<<<1, 256, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_direction(const CgBatch& c, cudaStream_t s) {
+  if (c.nchunks == 0) return cudaSuccess;
+  k_cg_direction<<<c.nchunks, NT, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_true_residual(const CgBatch& c, int mask, bool init, cudaStream_t s) {
+  k_cg_pre_residual<<<1, 256, 0, s>>>(c, mask);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (c.nblocks) {
+    e = c.items == 4 ? launch_res<4>(c, mask, s) : launch_res<8>(c, mask, s);
+    if (e != cudaSuccess) return e;
+  }
+  k_cg_post_residual<<<1, 256, 0, s>>>(c, mask, init ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_restart(const CgBatch& c, bool all, cudaStream_t s) {
+  if (c.nchunks) k_cg_restart<<<c.nchunks, NT, 0, s>>>(c, all ? 1 : 0);
+  k_cg_activate<<<1, 256, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_norms(const CgBatch& c, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(c.bb, 0, sizeof(double) * c.nsys, s);
+  if (e != cudaSuccess || c.nchunks == 0) return e;
+  k_cg_norms<<<c.nchunks, NT, 0, s>>>(c);
+  return cudaGetLastError();
+}
+
+cudaError_t csr_diag_inv(const int* rowptr, const int* colidx, const double* vals, long n,
+                         double* dinv, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (int)std::min<long>((n + 255) / 256, 152L * 16);
+  k_diag_inv<<<grid, 256, 0, s>>>(rowptr, colidx, vals, n, dinv);
+  return cudaGetLastError();
+}
+
+}  // namespace tbsla_gpu

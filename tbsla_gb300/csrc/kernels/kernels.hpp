@@ -31,6 +31,27 @@ struct CsrArgs {
 };
 // y[row] = (A x)[row] for every row of the partition.
 cudaError_t csr_spmv(const CsrArgs& a, const double* x, double* y, cudaStream_t s);
+// Merge-path CSR SpMV (the default CSR kernel): tiles of 256*items items of
+// the merged (row ends, entries) sequence; coord[ntiles+1] holds each tile's
+// first row, carry_row / carry_val[ntiles] are per-tile scratch.
+struct MergeArgs {
+  const void* vals;
+  int prec;
+  const int* rowptr;
+  const int* colidx;
+  int n;
+  long nnz;  // rowptr[n] - rowptr[0]
+  int f_col;
+  int items;  // 4, 8 or 16
+  const int* coord;
+  long ntiles;
+  int* carry_row;
+  double* carry_val;
+};
+long merge_tiles(int n, long nnz, int items);
+cudaError_t csr_merge_setup(const int* rowptr, int n, long nnz, int items, int* coord, cudaStream_t s);
+cudaError_t csr_merge_spmv(const MergeArgs& a, const double* x, double* y, cudaStream_t s);
+
 // Row-block partition of a CSR row pointer (host): blocks of consecutive
 // rows with at most `tile` entries and at most 256 rows each; a row longer
 // than `tile` forms a block on its own.  Returns the boundaries.
@@ -68,6 +89,52 @@ cudaError_t csr_pagerank_batched_step(const CsrArgs& a, int n_row, int nvec, con
 // CTAs of the persistent PageRank kernels (resident capacity of the GPU).
 int csr_pagerank_grid(int items, int prec);
 int csr_pagerank_batched_grid(int prec);
+
+// ---- batched CG over a block-diagonal concatenation of systems -------------------
+// Per-system status: ACTIVE iterates; VERIFY has a recursive residual below
+// the tolerance and waits for the FP64 true-residual check; DONE passed it;
+// STOPPED hit the iteration limit.
+enum CgStatus { kActive = 0, kVerify = 1, kDone = 2, kStopped = 3, kRestart = 4 };
+struct CgBatch {
+  int nsys;
+  long n;
+  const int* rowptr;
+  const int* colidx;
+  const void* vals;  // storage precision `prec` (the iteration's SpMV)
+  int prec;
+  const double* vals64;  // FP64 values (true residual)
+  const int* blocks;     // SpMV row-block partition, no block spans two systems
+  const int* block_sys;
+  int nblocks;
+  int items;
+  const int* chunks;  // vector row chunks, no chunk spans two systems
+  const int* chunk_sys;
+  int nchunks;
+  const double* dinv;  // Jacobi: 1/diag(A); nullptr = unpreconditioned
+  const double* b;
+  double *x, *r, *z, *p, *q;  // z == r when unpreconditioned
+  // per-system scalars (rrt: squared FP64 true residual of the last check)
+  double *rz, *rz_new, *pq, *rr, *bb, *beta, *rrt;
+  int* status;
+  int* iters;
+  double tol2;
+  int max_it;
+};
+cudaError_t cg_spmv_dot(const CgBatch& c, cudaStream_t s);   // q = A p; pq += p.q
+cudaError_t cg_update(const CgBatch& c, cudaStream_t s);     // x += a p; r -= a q; z = M r; dots
+cudaError_t cg_scalars(const CgBatch& c, cudaStream_t s);    // beta, status, iteration counts
+cudaError_t cg_direction(const CgBatch& c, cudaStream_t s);  // p = z + beta p
+// r = b - A64 x, z = M r, rr = r.r, rz = r.z for systems whose status is in
+// `mask` (bit per status); then each VERIFY system becomes DONE (true residual
+// within tolerance) or RESTART; with `init` every system is set from the result.
+cudaError_t cg_true_residual(const CgBatch& c, int mask, bool init, cudaStream_t s);
+// p = z for RESTART systems (then ACTIVE), or for every system with `all`.
+cudaError_t cg_restart(const CgBatch& c, bool all, cudaStream_t s);
+// bb = b.b per system.
+cudaError_t cg_norms(const CgBatch& c, cudaStream_t s);
+// Diagonal inverse of a CSR matrix (rows without a diagonal entry get 1).
+cudaError_t csr_diag_inv(const int* rowptr, const int* colidx, const double* vals, long n,
+                         double* dinv, cudaStream_t s);
 
 // ---- ELL (column-major device copy) -------------------------------------------
 cudaError_t ell_spmv(const void* vals, int prec, const int* cols, int ln_row, int max_col,

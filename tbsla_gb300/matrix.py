@@ -247,6 +247,11 @@ class MatrixCSR(Matrix):
     def set_tile(self, nnz_per_block: int):
         check(lib.tbsla_matrix_set_csr_tile(self._h, nnz_per_block), "set_csr_tile")
 
+    MERGE, ROWBLOCK = 0, 1
+
+    def set_algorithm(self, algorithm: int, items: int = 8):
+        check(lib.tbsla_matrix_set_csr_algorithm(self._h, algorithm, items), "set_csr_algorithm")
+
     # project generators
     def fill_uniform_rows(self, n, k, seed):
         check(lib.tbsla_matrix_fill_uniform_rows(self._h, n, k, seed), "fill_uniform_rows")
@@ -328,6 +333,41 @@ class MatrixDENSE(Matrix):
 
 FORMATS = {L.COO: MatrixCOO, L.SCOO: MatrixSCOO, L.CSR: MatrixCSR, L.ELL: MatrixELL,
            L.DENSE: MatrixDENSE}
+
+
+class Batch:
+    """Many SPD CSR systems solved together by batched CG (tbsla_batch_*)."""
+
+    def __init__(self, systems, precision=L.F64):
+        self._systems = list(systems)  # the device copy is built from their arrays
+        arr = (C.c_void_p * len(systems))(*[s._h.value for s in systems])
+        h = C.c_void_p()
+        check(lib.tbsla_batch_create(C.byref(h), arr, len(systems), precision), "batch_create")
+        self._h = h
+        ns = C.c_int()
+        off = (C.c_long * (len(systems) + 1))()
+        check(lib.tbsla_batch_rows(self._h, C.byref(ns), off))
+        self.offsets = np.array(off[:], np.int64)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib.tbsla_batch_destroy(h)
+            self._h = C.c_void_p()
+
+    def cg(self, rhs: np.ndarray, x: np.ndarray | None = None, max_iterations=10000, rel_tol=1e-8,
+           precond=0, refresh=50, graph_iters=0):
+        rhs = _f64(rhs, "rhs")
+        x = np.zeros_like(rhs) if x is None else _f64(x, "x")
+        ns = len(self.offsets) - 1
+        its = np.zeros(ns, np.int32)
+        rr = np.zeros(ns)
+        st = lib.tbsla_batch_cg(self._h, _ptr(rhs), _ptr(x), max_iterations, rel_tol, precond, refresh,
+                                graph_iters, its.ctypes.data_as(C.POINTER(C.c_int)),
+                                rr.ctypes.data_as(C.POINTER(C.c_double)))
+        if st not in (L.OK, L.ERR_NOT_CONVERGED):
+            check(st, "batch_cg")
+        return x, its, rr, st == L.OK
 
 
 def fill_uniform(n: int, lo: float, hi: float, seed: int, out: np.ndarray | None = None) -> np.ndarray:

@@ -1,0 +1,99 @@
+"""CG parity (src/mpi/matrix/CG.cpp:32-73, restated in the oracle with the
+argument order fixed and a relative stop test): GPU CG / Jacobi-PCG, single
+and batched over systems of uneven size, in FP64 and in FP32 / BF16 value
+storage with FP64 residual replacement, must reach the same 1e-8 relative
+residual as the oracle, verified in FP64 on the host."""
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-8
+
+
+def diffusion(T, n, seed):
+    m = T.MatrixCSR()
+    m.fill_diffusion7(n, 1.0, 8.0, seed)
+    return m
+
+
+def true_rel_residual(m, x, b):
+    a = m.arrays()
+    ax = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x)
+    return np.linalg.norm(b - ax) / np.linalg.norm(b)
+
+
+@pytest.mark.parametrize("precond", [0, 1])
+def test_cg_single_matches_oracle(gpu, precond):
+    T = gpu
+    m = diffusion(T, 16, 3)
+    n = 16 ** 3
+    b = T.fill_uniform(n, -1.0, 1.0, 3)
+    x, it, rr, ok = m.CG(b, max_iterations=5000, rel_tol=TOL, precond=precond)
+    assert ok and rr <= TOL
+    assert true_rel_residual(m, x, b) <= TOL
+    a = m.arrays()
+    dinv = None
+    if precond:
+        d = np.zeros(n)
+        rows = np.repeat(np.arange(n), np.diff(a["rowptr"]))
+        diag = rows == a["colidx"]
+        d[rows[diag]] = a["values"][diag]
+        dinv = 1.0 / d
+    xo, ito, rro = oracle.cg(a["rowptr"], a["colidx"], a["values"], b, rel_tol=TOL, diag_inv=dinv)
+    assert rro <= TOL
+    # same algorithm in FP64: the iteration counts agree closely
+    assert abs(it - ito) <= max(3, 0.05 * ito), (it, ito)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-6
+
+
+@pytest.mark.parametrize("prec", ["f32"])
+def test_cg_narrow_storage_reaches_fp64_residual(gpu, prec):
+    """FP32 SpMV inside the iteration, FP64 true residual every 50
+    iterations and at convergence: the FP64-verified 1e-8 is still met."""
+    T = gpu
+    m = diffusion(T, 20, 5)
+    m.set_precision(T.F32)
+    n = 20 ** 3
+    b = T.fill_uniform(n, -1.0, 1.0, 5)
+    x, it, rr, ok = m.CG(b, max_iterations=20000, rel_tol=TOL, precond=1, refresh=50)
+    assert ok and rr <= TOL
+    m.set_precision(T.F64)
+    assert true_rel_residual(m, x, b) <= TOL
+
+
+def test_batched_uneven_sizes(gpu):
+    T = gpu
+    sizes = [8, 12, 16, 6, 20, 10, 14]
+    systems = [diffusion(T, s, 100 + i) for i, s in enumerate(sizes)]
+    for precision in (T.F64, T.F32):
+        batch = T.Batch(systems, precision)
+        off = batch.offsets
+        rhs = np.concatenate([T.fill_uniform(s ** 3, -1.0, 1.0, 200 + i) for i, s in enumerate(sizes)])
+        for precond in (0, 1):
+            x, its, rr, ok = batch.cg(rhs, max_iterations=5000, rel_tol=TOL, precond=precond, graph_iters=7)
+            assert ok and (rr <= TOL).all()
+            for k, m in enumerate(systems):
+                xs, bs = x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]
+                assert true_rel_residual(m, xs, bs) <= TOL, (k, precision, precond)
+            # bigger systems need more iterations
+            assert its[sizes.index(20)] > its[sizes.index(6)]
+
+
+def test_iteration_limit_is_reported(gpu):
+    T = gpu
+    m = diffusion(T, 16, 7)
+    b = T.fill_uniform(16 ** 3, -1.0, 1.0, 7)
+    x, it, rr, ok = m.CG(b, max_iterations=5, rel_tol=TOL)
+    assert not ok and it == 5 and rr > TOL
+
+
+def test_start_vector_is_used(gpu):
+    """x0 = the solution: converged before the first iteration."""
+    T = gpu
+    m = diffusion(T, 10, 9)
+    b = T.fill_uniform(1000, -1.0, 1.0, 9)
+    x, it, rr, ok = m.CG(b, rel_tol=1e-12)
+    x2, it2, rr2, ok2 = m.CG(b, x=x.copy(), rel_tol=1e-6)
+    assert ok2 and it2 == 0

@@ -147,15 +147,27 @@ def powerlaw(T, n, seed=5, **kw):
     return m
 
 
-@pytest.mark.parametrize("tile", [1024, 2048, 4096])
-def test_powerlaw_csr_fp64(gpu, tile):
+CSR_KERNELS = [("merge", 4), ("merge", 8), ("merge", 16), ("rowblock", 1024), ("rowblock", 2048),
+               ("rowblock", 4096)]
+
+
+def set_kernel(m, kind, p):
+    if kind == "merge":
+        m.set_algorithm(m.MERGE, p)
+    else:
+        m.set_algorithm(m.ROWBLOCK)
+        m.set_tile(p)
+
+
+@pytest.mark.parametrize("kind,p", CSR_KERNELS)
+def test_powerlaw_csr_fp64(gpu, kind, p):
     """Zipf(2) rows (mean 16, up to 4096 entries, 30% near-diagonal) at
-    n = 2^18: every row within the FP64 tolerance of the oracle, for each
-    block budget of the row-block partition."""
+    n = 2^18: every row within the FP64 tolerance of the oracle, for both
+    CSR kernels and each of their work-split parameters."""
     T = gpu
     n = 1 << 18
     m = powerlaw(T, n)
-    m.set_tile(tile)
+    set_kernel(m, kind, p)
     a = m.arrays()
     x = T.fill_uniform(n, 0.0, 1.0, 1)
     y = m.spmv(x)
@@ -164,9 +176,11 @@ def test_powerlaw_csr_fp64(gpu, tile):
     assert oracle.rel_err_normalized(y, ref, scale) <= TOL
 
 
-def test_long_and_empty_rows(gpu):
-    """Rows longer than the block budget (single-row blocks, several CTA
-    passes), empty rows between them, a one-row matrix."""
+@pytest.mark.parametrize("kind,p", CSR_KERNELS)
+def test_long_and_empty_rows(gpu, kind, p):
+    """Rows longer than a tile / block (spanning several merge tiles, or
+    single-row blocks with several CTA passes), runs of empty rows, a
+    one-row matrix; for both CSR kernels."""
     T = gpu
     n = 3000
     lens = np.zeros(n, np.int64)
@@ -182,6 +196,7 @@ def test_long_and_empty_rows(gpu):
     va = rng.uniform(-1, 1, nnz)
     x = rng.uniform(0, 1, n)
     m = T.MatrixCSR.from_arrays(n, n, rp, ci, va)
+    set_kernel(m, kind, p)
     y = np.full(n, 7.0)
     m.Ax(y, x)
     ref = oracle.csr_ax(rp, ci, va, x)
@@ -189,7 +204,15 @@ def test_long_and_empty_rows(gpu):
     assert oracle.rel_err_normalized(y, ref, scale) <= TOL
     assert (y[lens == 0] == 0).all()
     one = T.MatrixCSR.from_arrays(1, 5, [0, 3], [0, 2, 4], [1.0, 2.0, 3.0])
+    set_kernel(one, kind, p)
     assert np.array_equal(one.spmv(np.array([1.0, 1, 1, 1, 2])), [9.0])
+    # all rows empty but the last; a matrix whose row pointer starts past 0
+    rp2 = np.array([5, 5, 5, 5, 9], np.int32)
+    ci2 = np.array([0, 0, 0, 0, 0, 1, 2, 3, 0], np.int32)
+    va2 = np.array([9.0] * 5 + [1.0, 2.0, 3.0, 4.0])
+    m2 = T.MatrixCSR.from_arrays(4, 4, rp2, ci2, va2, nnz=9)
+    set_kernel(m2, kind, p)
+    assert np.array_equal(m2.spmv(np.array([1.0, 10, 100, 1000])), [0, 0, 0, 3214.0])
 
 
 def test_empty_matrices_leave_output(gpu):
