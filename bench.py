@@ -47,7 +47,9 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--n", type=int, default=1 << 24)
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
-    p.add_argument("--tile", type=int, default=2048)
+    p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
+    p.add_argument("--algo", choices=["merge", "rowblock"], default="merge")
+    p.add_argument("--items", type=int, default=8, help="merge kernel: items per thread")
     p.add_argument("--no-forms", action="store_true", help="skip the FP32 / BF16 side measurements")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     a = p.parse_args()
@@ -133,6 +135,25 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def job_throughput(local_ms: float, local_bytes: int, ws: int, device: str = "cuda"):
+    """Replicas: the job's time is the slowest rank's, its bytes the sum over
+    ranks (every rank processes its own copy of the workload).  Returns
+    (max time in ms, whole-job GB/s)."""
+    total_ms = local_ms
+    total_bytes = local_bytes
+    if ws > 1:
+        import torch
+        import torch.distributed as td
+
+        t = torch.tensor([local_ms], device=device, dtype=torch.float64)
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        total_ms = float(t.item())
+        b = torch.tensor([float(local_bytes)], device=device, dtype=torch.float64)
+        td.all_reduce(b, op=td.ReduceOp.SUM)
+        total_bytes = float(b.item())
+    return total_ms, total_bytes / (total_ms * 1e-3) / 1e9
+
+
 def dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -202,6 +223,7 @@ def run_ours(a):
     nnz = m.get_nnz()
     t_gen = time.time() - t0
     m.set_tile(a.tile)
+    m.set_algorithm(m.MERGE if a.algo == "merge" else m.ROWBLOCK, a.items)
     prec = {"f64": T.F64, "f32": T.F32, "bf16": T.BF16}[a.prec]
     s_v = {"f64": 8, "f32": 4, "bf16": 2}[a.prec]
     m.set_precision(prec)
@@ -239,13 +261,8 @@ def run_ours(a):
     clocks = clk.stop()
     if ws > 1:
         torch.distributed.barrier()
-    total_ms = sum(step_ms)
-    if ws > 1:
-        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms, value = job_throughput(sum(step_ms), B * a.steps, ws, "cuda")
     ms_step = total_ms / a.steps
-    value = ws * B * a.steps / (total_ms * 1e-3) / 1e9
     kernel_gbs = B / (statistics.mean(step_ms) * 1e-3) / 1e9
     peak, peak_kind = peaks()
 
@@ -310,7 +327,8 @@ def run_ours(a):
         "data": "synthetic: seeded generator (power-law rows, seed 1), no dataset",
         "config": {"workload": f"csr_spmv_powerlaw_n{n}_mean16_zipf2_max4096_local30pct_{a.prec}",
                    "format": "CSR", "n": n, "nnz": nnz, "value_dtype": a.prec, "x_y_dtype": "f64",
-                   "bytes_per_step": B, "block_budget_nnz": a.tile,
+                   "bytes_per_step": B, "csr_kernel": a.algo,
+                   "work_split": (f"{a.items} items/thread" if a.algo == "merge" else f"{a.tile} nnz/block"),
                    "l2": "flushed (256 MB write) between steps; inputs 3.2+ GB > L2",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": kernel_gbs, "peak": peak, "unit": "GB/s",

@@ -35,10 +35,23 @@ namespace {
 
 constexpr int NT = 256;
 
+// Staged entries are stored at e + e/32 (one pad slot per 32): the striped
+// writes stay conflict-free and the per-thread sequential reads, whose lanes
+// sit about ITEMS entries apart, spread over more banks.
+__device__ __forceinline__ int padded(int e) { return e + (e >> 5); }
+
+// Padded staging slots, rounded up to a multiple of 8 so that every region
+// of the dynamic shared memory (doubles, then values of 8, 4 or 2 bytes,
+// then ints) starts 16-byte aligned.
+template <int ITEMS>
+constexpr int merge_slots() {
+  return ((NT * ITEMS + (NT * ITEMS) / 32 + 1) + 7) / 8 * 8;
+}
+
 template <class V, int ITEMS>
 constexpr size_t merge_smem() {
-  // row ends (TILE + 1 ints), x (TILE doubles), values (TILE V)
-  return (size_t)(NT * ITEMS + 1) * sizeof(int) + (size_t)NT * ITEMS * (sizeof(double) + sizeof(V)) + 16;
+  // x (padded TILE doubles), values (padded TILE V), row ends (TILE + 1 ints)
+  return (size_t)merge_slots<ITEMS>() * (sizeof(double) + sizeof(V)) + (size_t)(NT * ITEMS + 1) * sizeof(int);
 }
 
 struct ThreadState {
@@ -73,9 +86,11 @@ __global__ void __launch_bounds__(NT) k_csr_merge(const V* __restrict__ vals, co
                                                  double* __restrict__ carry_val) {
   constexpr int TILE = NT * ITEMS;
   extern __shared__ __align__(16) unsigned char smem[];
+  constexpr int SLOTS = merge_slots<ITEMS>();
+  static_assert(SLOTS % 8 == 0, "staging regions must stay 16-byte aligned");
   double* s_x = reinterpret_cast<double*>(smem);
-  V* s_v = reinterpret_cast<V*>(smem + (size_t)TILE * sizeof(double));
-  int* s_end = reinterpret_cast<int*>(smem + (size_t)TILE * (sizeof(double) + sizeof(V)));
+  V* s_v = reinterpret_cast<V*>(smem + (size_t)SLOTS * sizeof(double));
+  int* s_end = reinterpret_cast<int*>(smem + (size_t)SLOTS * (sizeof(double) + sizeof(V)));
   __shared__ ThreadState s_ts[NT];
   __shared__ int s_start[NT + 1];
 
@@ -107,8 +122,8 @@ __global__ void __launch_bounds__(NT) k_csr_merge(const V* __restrict__ vals, co
     for (int k = 0; k < ITEMS; k++) {
       const int e = k * NT + tid;
       if (e < nj) {
-        s_x[e] = ld_gather(x + c[k] - f_col);
-        s_v[e] = v[k];
+        s_x[padded(e)] = ld_gather(x + c[k] - f_col);
+        s_v[padded(e)] = v[k];
       }
     }
   }
@@ -152,8 +167,15 @@ __global__ void __launch_bounds__(NT) k_csr_merge(const V* __restrict__ vals, co
         acc = 0;
         it++;
       }
-      acc = fma_rn(widen(s_v[jt + k]), s_x[jt + k], acc);
     }
+    // Reconverge before the multiply-add so that it issues once for the
+    // whole warp (lanes past their last entry add 0 * 0).
+    __syncwarp();
+    const int e = padded(min(jt + k, TILE - 1));
+    const bool live = k < m;
+    const double av = live ? widen(s_v[e]) : 0.0;
+    const double xv = live ? s_x[e] : 0.0;
+    acc = fma_rn(av, xv, acc);
   }
   while (it < it_end) {  // row ends after the last entry of the range
     if (!ended) {

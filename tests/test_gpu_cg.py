@@ -73,7 +73,7 @@ def test_batched_uneven_sizes(gpu):
         rhs = np.concatenate([T.fill_uniform(s ** 3, -1.0, 1.0, 200 + i) for i, s in enumerate(sizes)])
         for precond in (0, 1):
             x, its, rr, ok = batch.cg(rhs, max_iterations=5000, rel_tol=TOL, precond=precond, graph_iters=7)
-            assert ok and (rr <= TOL).all()
+            assert ok and (rr <= TOL).all(), (precision, precond, its, rr)
             for k, m in enumerate(systems):
                 xs, bs = x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]
                 assert true_rel_residual(m, xs, bs) <= TOL, (k, precision, precond)
