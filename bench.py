@@ -48,7 +48,9 @@ def parse_args():
     p.add_argument("--n", type=int, default=1 << 24)
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
-    p.add_argument("--algo", choices=["merge", "rowblock"], default="merge")
+    p.add_argument("--algo", choices=["sell", "merge", "rowblock"], default="sell")
+    p.add_argument("--sell", type=str, default="128,1024,16384",
+                   help="sliced-ELL kernel: short_thr,long_thr,sigma")
     p.add_argument("--items", type=int, default=8, help="merge kernel: items per thread")
     p.add_argument("--no-forms", action="store_true", help="skip the FP32 / BF16 side measurements")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -223,7 +225,8 @@ def run_ours(a):
     nnz = m.get_nnz()
     t_gen = time.time() - t0
     m.set_tile(a.tile)
-    m.set_algorithm(m.MERGE if a.algo == "merge" else m.ROWBLOCK, a.items)
+    m.set_algorithm({"sell": m.SELL, "merge": m.MERGE, "rowblock": m.ROWBLOCK}[a.algo], a.items)
+    m.set_sell_params(*[int(t) for t in a.sell.split(",")])
     prec = {"f64": T.F64, "f32": T.F32, "bf16": T.BF16}[a.prec]
     s_v = {"f64": 8, "f32": 4, "bf16": 2}[a.prec]
     m.set_precision(prec)
@@ -328,7 +331,9 @@ def run_ours(a):
         "config": {"workload": f"csr_spmv_powerlaw_n{n}_mean16_zipf2_max4096_local30pct_{a.prec}",
                    "format": "CSR", "n": n, "nnz": nnz, "value_dtype": a.prec, "x_y_dtype": "f64",
                    "bytes_per_step": B, "csr_kernel": a.algo,
-                   "work_split": (f"{a.items} items/thread" if a.algo == "merge" else f"{a.tile} nnz/block"),
+                   "work_split": {"merge": f"{a.items} items/thread", "rowblock": f"{a.tile} nnz/block",
+                                  "sell": f"short<= {a.sell.split(',')[0]} per {a.sell.split(',')[2]}-row window, "
+                                          f"warp per row > {a.sell.split(',')[1]}"}[a.algo],
                    "l2": "flushed (256 MB write) between steps; inputs 3.2+ GB > L2",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": kernel_gbs, "peak": peak, "unit": "GB/s",

@@ -166,13 +166,22 @@ int tbsla_matrix_device_bytes(const tbsla_matrix* m, size_t* bytes);
 /* CSR: block budget of the row-block partition (nnz per block, multiple of
  * 256, default 2048); changing it rebuilds the partition. */
 int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
-/* CSR SpMV kernel: TBSLA_CSR_MERGE (default; merge-path split, `items`
- * row ends + entries per thread, 4/8/16) or TBSLA_CSR_ROWBLOCK (row-block
- * adaptive; items ignored, see tbsla_matrix_set_csr_tile).  Changing it
- * rebuilds the device copy. */
+/* CSR SpMV kernel: TBSLA_CSR_SELL (default; sliced-ELL device layout, one
+ * lane per row in slices of 32 rows of similar length, one warp per very
+ * long row; see tbsla_matrix_set_sell_params), TBSLA_CSR_MERGE (merge-path
+ * split, `items` row ends + entries per thread, 4/8/16) or
+ * TBSLA_CSR_ROWBLOCK (row-block adaptive, see tbsla_matrix_set_csr_tile).
+ * `items` is used by TBSLA_CSR_MERGE only.  Changing it rebuilds the device
+ * copy. */
 #define TBSLA_CSR_MERGE 0
 #define TBSLA_CSR_ROWBLOCK 1
+#define TBSLA_CSR_SELL 2
 int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items);
+/* Sliced-ELL classes: rows of at most short_thr (<= 255) entries are sorted
+ * by length within windows of `sigma` consecutive rows, rows up to long_thr
+ * over the whole matrix, longer rows get a warp each (defaults 128, 1024,
+ * 16384). */
+int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma);
 
 /* ---- SpMV: Matrix::Ax / Matrix::spmv (Matrix.hpp:14-15) ----------------------- */
 /* r <- A v (CSR, ELL: overwrite; returns without touching r when nnz == 0)

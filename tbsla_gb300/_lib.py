@@ -94,6 +94,7 @@ _SIGS = {
     "tbsla_matrix_device_bytes": (I, [P, C.POINTER(C.c_size_t)]),
     "tbsla_matrix_set_csr_tile": (I, [P, I]),
     "tbsla_matrix_set_csr_algorithm": (I, [P, I, I]),
+    "tbsla_matrix_set_sell_params": (I, [P, I, I, I]),
     "tbsla_batch_create": (I, [C.POINTER(P), C.POINTER(P), I, I]),
     "tbsla_batch_destroy": (I, [P]),
     "tbsla_batch_rows": (I, [P, IP, C.POINTER(L)]),

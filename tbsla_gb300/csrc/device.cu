@@ -88,6 +88,10 @@ struct DeviceMatrix {
   double* carry_val = nullptr;
   long ntiles = 0;
   int merge_items = 8;
+  SellPlan sell{};            // CSR sliced-ELL layout (device pointers)
+  void* svals = nullptr;
+  int* scols = nullptr;
+  unsigned* sell_counter = nullptr;
   long nnz = 0;  // entries on the device
   int min_row = 0, max_row = -1;
   double* x = nullptr;
@@ -107,7 +111,9 @@ struct DeviceMatrix {
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t,
                     (void*)counter, (void*)partials, (void*)result, (void*)coord, (void*)carry_row,
-                    (void*)carry_val})
+                    (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)sell.long_rows,
+                    (void*)sell.med_rows, (void*)sell.med_off, (void*)sell.short_meta,
+                    (void*)sell.short_base, (void*)sell.short_off})
       if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -213,6 +219,59 @@ int upload_ints(DeviceMatrix* d, int** dst, const int* host, size_t n) {
   return status_of(cudaMemcpyAsync(*dst, host, n * 4, cudaMemcpyHostToDevice, d->stream));
 }
 
+template <class T>
+int upload_array(DeviceMatrix* d, T** dst, const T* src, size_t n) {
+  int st = dalloc(dst, std::max<size_t>(n, 1));
+  if (st) return st;
+  d->bytes += n * sizeof(T);
+  if (n == 0) return TBSLA_OK;
+  return status_of(cudaMemcpyAsync(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice, d->stream));
+}
+
+SellArgs sell_args(const tbsla_matrix* m, const DeviceMatrix* d) {
+  SellArgs a;
+  a.vals = d->vals;
+  a.prec = d->prec;
+  a.rowptr = d->idx0;
+  a.colidx = d->idx1;
+  a.f_col = m->info.f_col;
+  a.svals = d->svals;
+  a.scols = d->scols;
+  a.plan = d->sell;
+  return a;
+}
+
+// Sliced-ELL device layout of a CSR matrix: the plan (row classes, slices,
+// offsets) is made on the host from the row pointer, the slice arrays are
+// filled on the device from the CSR copy.
+int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
+  SellPlan hp;
+  sell_plan_build(m->idx0.data(), m->info.ln_row, m->sell_short, m->sell_long, m->sell_sigma, &hp);
+  SellPlan& dp = d->sell;
+  dp = hp;
+  dp.long_rows = nullptr;
+  dp.med_rows = dp.short_meta = dp.short_base = nullptr;
+  dp.med_off = dp.short_off = nullptr;
+  int st = upload_array(d, &dp.long_rows, hp.long_rows, (size_t)hp.nlong);
+  if (!st) st = upload_array(d, &dp.med_rows, hp.med_rows, 32 * (size_t)hp.nmed);
+  if (!st) st = upload_array(d, &dp.med_off, hp.med_off, (size_t)hp.nmed + 1);
+  if (!st) st = upload_array(d, &dp.short_meta, hp.short_meta, 32 * (size_t)hp.nshort);
+  if (!st) st = upload_array(d, &dp.short_base, hp.short_base, (size_t)hp.nshort);
+  if (!st) st = upload_array(d, &dp.short_off, hp.short_off, (size_t)hp.nshort + 1);
+  if (!st) st = status_of(cudaStreamSynchronize(d->stream));  // host plan arrays are freed next
+  sell_plan_free(&hp);
+  if (st) return st;
+  if (cudaMalloc(&d->svals, std::max<size_t>(dp.sell_len, 1) * prec_size(d->prec)) != cudaSuccess) {
+    cudaGetLastError();
+    return TBSLA_ERR_ALLOC;
+  }
+  if ((st = dalloc(&d->scols, std::max<size_t>(dp.sell_len, 1))) || (st = dalloc(&d->sell_counter, 2))) return st;
+  d->bytes += (size_t)dp.sell_len * (prec_size(d->prec) + 4);
+  TRY(cudaMemsetAsync(d->sell_counter, 0, 2 * sizeof(unsigned), d->stream));
+  TRY(sell_fill(sell_args(m, d), d->svals, d->scols, d->stream));
+  return TBSLA_OK;
+}
+
 int build(const tbsla_matrix* m, DeviceMatrix* d) {
   const tbsla_info& I = m->info;
   TRY(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
@@ -243,6 +302,10 @@ int build(const tbsla_matrix* m, DeviceMatrix* d) {
         return st;
       d->bytes += (size_t)d->ntiles * 16 + 4;
       TRY(csr_merge_setup(d->idx0, I.ln_row, enz, d->merge_items, d->coord, d->stream));
+      if (d->algo == 2) {
+        st = build_sell(m, d);
+        if (st) return st;
+      }
       return status_of(cudaStreamSynchronize(d->stream));
     }
     case TBSLA_ELL: {
@@ -367,6 +430,7 @@ int ax_device(const tbsla_matrix* m, DeviceMatrix* d, double* r, const double* v
   switch (m->format) {
     case TBSLA_CSR:
       if (d->algo == 1) return status_of(csr_spmv(csr_args(m, d), v, r, s));
+      if (d->algo == 2) return status_of(sell_spmv(sell_args(m, d), v, r, d->sell_counter, s));
       {
         MergeArgs a{d->vals, d->prec, d->idx0, d->idx1, I.ln_row, d->nnz - m->idx0[0], I.f_col,
                     d->merge_items, d->coord, d->ntiles, d->carry_row, d->carry_val};
@@ -536,6 +600,7 @@ int dev_normalize_cols(tbsla_matrix* m, const double* s) {
   // keep the host arrays (the reference layout) in step with the device
   TRY(cudaMemcpyAsync(m->values.data(), v64, d->nnz * 8, cudaMemcpyDeviceToHost, str));
   if (owned) TRY(convert_values(v64, d->vals, d->prec, d->nnz, str));
+  if (d->algo == 2 && d->svals) TRY(sell_fill(sell_args(m, d), d->svals, d->scols, str));  // slice copy
   TRY(cudaStreamSynchronize(str));
   if (owned) cudaFree(v64);
   return TBSLA_OK;

@@ -55,8 +55,11 @@ struct tbsla_matrix {
   tbsla_impl::Buf<int> idx0, idx1;
   int precision = TBSLA_F64;
   int csr_tile = 2048;     // row-block budget (entries per block)
-  int csr_algo = 0;        // 0: merge path (default), 1: row blocks
+  int csr_algo = 2;        // 0: merge path, 1: row blocks, 2: sliced ELL (default)
   int merge_items = 8;     // merge path: items per thread
+  int sell_short = 128;    // sliced ELL: rows up to this length sorted per window
+  int sell_long = 1024;    // rows longer than this: one warp per row
+  int sell_sigma = 16384;  // window of consecutive rows sorted together
   int device = 0;
   mutable tbsla_impl::DeviceMatrix* dev = nullptr;
 

@@ -52,6 +52,45 @@ long merge_tiles(int n, long nnz, int items);
 cudaError_t csr_merge_setup(const int* rowptr, int n, long nnz, int items, int* coord, cudaStream_t s);
 cudaError_t csr_merge_spmv(const MergeArgs& a, const double* x, double* y, cudaStream_t s);
 
+// Sliced-ELL CSR SpMV (SELL-C-sigma with C = 32), for GB300's FP64 pipe that
+// costs one slot per warp-instruction whatever the active lanes.  Work items,
+// processed one per warp in this order (longest first, dynamically fetched):
+//   long rows   (len > long_thr):  one warp per row, read from the CSR arrays;
+//   medium rows (short_thr < len <= long_thr): slices of 32 rows sorted by
+//               length over the whole matrix, one lane per row;
+//   short rows  (len <= short_thr): slices of 32 rows sorted by length within
+//               windows of `sigma` consecutive rows, one lane per row.
+// Slices are stored lane-interleaved (entry j of lane l at off + 32 j + l);
+// lanes past their row's end issue no loads, so padding costs no traffic.
+struct SellPlan {
+  int n = 0, short_thr = 0, long_thr = 0, sigma = 0;
+  int nlong = 0, nmed = 0, nshort = 0;
+  long sell_len = 0;  // elements of the slice arrays
+  int* long_rows = nullptr;   // [nlong]
+  int* med_rows = nullptr;    // [32 * nmed], -1 for unused lanes
+  long* med_off = nullptr;    // [nmed + 1]
+  int* short_meta = nullptr;  // [32 * nshort]: (row - base) << 8 | len, -1 unused
+  int* short_base = nullptr;  // [nshort]
+  long* short_off = nullptr;  // [nshort + 1] (continues after the medium slices)
+};
+// Host: plan from a row pointer (arrays allocated with new[]).
+void sell_plan_build(const int* rowptr, int n, int short_thr, int long_thr, int sigma, SellPlan* p);
+void sell_plan_free(SellPlan* p);
+struct SellArgs {
+  const void* vals;  // CSR copy (long rows are read from it)
+  int prec;
+  const int* rowptr;
+  const int* colidx;
+  int f_col;
+  const void* svals;  // slice arrays (medium + short rows)
+  const int* scols;
+  SellPlan plan;  // device pointers
+};
+// Fills the slice arrays from the CSR device arrays.
+cudaError_t sell_fill(const SellArgs& a, void* svals, int* scols, cudaStream_t s);
+// y[row] = (A x)[row]; counter: 2 unsigned of zeroed scratch, reset by the kernel.
+cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s);
+
 // Row-block partition of a CSR row pointer (host): blocks of consecutive
 // rows with at most `tile` entries and at most 256 rows each; a row longer
 // than `tile` forms a block on its own.  Returns the boundaries.

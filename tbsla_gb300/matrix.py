@@ -247,10 +247,13 @@ class MatrixCSR(Matrix):
     def set_tile(self, nnz_per_block: int):
         check(lib.tbsla_matrix_set_csr_tile(self._h, nnz_per_block), "set_csr_tile")
 
-    MERGE, ROWBLOCK = 0, 1
+    MERGE, ROWBLOCK, SELL = 0, 1, 2
 
     def set_algorithm(self, algorithm: int, items: int = 8):
         check(lib.tbsla_matrix_set_csr_algorithm(self._h, algorithm, items), "set_csr_algorithm")
+
+    def set_sell_params(self, short_thr: int = 128, long_thr: int = 1024, sigma: int = 16384):
+        check(lib.tbsla_matrix_set_sell_params(self._h, short_thr, long_thr, sigma), "set_sell_params")
 
     # project generators
     def fill_uniform_rows(self, n, k, seed):

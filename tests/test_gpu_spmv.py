@@ -147,12 +147,16 @@ def powerlaw(T, n, seed=5, **kw):
     return m
 
 
-CSR_KERNELS = [("merge", 4), ("merge", 8), ("merge", 16), ("rowblock", 1024), ("rowblock", 2048),
+CSR_KERNELS = [("sell", (128, 1024, 16384)), ("sell", (4, 40, 64)), ("sell", (255, 255, 1 << 20)),
+               ("merge", 4), ("merge", 8), ("merge", 16), ("rowblock", 1024), ("rowblock", 2048),
                ("rowblock", 4096)]
 
 
 def set_kernel(m, kind, p):
-    if kind == "merge":
+    if kind == "sell":
+        m.set_algorithm(m.SELL)
+        m.set_sell_params(*p)
+    elif kind == "merge":
         m.set_algorithm(m.MERGE, p)
     else:
         m.set_algorithm(m.ROWBLOCK)
