@@ -249,12 +249,16 @@ void orc_csr_normalize_cols(int ln_row, int f_col, long nnz, double* values,
  *     applies it to a buffer that is then discarded);
  *   - the mass of dangling nodes is redistributed along the teleport vector
  *     instead of being lost and renormalised away;
- * so that, with S = sum(x_k) and D = sum over dangling j of x_k[j],
- *   x_{k+1}[i] = beta*(A x_k)[i] + (beta*D + (1-beta)*S) * t_i
+ * and each iterate is normalised by its sum before it is used, as
+ * pagerank_normalization does (Matrix.cpp:106-146).  With S = sum(x_k),
+ * D = sum over dangling j of x_k[j] and s = 1/S:
+ *   x_{k+1}[i] = (beta*(A x_k)[i])*s + (beta*D*s + (1-beta)) * t_i
  * with t_i = 1/n (uniform) or teleport[i] (personalised).  The error is the
- * L1 change sum_i |x_{k+1}[i] - x_k[i]|; the loop stops when it drops below
- * epsilon (if stop_early) or after max_iterations.  The result is divided
- * by its sum at the end.  Returns the number of iterations done.          */
+ * L1 change sum_i |x_{k+1}[i] - x_k[i]*s|; the loop stops when it drops
+ * below epsilon (if stop_early) or after max_iterations.  The result is
+ * divided by its sum at the end.  Returns the number of iterations done.
+ * (The normalisation keeps the iteration stationary when the stored
+ * column-stochastic values are rounded, e.g. to FP32.)                    */
 int orc_pagerank(int n, const int* rowptr, const int* colidx, const double* values,
                  const unsigned char* dangling, const double* teleport, double beta,
                  double epsilon, int max_iterations, int stop_early, double* x,
@@ -273,12 +277,13 @@ int orc_pagerank(int n, const int* rowptr, const int* colidx, const double* valu
     }
     for (int i = 0; i < n; i++) y[i] = 0;
     orc_csr_ax(n, 0, nnz, values, rowptr, colidx, cur, y);
-    double t = beta * D + (1.0 - beta) * S;
+    double s = 1.0 / S;
+    double t = beta * D * s + (1.0 - beta);
     double c = t / n;
     err = 0;
     for (int i = 0; i < n; i++) {
-      double xn = beta * y[i] + (teleport ? t * teleport[i] : c);
-      err += fabs(xn - cur[i]);
+      double xn = beta * y[i] * s + (teleport ? t * teleport[i] : c);
+      err += fabs(xn - cur[i] * s);
       y[i] = xn;
     }
     double* tmp = cur;

@@ -645,7 +645,7 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
     for (void* p : {(void*)x0, (void*)x1, (void*)coef, (void*)flags, (void*)dang})
       if (p) cudaFree(p);
   };
-  if ((st = dalloc(&x0, n)) || (st = dalloc(&x1, n)) || (st = dalloc(&coef, 2)) ||
+  if ((st = dalloc(&x0, n)) || (st = dalloc(&x1, n)) || (st = dalloc(&coef, 4)) ||
       (st = dalloc(&flags, 2)) || (st = d->ctl(3, grid)) || (st = dangling_flags(m, d, &dang))) {
     cleanup();
     return st;
@@ -662,12 +662,14 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
     S += x_init;
     if (hd[i]) D += x_init;
   }
-  double c0 = beta * D + (1.0 - beta) * S;
+  // scale and teleport weight of step 0, as the oracle forms them
+  const double s0 = 1.0 / S;
+  double c0[2] = {s0, beta * D * s0 + (1.0 - beta)};
   vec_fill(x0, x_init, n, s);
-  cudaMemcpyAsync(coef, &c0, 8, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(coef, c0, 16, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
   CsrArgs a = csr_args(m, d);
-  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 1, flags, flags + 1};
+  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 2, flags, flags + 1};
   Ctl ctl{d->counter, d->partials, d->result};
   int launched = 0, hflags[2] = {0, 0};
   const int chunk = 8;
@@ -675,8 +677,8 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
     int k = std::min(chunk, max_it - launched);
     for (int j = 0; j < k; j++, launched++) {
       const bool even = (launched % 2) == 0;
-      p.coef_in = coef + (even ? 0 : 1);
-      p.coef_out = coef + (even ? 1 : 0);
+      p.coef_in = coef + (even ? 0 : 2);
+      p.coef_out = coef + (even ? 2 : 0);
       cudaError_t e = I.nnz > 0 ? csr_pagerank_step(a, even ? x0 : x1, even ? x1 : x0, p, ctl, grid, s)
                                 : cudaErrorInvalidValue;
       if (e != cudaSuccess) {
@@ -729,7 +731,7 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
       if (p) cudaFree(p);
   };
   if ((st = dalloc(&X0, nn)) || (st = dalloc(&X1, nn)) || (st = dalloc(&T, nn)) ||
-      (st = dalloc(&coef, 64)) || (st = dalloc(&flags, 2)) || (st = d->ctl(96, grid)) ||
+      (st = dalloc(&coef, 128)) || (st = dalloc(&flags, 2)) || (st = d->ctl(96, grid)) ||
       (st = dangling_flags(m, d, &dang))) {
     cleanup();
     return st;
@@ -746,21 +748,26 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
     S += x_init;
     if (hd[i]) D += x_init;
   }
-  std::vector<double> c0(nvec, beta * D + (1.0 - beta) * S);
+  const double s0 = 1.0 / S;
+  std::vector<double> c0(64, 0.0);
+  for (int k = 0; k < nvec; k++) {
+    c0[k] = s0;
+    c0[32 + k] = beta * D * s0 + (1.0 - beta);
+  }
   vec_fill(X0, x_init, (long)nn, s);
   cudaMemcpyAsync(T, tele, nn * 8, cudaMemcpyHostToDevice, s);
-  cudaMemcpyAsync(coef, c0.data(), nvec * 8, cudaMemcpyHostToDevice, s);
+  cudaMemcpyAsync(coef, c0.data(), 64 * 8, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
   CsrArgs a = csr_args(m, d);
-  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 32, flags, flags + 1};
+  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 64, flags, flags + 1};
   Ctl ctl{d->counter, d->partials, d->result};
   int launched = 0, hflags[2] = {0, 0};
   while (launched < max_it && !hflags[0]) {
     int k = std::min(8, max_it - launched);
     for (int j = 0; j < k; j++, launched++) {
       const bool even = (launched % 2) == 0;
-      p.coef_in = coef + (even ? 0 : 32);
-      p.coef_out = coef + (even ? 32 : 0);
+      p.coef_in = coef + (even ? 0 : 64);
+      p.coef_out = coef + (even ? 64 : 0);
       cudaError_t e = csr_pagerank_batched_step(a, n, nvec, even ? X0 : X1, even ? X1 : X0, T, p, ctl, grid, s);
       if (e != cudaSuccess) {
         cleanup();

@@ -50,16 +50,19 @@ __global__ void __launch_bounds__(NT) k_csr_spmv(CsrArgs a, const double* __rest
   csr_block<V, ITEMS>(a, blockIdx.x, x, epi, nullptr, stage, sm, pol);
 }
 
+// x is used normalised by its sum S (scale s = 1/S, carried from the
+// previous step): y_i = (beta * (A x)_i) * s + c_i with c_i = t / n or
+// t * tele_i, t = (beta * D) * s + (1 - beta).
 struct EpiPageRank {
   double* y;
   const double* x;
   const unsigned char* dangling;
   const double* tele;
-  double beta, coef, coef_u;
-  __device__ __forceinline__ void emit(int row, double s, double* red) const {
-    const double t = tele ? mul_rn(coef, tele[row]) : coef_u;
-    const double yn = add_rn(mul_rn(beta, s), t);
-    red[0] = add_rn(red[0], fabs(yn - x[row]));
+  double beta, s, t, c_uniform;
+  __device__ __forceinline__ void emit(int row, double sum, double* red) const {
+    const double c = tele ? mul_rn(t, tele[row]) : c_uniform;
+    const double yn = add_rn(mul_rn(mul_rn(beta, sum), s), c);
+    red[0] = add_rn(red[0], fabs(yn - mul_rn(x[row], s)));
     red[1] = add_rn(red[1], yn);
     if (dangling[row]) red[2] = add_rn(red[2], yn);
     y[row] = yn;
@@ -74,8 +77,8 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   __shared__ Smem sm;
   if (*(volatile int*)p.done) return;  // converged in an earlier launch: no-op
   const uint64_t pol = policy_evict_first();
-  const double coef = p.coef_in[0];
-  EpiPageRank epi{y, x, p.dangling, p.tele, p.beta, coef, coef / p.n_nodes};
+  const double s = p.coef_in[0], t = p.coef_in[1];
+  EpiPageRank epi{y, x, p.dangling, p.tele, p.beta, s, t, t / p.n_nodes};
   double red[3] = {0, 0, 0};
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm))
     csr_block<V, ITEMS>(a, b, x, epi, red, stage, sm, pol);
@@ -84,7 +87,9 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   int* done = p.done;
   int* iters = p.iters;
   reduce_and_finish<3>(ctl, red, sm, [=] __device__(double* r) {
-    coef_out[0] = add_rn(mul_rn(beta, r[2]), mul_rn(1.0 - beta, r[1]));
+    const double s1 = 1.0 / r[1];
+    coef_out[0] = s1;
+    coef_out[1] = add_rn(mul_rn(mul_rn(beta, r[2]), s1), 1.0 - beta);
     *iters += 1;
     if (r[0] < eps) *done = 1;
   });
@@ -106,7 +111,8 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
   const V* vals = static_cast<const V*>(a.vals);
   const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   const bool active = lane < nvec;
-  const double coef = active ? p.coef_in[lane] : 0.0;
+  const double sc = active ? p.coef_in[lane] : 0.0;        // 1 / sum of the vector
+  const double tc = active ? p.coef_in[kWarp + lane] : 0.0;  // teleport weight
   double err = 0, sum = 0, dsum = 0;
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm)) {
     const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
@@ -130,8 +136,8 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
       }
       if (active) {
         const size_t o = (size_t)row * nvec + lane;
-        const double yn = add_rn(mul_rn(p.beta, acc), mul_rn(coef, T[o]));
-        err = add_rn(err, fabs(yn - X[o]));
+        const double yn = add_rn(mul_rn(mul_rn(p.beta, acc), sc), mul_rn(tc, T[o]));
+        err = add_rn(err, fabs(yn - mul_rn(X[o], sc)));
         sum = add_rn(sum, yn);
         if (p.dangling[row]) dsum = add_rn(dsum, yn);
         Y[o] = yn;
@@ -172,7 +178,9 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
       ctl.result[k] = e;
       ctl.result[nvec + k] = sm_;
       ctl.result[2 * nvec + k] = d;
-      p.coef_out[k] = add_rn(mul_rn(p.beta, d), mul_rn(1.0 - p.beta, sm_));
+      const double s1 = 1.0 / sm_;
+      p.coef_out[k] = s1;
+      p.coef_out[kWarp + k] = add_rn(mul_rn(mul_rn(p.beta, d), s1), 1.0 - p.beta);
       if (!(e < p.eps)) all = 0;
     }
     *p.iters += 1;
