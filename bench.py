@@ -49,7 +49,7 @@ def parse_args():
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
     p.add_argument("--algo", choices=["sell", "merge", "rowblock"], default="sell")
-    p.add_argument("--sell", type=str, default="128,1024,16384",
+    p.add_argument("--sell", type=str, default="64,64,16384",
                    help="sliced-ELL kernel: short_thr,long_thr,sigma")
     p.add_argument("--items", type=int, default=8, help="merge kernel: items per thread")
     p.add_argument("--no-forms", action="store_true", help="skip the FP32 / BF16 side measurements")
@@ -332,8 +332,9 @@ def run_ours(a):
                    "format": "CSR", "n": n, "nnz": nnz, "value_dtype": a.prec, "x_y_dtype": "f64",
                    "bytes_per_step": B, "csr_kernel": a.algo,
                    "work_split": {"merge": f"{a.items} items/thread", "rowblock": f"{a.tile} nnz/block",
-                                  "sell": f"short<= {a.sell.split(',')[0]} per {a.sell.split(',')[2]}-row window, "
-                                          f"warp per row > {a.sell.split(',')[1]}"}[a.algo],
+                                  "sell": f"one lane per row <= {a.sell.split(',')[0]} sorted per "
+                                          f"{a.sell.split(',')[2]}-row window, else 2..32 lanes per row, slices "
+                                          f"<= {a.sell.split(',')[1]} steps; {a.items} steps/lane in flight"}[a.algo],
                    "l2": "flushed (256 MB write) between steps; inputs 3.2+ GB > L2",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": kernel_gbs, "peak": peak, "unit": "GB/s",

@@ -166,21 +166,23 @@ int tbsla_matrix_device_bytes(const tbsla_matrix* m, size_t* bytes);
 /* CSR: block budget of the row-block partition (nnz per block, multiple of
  * 256, default 2048); changing it rebuilds the partition. */
 int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
-/* CSR SpMV kernel: TBSLA_CSR_SELL (default; sliced-ELL device layout, one
- * lane per row in slices of 32 rows of similar length, one warp per very
- * long row; see tbsla_matrix_set_sell_params), TBSLA_CSR_MERGE (merge-path
- * split, `items` row ends + entries per thread, 4/8/16) or
- * TBSLA_CSR_ROWBLOCK (row-block adaptive, see tbsla_matrix_set_csr_tile).
- * `items` is used by TBSLA_CSR_MERGE only.  Changing it rebuilds the device
- * copy. */
+/* CSR SpMV kernel: TBSLA_CSR_SELL (default; sliced-ELL device layout,
+ * slices of 32 lanes over rows of similar length, see
+ * tbsla_matrix_set_sell_params; `items` = steps per lane in flight, 4/8/16,
+ * default 8), TBSLA_CSR_MERGE (merge-path split, `items` row ends + entries
+ * per thread, 4/8/16) or TBSLA_CSR_ROWBLOCK (row-block adaptive, see
+ * tbsla_matrix_set_csr_tile; `items` unused).  Changing the kernel or the
+ * merge split rebuilds the device copy. */
 #define TBSLA_CSR_MERGE 0
 #define TBSLA_CSR_ROWBLOCK 1
 #define TBSLA_CSR_SELL 2
 int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items);
-/* Sliced-ELL classes: rows of at most short_thr (<= 255) entries are sorted
- * by length within windows of `sigma` consecutive rows, rows up to long_thr
- * over the whole matrix, longer rows get a warp each (defaults 128, 1024,
- * 16384). */
+/* Sliced-ELL layout: rows of at most short_thr (1..255) entries take one
+ * lane each and are sorted by length within windows of `sigma` (32..2^23)
+ * consecutive rows; longer rows take the fewest lanes (a power of two up to
+ * 32) that keep their slice at most long_thr steps wide and are sorted by
+ * length over the whole matrix (defaults 64, 64, 16384).  Changing them
+ * rebuilds the device copy. */
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma);
 
 /* ---- SpMV: Matrix::Ax / Matrix::spmv (Matrix.hpp:14-15) ----------------------- */
@@ -217,10 +219,14 @@ int tbsla_normalize_cols(tbsla_matrix* m, const double* s);
 int tbsla_make_stochastic(tbsla_matrix* m, double* s);
 
 /* ---- PageRank (src/mpi/matrix/Matrix.cpp:540-602, 641-790), CSR only --------
- * A column-stochastic (zero columns = dangling nodes).  x_0 = 1/n and
- *   x_{k+1} = beta*A x_k + (beta*D_k + (1-beta)*S_k) * t
- * with S_k = sum x_k, D_k = sum of x_k over dangling nodes, t = 1/n.  Stops
- * when sum|x_{k+1}-x_k| < epsilon or after max_iterations; the result is
+ * A column-stochastic (zero columns = dangling nodes).  x_0 = 1/n and, with
+ * each iterate normalised by its sum S_k before use,
+ *   x_{k+1} = beta*A x_k/S_k + (1 - beta*M_k/S_k) * t,  t = 1/n,
+ * M_k = sum_j w_j x_k[j], w_j = sum of column j of A as stored.  For exact
+ * column-stochastic A this is the usual (1-beta) + beta*D_k/S_k dangling-node
+ * redistribution (D_k = mass on dangling nodes); with FP32/BF16 storage it
+ * also returns the mass the rounding loses.  Stops when
+ * sum|x_{k+1} - x_k/S_k| < epsilon or after max_iterations; the result is
  * divided by its sum.  *iterations receives the count, *error the last L1
  * change.  Returns TBSLA_ERR_NOT_CONVERGED (result still written) when the
  * limit is hit first. */

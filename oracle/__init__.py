@@ -165,12 +165,11 @@ def dangling_of(rowptr, colidx, n):
 
 
 def pagerank(rowptr, colidx, values, beta=0.85, epsilon=1e-10, max_iterations=1000, stop_early=True,
-             teleport=None, dangling=None):
+             teleport=None):
     n = len(rowptr) - 1
-    dangling = dangling_of(rowptr, colidx, n) if dangling is None else dangling
     x = np.zeros(n)
     err = C.c_double()
-    it = lib().orc_pagerank(I(n), _p(rowptr), _p(colidx), _p(values), _p(dangling), _p(teleport), D(beta),
+    it = lib().orc_pagerank(I(n), _p(rowptr), _p(colidx), _p(values), _p(teleport), D(beta),
                             D(epsilon), I(max_iterations), I(int(stop_early)), _p(x), C.byref(err))
     return x, it, err.value
 

@@ -250,35 +250,41 @@ void orc_csr_normalize_cols(int ln_row, int f_col, long nnz, double* values,
  *   - the mass of dangling nodes is redistributed along the teleport vector
  *     instead of being lost and renormalised away;
  * and each iterate is normalised by its sum before it is used, as
- * pagerank_normalization does (Matrix.cpp:106-146).  With S = sum(x_k),
- * D = sum over dangling j of x_k[j] and s = 1/S:
- *   x_{k+1}[i] = (beta*(A x_k)[i])*s + (beta*D*s + (1-beta)) * t_i
- * with t_i = 1/n (uniform) or teleport[i] (personalised).  The error is the
- * L1 change sum_i |x_{k+1}[i] - x_k[i]*s|; the loop stops when it drops
- * below epsilon (if stop_early) or after max_iterations.  The result is
- * divided by its sum at the end.  Returns the number of iterations done.
- * (The normalisation keeps the iteration stationary when the stored
- * column-stochastic values are rounded, e.g. to FP32.)                    */
+ * pagerank_normalization does (Matrix.cpp:106-146).  With w_j the sum of
+ * column j of the values given (1 for a node with out-links when A is
+ * column-stochastic, 0 for a dangling node), S = sum(x_k),
+ * M = sum_j w_j x_k[j] and s = 1/S:
+ *   x_{k+1}[i] = (beta*(A x_k)[i])*s + (1 - (beta*M)*s) * t_i
+ * with t_i = 1/n (uniform) or teleport[i] (personalised, summing to 1).
+ * For exactly column-stochastic A, 1 - beta*M*s = (1 - beta) + beta*D*s
+ * (D = mass on dangling nodes): the usual dangling-node redistribution.
+ * For values rounded in storage (FP32, BF16) it also hands back the mass
+ * the rounding loses, so every iterate sums to 1 and the L1 change below
+ * goes to zero.  The error is sum_i |x_{k+1}[i] - x_k[i]*s|; the loop stops
+ * when it drops below epsilon (if stop_early) or after max_iterations.  The
+ * result is divided by its sum at the end.  Returns the iterations done.  */
 int orc_pagerank(int n, const int* rowptr, const int* colidx, const double* values,
-                 const unsigned char* dangling, const double* teleport, double beta,
-                 double epsilon, int max_iterations, int stop_early, double* x,
-                 double* last_error) {
+                 const double* teleport, double beta, double epsilon, int max_iterations,
+                 int stop_early, double* x, double* last_error) {
   double* y = (double*)calloc((size_t)n, sizeof(double));
   double* cur = (double*)malloc(sizeof(double) * (size_t)n);
+  double* w = (double*)calloc((size_t)n, sizeof(double));
   long nnz = rowptr[n];
+  for (int i = 0; i < n; i++)
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) w[colidx[j]] += values[j];
   for (int i = 0; i < n; i++) cur[i] = 1.0 / n;
   int it = 0;
   double err = 0;
   while (it < max_iterations) {
-    double S = 0, D = 0;
+    double S = 0, M = 0;
     for (int i = 0; i < n; i++) {
       S += cur[i];
-      if (dangling && dangling[i]) D += cur[i];
+      M += w[i] * cur[i];
     }
     for (int i = 0; i < n; i++) y[i] = 0;
     orc_csr_ax(n, 0, nnz, values, rowptr, colidx, cur, y);
     double s = 1.0 / S;
-    double t = beta * D * s + (1.0 - beta);
+    double t = 1.0 - beta * M * s;
     double c = t / n;
     err = 0;
     for (int i = 0; i < n; i++) {
@@ -296,6 +302,7 @@ int orc_pagerank(int n, const int* rowptr, const int* colidx, const double* valu
   for (int i = 0; i < n; i++) s += cur[i];
   for (int i = 0; i < n; i++) x[i] = cur[i] / s;
   if (last_error) *last_error = err;
+  free(w);
   free(y);
   free(cur);
   return it;

@@ -53,9 +53,8 @@ void orc_csr_normalize_cols(int ln_row, int f_col, long nnz, double* values,
 
 /* ---- PageRank / CG restatements (reference bugs fixed, see tbsla_oracle.c) */
 int orc_pagerank(int n, const int* rowptr, const int* colidx, const double* values,
-                 const unsigned char* dangling, const double* teleport, double beta,
-                 double epsilon, int max_iterations, int stop_early, double* x,
-                 double* last_error);
+                 const double* teleport, double beta, double epsilon, int max_iterations,
+                 int stop_early, double* x, double* last_error);
 int orc_cg(int n, const int* rowptr, const int* colidx, const double* values,
            const double* diag_inv, const double* b, double* x, int max_iterations,
            double rel_tol, double* rel_residual);

@@ -13,8 +13,6 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
-#include <cstdio>
-#include <cstdlib>
 #include <vector>
 
 #include "device.hpp"
@@ -302,7 +300,6 @@ int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterati
   std::vector<int> hs(ns);
   long it = 0, last_refresh = 0;
   const bool narrow = B->prec != TBSLA_F64;
-  const bool trace = std::getenv("TBSLA_CG_TRACE") != nullptr;  // per-replay scalars of system 0
   for (;;) {
     CK(cudaGraphLaunch(B->graph, s));
     it += K;
@@ -314,15 +311,6 @@ int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterati
       verify |= v == kVerify;
     }
     const bool refresh_due = narrow && refresh > 0 && active && it - last_refresh >= refresh;
-    if (trace) {
-      std::vector<double> sc((size_t)kNScal * ns);
-      std::vector<int> hi(ns);
-      cudaMemcpy(sc.data(), B->scal, sc.size() * 8, cudaMemcpyDeviceToHost);
-      cudaMemcpy(hi.data(), B->iters, ns * sizeof(int), cudaMemcpyDeviceToHost);
-      std::fprintf(stderr, "[cg] it %ld sys0 status %d iters %d rz %.3e rz_new %.3e pq %.3e rr %.3e bb %.3e beta %.3e rrt %.3e%s\n",
-                   it, hs[0], hi[0], sc[0], sc[ns], sc[2 * ns], sc[3 * ns], sc[4 * ns], sc[5 * ns], sc[6 * ns],
-                   refresh_due ? " refresh" : "");
-    }
     if (verify || refresh_due) {
       const int mask = (1 << kVerify) | (refresh_due ? 1 << kActive : 0);
       CK(cg_true_residual(c, mask, false, s));

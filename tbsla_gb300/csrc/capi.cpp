@@ -253,7 +253,7 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block) {
 }
 
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma) {
-  if (!m || short_thr < 1 || short_thr > 255 || long_thr < short_thr || sigma < 32 || sigma > (1 << 22))
+  if (!m || short_thr < 1 || short_thr > 255 || long_thr < 1 || sigma < 32 || sigma > (1 << 23))
     return TBSLA_ERR_INVALID_ARG;
   if (m->sell_short != short_thr || m->sell_long != long_thr || m->sell_sigma != sigma) {
     m->invalidate();
@@ -266,8 +266,9 @@ int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, i
 
 int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items) {
   if (!m || algorithm < TBSLA_CSR_MERGE || algorithm > TBSLA_CSR_SELL ||
-      (algorithm == TBSLA_CSR_MERGE && items != 4 && items != 8 && items != 16))
+      (algorithm != TBSLA_CSR_ROWBLOCK && items != 4 && items != 8 && items != 16))
     return TBSLA_ERR_INVALID_ARG;
+  if (algorithm == TBSLA_CSR_SELL) m->sell_unroll = items;  // a launch parameter only
   if (m->csr_algo != algorithm || (algorithm == TBSLA_CSR_MERGE && m->merge_items != items)) {
     m->invalidate();
     m->csr_algo = algorithm;

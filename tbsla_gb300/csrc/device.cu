@@ -14,6 +14,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <vector>
 
@@ -92,6 +93,8 @@ struct DeviceMatrix {
   void* svals = nullptr;
   int* scols = nullptr;
   unsigned* sell_counter = nullptr;
+  double* colw = nullptr;  // PageRank: column sums of the stored values
+  bool colw_ok = false;
   long nnz = 0;  // entries on the device
   int min_row = 0, max_row = -1;
   double* x = nullptr;
@@ -111,9 +114,8 @@ struct DeviceMatrix {
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t,
                     (void*)counter, (void*)partials, (void*)result, (void*)coord, (void*)carry_row,
-                    (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)sell.long_rows,
-                    (void*)sell.med_rows, (void*)sell.med_off, (void*)sell.short_meta,
-                    (void*)sell.short_base, (void*)sell.short_off})
+                    (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)sell.slice,
+                    (void*)sell.lane, (void*)colw})
       if (p) cudaFree(p);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -237,6 +239,7 @@ SellArgs sell_args(const tbsla_matrix* m, const DeviceMatrix* d) {
   a.f_col = m->info.f_col;
   a.svals = d->svals;
   a.scols = d->scols;
+  a.unroll = m->sell_unroll;
   a.plan = d->sell;
   return a;
 }
@@ -249,15 +252,10 @@ int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
   sell_plan_build(m->idx0.data(), m->info.ln_row, m->sell_short, m->sell_long, m->sell_sigma, &hp);
   SellPlan& dp = d->sell;
   dp = hp;
-  dp.long_rows = nullptr;
-  dp.med_rows = dp.short_meta = dp.short_base = nullptr;
-  dp.med_off = dp.short_off = nullptr;
-  int st = upload_array(d, &dp.long_rows, hp.long_rows, (size_t)hp.nlong);
-  if (!st) st = upload_array(d, &dp.med_rows, hp.med_rows, 32 * (size_t)hp.nmed);
-  if (!st) st = upload_array(d, &dp.med_off, hp.med_off, (size_t)hp.nmed + 1);
-  if (!st) st = upload_array(d, &dp.short_meta, hp.short_meta, 32 * (size_t)hp.nshort);
-  if (!st) st = upload_array(d, &dp.short_base, hp.short_base, (size_t)hp.nshort);
-  if (!st) st = upload_array(d, &dp.short_off, hp.short_off, (size_t)hp.nshort + 1);
+  dp.slice = nullptr;
+  dp.lane = nullptr;
+  int st = upload_array(d, &dp.slice, hp.slice, (size_t)hp.nslices);
+  if (!st) st = upload_array(d, &dp.lane, hp.lane, 32 * (size_t)hp.nslices);
   if (!st) st = status_of(cudaStreamSynchronize(d->stream));  // host plan arrays are freed next
   sell_plan_free(&hp);
   if (st) return st;
@@ -601,6 +599,7 @@ int dev_normalize_cols(tbsla_matrix* m, const double* s) {
   TRY(cudaMemcpyAsync(m->values.data(), v64, d->nnz * 8, cudaMemcpyDeviceToHost, str));
   if (owned) TRY(convert_values(v64, d->vals, d->prec, d->nnz, str));
   if (d->algo == 2 && d->svals) TRY(sell_fill(sell_args(m, d), d->svals, d->scols, str));  // slice copy
+  d->colw_ok = false;
   TRY(cudaStreamSynchronize(str));
   if (owned) cudaFree(v64);
   return TBSLA_OK;
@@ -615,13 +614,62 @@ int dev_make_stochastic(tbsla_matrix* m, double* s) {
 // ---- PageRank ------------------------------------------------------------------------
 
 namespace {
-int dangling_flags(const tbsla_matrix* m, DeviceMatrix* d, unsigned char** flags) {
-  int n = m->info.ln_row;
-  if (cudaMalloc((void**)flags, (size_t)n) != cudaSuccess) {
-    cudaGetLastError();
-    return TBSLA_ERR_ALLOC;
+// A value as the device stores it at precision `prec`, widened back: FP32
+// rounds to nearest even; BF16 rounds the double's bits to 8 significant
+// bits (ties to even), as the device narrowing does.
+double stored_value(double v, int prec) {
+  if (prec == TBSLA_F32) return (double)(float)v;
+  if (prec != TBSLA_BF16) return v;
+  uint64_t b;
+  std::memcpy(&b, &v, 8);
+  if ((b & 0x7ff0000000000000ull) != 0x7ff0000000000000ull) {
+    b += (1ull << 44) - 1 + ((b >> 45) & 1);
+    b &= ~((1ull << 45) - 1);
   }
-  return status_of(csr_dangling(d->idx0, d->idx1, m->info.ln_row, m->info.n_col, *flags, d->stream));
+  double r;
+  std::memcpy(&r, &b, 8);
+  float f = (float)r;
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  u &= 0xffff0000u;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+// PageRank column weights w_j = sum of column j of A as stored (0 for a
+// dangling node), summed on the host in entry order -- deterministic, and
+// the order the oracle uses -- then kept on the device until the values
+// change.
+int column_weights(const tbsla_matrix* m, DeviceMatrix* d) {
+  if (d->colw_ok) return TBSLA_OK;
+  const tbsla_info& I = m->info;
+  std::vector<double> w(I.ln_col, 0.0);
+  const int* rp = m->idx0.data();
+  const int* ci = m->idx1.data();
+  for (int i = 0; i < I.ln_row; i++)
+    for (int j = rp[i]; j < rp[i + 1]; j++) w[ci[j] - I.f_col] += stored_value(m->values[j], d->prec);
+  if (!d->colw) {
+    int st = dalloc(&d->colw, std::max<size_t>(I.ln_col, 1));
+    if (st) return st;
+  }
+  int st = status_of(cudaMemcpyAsync(d->colw, w.data(), w.size() * 8, cudaMemcpyHostToDevice, d->stream));
+  if (!st) st = status_of(cudaStreamSynchronize(d->stream));
+  if (!st) d->colw_ok = true;
+  return st;
+}
+
+// Scale and teleport weight of step 0 from x_0 = 1/n: S and M summed in
+// index order, as the oracle forms them.
+void initial_coefficients(const DeviceMatrix* d, int n, double beta, double x_init, double c[2]) {
+  std::vector<double> w(n);
+  cudaMemcpy(w.data(), d->colw, (size_t)n * 8, cudaMemcpyDeviceToHost);
+  double S = 0, M = 0;
+  for (int i = 0; i < n; i++) {
+    S += x_init;
+    M += w[i] * x_init;
+  }
+  c[0] = 1.0 / S;
+  c[1] = 1.0 - beta * M * c[0];
 }
 }  // namespace
 
@@ -638,38 +686,24 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
   cudaStream_t s = d->stream;
   double *x0 = nullptr, *x1 = nullptr, *coef = nullptr;
   int* flags = nullptr;  // [0] done, [1] iterations
-  unsigned char* dang = nullptr;
   int grid = I.nnz > 0 ? csr_pagerank_grid(d->items, d->prec) : 1;
-  std::vector<unsigned char> hd(n);
   auto cleanup = [&]() {
-    for (void* p : {(void*)x0, (void*)x1, (void*)coef, (void*)flags, (void*)dang})
+    for (void* p : {(void*)x0, (void*)x1, (void*)coef, (void*)flags})
       if (p) cudaFree(p);
   };
   if ((st = dalloc(&x0, n)) || (st = dalloc(&x1, n)) || (st = dalloc(&coef, 4)) ||
-      (st = dalloc(&flags, 2)) || (st = d->ctl(3, grid)) || (st = dangling_flags(m, d, &dang))) {
+      (st = dalloc(&flags, 2)) || (st = d->ctl(3, grid)) || (st = column_weights(m, d))) {
     cleanup();
     return st;
   }
-  // x_0 = 1/n; S_0 and D_0 summed in index order (the oracle's order).
   const double x_init = 1.0 / n;
-  double S = 0, D = 0;
-  if (cudaMemcpyAsync(hd.data(), dang, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess) {
-    cleanup();
-    return TBSLA_ERR_CUDA;
-  }
-  for (int i = 0; i < n; i++) {
-    S += x_init;
-    if (hd[i]) D += x_init;
-  }
-  // scale and teleport weight of step 0, as the oracle forms them
-  const double s0 = 1.0 / S;
-  double c0[2] = {s0, beta * D * s0 + (1.0 - beta)};
+  double c0[2];
+  initial_coefficients(d, n, beta, x_init, c0);
   vec_fill(x0, x_init, n, s);
   cudaMemcpyAsync(coef, c0, 16, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
   CsrArgs a = csr_args(m, d);
-  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 2, flags, flags + 1};
+  PageRankArgs p{beta, (double)n, eps, nullptr, d->colw, coef, coef + 2, flags, flags + 1};
   Ctl ctl{d->counter, d->partials, d->result};
   int launched = 0, hflags[2] = {0, 0};
   const int chunk = 8;
@@ -724,42 +758,31 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   cudaStream_t s = d->stream;
   double *X0 = nullptr, *X1 = nullptr, *T = nullptr, *coef = nullptr;
   int* flags = nullptr;
-  unsigned char* dang = nullptr;
   int grid = csr_pagerank_batched_grid(d->prec);
   auto cleanup = [&]() {
-    for (void* p : {(void*)X0, (void*)X1, (void*)T, (void*)coef, (void*)flags, (void*)dang})
+    for (void* p : {(void*)X0, (void*)X1, (void*)T, (void*)coef, (void*)flags})
       if (p) cudaFree(p);
   };
   if ((st = dalloc(&X0, nn)) || (st = dalloc(&X1, nn)) || (st = dalloc(&T, nn)) ||
       (st = dalloc(&coef, 128)) || (st = dalloc(&flags, 2)) || (st = d->ctl(96, grid)) ||
-      (st = dangling_flags(m, d, &dang))) {
+      (st = column_weights(m, d))) {
     cleanup();
     return st;
   }
-  std::vector<unsigned char> hd(n);
-  if (cudaMemcpyAsync(hd.data(), dang, n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess) {
-    cleanup();
-    return TBSLA_ERR_CUDA;
-  }
   const double x_init = 1.0 / n;
-  double S = 0, D = 0;
-  for (int i = 0; i < n; i++) {
-    S += x_init;
-    if (hd[i]) D += x_init;
-  }
-  const double s0 = 1.0 / S;
+  double cc[2];
+  initial_coefficients(d, n, beta, x_init, cc);
   std::vector<double> c0(64, 0.0);
   for (int k = 0; k < nvec; k++) {
-    c0[k] = s0;
-    c0[32 + k] = beta * D * s0 + (1.0 - beta);
+    c0[k] = cc[0];
+    c0[32 + k] = cc[1];
   }
   vec_fill(X0, x_init, (long)nn, s);
   cudaMemcpyAsync(T, tele, nn * 8, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(coef, c0.data(), 64 * 8, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
   CsrArgs a = csr_args(m, d);
-  PageRankArgs p{beta, (double)n, eps, nullptr, dang, coef, coef + 64, flags, flags + 1};
+  PageRankArgs p{beta, (double)n, eps, nullptr, d->colw, coef, coef + 64, flags, flags + 1};
   Ctl ctl{d->counter, d->partials, d->result};
   int launched = 0, hflags[2] = {0, 0};
   while (launched < max_it && !hflags[0]) {

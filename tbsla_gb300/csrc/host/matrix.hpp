@@ -57,9 +57,10 @@ struct tbsla_matrix {
   int csr_tile = 2048;     // row-block budget (entries per block)
   int csr_algo = 2;        // 0: merge path, 1: row blocks, 2: sliced ELL (default)
   int merge_items = 8;     // merge path: items per thread
-  int sell_short = 128;    // sliced ELL: rows up to this length sorted per window
-  int sell_long = 1024;    // rows longer than this: one warp per row
+  int sell_short = 64;     // sliced ELL: rows up to this length, one lane each, sorted per window
+  int sell_long = 64;      // longer rows: fewest lanes keeping a slice this many steps wide
   int sell_sigma = 16384;  // window of consecutive rows sorted together
+  int sell_unroll = 8;     // steps per lane in flight
   int device = 0;
   mutable tbsla_impl::DeviceMatrix* dev = nullptr;
 

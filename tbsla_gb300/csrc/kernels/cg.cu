@@ -159,6 +159,11 @@ __global__ void k_cg_post_residual(CgBatch c, int mask, int init) {
       c.status[s] = ok ? kDone : kRestart;
     } else if (c.status[s] == kVerify) {
       c.status[s] = ok ? kDone : (c.iters[s] >= c.max_it ? kStopped : kRestart);
+    } else if (c.status[s] == kActive) {
+      // Periodic refresh of a system iterating on a narrowed matrix: the
+      // FP64 residual belongs to another operator than the directions, so
+      // the iteration restarts from it (one step of iterative refinement).
+      c.status[s] = ok ? kDone : kRestart;
     }
   }
 }

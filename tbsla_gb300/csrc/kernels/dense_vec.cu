@@ -118,15 +118,6 @@ __global__ void k_normalize_cols(double* __restrict__ vals, const int* __restric
     }
 }
 
-__global__ void k_mark_cols(const int* __restrict__ rowptr, const int* __restrict__ colidx,
-                            int n_row, unsigned char* has_entry) {
-  const int lane = threadIdx.x % kWarp;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) / kWarp;
-  const int nw = gridDim.x * blockDim.x / kWarp;
-  for (int row = gw; row < n_row; row += nw)
-    for (int j = rowptr[row] + lane; j < rowptr[row + 1]; j += kWarp) has_entry[colidx[j]] = 0;
-}
-
 // Pass 1: CTA b sums rows b, b + grid, ... per column into partials[b][k].
 // With ncol == 1 all 256 threads stride over the vector.
 __global__ void __launch_bounds__(256) k_colsum_pass1(const double* __restrict__ x, long n, int ncol,
@@ -236,14 +227,6 @@ cudaError_t csr_normalize_cols(double* vals, const int* rowptr, const int* colid
                                int f_col, const double* s, cudaStream_t st) {
   if (n_row <= 0) return cudaSuccess;
   k_normalize_cols<<<grid_for((long)n_row * kWarp), 256, 0, st>>>(vals, rowptr, colidx, n_row, f_col, s);
-  return cudaGetLastError();
-}
-
-cudaError_t csr_dangling(const int* rowptr, const int* colidx, int n_row, int n_col,
-                         unsigned char* dangling, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(dangling, 1, (size_t)n_col, st);
-  if (e != cudaSuccess || n_row <= 0) return e;
-  k_mark_cols<<<grid_for((long)n_row * kWarp), 256, 0, st>>>(rowptr, colidx, n_row, dangling);
   return cudaGetLastError();
 }
 

@@ -52,38 +52,38 @@ long merge_tiles(int n, long nnz, int items);
 cudaError_t csr_merge_setup(const int* rowptr, int n, long nnz, int items, int* coord, cudaStream_t s);
 cudaError_t csr_merge_spmv(const MergeArgs& a, const double* x, double* y, cudaStream_t s);
 
-// Sliced-ELL CSR SpMV (SELL-C-sigma with C = 32), for GB300's FP64 pipe that
-// costs one slot per warp-instruction whatever the active lanes.  Work items,
-// processed one per warp in this order (longest first, dynamically fetched):
-//   long rows   (len > long_thr):  one warp per row, read from the CSR arrays;
-//   medium rows (short_thr < len <= long_thr): slices of 32 rows sorted by
-//               length over the whole matrix, one lane per row;
-//   short rows  (len <= short_thr): slices of 32 rows sorted by length within
-//               windows of `sigma` consecutive rows, one lane per row.
-// Slices are stored lane-interleaved (entry j of lane l at off + 32 j + l);
-// lanes past their row's end issue no loads, so padding costs no traffic.
+// Sliced-ELL CSR SpMV (SELL-C-sigma with C = 32) for GB300's FP64 pipe,
+// which costs one slot per warp-instruction whatever the active lanes.  A
+// slice is 32 lanes, each row owning G = 2^g consecutive lanes (entry j of
+// the row on lane j mod G of its group, at step j / G); its entries are
+// stored step-major (step t, lane l at 32 * (offset + t) + l).  Rows of at
+// most short_thr entries take one lane each and are sorted by length within
+// windows of `sigma` consecutive rows; longer rows take the fewest lanes (up
+// to 32) that keep their slice at most long_thr steps wide and are sorted by
+// length over the whole matrix.  One warp per slice, fetched dynamically,
+// widest slices first; lanes past their row's end issue no loads, so
+// padding costs no traffic.
 struct SellPlan {
   int n = 0, short_thr = 0, long_thr = 0, sigma = 0;
-  int nlong = 0, nmed = 0, nshort = 0;
+  int nwide = 0;      // slices sorted over the whole matrix (processed first)
+  int nslices = 0;    // all slices
   long sell_len = 0;  // elements of the slice arrays
-  int* long_rows = nullptr;   // [nlong]
-  int* med_rows = nullptr;    // [32 * nmed], -1 for unused lanes
-  long* med_off = nullptr;    // [nmed + 1]
-  int* short_meta = nullptr;  // [32 * nshort]: (row - base) << 8 | len, -1 unused
-  int* short_base = nullptr;  // [nshort]
-  long* short_off = nullptr;  // [nshort + 1] (continues after the medium slices)
+  int4* slice = nullptr;  // [nslices]: {step offset, width in steps, g, base}
+  int* lane = nullptr;    // [32 * nslices]: base >= 0: (row - base) << 8 | len;
+                          // base = -1: row; -1 for an unused lane
 };
 // Host: plan from a row pointer (arrays allocated with new[]).
 void sell_plan_build(const int* rowptr, int n, int short_thr, int long_thr, int sigma, SellPlan* p);
 void sell_plan_free(SellPlan* p);
 struct SellArgs {
-  const void* vals;  // CSR copy (long rows are read from it)
+  const void* vals;  // CSR copy (the slice arrays are filled from it)
   int prec;
   const int* rowptr;
   const int* colidx;
   int f_col;
-  const void* svals;  // slice arrays (medium + short rows)
+  const void* svals;  // slice arrays
   const int* scols;
+  int unroll;     // steps per lane in flight: 4, 8 or 16
   SellPlan plan;  // device pointers
 };
 // Fills the slice arrays from the CSR device arrays.
@@ -96,18 +96,19 @@ cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* c
 // than `tile` forms a block on its own.  Returns the boundaries.
 void csr_partition(const int* rowptr, int n_row, int tile, int** out, int* nblocks);
 
-// PageRank step on CSR: y = beta*(A x) + c_i, with c_i = coef / n
-// (tele == nullptr) or coef * tele[i]; coef = beta*D + (1-beta)*S read from
-// coef_in[0] (device).  Reductions: result[0] = sum |y - x|, result[1] =
-// sum y, result[2] = sum over dangling rows of y; the last CTA also writes
-// coef_out[0] = beta*result[2] + (1-beta)*result[1] and sets *done when
-// result[0] < eps (a done flag already set makes the launch a no-op).
+// PageRank step on CSR with the iterate carried unnormalised: with
+// s = coef_in[0] = 1/S (S = sum x) and t = coef_in[1],
+//   y_i = (beta * (A x)_i) * s + c_i,  c_i = t / n or t * tele_i.
+// Reductions: L1 change sum |y - x s|, S' = sum y, M' = sum_i colw_i y_i
+// (colw = column sums of A as stored; 0 for a dangling node); the last CTA
+// writes coef_out = {1/S', 1 - beta M'/S'} and sets *done when the change is
+// below eps (a done flag already set makes the launch a no-op).
 struct PageRankArgs {
   double beta;
   double n_nodes;
   double eps;
   const double* tele;
-  const unsigned char* dangling;
+  const double* colw;
   const double* coef_in;
   double* coef_out;
   int* done;
@@ -116,11 +117,11 @@ struct PageRankArgs {
 cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
                               const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s);
 // Batched personalised PageRank step: X, Y, T are n x nvec row-major
-// (nvec <= 32); per column k: Y = beta*A X + coef_k * T[:,k], with
-// coef_k = beta*D_k + (1-beta)*S_k from coef_in[k].  Reductions per column
-// k: result[k] = L1 change, result[nvec + k] = sum, result[2 nvec + k] =
-// dangling sum; the last CTA writes coef_out[k] and sets *done when every
-// column's change is < eps.
+// (nvec <= 32); column k as above with s_k = coef_in[k], t_k =
+// coef_in[32 + k] and c_i = t_k * T[i, k].  Reductions per column k:
+// result[k] = L1 change, result[nvec + k] = S', result[2 nvec + k] = M';
+// the last CTA writes coef_out[k], coef_out[32 + k] and sets *done when
+// every column's change is < eps.
 cudaError_t csr_pagerank_batched_step(const CsrArgs& a, int n_row, int nvec, const double* X,
                                       double* Y, const double* T, const PageRankArgs& p,
                                       Ctl ctl, int grid, cudaStream_t s);
@@ -205,9 +206,6 @@ cudaError_t csr_col_sums(const double* vals, const int* rowptr, const int* colid
 // value /= s[col - f_col] where that is > 0.
 cudaError_t csr_normalize_cols(double* vals, const int* rowptr, const int* colidx, int n_row,
                                int f_col, const double* s, cudaStream_t st);
-// dangling[j] = (column j has no entry), j < n_col.
-cudaError_t csr_dangling(const int* rowptr, const int* colidx, int n_row, int n_col,
-                         unsigned char* dangling, cudaStream_t st);
 // Narrowing copy of FP64 values to the storage precision.
 cudaError_t convert_values(const double* src, void* dst, int prec, long n, cudaStream_t s);
 // Row-major -> column-major transpose of ELL arrays.

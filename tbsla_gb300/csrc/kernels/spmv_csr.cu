@@ -52,11 +52,13 @@ __global__ void __launch_bounds__(NT) k_csr_spmv(CsrArgs a, const double* __rest
 
 // x is used normalised by its sum S (scale s = 1/S, carried from the
 // previous step): y_i = (beta * (A x)_i) * s + c_i with c_i = t / n or
-// t * tele_i, t = (beta * D) * s + (1 - beta).
+// t * tele_i and t = 1 - (beta * M) * s, M = sum_j w_j x_j (w = column sums
+// of A as stored), so that y sums to 1.  Reductions: L1 change, sum y and
+// sum w y (the next step's S and M).
 struct EpiPageRank {
   double* y;
   const double* x;
-  const unsigned char* dangling;
+  const double* colw;
   const double* tele;
   double beta, s, t, c_uniform;
   __device__ __forceinline__ void emit(int row, double sum, double* red) const {
@@ -64,10 +66,15 @@ struct EpiPageRank {
     const double yn = add_rn(mul_rn(mul_rn(beta, sum), s), c);
     red[0] = add_rn(red[0], fabs(yn - mul_rn(x[row], s)));
     red[1] = add_rn(red[1], yn);
-    if (dangling[row]) red[2] = add_rn(red[2], yn);
+    red[2] = add_rn(red[2], mul_rn(colw[row], yn));
     y[row] = yn;
   }
 };
+
+// t of the next step from its S (r1) and M (r2): 1 - (beta * M) / S.
+__device__ __forceinline__ double teleport_weight(double beta, double s1, double m) {
+  return add_rn(1.0, -mul_rn(mul_rn(beta, m), s1));
+}
 
 template <class V, int ITEMS>
 __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __restrict__ x,
@@ -78,7 +85,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   if (*(volatile int*)p.done) return;  // converged in an earlier launch: no-op
   const uint64_t pol = policy_evict_first();
   const double s = p.coef_in[0], t = p.coef_in[1];
-  EpiPageRank epi{y, x, p.dangling, p.tele, p.beta, s, t, t / p.n_nodes};
+  EpiPageRank epi{y, x, p.colw, p.tele, p.beta, s, t, t / p.n_nodes};
   double red[3] = {0, 0, 0};
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm))
     csr_block<V, ITEMS>(a, b, x, epi, red, stage, sm, pol);
@@ -89,7 +96,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   reduce_and_finish<3>(ctl, red, sm, [=] __device__(double* r) {
     const double s1 = 1.0 / r[1];
     coef_out[0] = s1;
-    coef_out[1] = add_rn(mul_rn(mul_rn(beta, r[2]), s1), 1.0 - beta);
+    coef_out[1] = teleport_weight(beta, s1, r[2]);
     *iters += 1;
     if (r[0] < eps) *done = 1;
   });
@@ -113,7 +120,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
   const bool active = lane < nvec;
   const double sc = active ? p.coef_in[lane] : 0.0;        // 1 / sum of the vector
   const double tc = active ? p.coef_in[kWarp + lane] : 0.0;  // teleport weight
-  double err = 0, sum = 0, dsum = 0;
+  double err = 0, sum = 0, dsum = 0;  // L1 change, sum y, sum w y
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm)) {
     const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
     for (int row = r0 + warp; row < r1; row += NT / kWarp) {
@@ -139,7 +146,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
         const double yn = add_rn(mul_rn(mul_rn(p.beta, acc), sc), mul_rn(tc, T[o]));
         err = add_rn(err, fabs(yn - mul_rn(X[o], sc)));
         sum = add_rn(sum, yn);
-        if (p.dangling[row]) dsum = add_rn(dsum, yn);
+        dsum = add_rn(dsum, mul_rn(p.colw[row], yn));
         Y[o] = yn;
       }
     }
@@ -180,7 +187,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
       ctl.result[2 * nvec + k] = d;
       const double s1 = 1.0 / sm_;
       p.coef_out[k] = s1;
-      p.coef_out[kWarp + k] = add_rn(mul_rn(mul_rn(p.beta, d), s1), 1.0 - p.beta);
+      p.coef_out[kWarp + k] = teleport_weight(p.beta, s1, d);
       if (!(e < p.eps)) all = 0;
     }
     *p.iters += 1;

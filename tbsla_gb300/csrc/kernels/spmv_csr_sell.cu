@@ -1,25 +1,26 @@
 // CSR SpMV through a sliced-ELL device layout (SELL-C-sigma, Kreutzer et
-// al., SIAM J. Sci. Comput. 2014, with C = 32 = the warp) -- the default CSR
-// kernel on GB300.
+// al., SIAM J. Sci. Comput. 2014, with C = 32 = the warp, extended with G
+// lanes per row for long rows) -- the default CSR kernel on GB300.
 //
 // Replaces tbsla::cpp::MatrixCSR::Ax (src/cpp/matrix/MatrixCSR.cpp:209-233):
 // y_i = sum_j values_j * v[colidx_j - f_col], overwriting y.
 //
 // Why this layout on GB300: its FP64 pipe accepts one warp-instruction per
-// ~17 cycles per SM whatever the number of active lanes, so the only way to
-// reach the HBM roofline is to issue the one DFMA per entry from full warps
-// and to spend almost nothing else.  Rows are grouped 32 at a time into
-// slices of similar length (one lane per row), so a warp's DFMAs are nearly
-// all live, no reduction across lanes is needed, and the entries of a step
-// are 32 consecutive words (256-byte coalesced loads).  Sorting is done
-// within windows of `sigma` consecutive rows for short rows (x near the
-// diagonal and y stay local), over the whole matrix for medium rows (so that
-// a slice's rows have nearly equal lengths), and the few rows longer than
-// `long_thr` are read straight from the CSR arrays by a whole warp each.
-// Work items (long rows, medium slices, short slices, in that order) are
-// fetched dynamically per warp, longest first.
+// ~16 cycles per SM whatever the number of active lanes, so the only way to
+// reach the memory roofline is to issue the one DFMA per entry from full
+// warps and to spend almost nothing else.  A slice is 32 lanes wide; each
+// row gets G = 2^g consecutive lanes (entry j of a row on lane j mod G of
+// its group, at step j / G), with G the smallest power of two that keeps the
+// slice at most `long_thr` steps wide (G = 1 for rows of up to `short_thr`
+// entries; those are sorted by length within windows of `sigma` consecutive
+// rows, so x near the diagonal and y stay local; longer rows are sorted by
+// length over the whole matrix).  A slice's rows thus have nearly equal
+// lengths, its DFMAs are nearly all live, the entries of a step are 32
+// consecutive words (256-byte coalesced loads) and no work item takes much
+// longer than another: one warp per slice, fetched dynamically, widest first.
 //
-// Each row is summed in entry order with fused multiply-adds.
+// Each lane sums its entries in entry order with fused multiply-adds; G > 1
+// lanes of a row are combined by a fixed butterfly of additions.
 #include <algorithm>
 #include <numeric>
 #include <vector>
@@ -33,124 +34,126 @@ namespace tbsla_gpu {
 namespace {
 
 constexpr int NT = 256;
-constexpr int UNROLL = 4;
+constexpr unsigned FULL = 0xffffffffu;
 
-template <class V>
-__device__ __forceinline__ double slice_rows(const V* __restrict__ sv, const int* __restrict__ sc, long off,
-                                             int len, int width, const double* __restrict__ x, int f_col,
-                                             uint64_t pol) {
-  double acc = 0;
-  for (int j = 0; j < width; j += UNROLL) {
-    // dead lanes keep a zero value and a valid column, so nothing they
-    // might touch is out of bounds
-    V v[UNROLL];
-    int c[UNROLL];
+// K steps of one lane's row: predicated loads (lanes past their row's end
+// issue none, so padding costs no traffic), the K gathers of x in flight
+// together, then K full-warp DFMAs (dead lanes add 0 * 0).
+template <class V, int K>
+__device__ __forceinline__ double steps_k(const V* __restrict__ sv, const int* __restrict__ sc, long off, int j,
+                                          int steps, const double* __restrict__ x, int f_col, uint64_t pol,
+                                          double acc) {
+  V v[K];
+  int c[K];
 #pragma unroll
-    for (int u = 0; u < UNROLL; u++) {
-      v[u] = V(0.0f);
-      c[u] = f_col;
-    }
-#pragma unroll
-    for (int u = 0; u < UNROLL; u++) {
-      if (j + u < len) {
-        v[u] = ld_stream(sv + off + (long)(j + u) * 32, pol);
-        c[u] = ld_stream(sc + off + (long)(j + u) * 32, pol);
-      }
-    }
-    double xv[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; u++) xv[u] = (j + u < len) ? ld_gather(x + c[u] - f_col) : 0.0;
-    __syncwarp();
-#pragma unroll
-    for (int u = 0; u < UNROLL; u++) acc = fma_rn((j + u < len) ? widen(v[u]) : 0.0, xv[u], acc);
+  for (int u = 0; u < K; u++) {
+    v[u] = V(0.0f);
+    c[u] = f_col;
   }
+#pragma unroll
+  for (int u = 0; u < K; u++) {
+    if (j + u < steps) {
+      v[u] = ld_stream(sv + off + (long)(j + u) * 32, pol);
+      c[u] = ld_stream(sc + off + (long)(j + u) * 32, pol);
+    }
+  }
+  double xv[K];
+#pragma unroll
+  for (int u = 0; u < K; u++) xv[u] = (j + u < steps) ? ld_gather(x + c[u] - f_col) : 0.0;
+  __syncwarp();
+#pragma unroll
+  for (int u = 0; u < K; u++) acc = fma_rn(widen(v[u]), xv[u], acc);
   return acc;
 }
 
-template <class V>
-__device__ __forceinline__ double warp_row(const V* __restrict__ vals, const int* __restrict__ colidx, int s,
-                                           int e, const double* __restrict__ x, int f_col, int lane,
-                                           uint64_t pol) {
+// Sum of one lane's `steps` entries of a slice `width` steps wide (width is
+// warp-uniform, so every branch below is too and no DFMA is issued past it).
+template <class V, int U>
+__device__ __forceinline__ double slice_rows(const V* __restrict__ sv, const int* __restrict__ sc, long off,
+                                             int steps, int width, const double* __restrict__ x, int f_col,
+                                             uint64_t pol) {
   double acc = 0;
-  for (int base = s; base < e; base += 32 * UNROLL) {
-    // dead lanes keep a zero value and a valid column, so nothing they
-    // might touch is out of bounds
-    V v[UNROLL];
-    int c[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; u++) {
-      v[u] = V(0.0f);
-      c[u] = f_col;
-    }
-#pragma unroll
-    for (int u = 0; u < UNROLL; u++) {
-      const int j = base + u * 32 + lane;
-      if (j < e) {
-        v[u] = ld_stream(vals + j, pol);
-        c[u] = ld_stream(colidx + j, pol);
-      }
-    }
-    double xv[UNROLL];
-#pragma unroll
-    for (int u = 0; u < UNROLL; u++) xv[u] = (base + u * 32 + lane < e) ? ld_gather(x + c[u] - f_col) : 0.0;
-    __syncwarp();
-#pragma unroll
-    for (int u = 0; u < UNROLL; u++)
-      acc = fma_rn((base + u * 32 + lane < e) ? widen(v[u]) : 0.0, xv[u], acc);
+  int j = 0;
+  for (; j + U <= width; j += U) acc = steps_k<V, U>(sv, sc, off, j, steps, x, f_col, pol, acc);
+  if (U > 4 && j + 4 <= width) {
+    acc = steps_k<V, 4>(sv, sc, off, j, steps, x, f_col, pol, acc);
+    j += 4;
   }
-  return warp_sum(acc);
+  if (j + 2 <= width) {
+    acc = steps_k<V, 2>(sv, sc, off, j, steps, x, f_col, pol, acc);
+    j += 2;
+  }
+  if (j < width) acc = steps_k<V, 1>(sv, sc, off, j, steps, x, f_col, pol, acc);
+  return acc;
 }
 
 struct Lane {
-  int row;
-  int len;
-  long off;
+  int row;    // -1: unused lane
+  int steps;  // live steps of this lane
 };
 
-// Decodes lane `lane` of medium / short item k (k counted from the first
-// medium slice).
-__device__ __forceinline__ Lane slice_lane(const SellPlan& p, const int* rowptr, int k, int lane) {
-  Lane l;
-  if (k < p.nmed) {
-    l.row = p.med_rows[(long)k * 32 + lane];
-    l.len = l.row >= 0 ? rowptr[l.row + 1] - rowptr[l.row] : 0;
-    l.off = p.med_off[k] + lane;
+// Decodes lane `lane` of slice `d` = {step offset, width, g, base}: a
+// window slice (base >= 0) packs (row - base) << 8 | length per lane, a
+// slice sorted over the whole matrix (base = -1) holds the row.
+__device__ __forceinline__ Lane slice_lane(const int4& d, int meta, const int* rowptr, int lane) {
+  Lane l{-1, 0};
+  if (meta < 0) return l;
+  if (d.w >= 0) {
+    l.row = d.w + (meta >> 8);
+    l.steps = meta & 255;
   } else {
-    k -= p.nmed;
-    const int m = p.short_meta[(long)k * 32 + lane];
-    l.row = m >= 0 ? p.short_base[k] + (m >> 8) : -1;
-    l.len = m >= 0 ? (m & 255) : 0;
-    l.off = p.short_off[k] + lane;
+    l.row = meta;
+    const int len = rowptr[meta + 1] - rowptr[meta];
+    const int sub = lane & ((1 << d.z) - 1);
+    l.steps = len > sub ? (len - sub + (1 << d.z) - 1) >> d.z : 0;
   }
   return l;
 }
 
-template <class V>
+template <class V, int U>
 __global__ void __launch_bounds__(NT) k_sell(SellArgs a, const double* __restrict__ x, double* __restrict__ y,
                                             unsigned* __restrict__ counter) {
   const int lane = threadIdx.x & 31;
   const SellPlan& p = a.plan;
-  const int nitems = p.nlong + p.nmed + p.nshort;
+  const int nitems = p.nslices;
   const uint64_t pol = policy_evict_first();
-  const V* vals = static_cast<const V*>(a.vals);
   const V* sv = static_cast<const V*>(a.svals);
-  for (;;) {
-    int item = 0;
-    if (lane == 0) item = (int)atomicAdd(counter, 1u);
-    item = __shfl_sync(0xffffffffu, item, 0);
-    if (item >= nitems) break;
-    if (item < p.nlong) {
-      const int row = p.long_rows[item];
-      const double acc = warp_row(vals, a.colidx, a.rowptr[row], a.rowptr[row + 1], x, a.f_col, lane, pol);
-      if (lane == 0) y[row] = acc;
-    } else {
-      const Lane l = slice_lane(p, a.rowptr, item - p.nlong, lane);
-      const int width = __reduce_max_sync(0xffffffffu, l.len);
-      const double acc = slice_rows(sv, a.scols, l.off, l.len, width, x, a.f_col, pol);
-      if (l.row >= 0) y[l.row] = acc;
-    }
+  // Two items are claimed ahead, and the descriptor of the next one is
+  // loaded while the current one runs, so neither the work counter's
+  // atomics nor the descriptor loads sit on the critical path.
+  int cur = 0, nxt = 0;
+  if (lane == 0) {
+    cur = (int)atomicAdd(counter, 1u);
+    nxt = (int)atomicAdd(counter, 1u);
   }
-  // The last warp to finish resets the work counter for the next launch.
+  cur = __shfl_sync(FULL, cur, 0);
+  nxt = __shfl_sync(FULL, nxt, 0);
+  int4 d = make_int4(0, 0, 0, 0);
+  int meta = -1;
+  if (cur < nitems) {
+    d = __ldg(p.slice + cur);
+    meta = __ldg(p.lane + (long)cur * 32 + lane);
+  }
+  while (cur < nitems) {
+    int after = 0;
+    if (lane == 0) after = (int)atomicAdd(counter, 1u);
+    int4 dn = make_int4(0, 0, 0, 0);
+    int mn = -1;
+    if (nxt < nitems) {
+      dn = __ldg(p.slice + nxt);
+      mn = __ldg(p.lane + (long)nxt * 32 + lane);
+    }
+    const Lane l = slice_lane(d, meta, a.rowptr, lane);
+    double acc = slice_rows<V, U>(sv, a.scols, (long)d.x * 32 + lane, l.steps, d.y, x, a.f_col, pol);
+    for (int o = (1 << d.z) >> 1; o > 0; o >>= 1) acc = add_rn(acc, __shfl_xor_sync(FULL, acc, o));
+    if (l.row >= 0 && (lane & ((1 << d.z) - 1)) == 0) y[l.row] = acc;
+    cur = nxt;
+    nxt = __shfl_sync(FULL, after, 0);
+    d = dn;
+    meta = mn;
+  }
+  // The last warp to finish resets the work counter for the next launch:
+  // every warp's claims were answered before it counts itself out here.
   if (lane == 0) {
     const unsigned total = gridDim.x * (NT / 32);
     if (atomicAdd(counter + 1, 1u) == total - 1) {
@@ -165,36 +168,52 @@ __global__ void __launch_bounds__(NT) k_sell_fill(SellArgs a, V* __restrict__ sv
   const int lane = threadIdx.x & 31;
   const SellPlan& p = a.plan;
   const V* vals = static_cast<const V*>(a.vals);
-  const long nitems = (long)p.nmed + p.nshort;
   const long warps = (long)gridDim.x * (NT / 32);
-  for (long k = (blockIdx.x * (long)NT + threadIdx.x) / 32; k < nitems; k += warps) {
-    const Lane l = slice_lane(p, a.rowptr, (int)k, lane);
-    if (l.row < 0) continue;
-    const int s = a.rowptr[l.row];
-    for (int j = 0; j < l.len; j++) {
-      sv[l.off + (long)j * 32] = vals[s + j];
-      sc[l.off + (long)j * 32] = a.colidx[s + j];
+  for (long k = (blockIdx.x * (long)NT + threadIdx.x) / 32; k < p.nslices; k += warps) {
+    const int4 d = p.slice[k];
+    const Lane l = slice_lane(d, p.lane[k * 32 + lane], a.rowptr, lane);
+    const long off = (long)d.x * 32 + lane;
+    const int s = l.row >= 0 ? a.rowptr[l.row] + (lane & ((1 << d.z) - 1)) : 0;
+    for (int t = 0; t < d.y; t++) {
+      // padding: a zero value on a valid column (never read by the kernel)
+      V v = V(0.0f);
+      int c = a.f_col;
+      if (t < l.steps) {
+        v = vals[s + ((long)t << d.z)];
+        c = a.colidx[s + ((long)t << d.z)];
+      }
+      sv[off + (long)t * 32] = v;
+      sc[off + (long)t * 32] = c;
     }
   }
 }
 
-template <class V>
+template <class V, int U>
 cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V>, NT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V, U>, NT, 0);
   const int grid = std::max(1, sms * std::max(1, per));
-  k_sell<V><<<grid, NT, 0, s>>>(a, x, y, counter);
+  k_sell<V, U><<<grid, NT, 0, s>>>(a, x, y, counter);
   return cudaGetLastError();
 }
 
 template <class V>
 cudaError_t launch_fill(const SellArgs& a, void* sv, int* sc, cudaStream_t s) {
-  const long items = (long)a.plan.nmed + a.plan.nshort;
+  const long items = a.plan.nslices;
   const int grid = (int)std::max<long>(1, std::min<long>((items + 7) / 8, 152L * 32));
   k_sell_fill<V><<<grid, NT, 0, s>>>(a, static_cast<V*>(sv), sc);
   return cudaGetLastError();
+}
+
+template <class V>
+cudaError_t launch_u(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s) {
+  switch (a.unroll) {
+    case 4: return launch<V, 4>(a, x, y, counter, s);
+    case 16: return launch<V, 16>(a, x, y, counter, s);
+    default: return launch<V, 8>(a, x, y, counter, s);
+  }
 }
 
 }  // namespace
@@ -203,41 +222,52 @@ void sell_plan_build(const int* rp, int n, int sthr, int lthr, int sigma, SellPl
   using tbsla_impl::parallel_for;
   *p = SellPlan{};
   p->n = n;
-  p->short_thr = sthr = std::min(sthr, 255);
-  p->long_thr = lthr = std::max(lthr, sthr);
-  p->sigma = sigma;
+  p->short_thr = sthr = std::max(1, std::min(sthr, 255));
+  p->long_thr = lthr = std::max(lthr, 1);
+  p->sigma = sigma = std::max(32, std::min(sigma, 1 << 23));
   auto len = [&](int i) { return rp[i + 1] - rp[i]; };
-  // long rows: longest first
-  std::vector<int> lng, med;
+  // lanes per row (log2) of a row longer than short_thr
+  auto lanes_log2 = [&](int l) {
+    int g = 0;
+    while (g < 5 && (l + (1 << g) - 1) >> g > lthr) g++;
+    return g;
+  };
+  // Rows past short_thr: per lane count, sorted by length over the matrix.
+  std::vector<int> lng[6];
   for (int i = 0; i < n; i++) {
     const int l = len(i);
-    if (l > lthr) lng.push_back(i);
-    else if (l > sthr) med.push_back(i);
+    if (l > sthr) lng[lanes_log2(l)].push_back(i);
   }
+  struct Slice {
+    int width, g, base;
+    long first;  // index into `rows` of its first row (g > 0)
+  };
+  std::vector<int4> desc;
+  std::vector<int> meta;
+  std::vector<std::pair<int, int>> order;  // (width, slice) of the g > 0 slices
+  std::vector<Slice> wide;
+  std::vector<int> wide_rows;
   auto by_len = [&](int a, int b) { return len(a) > len(b); };
-  std::stable_sort(lng.begin(), lng.end(), by_len);
-  std::stable_sort(med.begin(), med.end(), by_len);
-  p->nlong = (int)lng.size();
-  p->long_rows = new int[std::max<size_t>(lng.size(), 1)];
-  std::copy(lng.begin(), lng.end(), p->long_rows);
-  // medium slices over the whole matrix
-  p->nmed = (int)((med.size() + 31) / 32);
-  p->med_rows = new int[std::max(32L * p->nmed, 1L)];
-  p->med_off = new long[p->nmed + 1];
-  long off = 0;
-  for (int k = 0; k < p->nmed; k++) {
-    p->med_off[k] = off;
-    int width = 0;
-    for (int l = 0; l < 32; l++) {
-      const size_t q = (size_t)k * 32 + l;
-      const int row = q < med.size() ? med[q] : -1;
-      p->med_rows[q] = row;
-      if (row >= 0) width = std::max(width, len(row));
+  for (int g = 0; g <= 5; g++) {
+    auto& v = lng[g];
+    std::stable_sort(v.begin(), v.end(), by_len);
+    const int per = 32 >> g;
+    for (size_t q = 0; q < v.size(); q += per) {
+      Slice s{(len(v[q]) + (1 << g) - 1) >> g, g, 0, (long)wide_rows.size()};
+      for (int r = 0; r < per; r++) wide_rows.push_back(q + r < v.size() ? v[q + r] : -1);
+      order.push_back({s.width, (int)wide.size()});
+      wide.push_back(s);
     }
-    off += 32L * width;
   }
-  p->med_off[p->nmed] = off;
-  // short slices, sorted within windows
+  std::stable_sort(order.begin(), order.end(), [](auto& a, auto& b) { return a.first > b.first; });
+  long off = 0;  // in steps of 32 entries
+  for (auto& o : order) {
+    const Slice& s = wide[o.second];
+    desc.push_back(make_int4((int)off, s.width, s.g, -1));
+    for (int l = 0; l < 32; l++) meta.push_back(wide_rows[s.first + (l >> s.g)]);
+    off += s.width;
+  }
+  // Short rows: one lane each, sorted by length within windows.
   const int nwin = (n + sigma - 1) / sigma;
   std::vector<std::vector<int>> win(nwin);
   parallel_for(nwin, [&](long b, long e) {
@@ -251,17 +281,15 @@ void sell_plan_build(const int* rp, int n, int sthr, int lthr, int sigma, SellPl
   });
   std::vector<long> first(nwin + 1, 0);
   for (int w = 0; w < nwin; w++) first[w + 1] = first[w] + (long)((win[w].size() + 31) / 32);
-  p->nshort = (int)first[nwin];
-  p->short_meta = new int[std::max(32L * p->nshort, 1L)];
-  p->short_base = new int[std::max(p->nshort, 1)];
-  p->short_off = new long[p->nshort + 1];
-  std::vector<long> width(std::max(p->nshort, 1), 0);
+  const long nwide = (long)desc.size();
+  const long nshort = first[nwin];
+  desc.resize(nwide + nshort);
+  meta.resize(32 * (nwide + nshort));
   parallel_for(nwin, [&](long b, long e) {
     for (long w = b; w < e; w++) {
       const auto& v = win[w];
       const int base = (int)(w * sigma);
       for (long k = first[w]; k < first[w + 1]; k++) {
-        p->short_base[k] = base;
         int wd = 0;
         for (int l = 0; l < 32; l++) {
           const size_t q = (size_t)(k - first[w]) * 32 + l;
@@ -270,32 +298,33 @@ void sell_plan_build(const int* rp, int n, int sthr, int lthr, int sigma, SellPl
             m = ((v[q] - base) << 8) | len(v[q]);
             wd = std::max(wd, len(v[q]));
           }
-          p->short_meta[k * 32 + l] = m;
+          meta[(nwide + k) * 32 + l] = m;
         }
-        width[k] = wd;
+        desc[nwide + k] = make_int4(0, wd, 0, base);
       }
     }
   });
-  for (int k = 0; k < p->nshort; k++) {
-    p->short_off[k] = off;
-    off += 32L * width[k];
+  for (long k = nwide; k < nwide + nshort; k++) {
+    desc[k].x = (int)off;
+    off += desc[k].y;
   }
-  p->short_off[p->nshort] = off;
-  p->sell_len = off;
+  p->nwide = (int)nwide;
+  p->nslices = (int)(nwide + nshort);
+  p->sell_len = off * 32;
+  p->slice = new int4[std::max<size_t>(desc.size(), 1)];
+  std::copy(desc.begin(), desc.end(), p->slice);
+  p->lane = new int[std::max<size_t>(meta.size(), 1)];
+  std::copy(meta.begin(), meta.end(), p->lane);
 }
 
 void sell_plan_free(SellPlan* p) {
-  delete[] p->long_rows;
-  delete[] p->med_rows;
-  delete[] p->med_off;
-  delete[] p->short_meta;
-  delete[] p->short_base;
-  delete[] p->short_off;
+  delete[] p->slice;
+  delete[] p->lane;
   *p = SellPlan{};
 }
 
 cudaError_t sell_fill(const SellArgs& a, void* svals, int* scols, cudaStream_t s) {
-  if ((long)a.plan.nmed + a.plan.nshort == 0) return cudaSuccess;
+  if (a.plan.nslices == 0) return cudaSuccess;
   switch (a.prec) {
     case kF64: return launch_fill<double>(a, svals, scols, s);
     case kF32: return launch_fill<float>(a, svals, scols, s);
@@ -305,11 +334,11 @@ cudaError_t sell_fill(const SellArgs& a, void* svals, int* scols, cudaStream_t s
 }
 
 cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s) {
-  if ((long)a.plan.nlong + a.plan.nmed + a.plan.nshort == 0) return cudaSuccess;
+  if (a.plan.nslices == 0) return cudaSuccess;
   switch (a.prec) {
-    case kF64: return launch<double>(a, x, y, counter, s);
-    case kF32: return launch<float>(a, x, y, counter, s);
-    case kBF16: return launch<__nv_bfloat16>(a, x, y, counter, s);
+    case kF64: return launch_u<double>(a, x, y, counter, s);
+    case kF32: return launch_u<float>(a, x, y, counter, s);
+    case kBF16: return launch_u<__nv_bfloat16>(a, x, y, counter, s);
   }
   return cudaErrorInvalidValue;
 }

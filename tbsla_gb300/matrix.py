@@ -252,7 +252,7 @@ class MatrixCSR(Matrix):
     def set_algorithm(self, algorithm: int, items: int = 8):
         check(lib.tbsla_matrix_set_csr_algorithm(self._h, algorithm, items), "set_csr_algorithm")
 
-    def set_sell_params(self, short_thr: int = 128, long_thr: int = 1024, sigma: int = 16384):
+    def set_sell_params(self, short_thr: int = 64, long_thr: int = 64, sigma: int = 16384):
         check(lib.tbsla_matrix_set_sell_params(self._h, short_thr, long_thr, sigma), "set_sell_params")
 
     # project generators

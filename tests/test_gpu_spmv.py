@@ -147,15 +147,15 @@ def powerlaw(T, n, seed=5, **kw):
     return m
 
 
-CSR_KERNELS = [("sell", (128, 1024, 16384)), ("sell", (4, 40, 64)), ("sell", (255, 255, 1 << 20)),
+CSR_KERNELS = [("sell", (64, 64, 16384, 8)), ("sell", (4, 3, 64, 4)), ("sell", (255, 1000, 1 << 20, 16)),
                ("merge", 4), ("merge", 8), ("merge", 16), ("rowblock", 1024), ("rowblock", 2048),
                ("rowblock", 4096)]
 
 
 def set_kernel(m, kind, p):
     if kind == "sell":
-        m.set_algorithm(m.SELL)
-        m.set_sell_params(*p)
+        m.set_algorithm(m.SELL, p[3])
+        m.set_sell_params(*p[:3])
     elif kind == "merge":
         m.set_algorithm(m.MERGE, p)
     else:

@@ -184,6 +184,16 @@ def test_oracle_pagerank_and_cg_fixed_points():
     ax = oracle.csr_ax(a["rowptr"], a["colidx"], vals, x)
     fp = 0.85 * ax + (0.85 * x[d].sum() + 0.15) / 2000
     assert np.abs(fp - x).sum() < 1e-11
+    # FP32-rounded values: column sums are 1 +- 6e-8, yet the iteration
+    # still converges (the teleport weight returns the rounding's mass loss)
+    v32 = vals.astype(np.float32).astype(np.float64)
+    x32, it32, err32 = oracle.pagerank(a["rowptr"], a["colidx"], v32, 0.85, 1e-13, 500)
+    assert err32 < 1e-13 and abs(x32.sum() - 1) < 1e-12
+    w = oracle.csr_col_sums(a["rowptr"], a["colidx"], v32, 2000)
+    ax32 = oracle.csr_ax(a["rowptr"], a["colidx"], v32, x32)
+    fp32 = 0.85 * ax32 + (1 - 0.85 * (w * x32).sum()) / 2000
+    assert np.abs(fp32 - x32).sum() < 1e-11
+    assert np.abs(x32 - x).sum() < 1e-5
     m = T.MatrixCSR()
     m.fill_diffusion7(12, 1.0, 4.0, 5)
     a = m.arrays()
