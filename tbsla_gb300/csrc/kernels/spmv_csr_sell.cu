@@ -75,6 +75,11 @@ __device__ __forceinline__ double slice_rows(const V* __restrict__ sv, const int
   double acc = 0;
   int j = 0;
   for (; j + U <= width; j += U) acc = steps_k<V, U>(sv, sc, off, j, steps, x, f_col, pol, acc);
+  // remainder (< U steps) in binary pieces
+  if (U > 8 && j + 8 <= width) {
+    acc = steps_k<V, 8>(sv, sc, off, j, steps, x, f_col, pol, acc);
+    j += 8;
+  }
   if (U > 4 && j + 4 <= width) {
     acc = steps_k<V, 4>(sv, sc, off, j, steps, x, f_col, pol, acc);
     j += 4;
