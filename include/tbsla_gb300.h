@@ -199,6 +199,25 @@ int tbsla_Ax_device(const tbsla_matrix* m, double* r, const double* v, int vect_
 int tbsla_spmv_device(const tbsla_matrix* m, double* r, const double* v, int vect_incr,
                       void* stream);
 
+/* Allocation-free CSR SpMV: r <- A v for a CSR matrix already in device
+ * memory owned by the caller (rowptr: n_row + 1 ints, nnz = rowptr[n_row] -
+ * rowptr[0]; colidx, FP64 values: nnz; v indexed by colidx - f_col; r:
+ * n_row), on `stream` of the current device.  No reference counterpart: the
+ * reference has no device memory.  It is for callers that may not allocate
+ * on the call path -- an application whose memory pool owns the device, or
+ * a loop that must not call the CUDA allocator -- and that cannot build a
+ * handle, which copies the matrix and allocates per-matrix scratch.  The
+ * merge-path kernel's scratch (tile starts and carries) lives in a fixed
+ * 1.25 MiB device array inside the library, so n_row + nnz may not exceed
+ * TBSLA_NOALLOC_MAX_ITEMS (TBSLA_ERR_INVALID_ARG otherwise).  The first call
+ * on a device looks the array up and should come before any stream capture.
+ * Calls that overlap in time share the array and race: serialise them.
+ * Results equal tbsla_Ax_device on a handle set to TBSLA_CSR_MERGE with 8
+ * items. */
+#define TBSLA_NOALLOC_MAX_ITEMS 134217728L
+int tbsla_csr_Ax_device_noalloc(int n_row, long nnz, int f_col, const int* rowptr, const int* colidx,
+                                const double* values, const double* v, double* r, void* stream);
+
 /* ---- composite ops: Matrix.cpp:5-31 ------------------------------------------ */
 /* r <- A(Av + v) (a_axpx_, returns a new array in the reference). */
 int tbsla_a_axpx_(const tbsla_matrix* m, double* r, const double* v, int vect_incr);

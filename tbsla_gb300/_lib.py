@@ -103,6 +103,7 @@ _SIGS = {
     "tbsla_spmv": (I, [P, P, P, I]),
     "tbsla_Ax_device": (I, [P, P, P, I, P]),
     "tbsla_spmv_device": (I, [P, P, P, I, P]),
+    "tbsla_csr_Ax_device_noalloc": (I, [I, L, I, P, P, P, P, P, P]),
     "tbsla_a_axpx_": (I, [P, P, P, I]),
     "tbsla_AAxpAx": (I, [P, P, P, P, I]),
     "tbsla_AAxpAxpx": (I, [P, P, P, P, I]),

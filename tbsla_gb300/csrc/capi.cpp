@@ -299,6 +299,16 @@ int tbsla_spmv_device(const tbsla_matrix* m, double* r, const double* v, int vec
   return dev_ax(m, r, v, vect_incr, true, false, stream);
 }
 
+int tbsla_csr_Ax_device_noalloc(int n_row, long nnz, int f_col, const int* rowptr, const int* colidx,
+                                const double* values, const double* v, double* r, void* stream) {
+  if (n_row < 0 || nnz < 0 || f_col < 0 ||
+      (nnz > 0 && (!rowptr || !colidx || !values || !v || !r)))
+    return TBSLA_ERR_INVALID_ARG;
+  if ((long)n_row + nnz > dev_noalloc_max_items()) return TBSLA_ERR_INVALID_ARG;
+  if (nnz == 0) return TBSLA_OK;  // MatrixCSR::Ax leaves r untouched
+  return dev_csr_ax_noalloc(n_row, nnz, f_col, rowptr, colidx, values, v, r, stream);
+}
+
 int tbsla_a_axpx_(const tbsla_matrix* m, double* r, const double* v, int vect_incr) {
   if (!m || !r || !v) return TBSLA_ERR_INVALID_ARG;
   return dev_a_axpx(m, r, v, vect_incr);

@@ -816,4 +816,12 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   return hflags[0] ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
 }
 
+long dev_noalloc_max_items() { return csr_merge_noalloc_max_items(); }
+
+int dev_csr_ax_noalloc(int n_row, long nnz, int f_col, const int* rowptr, const int* colidx,
+                       const double* values, const double* v, double* r, void* stream) {
+  return status_of(csr_merge_spmv_noalloc(values, rowptr, colidx, n_row, nnz, f_col, v, r,
+                                          static_cast<cudaStream_t>(stream)));
+}
+
 }  // namespace tbsla_impl

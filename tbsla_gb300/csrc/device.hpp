@@ -34,4 +34,10 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
 int dev_cg(tbsla_matrix* m, const double* b, double* x, int max_it, double rel_tol, int precond,
            int refresh, int* iterations, double* rel_residual);
 
+// Merge-path CSR SpMV on caller-owned device arrays with file-scope scratch
+// (allocates nothing); n_row + nnz at most dev_noalloc_max_items().
+long dev_noalloc_max_items();
+int dev_csr_ax_noalloc(int n_row, long nnz, int f_col, const int* rowptr, const int* colidx,
+                       const double* values, const double* v, double* r, void* stream);
+
 }  // namespace tbsla_impl

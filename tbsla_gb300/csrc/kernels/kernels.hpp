@@ -51,6 +51,12 @@ struct MergeArgs {
 long merge_tiles(int n, long nnz, int items);
 cudaError_t csr_merge_setup(const int* rowptr, int n, long nnz, int items, int* coord, cudaStream_t s);
 cudaError_t csr_merge_spmv(const MergeArgs& a, const double* x, double* y, cudaStream_t s);
+// The merge-path SpMV (FP64 values, 8 items per thread) with its scratch in
+// a file-scope device array: allocates nothing; n + nnz at most
+// csr_merge_noalloc_max_items(); concurrent calls race on the scratch.
+long csr_merge_noalloc_max_items();
+cudaError_t csr_merge_spmv_noalloc(const double* vals, const int* rowptr, const int* colidx, int n, long nnz,
+                                   int f_col, const double* x, double* y, cudaStream_t s);
 
 // Sliced-ELL CSR SpMV (SELL-C-sigma with C = 32) for GB300's FP64 pipe,
 // which costs one slot per warp-instruction whatever the active lanes.  A

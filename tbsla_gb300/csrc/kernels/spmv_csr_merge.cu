@@ -25,6 +25,7 @@
 //      the carries, in tile order, to the rows they belong to.
 // Results are deterministic (no atomics).
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "kernels.hpp"
@@ -279,6 +280,69 @@ cudaError_t csr_merge_spmv(const MergeArgs& a, const double* x, double* y, cudaS
     case kBF16: return by_items<__nv_bfloat16>(a, x, y, s);
   }
   return cudaErrorInvalidValue;
+}
+
+// ---- Allocation-free variant ---------------------------------------------------
+// The same merge-path SpMV (FP64 values, 8 items per thread) with its
+// scratch -- tile starts and per-tile carries -- in a file-scope device
+// array instead of per-matrix allocations, for callers that hold a CSR
+// matrix in their own device memory and may not allocate on the call path
+// (an application whose memory pool owns the whole device, or a loop that
+// must not call the CUDA allocator).  The array serves up to
+// kNoAllocTiles tiles of 2048 merge items (n_row + nnz <= 134,217,728);
+// bigger inputs are rejected.  Every scratch word is written before it is
+// read within a call, so nothing needs clearing between calls.  Calls that
+// overlap in time (other streams, other host threads) share the array and
+// race: the caller serialises them.
+namespace {
+
+constexpr long kNoAllocTiles = 65536;
+constexpr size_t kNoAllocBytes =
+    (size_t)kNoAllocTiles * sizeof(double) + (size_t)kNoAllocTiles * sizeof(int) + (kNoAllocTiles + 1) * sizeof(int);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[(kNoAllocBytes + 255) / 256 * 256];
+
+constexpr int kNoAllocDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_base[kNoAllocDevices] = {};
+
+// Device address of the scratch array on the current device, looked up once
+// per device (the first call on a device therefore belongs before any stream
+// capture).
+cudaError_t noalloc_base(void** base) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoAllocDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_base[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    g_noalloc_base[dev] = p;
+  }
+  *base = g_noalloc_base[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+long csr_merge_noalloc_max_items() { return kNoAllocTiles * NT * 8L; }
+
+cudaError_t csr_merge_spmv_noalloc(const double* vals, const int* rowptr, const int* colidx, int n, long nnz,
+                                   int f_col, const double* x, double* y, cudaStream_t s) {
+  const long ntiles = merge_tiles(n, nnz, 8);
+  if (ntiles > kNoAllocTiles) return cudaErrorInvalidValue;
+  if (ntiles == 0) return cudaSuccess;
+  void* base = nullptr;
+  cudaError_t e = noalloc_base(&base);
+  if (e != cudaSuccess) return e;
+  double* carry_val = static_cast<double*>(base);
+  int* carry_row = reinterpret_cast<int*>(carry_val + kNoAllocTiles);
+  int* coord = carry_row + kNoAllocTiles;
+  e = csr_merge_setup(rowptr, n, nnz, 8, coord, s);
+  if (e != cudaSuccess) return e;
+  const MergeArgs a{vals, kF64, rowptr, colidx, n, nnz, f_col, 8, coord, ntiles, carry_row, carry_val};
+  return csr_merge_spmv(a, x, y, s);
 }
 
 }  // namespace tbsla_gpu
