@@ -45,17 +45,24 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--n", type=int, default=1 << 24)
+    p.add_argument("--workload", choices=["spmv", "pagerank", "cg"], default="spmv",
+                   help="spmv: the large-SpMV headline; pagerank: the PageRank graph; cg: batched CG")
+    p.add_argument("--n", type=int, default=None, help="rows (spmv: 2^24, pagerank: 2^22)")
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
     p.add_argument("--algo", choices=["sell", "merge", "rowblock"], default="sell")
-    p.add_argument("--sell", type=str, default="64,64,16384",
-                   help="sliced-ELL kernel: short_thr,long_thr,sigma")
-    p.add_argument("--items", type=int, default=8, help="merge kernel: items per thread")
+    p.add_argument("--sell", type=str, default="64,64,16384,0",
+                   help="sliced-ELL kernel: short_thr,long_thr,sigma,col_block (0: 2^22 columns)")
+    p.add_argument("--items", type=int, default=0,
+                   help="merge: items per thread (0 = 8); sell: steps per lane in flight (0 = automatic)")
     p.add_argument("--no-forms", action="store_true", help="skip the FP32 / BF16 side measurements")
+    p.add_argument("--autotune", action="store_true",
+                   help="time the CSR kernel configurations on the matrix first and keep the fastest")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     a = p.parse_args()
     a.warmup = max(a.warmup, 3)
+    if a.n is None:
+        a.n = 1 << 22 if a.workload == "pagerank" else 1 << 24
     return a
 
 
@@ -233,6 +240,16 @@ def run_ours(a):
     t0 = time.time()
     m.upload()
     t_up = time.time() - t0
+    tuned = None
+    if a.autotune:
+        t0 = time.time()
+        best, trials = m.autotune(reps=3)
+        names = {m.SELL: "sell", m.MERGE: "merge", m.ROWBLOCK: "rowblock"}
+        a.algo = names[best["algorithm"]]
+        a.items, a.tile = best["items"], best["tile"]
+        a.sell = f"{best['short_thr']},{best['long_thr']},{best['sigma']},{best['col_block']}"
+        tuned = {"chosen": {k: v for k, v in best.items()}, "trials": len(trials),
+                 "seconds": round(time.time() - t0, 2)}
     x = T.fill_uniform(n, 0.0, 1.0, 1)
     xt = torch.from_numpy(x).cuda()
     yt = torch.empty(n, dtype=torch.float64, device="cuda")
@@ -330,11 +347,12 @@ def run_ours(a):
         "data": "synthetic: seeded generator (power-law rows, seed 1), no dataset",
         "config": {"workload": f"csr_spmv_powerlaw_n{n}_mean16_zipf2_max4096_local30pct_{a.prec}",
                    "format": "CSR", "n": n, "nnz": nnz, "value_dtype": a.prec, "x_y_dtype": "f64",
-                   "bytes_per_step": B, "csr_kernel": a.algo,
+                   "bytes_per_step": B, "csr_kernel": a.algo, "autotune": tuned,
                    "work_split": {"merge": f"{a.items} items/thread", "rowblock": f"{a.tile} nnz/block",
                                   "sell": f"one lane per row <= {a.sell.split(',')[0]} sorted per "
                                           f"{a.sell.split(',')[2]}-row window, else 2..32 lanes per row, slices "
-                                          f"<= {a.sell.split(',')[1]} steps; {a.items} steps/lane in flight"}[a.algo],
+                                          f"<= {a.sell.split(',')[1]} steps; {a.items or 'automatic'} steps/lane in flight; "
+                                          f"column blocks of {int(a.sell.split(',')[3]) or 8388608} columns"}[a.algo],
                    "l2": "flushed (256 MB write) between steps; inputs 3.2+ GB > L2",
                    "parallelism": f"replicas x{ws}"},
         "roofline": {"bound": "hbm", "achieved": kernel_gbs, "peak": peak, "unit": "GB/s",
@@ -398,9 +416,169 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def run_pagerank(a):
+    """The PageRank workload: preferential-attachment graph, n = 2^22 nodes,
+    Zipf(2.1) out-degrees of mean 16, 5% dangling, seed 2; column-stochastic
+    (make_stochastic on the device), FP32 values, beta 0.85, uniform teleport,
+    stop at L1 change < 1e-10; then 32 personalised teleport vectors (100
+    random nodes each) in one batched solve.  value: GB/s of algorithmic
+    bytes over whole solves (host call to host result, wall clock)."""
+    import numpy as np
+    import torch
+
+    import oracle
+    import tbsla_gb300 as T
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    T.device_init(local)
+    n = a.n
+    g = T.MatrixCSR()
+    g.fill_pa_graph(n, 16.0, 2.1, 4096, 0.05, 2)
+    nnz = g.get_nnz()
+    s = np.zeros(n)
+    g.make_stochastic(s)
+    g.set_precision(T.F32)
+    g.upload()
+    b_it = nnz * 8 + 4 * (n + 1) + 16 * n  # FP32 values + int32 indices, x gathered once, y
+    for _ in range(a.warmup):
+        g.page_rank(0.85, 1e-10, 3)
+    clk = Clocks(local)
+    clk.start()
+    times = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        x, it, err, ok = g.page_rank(0.85, 1e-10, 1000)
+        times.append(time.perf_counter() - t0)
+    clocks = clk.stop()
+    sec = statistics.mean(times)
+    value = b_it * it / sec / 1e9
+    rng = np.random.default_rng(2)
+    tele = np.zeros((n, 32))
+    for k in range(32):
+        tele[rng.choice(n, 100, replace=False), k] = 1.0 / 100
+    g.page_rank_batched(tele, 0.85, 1e-10, 3)
+    t0 = time.perf_counter()
+    X, itb, okb = g.page_rank_batched(tele, 0.85, 1e-10, 1000)
+    tb = time.perf_counter() - t0
+    b_itb = nnz * 8 + 4 * (n + 1) + 32 * 24 * n  # X gathered once, Y written, T read
+    peak, peak_kind = peaks()
+    # oracle on the same FP32-rounded values: equal iteration count, L1 gap;
+    # its per-iteration time is the CPU baseline (one host thread)
+    arr = g.arrays()
+    v32 = arr["values"].astype(np.float32).astype(np.float64)
+    t0 = time.perf_counter()
+    xo, ito, erro = oracle.pagerank(arr["rowptr"], arr["colidx"], v32, 0.85, 1e-10, it, stop_early=False)
+    to = time.perf_counter() - t0
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 values, f64 vectors and sums", "data": "synthetic: seeded PA graph (seed 2), no dataset",
+        "config": {"workload": f"pagerank_pa_graph_n{n}_mean16_zipf2.1_dangling5pct_f32", "n": n, "nnz": nnz,
+                   "beta": 0.85, "epsilon": 1e-10, "bytes_per_iteration": b_it,
+                   "step": "one PageRank solve to 1e-10 (host call, wall clock)", "parallelism": "1 GPU"},
+        "iterations": it, "converged": bool(ok), "last_l1_change": err,
+        "per_iteration_ms": sec * 1e3 / it,
+        "roofline": {"bound": "hbm", "achieved": value, "peak": peak, "unit": "GB/s", "frac": value / peak,
+                     "peak_source": peak_kind, "traffic": None, "note": "whole solves incl. host set-up"},
+        "l1_vs_oracle_equal_iterations": float(np.abs(x - xo).sum()),
+        "cpu_baseline": {"value": b_it * ito / to / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                         "sample": f"oracle PageRank, {ito} iterations on the same FP32-rounded graph"},
+        "batched": {"nvec": 32, "iterations": itb, "converged": bool(okb), "ms": tb * 1e3,
+                    "GB/s": b_itb * itb / tb / 1e9, "bytes_per_iteration": b_itb},
+        "clocks": clocks, "gpu_launches": it,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_cg(a):
+    """The batched-CG workload: 64 SPD 7-point diffusion systems, n^3 grids
+    with n cycling through 16, 24, ..., 96, coefficients exp(g) of a Gaussian
+    field (sigma 1, correlation 8 cells), Dirichlet boundaries, RHS U[-1,1),
+    seed 3; FP32 values, FP64 residual refresh every 50 iterations, relative
+    residual 1e-8.  value: wall time of one batched Jacobi-PCG solve (host
+    call to host result); plain CG beside it."""
+    import numpy as np
+    import torch
+
+    import oracle
+    import tbsla_gb300 as T
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    T.device_init(local)
+    sizes = [16 + 8 * (i % 11) for i in range(64)]
+    systems = []
+    for i, sz in enumerate(sizes):
+        m = T.MatrixCSR()
+        m.fill_diffusion7(sz, 1.0, 8.0, 3000 + i)
+        systems.append(m)
+    rhs = np.concatenate([T.fill_uniform(sz ** 3, -1.0, 1.0, 4000 + i) for i, sz in enumerate(sizes)])
+    N = np.array([sz ** 3 for sz in sizes])
+    nnz = np.array([m.get_nnz() for m in systems])
+    res = {}
+    clk = Clocks(local)
+    for pre, name in ((0, "cg"), (1, "jacobi_pcg")):
+        bt = T.Batch(systems, T.F32)
+        for _ in range(a.warmup):
+            bt.cg(rhs, max_iterations=20, rel_tol=1e-8, precond=pre, refresh=50, graph_iters=10)
+        if pre == 1:
+            clk.start()
+        times = []
+        for _ in range(a.steps):
+            t0 = time.perf_counter()
+            x, its, rr, ok = bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=pre, refresh=50,
+                                   graph_iters=10)
+            times.append(time.perf_counter() - t0)
+        # algorithmic bytes per iteration of a system: SpMV (FP32 values,
+        # int32 indices, p gathered once, q), update (p, q, x, r read; x, r
+        # written), direction (r or z, p read; p written); Jacobi adds
+        # diag^-1 read and z written
+        per_it = nnz * 8 + 4 * (N + 1) + 16 * N + 72 * N + (16 * N if pre else 0)
+        sec = statistics.mean(times)
+        res[name] = {"ms": sec * 1e3, "solves_per_s": len(sizes) / sec, "iterations_max": int(its.max()),
+                     "iterations_mean": float(its.mean()), "all_converged": bool(ok),
+                     "max_rel_residual_fp64": float(rr.max()),
+                     "GB/s": float((per_it * its).sum()) / sec / 1e9}
+        del bt
+    clocks = clk.stop()
+    # CPU baseline: the oracle's Jacobi-PCG on one 48^3 system (one thread)
+    k = sizes.index(48)
+    arr = systems[k].arrays()
+    b48 = rhs[int(N[:k].sum()):int(N[:k + 1].sum())]
+    dinv = 1.0 / np.array([arr["values"][arr["rowptr"][i]:arr["rowptr"][i + 1]][
+        arr["colidx"][arr["rowptr"][i]:arr["rowptr"][i + 1]] == i].sum() for i in range(N[k])])
+    t0 = time.perf_counter()
+    _, ito, rro = oracle.cg(arr["rowptr"], arr["colidx"], arr["values"], b48, rel_tol=1e-8, diag_inv=dinv)
+    to = time.perf_counter() - t0
+    peak, peak_kind = peaks()
+    j = res["jacobi_pcg"]
+    line = {
+        "metric": METRIC, "value": j["ms"], "unit": "ms", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": j["ms"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 values, f64 vectors, f64 residual refresh", "data": "synthetic: seeded diffusion systems (seed 3)",
+        "config": {"workload": "batched_cg_diffusion7_64_systems_n16to96_grf_sigma1_corr8_f32_refresh50",
+                   "systems": len(sizes), "unknowns": int(N.sum()), "nnz": int(nnz.sum()), "rel_tol": 1e-8,
+                   "step": "one batched Jacobi-PCG solve of all 64 systems (host call, wall clock)",
+                   "parallelism": "1 GPU, one block-diagonal matrix, CUDA graph of 10 iterations"},
+        "solvers": res,
+        "roofline": {"bound": "hbm", "achieved": j["GB/s"], "peak": peak, "unit": "GB/s",
+                     "frac": j["GB/s"] / peak, "peak_source": peak_kind, "traffic": None},
+        "cpu_baseline": {"value": to * 1e3, "unit": "ms", "cores": 1, "kind": "port",
+                         "sample": f"oracle Jacobi-PCG on the one 48^3 system: {ito} iterations, "
+                                   f"residual {rro:.2e}"},
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "pagerank":
+        run_pagerank(args)
+    elif args.workload == "cg":
+        run_cg(args)
     else:
         run_ours(args)

@@ -169,21 +169,43 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
 /* CSR SpMV kernel: TBSLA_CSR_SELL (default; sliced-ELL device layout,
  * slices of 32 lanes over rows of similar length, see
  * tbsla_matrix_set_sell_params; `items` = steps per lane in flight, 4/8/16,
- * default 8), TBSLA_CSR_MERGE (merge-path split, `items` row ends + entries
- * per thread, 4/8/16) or TBSLA_CSR_ROWBLOCK (row-block adaptive, see
+ * or 0 for 8, 16 past 2^23 columns), TBSLA_CSR_MERGE (merge-path split,
+ * `items` row ends + entries per thread, 4/8/16, 0 = 8) or
+ * TBSLA_CSR_ROWBLOCK (row-block adaptive, see
  * tbsla_matrix_set_csr_tile; `items` unused).  Changing the kernel or the
  * merge split rebuilds the device copy. */
 #define TBSLA_CSR_MERGE 0
 #define TBSLA_CSR_ROWBLOCK 1
 #define TBSLA_CSR_SELL 2
 int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items);
-/* Sliced-ELL layout: rows of at most short_thr (1..255) entries take one
+/* Sliced-ELL layout: the columns are split into blocks of at most
+ * col_block columns (0 = 8,388,608, i.e. 64 MiB of FP64 x, about what L2
+ * keeps for gathers), processed one launch each, the first writing r and the
+ * others adding to it.  Within a block, rows of at most short_thr (1..255) entries take one
  * lane each and are sorted by length within windows of `sigma` (32..2^23)
  * consecutive rows; longer rows take the fewest lanes (a power of two up to
  * 32) that keep their slice at most long_thr steps wide and are sorted by
- * length over the whole matrix (defaults 64, 64, 16384).  Changing them
+ * length over the whole block (defaults 64, 64, 16384, 0).  Changing them
  * rebuilds the device copy. */
-int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma);
+int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block);
+
+/* One CSR kernel configuration and its measured time. */
+typedef struct {
+  int algorithm;  /* TBSLA_CSR_SELL / _MERGE / _ROWBLOCK */
+  int items;      /* set_csr_algorithm's `items` (SELL: steps in flight) */
+  int short_thr, long_thr, sigma, col_block; /* SELL layout */
+  int tile;       /* ROWBLOCK entries per block */
+  double ms;      /* mean device time of one Ax, CUDA events, L2 warm */
+} tbsla_tuning;
+/* Autotuner (CSR): times every candidate configuration -- the sliced-ELL
+ * kernel over its layout thresholds, column blocks and steps in flight, the
+ * merge-path kernel and the row-block kernel -- on this matrix (`reps` Ax
+ * each after one warm-up, x = 1), leaves the handle set to the fastest and
+ * writes it to *best.  trials (optional): the first max_trials timings in
+ * candidate order, their count in *ntrials.  The device copy is rebuilt for
+ * every layout tried. */
+int tbsla_matrix_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* trials, int max_trials,
+                          int* ntrials);
 
 /* ---- SpMV: Matrix::Ax / Matrix::spmv (Matrix.hpp:14-15) ----------------------- */
 /* r <- A v (CSR, ELL: overwrite; returns without touching r when nnz == 0)

@@ -36,6 +36,14 @@ class Info(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class Tuning(C.Structure):
+    _fields_ = [("algorithm", C.c_int), ("items", C.c_int), ("short_thr", C.c_int), ("long_thr", C.c_int),
+                ("sigma", C.c_int), ("col_block", C.c_int), ("tile", C.c_int), ("ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class TbslaError(RuntimeError):
     def __init__(self, status: int, what: str = ""):
         self.status = status
@@ -94,7 +102,8 @@ _SIGS = {
     "tbsla_matrix_device_bytes": (I, [P, C.POINTER(C.c_size_t)]),
     "tbsla_matrix_set_csr_tile": (I, [P, I]),
     "tbsla_matrix_set_csr_algorithm": (I, [P, I, I]),
-    "tbsla_matrix_set_sell_params": (I, [P, I, I, I]),
+    "tbsla_matrix_set_sell_params": (I, [P, I, I, I, I]),
+    "tbsla_matrix_autotune": (I, [P, I, C.POINTER(Tuning), C.POINTER(Tuning), I, IP]),
     "tbsla_batch_create": (I, [C.POINTER(P), C.POINTER(P), I, I]),
     "tbsla_batch_destroy": (I, [P]),
     "tbsla_batch_rows": (I, [P, IP, C.POINTER(L)]),

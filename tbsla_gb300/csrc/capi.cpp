@@ -252,23 +252,33 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block) {
   return TBSLA_OK;
 }
 
-int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma) {
-  if (!m || short_thr < 1 || short_thr > 255 || long_thr < 1 || sigma < 32 || sigma > (1 << 23))
+int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block) {
+  if (!m || short_thr < 1 || short_thr > 255 || long_thr < 1 || sigma < 32 || sigma > (1 << 23) ||
+      col_block < 0)
     return TBSLA_ERR_INVALID_ARG;
-  if (m->sell_short != short_thr || m->sell_long != long_thr || m->sell_sigma != sigma) {
+  if (m->sell_short != short_thr || m->sell_long != long_thr || m->sell_sigma != sigma ||
+      m->sell_colblock != col_block) {
     m->invalidate();
     m->sell_short = short_thr;
     m->sell_long = long_thr;
     m->sell_sigma = sigma;
+    m->sell_colblock = col_block;
   }
   return TBSLA_OK;
 }
 
+int tbsla_matrix_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* trials, int max_trials,
+                          int* ntrials) {
+  if (!m || max_trials < 0 || (max_trials > 0 && !trials)) return TBSLA_ERR_INVALID_ARG;
+  return dev_autotune(m, reps, best, trials, max_trials, ntrials);
+}
+
 int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items) {
   if (!m || algorithm < TBSLA_CSR_MERGE || algorithm > TBSLA_CSR_SELL ||
-      (algorithm != TBSLA_CSR_ROWBLOCK && items != 4 && items != 8 && items != 16))
+      (algorithm != TBSLA_CSR_ROWBLOCK && items != 0 && items != 4 && items != 8 && items != 16))
     return TBSLA_ERR_INVALID_ARG;
-  if (algorithm == TBSLA_CSR_SELL) m->sell_unroll = items;  // a launch parameter only
+  if (algorithm == TBSLA_CSR_MERGE && items == 0) items = 8;
+  if (algorithm == TBSLA_CSR_SELL) m->sell_unroll = items;  // a launch parameter only; 0 = automatic
   if (m->csr_algo != algorithm || (algorithm == TBSLA_CSR_MERGE && m->merge_items != items)) {
     m->invalidate();
     m->csr_algo = algorithm;

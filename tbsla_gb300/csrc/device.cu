@@ -13,12 +13,14 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <vector>
 
 #include "device.hpp"
+#include "host/parallel.hpp"
 #include "kernels/kernels.hpp"
 
 namespace tbsla_impl {
@@ -89,7 +91,7 @@ struct DeviceMatrix {
   double* carry_val = nullptr;
   long ntiles = 0;
   int merge_items = 8;
-  SellPlan sell{};            // CSR sliced-ELL layout (device pointers)
+  std::vector<SellPlan> sell;  // CSR sliced-ELL layout, one plan per column block (device pointers)
   void* svals = nullptr;
   int* scols = nullptr;
   unsigned* sell_counter = nullptr;
@@ -114,9 +116,11 @@ struct DeviceMatrix {
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t,
                     (void*)counter, (void*)partials, (void*)result, (void*)coord, (void*)carry_row,
-                    (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)sell.slice,
-                    (void*)sell.lane, (void*)colw})
+                    (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)colw})
       if (p) cudaFree(p);
+    for (SellPlan& p : sell)
+      for (void* q : {(void*)p.slice, (void*)p.lane, (void*)p.lane_len})
+        if (q) cudaFree(q);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -239,34 +243,70 @@ SellArgs sell_args(const tbsla_matrix* m, const DeviceMatrix* d) {
   a.f_col = m->info.f_col;
   a.svals = d->svals;
   a.scols = d->scols;
-  a.unroll = m->sell_unroll;
-  a.plan = d->sell;
+  // automatic: 8 steps in flight while x stays in L2, 16 when most gathers
+  // go to HBM and more of them must be in flight
+  a.unroll = m->sell_unroll > 0 ? m->sell_unroll : (m->info.ln_col > (1 << 23) ? 16 : 8);
+  a.nblocks = (int)d->sell.size();
+  a.blocks = d->sell.data();
   return a;
 }
 
-// Sliced-ELL device layout of a CSR matrix: the plan (row classes, slices,
-// offsets) is made on the host from the row pointer, the slice arrays are
-// filled on the device from the CSR copy.
+// Sliced-ELL device layout of a CSR matrix: the columns are split into
+// blocks of at most `sell_colblock` columns (0: 8,388,608, 64 MiB of x), the
+// plans (row classes, slices, offsets) are made on the host
+// from the per-block row lengths, and the slice arrays are filled on the
+// device from the CSR copy.
 int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
-  SellPlan hp;
-  sell_plan_build(m->idx0.data(), m->info.ln_row, m->sell_short, m->sell_long, m->sell_sigma, &hp);
-  SellPlan& dp = d->sell;
-  dp = hp;
-  dp.slice = nullptr;
-  dp.lane = nullptr;
-  int st = upload_array(d, &dp.slice, hp.slice, (size_t)hp.nslices);
-  if (!st) st = upload_array(d, &dp.lane, hp.lane, 32 * (size_t)hp.nslices);
-  if (!st) st = status_of(cudaStreamSynchronize(d->stream));  // host plan arrays are freed next
-  sell_plan_free(&hp);
+  using tbsla_impl::parallel_for;
+  const tbsla_info& I = m->info;
+  const int n = I.ln_row, nc = std::max(I.ln_col, 1);
+  const long cb = m->sell_colblock > 0 ? m->sell_colblock : 8388608L;
+  const int P = (int)std::max<long>(1, (nc + cb - 1) / cb);
+  const int W = (int)(((long)nc + P - 1) / P);
+  const int* rp = m->idx0.data();
+  const int* ci = m->idx1.data();
+  std::vector<int> lens((size_t)P * n, 0);
+  if (P == 1) {
+    for (int i = 0; i < n; i++) lens[i] = rp[i + 1] - rp[i];
+  } else {
+    parallel_for(n, [&](long b, long e) {
+      for (long i = b; i < e; i++)
+        for (int j = rp[i]; j < rp[i + 1]; j++) {
+          const int k = std::min(P - 1, std::max(0, (ci[j] - I.f_col) / W));
+          lens[(size_t)k * n + i]++;
+        }
+    });
+  }
+  long steps = 0;
+  d->sell.assign(P, SellPlan{});
+  int st = TBSLA_OK;
+  for (int k = 0; k < P && !st; k++) {
+    SellPlan hp;
+    sell_plan_build(lens.data() + (size_t)k * n, n, m->sell_short, m->sell_long, m->sell_sigma, k > 0, steps, &hp);
+    hp.col_lo = k * W;
+    hp.col_hi = k == P - 1 ? INT_MAX : (k + 1) * W;
+    SellPlan& dp = d->sell[k];
+    dp = hp;
+    dp.slice = nullptr;
+    dp.lane = nullptr;
+    dp.lane_len = nullptr;
+    st = upload_array(d, &dp.slice, hp.slice, (size_t)hp.nslices);
+    if (!st) st = upload_array(d, &dp.lane, hp.lane, 32 * (size_t)hp.nslices);
+    if (!st) st = upload_array(d, &dp.lane_len, hp.lane_len, 32 * (size_t)hp.nwide);
+    if (!st) st = status_of(cudaStreamSynchronize(d->stream));  // host plan arrays are freed next
+    sell_plan_free(&hp);
+    steps += dp.sell_len / 32;
+  }
   if (st) return st;
-  if (cudaMalloc(&d->svals, std::max<size_t>(dp.sell_len, 1) * prec_size(d->prec)) != cudaSuccess) {
+  const size_t len = (size_t)steps * 32;
+  if (cudaMalloc(&d->svals, std::max<size_t>(len, 1) * prec_size(d->prec)) != cudaSuccess) {
     cudaGetLastError();
     return TBSLA_ERR_ALLOC;
   }
-  if ((st = dalloc(&d->scols, std::max<size_t>(dp.sell_len, 1))) || (st = dalloc(&d->sell_counter, 2))) return st;
-  d->bytes += (size_t)dp.sell_len * (prec_size(d->prec) + 4);
+  if ((st = dalloc(&d->scols, std::max<size_t>(len, 1))) || (st = dalloc(&d->sell_counter, 2))) return st;
+  d->bytes += len * (prec_size(d->prec) + 4);
   TRY(cudaMemsetAsync(d->sell_counter, 0, 2 * sizeof(unsigned), d->stream));
-  TRY(sell_fill(sell_args(m, d), d->svals, d->scols, d->stream));
+  TRY(sell_fill(sell_args(m, d), d->stream));
   return TBSLA_OK;
 }
 
@@ -598,7 +638,7 @@ int dev_normalize_cols(tbsla_matrix* m, const double* s) {
   // keep the host arrays (the reference layout) in step with the device
   TRY(cudaMemcpyAsync(m->values.data(), v64, d->nnz * 8, cudaMemcpyDeviceToHost, str));
   if (owned) TRY(convert_values(v64, d->vals, d->prec, d->nnz, str));
-  if (d->algo == 2 && d->svals) TRY(sell_fill(sell_args(m, d), d->svals, d->scols, str));  // slice copy
+  if (d->algo == 2 && d->svals) TRY(sell_fill(sell_args(m, d), str));  // slice copy
   d->colw_ok = false;
   TRY(cudaStreamSynchronize(str));
   if (owned) cudaFree(v64);
@@ -686,13 +726,19 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
   cudaStream_t s = d->stream;
   double *x0 = nullptr, *x1 = nullptr, *coef = nullptr;
   int* flags = nullptr;  // [0] done, [1] iterations
-  int grid = I.nnz > 0 ? csr_pagerank_grid(d->items, d->prec) : 1;
+  // the sliced-ELL kernel (FP64-efficient on skewed rows) with a separate
+  // epilogue pass, or the row-block kernel with the epilogue fused
+  const bool sell = d->algo == 2;
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device);
+  int grid = sell ? 8 * sms : (I.nnz > 0 ? csr_pagerank_grid(d->items, d->prec) : 1);
   auto cleanup = [&]() {
     for (void* p : {(void*)x0, (void*)x1, (void*)coef, (void*)flags})
       if (p) cudaFree(p);
   };
   if ((st = dalloc(&x0, n)) || (st = dalloc(&x1, n)) || (st = dalloc(&coef, 4)) ||
-      (st = dalloc(&flags, 2)) || (st = d->ctl(3, grid)) || (st = column_weights(m, d))) {
+      (st = dalloc(&flags, 2)) || (st = d->ctl(3, grid)) || (st = column_weights(m, d)) ||
+      (sell && (st = d->vec(&d->t, &d->t_len, (size_t)n)))) {
     cleanup();
     return st;
   }
@@ -713,8 +759,13 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
       const bool even = (launched % 2) == 0;
       p.coef_in = coef + (even ? 0 : 2);
       p.coef_out = coef + (even ? 2 : 0);
-      cudaError_t e = I.nnz > 0 ? csr_pagerank_step(a, even ? x0 : x1, even ? x1 : x0, p, ctl, grid, s)
-                                : cudaErrorInvalidValue;
+      cudaError_t e = cudaErrorInvalidValue;
+      if (I.nnz > 0 && sell) {
+        e = sell_spmv(sell_args(m, d), even ? x0 : x1, d->t, d->sell_counter, s, flags);
+        if (e == cudaSuccess) e = pagerank_epilogue(d->t, even ? x0 : x1, even ? x1 : x0, n, p, ctl, grid, s);
+      } else if (I.nnz > 0) {
+        e = csr_pagerank_step(a, even ? x0 : x1, even ? x1 : x0, p, ctl, grid, s);
+      }
       if (e != cudaSuccess) {
         cleanup();
         return I.nnz > 0 ? status_of(e) : TBSLA_ERR_BAD_MATRIX;
@@ -814,6 +865,94 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   if (st) return st;
   if (iterations) *iterations = iters;
   return hflags[0] ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
+}
+
+// ---- autotuner ------------------------------------------------------------------------
+
+namespace {
+void apply_tuning(tbsla_matrix* m, const tbsla_tuning& t) {
+  const bool rebuild = m->csr_algo != t.algorithm ||
+                       (t.algorithm == TBSLA_CSR_MERGE && m->merge_items != t.items) ||
+                       (t.algorithm == TBSLA_CSR_ROWBLOCK && m->csr_tile != t.tile) ||
+                       (t.algorithm == TBSLA_CSR_SELL &&
+                        (m->sell_short != t.short_thr || m->sell_long != t.long_thr ||
+                         m->sell_sigma != t.sigma || m->sell_colblock != t.col_block));
+  if (rebuild) m->invalidate();
+  m->csr_algo = t.algorithm;
+  if (t.algorithm == TBSLA_CSR_MERGE) m->merge_items = t.items;
+  if (t.algorithm == TBSLA_CSR_ROWBLOCK) m->csr_tile = t.tile;
+  if (t.algorithm == TBSLA_CSR_SELL) {
+    m->sell_unroll = t.items;
+    m->sell_short = t.short_thr;
+    m->sell_long = t.long_thr;
+    m->sell_sigma = t.sigma;
+    m->sell_colblock = t.col_block;
+  }
+}
+}  // namespace
+
+int dev_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* trials, int max_trials,
+                 int* ntrials) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  const tbsla_info& I = m->info;
+  reps = std::max(reps, 1);
+  // candidates, grouped so that consecutive ones share a device layout
+  std::vector<tbsla_tuning> cand;
+  std::vector<int> blocks = {0};
+  if (I.ln_col > 8388608) blocks.push_back(I.ln_col);  // one block
+  if (I.ln_col > 4194304) blocks.push_back(4194304);
+  const int thr[4][2] = {{64, 64}, {128, 128}, {32, 32}, {64, 255}};
+  for (int cb : blocks)
+    for (auto& t : thr)
+      for (int u : {8, 16}) cand.push_back({TBSLA_CSR_SELL, u, t[0], t[1], 16384, cb, m->csr_tile, 0.0});
+  const tbsla_tuning keep{m->csr_algo, m->csr_algo == TBSLA_CSR_MERGE ? m->merge_items : m->sell_unroll,
+                          m->sell_short, m->sell_long, m->sell_sigma, m->sell_colblock, m->csr_tile, 0.0};
+  cand.push_back({TBSLA_CSR_MERGE, 8, keep.short_thr, keep.long_thr, keep.sigma, keep.col_block, keep.tile, 0});
+  cand.push_back({TBSLA_CSR_ROWBLOCK, 0, keep.short_thr, keep.long_thr, keep.sigma, keep.col_block, 2048, 0});
+  double *x = nullptr, *y = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int st = TBSLA_OK;
+  if ((st = check_device())) return st;
+  cudaSetDevice(g_device);
+  if ((st = dalloc(&x, std::max(I.ln_col, 1))) || (st = dalloc(&y, std::max(I.ln_row, 1)))) {
+    cudaFree(x);
+    return st;
+  }
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int bestk = -1, count = 0;
+  for (size_t k = 0; k < cand.size() && !st; k++) {
+    apply_tuning(m, cand[k]);
+    DeviceMatrix* d = ensure(m, &st);
+    if (st) break;
+    cudaStream_t s = d->stream;
+    if ((st = status_of(vec_fill(x, 1.0, I.ln_col, s)))) break;
+    if ((st = ax_device(m, d, y, x, 0, s))) break;  // warm-up
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps && !st; r++) st = ax_device(m, d, y, x, 0, s);
+    cudaEventRecord(e1, s);
+    if (!st) st = status_of(cudaEventSynchronize(e1));
+    if (st) break;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cand[k].ms = ms / reps;
+    if (trials && count < max_trials) trials[count] = cand[k];
+    count++;
+    if (bestk < 0 || cand[k].ms < cand[bestk].ms) bestk = (int)k;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(x);
+  cudaFree(y);
+  if (ntrials) *ntrials = std::min(count, std::max(max_trials, 0));
+  if (st || bestk < 0) {
+    apply_tuning(m, keep);
+    return st ? st : TBSLA_ERR_CUDA;
+  }
+  apply_tuning(m, cand[bestk]);
+  if (best) *best = cand[bestk];
+  ensure(m, &st);
+  return st;
 }
 
 long dev_noalloc_max_items() { return csr_merge_noalloc_max_items(); }

@@ -34,6 +34,10 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
 int dev_cg(tbsla_matrix* m, const double* b, double* x, int max_it, double rel_tol, int precond,
            int refresh, int* iterations, double* rel_residual);
 
+// Autotuner: times the CSR kernel configurations, keeps the fastest.
+int dev_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* trials, int max_trials,
+                 int* ntrials);
+
 // Merge-path CSR SpMV on caller-owned device arrays with file-scope scratch
 // (allocates nothing); n_row + nnz at most dev_noalloc_max_items().
 long dev_noalloc_max_items();

@@ -66,20 +66,30 @@ cudaError_t csr_merge_spmv_noalloc(const double* vals, const int* rowptr, const 
 // most short_thr entries take one lane each and are sorted by length within
 // windows of `sigma` consecutive rows; longer rows take the fewest lanes (up
 // to 32) that keep their slice at most long_thr steps wide and are sorted by
-// length over the whole matrix.  One warp per slice, fetched dynamically,
+// length over the whole block.  One warp per slice, fetched dynamically,
 // widest slices first; lanes past their row's end issue no loads, so
 // padding costs no traffic.
+//
+// The columns are split into blocks small enough for their part of x to
+// stay in L2 while the block runs (x beyond ~60 MB misses L2 for most
+// gathers on GB300); each block has its own plan and launch, the first
+// writing y, the others adding to it in block order.
 struct SellPlan {
-  int n = 0, short_thr = 0, long_thr = 0, sigma = 0;
-  int nwide = 0;      // slices sorted over the whole matrix (processed first)
-  int nslices = 0;    // all slices
-  long sell_len = 0;  // elements of the slice arrays
-  int4* slice = nullptr;  // [nslices]: {step offset, width in steps, g, base}
-  int* lane = nullptr;    // [32 * nslices]: base >= 0: (row - base) << 8 | len;
-                          // base = -1: row; -1 for an unused lane
+  int n = 0;
+  int col_lo = 0, col_hi = 0;  // the block's columns, relative to f_col
+  int nwide = 0;               // slices sorted over the whole block (processed first)
+  int nslices = 0;             // all slices of the block
+  long sell_len = 0;           // elements of the block's slices
+  int4* slice = nullptr;       // [nslices]: {step offset, width in steps, g, base}
+  int* lane = nullptr;         // [32 * nslices]: base >= 0: (row - base) << 8 | len;
+                               // base = -1: row; -1 for an unused lane
+  int* lane_len = nullptr;     // [32 * nwide]: the row's entries in the block
 };
-// Host: plan from a row pointer (arrays allocated with new[]).
-void sell_plan_build(const int* rowptr, int n, int short_thr, int long_thr, int sigma, SellPlan* p);
+// Host: plan of one column block from its per-row entry counts L[n]
+// (arrays allocated with new[]); rows with no entry are left out when
+// skip_empty; step offsets start at step0.
+void sell_plan_build(const int* L, int n, int short_thr, int long_thr, int sigma, bool skip_empty, long step0,
+                     SellPlan* p);
 void sell_plan_free(SellPlan* p);
 struct SellArgs {
   const void* vals;  // CSR copy (the slice arrays are filled from it)
@@ -87,15 +97,19 @@ struct SellArgs {
   const int* rowptr;
   const int* colidx;
   int f_col;
-  const void* svals;  // slice arrays
-  const int* scols;
-  int unroll;     // steps per lane in flight: 4, 8 or 16
-  SellPlan plan;  // device pointers
+  void* svals;  // slice arrays of all blocks
+  int* scols;
+  int unroll;               // steps per lane in flight: 4, 8 or 16
+  int nblocks;              // column blocks
+  const SellPlan* blocks;   // host array of plans holding device pointers
 };
-// Fills the slice arrays from the CSR device arrays.
-cudaError_t sell_fill(const SellArgs& a, void* svals, int* scols, cudaStream_t s);
-// y[row] = (A x)[row]; counter: 2 unsigned of zeroed scratch, reset by the kernel.
-cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s);
+// Fills the slice arrays of every block from the CSR device arrays.
+cudaError_t sell_fill(const SellArgs& a, cudaStream_t s);
+// y = A x, one launch per column block; counter: 2 unsigned of zeroed
+// scratch, reset by each launch; a set *done (device) makes the launches
+// no-ops.
+cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s,
+                      const int* done = nullptr);
 
 // Row-block partition of a CSR row pointer (host): blocks of consecutive
 // rows with at most `tile` entries and at most 256 rows each; a row longer
@@ -131,6 +145,12 @@ cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
 cudaError_t csr_pagerank_batched_step(const CsrArgs& a, int n_row, int nvec, const double* X,
                                       double* Y, const double* T, const PageRankArgs& p,
                                       Ctl ctl, int grid, cudaStream_t s);
+
+// PageRank step after a separate SpMV t = A x (the sliced-ELL path): the
+// same y, reductions and coefficients as csr_pagerank_step, over n rows, in
+// `grid` CTAs (ctl sized for grid x 3 partials).
+cudaError_t pagerank_epilogue(const double* t, const double* x, double* y, long n, const PageRankArgs& p,
+                              Ctl ctl, int grid, cudaStream_t s);
 
 // CTAs of the persistent PageRank kernels (resident capacity of the GPU).
 int csr_pagerank_grid(int items, int prec);

@@ -102,6 +102,32 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   });
 }
 
+// PageRank epilogue over a separately computed t = A x: the EpiPageRank
+// step of every row (grid-stride, fixed grid, so the reduction order is
+// fixed), then the deterministic CTA reduction and the next coefficients.
+__global__ void __launch_bounds__(NT) k_pagerank_epilogue(const double* __restrict__ t,
+                                                         const double* __restrict__ x, double* __restrict__ y,
+                                                         long n, PageRankArgs p, Ctl ctl) {
+  __shared__ Smem sm;
+  if (*(volatile int*)p.done) return;
+  const double s = p.coef_in[0], tw = p.coef_in[1];
+  EpiPageRank epi{y, x, p.colw, p.tele, p.beta, s, tw, tw / p.n_nodes};
+  double red[3] = {0, 0, 0};
+  for (long i = blockIdx.x * (long)NT + threadIdx.x; i < n; i += (long)gridDim.x * NT)
+    epi.emit((int)i, t[i], red);
+  const double beta = p.beta, eps = p.eps;
+  double* coef_out = p.coef_out;
+  int* done = p.done;
+  int* iters = p.iters;
+  reduce_and_finish<3>(ctl, red, sm, [=] __device__(double* r) {
+    const double s1 = 1.0 / r[1];
+    coef_out[0] = s1;
+    coef_out[1] = teleport_weight(beta, s1, r[2]);
+    *iters += 1;
+    if (r[0] < eps) *done = 1;
+  });
+}
+
 // Batched personalised PageRank: lanes of a warp are the nvec vectors; the
 // warps of the CTA take the rows of a block in turn.  Each lane sums its
 // row's products in entry order.
@@ -135,7 +161,21 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
           v = widen(ld_stream(vals + j, pol));
         }
         const int m = min(kWarp, e - base);
-        for (int t = 0; t < m; t++) {
+        int t = 0;
+        // 8 entries' gathers of X in flight, then their multiply-adds in
+        // entry order
+        for (; t + 8 <= m; t += 8) {
+          double xv[8], vv[8];
+#pragma unroll
+          for (int u = 0; u < 8; u++) {
+            const int ct = __shfl_sync(0xffffffffu, c, t + u);
+            vv[u] = __shfl_sync(0xffffffffu, v, t + u);
+            xv[u] = active ? ld_gather(X + (size_t)(ct - a.f_col) * nvec + lane) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; u++) acc = fma_rn(vv[u], xv[u], acc);
+        }
+        for (; t < m; t++) {
           const int ct = __shfl_sync(0xffffffffu, c, t);
           const double vt = __shfl_sync(0xffffffffu, v, t);
           if (active) acc = fma_rn(vt, ld_gather(X + (size_t)(ct - a.f_col) * nvec + lane), acc);
@@ -322,6 +362,12 @@ cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
     case kBF16: return pr_items<__nv_bfloat16>(a, x, y, p, ctl, grid, s);
   }
   return cudaErrorInvalidValue;
+}
+
+cudaError_t pagerank_epilogue(const double* t, const double* x, double* y, long n, const PageRankArgs& p,
+                              Ctl ctl, int grid, cudaStream_t s) {
+  k_pagerank_epilogue<<<grid, NT, 0, s>>>(t, x, y, n, p, ctl);
+  return cudaGetLastError();
 }
 
 cudaError_t csr_pagerank_batched_step(const CsrArgs& a, int n_row, int nvec, const double* X,

@@ -94,35 +94,42 @@ __device__ __forceinline__ double slice_rows(const V* __restrict__ sv, const int
 
 struct Lane {
   int row;    // -1: unused lane
+  int len;    // the row's entries in this column block
   int steps;  // live steps of this lane
 };
 
-// Decodes lane `lane` of slice `d` = {step offset, width, g, base}: a
-// window slice (base >= 0) packs (row - base) << 8 | length per lane, a
-// slice sorted over the whole matrix (base = -1) holds the row.
-__device__ __forceinline__ Lane slice_lane(const int4& d, int meta, const int* rowptr, int lane) {
-  Lane l{-1, 0};
+// Decodes lane `lane` of slice k with descriptor d = {step offset, width, g,
+// base}: a window slice (base >= 0) packs (row - base) << 8 | length per
+// lane; a slice sorted over the whole block (base = -1) holds the row, with
+// its length in lane_len.
+__device__ __forceinline__ Lane slice_lane(const SellPlan& p, const int4& d, int meta, long k, int lane) {
+  Lane l{-1, 0, 0};
   if (meta < 0) return l;
   if (d.w >= 0) {
     l.row = d.w + (meta >> 8);
-    l.steps = meta & 255;
+    l.len = l.steps = meta & 255;
   } else {
     l.row = meta;
-    const int len = rowptr[meta + 1] - rowptr[meta];
+    l.len = __ldg(p.lane_len + k * 32 + lane);
     const int sub = lane & ((1 << d.z) - 1);
-    l.steps = len > sub ? (len - sub + (1 << d.z) - 1) >> d.z : 0;
+    l.steps = l.len > sub ? (l.len - sub + (1 << d.z) - 1) >> d.z : 0;
   }
   return l;
 }
 
+// One column block: y = A_block x (block 0) or y += A_block x (later blocks,
+// whose plans leave out the rows without entries in the block).
 template <class V, int U>
-__global__ void __launch_bounds__(NT) k_sell(SellArgs a, const double* __restrict__ x, double* __restrict__ y,
-                                            unsigned* __restrict__ counter) {
+__global__ void __launch_bounds__(NT) k_sell(SellPlan p, const V* __restrict__ sv, const int* __restrict__ sc,
+                                            int f_col, int accumulate, const double* __restrict__ x,
+                                            double* __restrict__ y, unsigned* __restrict__ counter,
+                                            const int* __restrict__ done) {
+  // a set done flag (an iteration that has converged) makes the launch a
+  // no-op; no warp has touched the counter then
+  if (done && *(volatile const int*)done) return;
   const int lane = threadIdx.x & 31;
-  const SellPlan& p = a.plan;
   const int nitems = p.nslices;
   const uint64_t pol = policy_evict_first();
-  const V* sv = static_cast<const V*>(a.svals);
   // Two items are claimed ahead, and the descriptor of the next one is
   // loaded while the current one runs, so neither the work counter's
   // atomics nor the descriptor loads sit on the critical path.
@@ -148,10 +155,12 @@ __global__ void __launch_bounds__(NT) k_sell(SellArgs a, const double* __restric
       dn = __ldg(p.slice + nxt);
       mn = __ldg(p.lane + (long)nxt * 32 + lane);
     }
-    const Lane l = slice_lane(d, meta, a.rowptr, lane);
-    double acc = slice_rows<V, U>(sv, a.scols, (long)d.x * 32 + lane, l.steps, d.y, x, a.f_col, pol);
+    const Lane l = slice_lane(p, d, meta, cur, lane);
+    const bool head = l.row >= 0 && (lane & ((1 << d.z) - 1)) == 0;
+    const double y0 = (accumulate && head) ? y[l.row] : 0.0;  // issued before the sum
+    double acc = slice_rows<V, U>(sv, sc, (long)d.x * 32 + lane, l.steps, d.y, x, f_col, pol);
     for (int o = (1 << d.z) >> 1; o > 0; o >>= 1) acc = add_rn(acc, __shfl_xor_sync(FULL, acc, o));
-    if (l.row >= 0 && (lane & ((1 << d.z) - 1)) == 0) y[l.row] = acc;
+    if (head) y[l.row] = accumulate ? add_rn(y0, acc) : acc;
     cur = nxt;
     nxt = __shfl_sync(FULL, after, 0);
     d = dn;
@@ -168,88 +177,118 @@ __global__ void __launch_bounds__(NT) k_sell(SellArgs a, const double* __restric
   }
 }
 
+// Fills one column block's slices from the CSR arrays: the G lanes of a row
+// walk its entries G at a time and place those of the block, in entry
+// order, at position q -> (step q / G, lane q mod G of the group).  Unused
+// positions get a zero value on a valid column (never read by k_sell).
 template <class V>
-__global__ void __launch_bounds__(NT) k_sell_fill(SellArgs a, V* __restrict__ sv, int* __restrict__ sc) {
+__global__ void __launch_bounds__(NT) k_sell_fill(SellPlan p, const V* __restrict__ vals,
+                                                 const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                                                 int f_col, V* __restrict__ sv, int* __restrict__ sc) {
   const int lane = threadIdx.x & 31;
-  const SellPlan& p = a.plan;
-  const V* vals = static_cast<const V*>(a.vals);
   const long warps = (long)gridDim.x * (NT / 32);
   for (long k = (blockIdx.x * (long)NT + threadIdx.x) / 32; k < p.nslices; k += warps) {
     const int4 d = p.slice[k];
-    const Lane l = slice_lane(d, p.lane[k * 32 + lane], a.rowptr, lane);
-    const long off = (long)d.x * 32 + lane;
-    const int s = l.row >= 0 ? a.rowptr[l.row] + (lane & ((1 << d.z) - 1)) : 0;
-    for (int t = 0; t < d.y; t++) {
-      // padding: a zero value on a valid column (never read by the kernel)
-      V v = V(0.0f);
-      int c = a.f_col;
-      if (t < l.steps) {
-        v = vals[s + ((long)t << d.z)];
-        c = a.colidx[s + ((long)t << d.z)];
+    const Lane l = slice_lane(p, d, p.lane[k * 32 + lane], k, lane);
+    const int G = 1 << d.z, sub = lane & (G - 1), group = lane & ~(G - 1);
+    const long off = (long)d.x * 32;
+    const int s = l.row >= 0 ? rowptr[l.row] : 0;
+    const int e = l.row >= 0 ? rowptr[l.row + 1] : 0;
+    const int span = __reduce_max_sync(FULL, e - s);
+    int placed = 0;  // entries of this lane's row placed so far
+    for (int base = 0; base < span; base += G) {
+      const int j = s + base + sub;
+      const int col = j < e ? colidx[j] - f_col : -1;
+      const bool in = col >= p.col_lo && col < p.col_hi;
+      const unsigned m = (__ballot_sync(FULL, in) >> group) & (G == 32 ? FULL : (1u << G) - 1);
+      if (in) {
+        const int q = placed + __popc(m & ((1u << sub) - 1));
+        const long o = off + (long)(q >> d.z) * 32 + group + (q & (G - 1));
+        sv[o] = vals[j];
+        sc[o] = colidx[j];
       }
-      sv[off + (long)t * 32] = v;
-      sc[off + (long)t * 32] = c;
+      placed += __popc(m);
+    }
+    for (int t = l.steps; t < d.y; t++) {
+      sv[off + (long)t * 32 + lane] = V(0.0f);
+      sc[off + (long)t * 32 + lane] = f_col;
     }
   }
 }
 
 template <class V, int U>
-cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s) {
+cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* counter, const int* done,
+                   cudaStream_t s) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V, U>, NT, 0);
   const int grid = std::max(1, sms * std::max(1, per));
-  k_sell<V, U><<<grid, NT, 0, s>>>(a, x, y, counter);
-  return cudaGetLastError();
+  for (int b = 0; b < a.nblocks; b++) {
+    const SellPlan& p = a.blocks[b];
+    if (p.nslices == 0) continue;
+    k_sell<V, U><<<grid, NT, 0, s>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
+                                     counter, done);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 template <class V>
-cudaError_t launch_fill(const SellArgs& a, void* sv, int* sc, cudaStream_t s) {
-  const long items = a.plan.nslices;
-  const int grid = (int)std::max<long>(1, std::min<long>((items + 7) / 8, 152L * 32));
-  k_sell_fill<V><<<grid, NT, 0, s>>>(a, static_cast<V*>(sv), sc);
-  return cudaGetLastError();
+cudaError_t launch_fill(const SellArgs& a, cudaStream_t s) {
+  for (int b = 0; b < a.nblocks; b++) {
+    const SellPlan& p = a.blocks[b];
+    if (p.nslices == 0) continue;
+    const int grid = (int)std::max<long>(1, std::min<long>((p.nslices + 7) / 8, 152L * 32));
+    k_sell_fill<V><<<grid, NT, 0, s>>>(p, static_cast<const V*>(a.vals), a.rowptr, a.colidx, a.f_col,
+                                       static_cast<V*>(a.svals), a.scols);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 template <class V>
-cudaError_t launch_u(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s) {
+cudaError_t launch_u(const SellArgs& a, const double* x, double* y, unsigned* counter, const int* done,
+                     cudaStream_t s) {
   switch (a.unroll) {
-    case 4: return launch<V, 4>(a, x, y, counter, s);
-    case 16: return launch<V, 16>(a, x, y, counter, s);
-    default: return launch<V, 8>(a, x, y, counter, s);
+    case 4: return launch<V, 4>(a, x, y, counter, done, s);
+    case 16: return launch<V, 16>(a, x, y, counter, done, s);
+    default: return launch<V, 8>(a, x, y, counter, done, s);
   }
 }
 
 }  // namespace
 
-void sell_plan_build(const int* rp, int n, int sthr, int lthr, int sigma, SellPlan* p) {
+void sell_plan_build(const int* L, int n, int sthr, int lthr, int sigma, bool skip_empty, long step0,
+                     SellPlan* p) {
   using tbsla_impl::parallel_for;
   *p = SellPlan{};
   p->n = n;
-  p->short_thr = sthr = std::max(1, std::min(sthr, 255));
-  p->long_thr = lthr = std::max(lthr, 1);
-  p->sigma = sigma = std::max(32, std::min(sigma, 1 << 23));
-  auto len = [&](int i) { return rp[i + 1] - rp[i]; };
+  sthr = std::max(1, std::min(sthr, 255));
+  lthr = std::max(lthr, 1);
+  sigma = std::max(32, std::min(sigma, 1 << 23));
+  auto len = [&](int i) { return L[i]; };
   // lanes per row (log2) of a row longer than short_thr
   auto lanes_log2 = [&](int l) {
     int g = 0;
     while (g < 5 && (l + (1 << g) - 1) >> g > lthr) g++;
     return g;
   };
-  // Rows past short_thr: per lane count, sorted by length over the matrix.
+  // Rows past short_thr: per lane count, sorted by length over the block.
   std::vector<int> lng[6];
   for (int i = 0; i < n; i++) {
     const int l = len(i);
     if (l > sthr) lng[lanes_log2(l)].push_back(i);
   }
   struct Slice {
-    int width, g, base;
-    long first;  // index into `rows` of its first row (g > 0)
+    int width, g;
+    long first;  // index into wide_rows of its first row
   };
   std::vector<int4> desc;
-  std::vector<int> meta;
-  std::vector<std::pair<int, int>> order;  // (width, slice) of the g > 0 slices
+  std::vector<int> meta, meta_len;
+  std::vector<std::pair<int, int>> order;  // (width, slice) of the wide slices
   std::vector<Slice> wide;
   std::vector<int> wide_rows;
   auto by_len = [&](int a, int b) { return len(a) > len(b); };
@@ -258,18 +297,22 @@ void sell_plan_build(const int* rp, int n, int sthr, int lthr, int sigma, SellPl
     std::stable_sort(v.begin(), v.end(), by_len);
     const int per = 32 >> g;
     for (size_t q = 0; q < v.size(); q += per) {
-      Slice s{(len(v[q]) + (1 << g) - 1) >> g, g, 0, (long)wide_rows.size()};
+      Slice s{(len(v[q]) + (1 << g) - 1) >> g, g, (long)wide_rows.size()};
       for (int r = 0; r < per; r++) wide_rows.push_back(q + r < v.size() ? v[q + r] : -1);
       order.push_back({s.width, (int)wide.size()});
       wide.push_back(s);
     }
   }
   std::stable_sort(order.begin(), order.end(), [](auto& a, auto& b) { return a.first > b.first; });
-  long off = 0;  // in steps of 32 entries
+  long off = step0;  // in steps of 32 entries
   for (auto& o : order) {
     const Slice& s = wide[o.second];
     desc.push_back(make_int4((int)off, s.width, s.g, -1));
-    for (int l = 0; l < 32; l++) meta.push_back(wide_rows[s.first + (l >> s.g)]);
+    for (int l = 0; l < 32; l++) {
+      const int row = wide_rows[s.first + (l >> s.g)];
+      meta.push_back(row);
+      meta_len.push_back(row >= 0 ? len(row) : 0);
+    }
     off += s.width;
   }
   // Short rows: one lane each, sorted by length within windows.
@@ -280,7 +323,7 @@ void sell_plan_build(const int* rp, int n, int sthr, int lthr, int sigma, SellPl
       const int r0 = (int)(w * sigma), r1 = (int)std::min<long>((w + 1) * (long)sigma, n);
       auto& v = win[w];
       for (int i = r0; i < r1; i++)
-        if (len(i) <= sthr) v.push_back(i);
+        if (len(i) <= sthr && (len(i) > 0 || !skip_empty)) v.push_back(i);
       std::stable_sort(v.begin(), v.end(), by_len);
     }
   });
@@ -315,35 +358,37 @@ void sell_plan_build(const int* rp, int n, int sthr, int lthr, int sigma, SellPl
   }
   p->nwide = (int)nwide;
   p->nslices = (int)(nwide + nshort);
-  p->sell_len = off * 32;
+  p->sell_len = (off - step0) * 32;
   p->slice = new int4[std::max<size_t>(desc.size(), 1)];
   std::copy(desc.begin(), desc.end(), p->slice);
   p->lane = new int[std::max<size_t>(meta.size(), 1)];
   std::copy(meta.begin(), meta.end(), p->lane);
+  p->lane_len = new int[std::max<size_t>(meta_len.size(), 1)];
+  std::copy(meta_len.begin(), meta_len.end(), p->lane_len);
 }
 
 void sell_plan_free(SellPlan* p) {
   delete[] p->slice;
   delete[] p->lane;
+  delete[] p->lane_len;
   *p = SellPlan{};
 }
 
-cudaError_t sell_fill(const SellArgs& a, void* svals, int* scols, cudaStream_t s) {
-  if (a.plan.nslices == 0) return cudaSuccess;
+cudaError_t sell_fill(const SellArgs& a, cudaStream_t s) {
   switch (a.prec) {
-    case kF64: return launch_fill<double>(a, svals, scols, s);
-    case kF32: return launch_fill<float>(a, svals, scols, s);
-    case kBF16: return launch_fill<__nv_bfloat16>(a, svals, scols, s);
+    case kF64: return launch_fill<double>(a, s);
+    case kF32: return launch_fill<float>(a, s);
+    case kBF16: return launch_fill<__nv_bfloat16>(a, s);
   }
   return cudaErrorInvalidValue;
 }
 
-cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s) {
-  if (a.plan.nslices == 0) return cudaSuccess;
+cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s,
+                      const int* done) {
   switch (a.prec) {
-    case kF64: return launch_u<double>(a, x, y, counter, s);
-    case kF32: return launch_u<float>(a, x, y, counter, s);
-    case kBF16: return launch_u<__nv_bfloat16>(a, x, y, counter, s);
+    case kF64: return launch_u<double>(a, x, y, counter, done, s);
+    case kF32: return launch_u<float>(a, x, y, counter, done, s);
+    case kBF16: return launch_u<__nv_bfloat16>(a, x, y, counter, done, s);
   }
   return cudaErrorInvalidValue;
 }

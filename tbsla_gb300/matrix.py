@@ -249,11 +249,20 @@ class MatrixCSR(Matrix):
 
     MERGE, ROWBLOCK, SELL = 0, 1, 2
 
-    def set_algorithm(self, algorithm: int, items: int = 8):
+    def set_algorithm(self, algorithm: int, items: int = 0):
         check(lib.tbsla_matrix_set_csr_algorithm(self._h, algorithm, items), "set_csr_algorithm")
 
-    def set_sell_params(self, short_thr: int = 64, long_thr: int = 64, sigma: int = 16384):
-        check(lib.tbsla_matrix_set_sell_params(self._h, short_thr, long_thr, sigma), "set_sell_params")
+    def autotune(self, reps: int = 5, max_trials: int = 64):
+        """Times the CSR kernel configurations on this matrix, keeps the
+        fastest; returns (best, trials) as dicts."""
+        best = L.Tuning()
+        trials = (L.Tuning * max_trials)()
+        nt = C.c_int()
+        check(lib.tbsla_matrix_autotune(self._h, reps, C.byref(best), trials, max_trials, C.byref(nt)), "autotune")
+        return best.as_dict(), [trials[i].as_dict() for i in range(nt.value)]
+
+    def set_sell_params(self, short_thr: int = 64, long_thr: int = 64, sigma: int = 16384, col_block: int = 0):
+        check(lib.tbsla_matrix_set_sell_params(self._h, short_thr, long_thr, sigma, col_block), "set_sell_params")
 
     # project generators
     def fill_uniform_rows(self, n, k, seed):

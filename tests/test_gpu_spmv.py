@@ -147,7 +147,8 @@ def powerlaw(T, n, seed=5, **kw):
     return m
 
 
-CSR_KERNELS = [("sell", (64, 64, 16384, 8)), ("sell", (4, 3, 64, 4)), ("sell", (255, 1000, 1 << 20, 16)),
+CSR_KERNELS = [("sell", (64, 64, 16384, 8, 0)), ("sell", (4, 3, 64, 4, 50000)),
+               ("sell", (255, 1000, 1 << 20, 16, 100000)), ("sell", (128, 128, 16384, 16, 4096)),
                ("merge", 4), ("merge", 8), ("merge", 16), ("rowblock", 1024), ("rowblock", 2048),
                ("rowblock", 4096)]
 
@@ -155,7 +156,7 @@ CSR_KERNELS = [("sell", (64, 64, 16384, 8)), ("sell", (4, 3, 64, 4)), ("sell", (
 def set_kernel(m, kind, p):
     if kind == "sell":
         m.set_algorithm(m.SELL, p[3])
-        m.set_sell_params(*p[:3])
+        m.set_sell_params(*p[:3], p[4])
     elif kind == "merge":
         m.set_algorithm(m.MERGE, p)
     else:
@@ -316,3 +317,21 @@ def test_col_sums_normalize_match_reference(gpu, golden):
         a = m.arrays()
         end = int(a["rowptr"][-1])
         assert np.array_equal(a["values"][:end], ops[f"colsum/{key}/values"][:end])
+
+
+def test_autotune_keeps_the_fastest_and_stays_exact(gpu):
+    """The autotuner times every candidate, leaves the handle on the fastest,
+    and the tuned SpMV still meets the FP64 bar."""
+    T = gpu
+    n = 1 << 17
+    m = powerlaw(T, n, seed=9)
+    best, trials = m.autotune(reps=3)
+    assert len(trials) >= 10 and all(t["ms"] > 0 for t in trials)
+    assert best["ms"] == min(t["ms"] for t in trials)
+    assert {t["algorithm"] for t in trials} == {m.SELL, m.MERGE, m.ROWBLOCK}
+    a = m.arrays()
+    x = T.fill_uniform(n, 0.0, 1.0, 3)
+    y = m.spmv(x)
+    ref = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x, threads=True)
+    scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x)
+    assert oracle.rel_err_normalized(y, ref, scale) <= TOL
