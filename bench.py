@@ -45,8 +45,12 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["spmv", "pagerank", "cg"], default="spmv",
-                   help="spmv: the large-SpMV headline; pagerank: the PageRank graph; cg: batched CG")
+    p.add_argument("--workload", choices=["spmv", "pagerank", "cg", "learned"], default="spmv",
+                   help="spmv: the large-SpMV headline; pagerank: the PageRank graph; cg: batched CG; "
+                        "learned: learned-preconditioner PCG against Jacobi-PCG")
+    p.add_argument("--train-systems", type=int, default=2000, help="learned: training systems (seeds 1000..)")
+    p.add_argument("--eval-systems", type=int, default=32, help="learned: held-out systems (seeds 9000..)")
+    p.add_argument("--eval-n", type=int, default=128, help="learned: held-out grid size n (n^3 unknowns)")
     p.add_argument("--n", type=int, default=None, help="rows (spmv: 2^24, pagerank: 2^22)")
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
@@ -572,6 +576,87 @@ def run_cg(a):
     print(json.dumps(line), flush=True)
 
 
+def run_learned(a):
+    """The learned-preconditioner workload: the network is trained on the
+    GPU (one Adam step per system, lr 1e-3, 8 Gaussian probes) on diffusion
+    systems with n in [32, 64] (seeds 1000..), then 32 held-out 128^3 systems
+    (seeds 9000..9031, RHS U[-1,1)) are solved in one batch by Jacobi-PCG and
+    by PCG with M^-1 = L L^T from the network, both with FP32 values, FP64
+    refresh every 50 iterations, to a 1e-8 FP64-verified relative residual.
+    value: learned-PCG wall time / Jacobi-PCG wall time (lower is better)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import numpy as np
+    import torch
+
+    import tbsla_gb300 as T
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    T.device_init(local)
+
+    def system(n, seed):
+        m = T.MatrixCSR()
+        m.fill_diffusion7(n, 1.0, 8.0, seed)
+        return m
+
+    rng = np.random.default_rng(5)
+    sizes = rng.integers(32, 65, a.train_systems)
+    net = T.MPNN(1)
+    t0 = time.time()
+    losses = []
+    with ThreadPoolExecutor(4) as pool:
+        futs = [pool.submit(system, int(sizes[k]), 1000 + k) for k in range(min(8, a.train_systems))]
+        for k in range(a.train_systems):
+            A = futs[k].result()
+            if k + 8 < a.train_systems:
+                futs.append(pool.submit(system, int(sizes[k + 8]), 1000 + k + 8))
+            losses.append(net.train_step(A, probes=8, seed=k, lr=1e-3))
+            futs[k] = None
+    t_train = time.time() - t0
+    held = [system(a.eval_n, 9000 + k) for k in range(a.eval_systems)]
+    N = a.eval_n ** 3
+    rhs = np.concatenate([T.fill_uniform(N, -1.0, 1.0, 9100 + k) for k in range(a.eval_systems)])
+    t0 = time.time()
+    factors = [net.factor(A) for A in held]
+    t_factor = time.time() - t0
+    res = {}
+    clk = Clocks(local)
+    for name, pre in (("jacobi_pcg", 1), ("learned_pcg", 2)):
+        bt = T.Batch(held, T.F32)
+        if pre == 2:
+            bt.set_factors(factors)
+        bt.cg(rhs, max_iterations=20, rel_tol=1e-8, precond=pre, refresh=50, graph_iters=10)  # warm-up
+        if pre == 2:
+            clk.start()
+        times = []
+        for _ in range(a.steps):
+            t1 = time.perf_counter()
+            x, its, rr, ok = bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=pre, refresh=50,
+                                   graph_iters=10)
+            times.append(time.perf_counter() - t1)
+        res[name] = {"ms": statistics.mean(times) * 1e3, "iterations_mean": float(its.mean()),
+                     "iterations_max": int(its.max()), "all_converged": bool(ok),
+                     "max_rel_residual_fp64": float(rr.max())}
+        del bt
+    clocks = clk.stop()
+    ratio = res["learned_pcg"]["ms"] / res["jacobi_pcg"]["ms"]
+    line = {
+        "metric": METRIC, "value": ratio, "unit": "learned-PCG time / Jacobi-PCG time", "n_gpus": ws,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": res["learned_pcg"]["ms"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 weights / f32 network; f32 values, f64 vectors",
+        "data": "synthetic: seeded diffusion systems (train seeds 1000.., held-out 9000..)",
+        "config": {"workload": f"learned_pcg_mpnn3x32_train{a.train_systems}_n32to64_eval{a.eval_systems}x{a.eval_n}^3",
+                   "unknowns_per_system": N, "rel_tol": 1e-8,
+                   "step": "one batched PCG solve of the held-out systems (host call, wall clock)",
+                   "parallelism": "1 GPU"},
+        "train": {"systems": a.train_systems, "seconds": round(t_train, 1),
+                  "loss_first_50": float(np.mean(losses[:50])), "loss_last_50": float(np.mean(losses[-50:]))},
+        "factor_seconds": round(t_factor, 2), "solvers": res, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     args = parse_args()
     if args.impl == "reference":
@@ -580,5 +665,7 @@ if __name__ == "__main__":
         run_pagerank(args)
     elif args.workload == "cg":
         run_cg(args)
+    elif args.workload == "learned":
+        run_learned(args)
     else:
         run_ours(args)

@@ -299,8 +299,10 @@ int tbsla_cg(tbsla_matrix* m, const double* b, double* x, int max_iterations, do
  * tbsla_batch_rows).  Each system stops on its own when its FP64 true
  * residual satisfies ||b - A x|| <= rel_tol ||b||; iterations[s] and
  * rel_residual[s] receive its count and final true relative residual.
- * graph_iters: iterations captured per CUDA graph replay (0: 10).  Returns
- * TBSLA_ERR_NOT_CONVERGED if some system hit max_iterations. */
+ * precond: 0 none, 1 Jacobi, 2 the factors of tbsla_batch_set_factors
+ * (z = L L^T r).  graph_iters: iterations captured per CUDA graph replay
+ * (0: 10).  Returns TBSLA_ERR_NOT_CONVERGED if some system hit
+ * max_iterations. */
 typedef struct tbsla_batch tbsla_batch;
 int tbsla_batch_create(tbsla_batch** b, tbsla_matrix* const* systems, int nsys, int precision);
 int tbsla_batch_destroy(tbsla_batch* b);
@@ -308,6 +310,36 @@ int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets);
 int tbsla_batch_cg(tbsla_batch* b, const double* rhs, double* x, int max_iterations, double rel_tol,
                    int precond, int refresh, int graph_iters, int* iterations,
                    double* rel_residual);
+/* Factored preconditioner M^-1 = L L^T for every system of the batch (L:
+ * lower-triangular CSR handles, one per system, same sizes), used by
+ * tbsla_batch_cg with precond = 2.  Values are stored in the batch's
+ * precision. */
+int tbsla_batch_set_factors(tbsla_batch* b, tbsla_matrix* const* factors, int nsys);
+
+/* ---- learned preconditioner (no reference counterpart) ------------------------
+ * A message-passing network over the pattern of an SPD CSR matrix A that
+ * emits L on the pattern of tril(A) with a positive diagonal, so that
+ * M^-1 = L L^T is SPD; untrained it is Jacobi (L = D^-1/2).  6,467
+ * parameters (3 layers, width 32), bfloat16 weights in the forward pass,
+ * FP32 master weights and Adam state.  Trained on the GPU with the loss
+ * sum (L L^T A Z - Z)^2 / (n P) over P Gaussian probes (P <= 16).  A must be
+ * symmetric with a positive diagonal (TBSLA_ERR_BAD_MATRIX otherwise). */
+typedef struct tbsla_mpnn tbsla_mpnn;
+int tbsla_mpnn_create(tbsla_mpnn** net, unsigned long long seed);
+int tbsla_mpnn_destroy(tbsla_mpnn* net);
+/* FP32 master parameters (nparams = 6467); theta may be NULL. */
+int tbsla_mpnn_params(const tbsla_mpnn* net, float* theta, int* nparams);
+/* Loads parameters and resets the Adam state. */
+int tbsla_mpnn_set_params(tbsla_mpnn* net, const float* theta, int nparams);
+/* Loss and its gradient (FP32, 6467) on the probes Z (n x nprobes row-major). */
+int tbsla_mpnn_loss_grad(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, const double* Z, double* loss,
+                         float* grad);
+/* One Adam step (betas 0.9 / 0.999) on A with nprobes probes drawn from `seed`. */
+int tbsla_mpnn_train_step(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, unsigned long long seed, float lr,
+                          double* loss);
+/* Writes L (CSR: per row its strictly lower entries, then the diagonal)
+ * into the CSR handle L. */
+int tbsla_mpnn_factor(tbsla_mpnn* net, const tbsla_matrix* A, tbsla_matrix* L);
 
 #ifdef __cplusplus
 }

@@ -7,9 +7,9 @@ is its Python mirror.  Import fails if the library has not been built.
 """
 from . import _lib
 from ._lib import BF16, COO, CSR, DENSE, ELL, F32, F64, SCOO, TbslaError, check, lib
-from .matrix import (FORMATS, Batch, Matrix, MatrixCOO, MatrixCSR, MatrixDENSE, MatrixELL, MatrixSCOO,
+from .matrix import (FORMATS, MPNN, Batch, Matrix, MatrixCOO, MatrixCSR, MatrixDENSE, MatrixELL, MatrixSCOO,
                      device_init, fill_uniform)
 
-__all__ = ["Matrix", "MatrixCOO", "MatrixSCOO", "MatrixCSR", "MatrixELL", "MatrixDENSE", "FORMATS",
+__all__ = ["MPNN", "Matrix", "MatrixCOO", "MatrixSCOO", "MatrixCSR", "MatrixELL", "MatrixDENSE", "FORMATS",
            "fill_uniform", "device_init", "TbslaError", "check", "lib", "COO", "SCOO", "CSR", "ELL",
            "DENSE", "F64", "F32", "BF16"]

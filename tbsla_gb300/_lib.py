@@ -108,6 +108,14 @@ _SIGS = {
     "tbsla_batch_destroy": (I, [P]),
     "tbsla_batch_rows": (I, [P, IP, C.POINTER(L)]),
     "tbsla_batch_cg": (I, [P, P, P, I, D, I, I, I, IP, DP]),
+    "tbsla_batch_set_factors": (I, [P, C.POINTER(P), I]),
+    "tbsla_mpnn_create": (I, [C.POINTER(P), ULL]),
+    "tbsla_mpnn_destroy": (I, [P]),
+    "tbsla_mpnn_params": (I, [P, P, IP]),
+    "tbsla_mpnn_set_params": (I, [P, P, I]),
+    "tbsla_mpnn_loss_grad": (I, [P, P, I, P, DP, P]),
+    "tbsla_mpnn_train_step": (I, [P, P, I, ULL, C.c_float, DP]),
+    "tbsla_mpnn_factor": (I, [P, P, P]),
     "tbsla_Ax": (I, [P, P, P, I]),
     "tbsla_spmv": (I, [P, P, P, I]),
     "tbsla_Ax_device": (I, [P, P, P, I, P]),

@@ -60,6 +60,10 @@ struct tbsla_batch {
   int *chunks = nullptr, *chunk_sys = nullptr;
   int nchunks = 0;
   double* dinv = nullptr;
+  // factored preconditioner L L^T (block-diagonal over the systems)
+  int *lrowptr = nullptr, *lcolidx = nullptr, *trowptr = nullptr, *tcolidx = nullptr;
+  void *lvals = nullptr, *tvals = nullptr;
+  double* t = nullptr;
   double *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
   double* scal = nullptr;
   int *status = nullptr, *iters = nullptr;
@@ -72,14 +76,15 @@ struct tbsla_batch {
     if (stream) cudaStreamSynchronize(stream);
     if (graph) cudaGraphExecDestroy(graph);
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
-                  scal, status, iters};
+                  scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, t};
     for (void* v : ps)
       if (v) cudaFree(v);
     if (vals && vals != vals64) cudaFree(vals);
     if (stream) cudaStreamDestroy(stream);
   }
 
-  CgBatch view(bool precond, double tol2, int max_it) const {
+  // precond: 0 none, 1 Jacobi, 2 factored L L^T
+  CgBatch view(int precond, double tol2, int max_it) const {
     CgBatch c{};
     c.nsys = nsys;
     c.n = n;
@@ -95,7 +100,15 @@ struct tbsla_batch {
     c.chunks = chunks;
     c.chunk_sys = chunk_sys;
     c.nchunks = nchunks;
-    c.dinv = precond ? dinv : nullptr;
+    c.dinv = precond == 1 ? dinv : nullptr;
+    const bool f = precond == 2;
+    c.lrowptr = f ? lrowptr : nullptr;
+    c.lcolidx = f ? lcolidx : nullptr;
+    c.trowptr = f ? trowptr : nullptr;
+    c.tcolidx = f ? tcolidx : nullptr;
+    c.lvals = f ? lvals : nullptr;
+    c.tvals = f ? tvals : nullptr;
+    c.t = f ? t : nullptr;
     c.b = b;
     c.x = x;
     c.r = r;
@@ -213,6 +226,7 @@ int capture(tbsla_batch* B, const CgBatch& c, int K) {
   for (int i = 0; i < K; i++) {
     cudaError_t e = cg_spmv_dot(c, s);
     if (e == cudaSuccess) e = cg_update(c, s);
+    if (e == cudaSuccess) e = cg_factor_apply(c, 1 << kActive, c.rz_new, s);
     if (e == cudaSuccess) e = cg_scalars(c, s);
     if (e == cudaSuccess) e = cg_direction(c, s);
     if (e != cudaSuccess) {
@@ -257,6 +271,74 @@ int tbsla_batch_destroy(tbsla_batch* b) {
   return TBSLA_OK;
 }
 
+int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int nsys) {
+  using namespace tbsla_impl;
+  if (!B || !factors || nsys != B->nsys) return TBSLA_ERR_INVALID_ARG;
+  // L concatenated block-diagonally, and L^T built by a counting sort
+  std::vector<int> rp(B->n + 1, 0), ci;
+  std::vector<double> va;
+  for (int s = 0; s < nsys; s++) {
+    const tbsla_matrix* m = factors[s];
+    if (!m || m->format != TBSLA_CSR) return TBSLA_ERR_INVALID_ARG;
+    const tbsla_info& I = m->info;
+    const long o = B->off[s], ns = B->off[s + 1] - o;
+    if (I.n_row != ns || I.n_col != ns || I.ln_row != ns || I.f_col != 0) return TBSLA_ERR_INVALID_ARG;
+    int v = validate(m);
+    if (v) return v;
+    const int* mrp = m->idx0.data();
+    for (long i = 0; i < ns; i++) {
+      for (int j = mrp[i]; j < mrp[i + 1]; j++) {
+        if (m->idx1[j] > i) return TBSLA_ERR_BAD_MATRIX;  // not lower-triangular
+        ci.push_back(m->idx1[j] + (int)o);
+        va.push_back(m->values[j]);
+      }
+      rp[o + i + 1] = (int)ci.size();
+    }
+  }
+  const long nl = (long)ci.size();
+  std::vector<int> trp(B->n + 1, 0), tci(nl);
+  std::vector<double> tva(nl);
+  for (long k = 0; k < nl; k++) trp[ci[k] + 1]++;
+  for (long i = 0; i < B->n; i++) trp[i + 1] += trp[i];
+  std::vector<int> fill(trp.begin(), trp.end() - 1);
+  for (long i = 0; i < B->n; i++)
+    for (int k = rp[i]; k < rp[i + 1]; k++) {
+      const int q = fill[ci[k]]++;
+      tci[q] = (int)i;
+      tva[q] = va[k];
+    }
+  cudaSetDevice(B->device);
+  cudaStream_t st = B->stream;
+  for (void* p : {(void*)B->lrowptr, (void*)B->lcolidx, (void*)B->trowptr, (void*)B->tcolidx, B->lvals, B->tvals,
+                  (void*)B->t})
+    if (p) cudaFree(p);
+  B->lrowptr = B->lcolidx = B->trowptr = B->tcolidx = nullptr;
+  B->lvals = B->tvals = nullptr;
+  B->t = nullptr;
+  double* tmp = nullptr;
+  const size_t es = B->prec == TBSLA_F64 ? 8 : B->prec == TBSLA_F32 ? 4 : 2;
+  CK(alloc(&B->lrowptr, rp.size()));
+  CK(alloc(&B->lcolidx, std::max<size_t>(ci.size(), 1)));
+  CK(alloc(&B->trowptr, trp.size()));
+  CK(alloc(&B->tcolidx, std::max<size_t>(tci.size(), 1)));
+  CK(alloc(&B->t, B->n));
+  CK(cudaMalloc(&B->lvals, std::max<size_t>(nl, 1) * es));
+  CK(cudaMalloc(&B->tvals, std::max<size_t>(nl, 1) * es));
+  CK(alloc(&tmp, std::max<size_t>(nl, 1) * 2));
+  CK(cudaMemcpyAsync(B->lrowptr, rp.data(), rp.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(B->lcolidx, ci.data(), ci.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(B->trowptr, trp.data(), trp.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(B->tcolidx, tci.data(), tci.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(tmp, va.data(), nl * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(tmp + nl, tva.data(), nl * 8, cudaMemcpyHostToDevice, st));
+  CK(convert_values(tmp, B->lvals, B->prec, nl, st));
+  CK(convert_values(tmp + nl, B->tvals, B->prec, nl, st));
+  CK(cudaStreamSynchronize(st));
+  cudaFree(tmp);
+  if (B->graph_pre == 2) B->graph_pre = -1;  // recapture with the new arrays
+  return TBSLA_OK;
+}
+
 int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets) {
   if (!b) return TBSLA_ERR_INVALID_ARG;
   if (nsys) *nsys = b->nsys;
@@ -266,12 +348,13 @@ int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets) {
 
 int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterations, double rel_tol,
                    int precond, int refresh, int graph_iters, int* iterations, double* rel_residual) {
-  if (!B || !rhs || !x || max_iterations < 0 || rel_tol < 0 || precond < 0 || precond > 1 || refresh < 0)
+  if (!B || !rhs || !x || max_iterations < 0 || rel_tol < 0 || precond < 0 || precond > 2 || refresh < 0 ||
+      (precond == 2 && !B->lrowptr))
     return TBSLA_ERR_INVALID_ARG;
   cudaSetDevice(B->device);
   const int K = graph_iters > 0 ? graph_iters : 10;
   const double tol2 = rel_tol * rel_tol;
-  const CgBatch c = B->view(precond == 1, tol2, max_iterations);
+  const CgBatch c = B->view(precond, tol2, max_iterations);
   cudaStream_t s = B->stream;
   const int ns = B->nsys;
   CK(cudaMemcpyAsync(B->b, rhs, B->n * 8, cudaMemcpyHostToDevice, s));
@@ -288,6 +371,7 @@ int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterati
     // one eager iteration first: kernel attributes are set outside capture
     CK(cg_spmv_dot(c, s));
     CK(cg_update(c, s));
+    CK(cg_factor_apply(c, 1 << kActive, c.rz_new, s));
     CK(cg_scalars(c, s));
     CK(cg_direction(c, s));
     int st = capture(B, c, K);

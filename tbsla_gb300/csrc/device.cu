@@ -955,6 +955,12 @@ int dev_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* tr
   return st;
 }
 
+int dev_ready(int* device) {
+  const int st = check_device();
+  if (!st) *device = g_device;
+  return st;
+}
+
 long dev_noalloc_max_items() { return csr_merge_noalloc_max_items(); }
 
 int dev_csr_ax_noalloc(int n_row, long nnz, int f_col, const int* rowptr, const int* colidx,

@@ -9,6 +9,8 @@
 namespace tbsla_impl {
 
 int dev_select(int device);
+// Device of the compute calls, after checking that it is usable.
+int dev_ready(int* device);
 int dev_host_alloc(void** p, size_t bytes);
 int dev_host_free(void* p);
 

@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(NT) k_cg_residual(CgBatch c, int mask) {
   const double rz = block_sum<NT>(red[1], sm.red);
   if (threadIdx.x == 0) {
     atomicAdd(c.rrt + sys, rr);
-    atomicAdd(c.rz + sys, rz);
+    if (!c.lrowptr) atomicAdd(c.rz + sys, rz);  // factored: r.z comes with z
   }
 }
 
@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(CgBatch c) {
       zi = c.dinv[i] * ri;
       c.z[i] = zi;
     }
-    rz = fma_rn(ri, zi, rz);
+    if (!c.lrowptr) rz = fma_rn(ri, zi, rz);  // factored: r.z comes with z
     rr = fma_rn(ri, ri, rr);
   }
   rz = block_sum<NT>(rz, red_s);
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(NT) k_cg_direction(CgBatch c) {
   const int sys = c.chunk_sys[ch];
   if (c.status[sys] != kActive) return;
   const double beta = c.beta[sys];
-  const double* z = c.dinv ? c.z : c.r;
+  const double* z = c.z;
   const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
   for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = fma_rn(beta, c.p[i], z[i]);
 }
@@ -172,9 +172,35 @@ __global__ void __launch_bounds__(NT) k_cg_restart(CgBatch c, int all) {
   const int ch = blockIdx.x;
   const int sys = c.chunk_sys[ch];
   if (!all && c.status[sys] != kRestart) return;
-  const double* z = c.dinv ? c.z : c.r;
+  const double* z = c.z;
   const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
   for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = z[i];
+}
+
+// out = M in over the chunks of the masked systems, M = L or L^T in CSR
+// (values in V); with `acc`, acc[sys] += r . out per chunk.
+template <class V>
+__global__ void __launch_bounds__(NT) k_cg_factor(CgBatch c, int mask, const int* __restrict__ rp,
+                                                 const int* __restrict__ ci, const void* vals,
+                                                 const double* __restrict__ in, double* __restrict__ out,
+                                                 double* acc) {
+  __shared__ double red_s[NT / kWarp];
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  if (!((mask >> c.status[sys]) & 1)) return;
+  const V* v = static_cast<const V*>(vals);
+  const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  double d = 0;
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+    double s = 0;
+    for (int k = rp[i]; k < rp[i + 1]; k++) s = fma_rn(widen(v[k]), in[ci[k]], s);
+    out[i] = s;
+    if (acc) d = fma_rn(c.r[i], s, d);
+  }
+  if (acc) {
+    d = block_sum<NT>(d, red_s);
+    if (threadIdx.x == 0) atomicAdd(acc + sys, d);
+  }
 }
 
 __global__ void k_cg_activate(CgBatch c) {
@@ -267,6 +293,10 @@ cudaError_t cg_true_residual(const CgBatch& c, int mask, bool init, cudaStream_t
     e = c.items == 4 ? launch_res<4>(c, mask, s) : launch_res<8>(c, mask, s);
     if (e != cudaSuccess) return e;
   }
+  if (c.lrowptr) {  // z = L L^T r, rz = r.z of the masked systems
+    e = cg_factor_apply(c, mask, c.rz, s);
+    if (e != cudaSuccess) return e;
+  }
   k_cg_post_residual<<<1, 256, 0, s>>>(c, mask, init ? 1 : 0);
   return cudaGetLastError();
 }
@@ -275,6 +305,23 @@ cudaError_t cg_restart(const CgBatch& c, bool all, cudaStream_t s) {
   if (c.nchunks) k_cg_restart<<<c.nchunks, NT, 0, s>>>(c, all ? 1 : 0);
   k_cg_activate<<<1, 256, 0, s>>>(c);
   return cudaGetLastError();
+}
+
+template <class V>
+cudaError_t factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s) {
+  k_cg_factor<V><<<c.nchunks, NT, 0, s>>>(c, mask, c.trowptr, c.tcolidx, c.tvals, c.r, c.t, nullptr);
+  k_cg_factor<V><<<c.nchunks, NT, 0, s>>>(c, mask, c.lrowptr, c.lcolidx, c.lvals, c.t, c.z, acc);
+  return cudaGetLastError();
+}
+
+cudaError_t cg_factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s) {
+  if (!c.lrowptr || c.nchunks == 0) return cudaSuccess;
+  switch (c.prec) {
+    case kF64: return factor_apply<double>(c, mask, acc, s);
+    case kF32: return factor_apply<float>(c, mask, acc, s);
+    case kBF16: return factor_apply<__nv_bfloat16>(c, mask, acc, s);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t cg_norms(const CgBatch& c, cudaStream_t s) {

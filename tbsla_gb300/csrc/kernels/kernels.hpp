@@ -177,6 +177,11 @@ struct CgBatch {
   const int* chunk_sys;
   int nchunks;
   const double* dinv;  // Jacobi: 1/diag(A); nullptr = unpreconditioned
+  // factored preconditioner z = L (L^T r) (nullptr lrowptr = none): L and
+  // L^T as CSR, values in `prec`; t = L^T r
+  const int *lrowptr, *lcolidx, *trowptr, *tcolidx;
+  const void *lvals, *tvals;
+  double* t;
   const double* b;
   double *x, *r, *z, *p, *q;  // z == r when unpreconditioned
   // per-system scalars (rrt: squared FP64 true residual of the last check)
@@ -190,6 +195,9 @@ cudaError_t cg_spmv_dot(const CgBatch& c, cudaStream_t s);   // q = A p; pq += p
 cudaError_t cg_update(const CgBatch& c, cudaStream_t s);     // x += a p; r -= a q; z = M r; dots
 cudaError_t cg_scalars(const CgBatch& c, cudaStream_t s);    // beta, status, iteration counts
 cudaError_t cg_direction(const CgBatch& c, cudaStream_t s);  // p = z + beta p
+// Factored preconditioner for the systems whose status is in `mask`:
+// t = L^T r, z = L t, acc[sys] += r.z.
+cudaError_t cg_factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s);
 // r = b - A64 x, z = M r, rr = r.r, rz = r.z for systems whose status is in
 // `mask` (bit per status); then each VERIFY system becomes DONE (true residual
 // within tolerance) or RESTART; with `init` every system is set from the result.

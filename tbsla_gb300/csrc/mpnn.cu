@@ -1,0 +1,758 @@
+// Learned preconditioner for CG: a small message-passing network over the
+// pattern of an SPD CSR matrix A that emits a lower-triangular factor L on
+// the pattern of tril(A), so that M^-1 = L L^T stays SPD (every L_ii > 0).
+// The reference has no preconditioner (src/mpi/matrix/CG.cpp:32-73 is plain
+// CG); this is the project's own model, with Jacobi (L = D^-1/2, the
+// network's starting point) as its fallback.
+//
+//   s_i = a_ii^-1/2, e_ij = a_ij s_i s_j on the stored entries (symmetric A)
+//   x_i = [1, sum_{j!=i} e_ij, sum_{j!=i} e_ij^2, deg_i / 8]
+//   h0  = relu(W0 x + b0)                                  (width H = 32)
+//   3 layers: m_i = sum_{j!=i} e_ij h_j;  z = W_l [h; m] + b_l;  h += relu(z)
+//   L_ij = s_i (w_e . (h_i * h_j) + c_e e_ij + b_e)   (j < i)
+//   L_ii = s_i softplus(w_d . h_i + b_d)
+//   training loss over Gaussian probes Z (n x P): sum (L L^T A Z - Z)^2 / (nP)
+//
+// GPU mapping: one warp per node with the 32 features on the 32 lanes, so
+// every gather of a neighbour's features is one 128-byte load and every
+// dense layer is 64 shuffles + 64 FMAs per lane against weights in shared
+// memory.  Forward and backward are hand-written kernels in FP32 with the
+// weights rounded to bfloat16 (FP32 master copy in the Adam state);
+// parameter gradients are reduced per CTA in shared memory, then added to
+// global memory once per CTA.
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+
+#include "device.hpp"
+#include "host/matrix.hpp"
+#include "kernels/common.cuh"
+#include "tbsla_gb300.h"
+
+namespace {
+
+using tbsla_gpu::kWarp;
+
+constexpr int H = 32, F0 = 4, NL = 3, NT = 256;
+constexpr int LSZ = 2 * H * H + H;  // one message layer: W (H x 2H) then b
+constexpr int OFF_W0 = 0, OFF_B0 = H * F0, OFF_L = OFF_B0 + H;
+constexpr int OFF_WE = OFF_L + NL * LSZ, OFF_CE = OFF_WE + H, OFF_BE = OFF_CE + 1;
+constexpr int OFF_WD = OFF_BE + 1, OFF_BD = OFF_WD + H;
+constexpr int NPARAMS = OFF_BD + 1;
+static_assert(NPARAMS == 6467, "parameter layout");
+constexpr unsigned FULL = 0xffffffffu;
+
+__host__ __device__ inline int off_layer(int l) { return OFF_L + (l - 1) * LSZ; }  // l = 1..NL
+
+// ---- host: one system's graph --------------------------------------------------------
+
+struct HostGraph {
+  int n = 0;
+  std::vector<int> rowptr, colidx;
+  std::vector<float> aval, e, s, x;
+  // L: per row its strictly lower entries (in A's order), then the diagonal
+  std::vector<int> lrowptr, lcol, lsrc, lrow;
+  // L^T: per column j the L entries of that column
+  std::vector<int> trowptr, tidx;
+};
+
+// Builds the graph of a square CSR handle; TBSLA_ERR_BAD_MATRIX unless every
+// row holds a positive diagonal entry.
+int build_graph(const tbsla_matrix* m, HostGraph* g) {
+  const tbsla_info& I = m->info;
+  if (m->format != TBSLA_CSR || I.ln_row != I.ln_col || I.f_col != 0) return TBSLA_ERR_INVALID_ARG;
+  const int n = I.ln_row;
+  const int* rp = m->idx0.data();
+  const int* ci = m->idx1.data();
+  const int base = rp[0];
+  g->n = n;
+  g->rowptr.resize(n + 1);
+  for (int i = 0; i <= n; i++) g->rowptr[i] = rp[i] - base;
+  const long nnz = g->rowptr[n];
+  g->colidx.assign(ci + base, ci + base + nnz);
+  g->aval.resize(nnz);
+  std::vector<double> d(n, 0.0);
+  for (int i = 0; i < n; i++)
+    for (long k = g->rowptr[i]; k < g->rowptr[i + 1]; k++) {
+      g->aval[k] = (float)m->values[base + k];
+      if (g->colidx[k] == i) d[i] += m->values[base + k];
+    }
+  g->s.resize(n);
+  for (int i = 0; i < n; i++) {
+    if (!(d[i] > 0)) return TBSLA_ERR_BAD_MATRIX;
+    g->s[i] = (float)(1.0 / std::sqrt(d[i]));
+  }
+  g->e.resize(nnz);
+  g->x.assign((size_t)n * F0, 0.f);
+  g->lrowptr.assign(n + 1, 0);
+  for (int i = 0; i < n; i++) {
+    double se = 0, se2 = 0;
+    int deg = 0, nl = 0;
+    for (long k = g->rowptr[i]; k < g->rowptr[i + 1]; k++) {
+      const int j = g->colidx[k];
+      const double e = m->values[base + k] / std::sqrt(d[i]) / std::sqrt(d[j]);
+      g->e[k] = (float)e;
+      if (j != i) {
+        se += e;
+        se2 += e * e;
+        deg++;
+      }
+      if (j < i) nl++;
+    }
+    g->x[(size_t)i * F0 + 0] = 1.f;
+    g->x[(size_t)i * F0 + 1] = (float)se;
+    g->x[(size_t)i * F0 + 2] = (float)se2;
+    g->x[(size_t)i * F0 + 3] = deg / 8.f;
+    g->lrowptr[i + 1] = g->lrowptr[i] + nl + 1;
+  }
+  const long nl = g->lrowptr[n];
+  g->lcol.resize(nl);
+  g->lsrc.resize(nl);
+  g->lrow.resize(nl);
+  for (int i = 0; i < n; i++) {
+    long q = g->lrowptr[i];
+    for (long k = g->rowptr[i]; k < g->rowptr[i + 1]; k++)
+      if (g->colidx[k] < i) {
+        g->lcol[q] = g->colidx[k];
+        g->lsrc[q] = (int)k;
+        g->lrow[q++] = i;
+      }
+    g->lcol[q] = i;
+    g->lsrc[q] = -1;
+    g->lrow[q] = i;
+  }
+  g->trowptr.assign(n + 1, 0);
+  for (long q = 0; q < nl; q++) g->trowptr[g->lcol[q] + 1]++;
+  for (int j = 0; j < n; j++) g->trowptr[j + 1] += g->trowptr[j];
+  g->tidx.resize(nl);
+  std::vector<int> fill(g->trowptr.begin(), g->trowptr.end() - 1);
+  for (long q = 0; q < nl; q++) g->tidx[fill[g->lcol[q]]++] = (int)q;
+  return TBSLA_OK;
+}
+
+// ---- device kernels: forward ---------------------------------------------------------
+
+__device__ __forceinline__ float relu(float v) { return v > 0.f ? v : 0.f; }
+__device__ __forceinline__ float wsum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+__device__ __forceinline__ float softplus(float v) { return v > 20.f ? v : log1pf(expf(v)); }
+__device__ __forceinline__ float sigmoid(float v) { return 1.f / (1.f + expf(-v)); }
+
+__device__ __forceinline__ long warp_id() { return ((long)blockIdx.x * NT + threadIdx.x) / kWarp; }
+__device__ __forceinline__ long warp_count() { return (long)gridDim.x * NT / kWarp; }
+
+// h0 = relu(W0 x + b0); lane o is feature o.
+__global__ void __launch_bounds__(NT) k_layer0(int n, const float* __restrict__ x, const float* __restrict__ w,
+                                              float* __restrict__ z0, float* __restrict__ h0) {
+  const int o = threadIdx.x & 31;
+  float wr[F0];
+#pragma unroll
+  for (int k = 0; k < F0; k++) wr[k] = w[OFF_W0 + o * F0 + k];
+  const float b = w[OFF_B0 + o];
+  for (long i = warp_id(); i < n; i += warp_count()) {
+    float z = b;
+#pragma unroll
+    for (int k = 0; k < F0; k++) z += wr[k] * x[i * F0 + k];
+    z0[i * H + o] = z;
+    h0[i * H + o] = relu(z);
+  }
+}
+
+// out_i (+)= sum_{j != i} e_ij in_j over A's pattern (e symmetric, so this
+// is also the transpose product the backward pass needs).
+__global__ void __launch_bounds__(NT) k_aggregate(int n, const int* __restrict__ rowptr,
+                                                 const int* __restrict__ colidx, const float* __restrict__ e,
+                                                 const float* __restrict__ in, float* __restrict__ out,
+                                                 int accumulate) {
+  const int f = threadIdx.x & 31;
+  for (long i = warp_id(); i < n; i += warp_count()) {
+    float acc = 0.f;
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      const int j = colidx[k];
+      if (j != i) acc += e[k] * in[(long)j * H + f];
+    }
+    out[i * H + f] = accumulate ? out[i * H + f] + acc : acc;
+  }
+}
+
+// z = W [h; m] + b, h_out = h + relu(z); W (H x 2H) kept transposed in
+// shared memory so that lane o reads W[o][k] without bank conflicts.
+__global__ void __launch_bounds__(NT) k_layer(int n, const float* __restrict__ w, const float* __restrict__ h,
+                                             const float* __restrict__ m, float* __restrict__ z,
+                                             float* __restrict__ hout) {
+  __shared__ float wt[2 * H][H + 1];
+  __shared__ float bs[H];
+  for (int t = threadIdx.x; t < 2 * H * H; t += NT) wt[t % (2 * H)][t / (2 * H)] = w[t];
+  if (threadIdx.x < H) bs[threadIdx.x] = w[2 * H * H + threadIdx.x];
+  __syncthreads();
+  const int o = threadIdx.x & 31;
+  for (long i = warp_id(); i < n; i += warp_count()) {
+    const float hi = h[i * H + o], mi = m[i * H + o];
+    float acc = bs[o];
+#pragma unroll
+    for (int k = 0; k < H; k++) {
+      acc += wt[k][o] * __shfl_sync(FULL, hi, k);
+      acc += wt[H + k][o] * __shfl_sync(FULL, mi, k);
+    }
+    z[i * H + o] = acc;
+    hout[i * H + o] = hi + relu(acc);
+  }
+}
+
+// L values: warp per row; lower entries then the diagonal.  xi (the
+// diagonal's pre-activation) is kept for the backward pass.
+__global__ void __launch_bounds__(NT) k_head(int n, const int* __restrict__ lrowptr, const int* __restrict__ lcol,
+                                            const int* __restrict__ lsrc, const float* __restrict__ e,
+                                            const float* __restrict__ s, const float* __restrict__ w,
+                                            const float* __restrict__ h, float* __restrict__ lval,
+                                            float* __restrict__ xi) {
+  const int f = threadIdx.x & 31;
+  const float we = w[OFF_WE + f], wd = w[OFF_WD + f];
+  const float ce = w[OFF_CE], be = w[OFF_BE], bd = w[OFF_BD];
+  for (long i = warp_id(); i < n; i += warp_count()) {
+    const float hi = h[i * H + f];
+    const int q0 = lrowptr[i], q1 = lrowptr[i + 1] - 1;  // q1: the diagonal
+    for (int q = q0; q < q1; q++) {
+      const float o = wsum(we * hi * h[(long)lcol[q] * H + f]) + ce * e[lsrc[q]] + be;
+      if (f == 0) lval[q] = s[i] * o;
+    }
+    const float x = wsum(wd * hi) + bd;
+    if (f == 0) {
+      xi[i] = x;
+      lval[q1] = s[i] * softplus(x);
+    }
+  }
+}
+
+// ---- device kernels: loss ------------------------------------------------------------
+// Probe blocks are n x P row-major (P <= 16), one thread per row.
+
+constexpr int PMAX = 16;
+
+// Y = A X on A's pattern (FP32 values).
+__global__ void k_spmm_a(int n, int P, const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                         const float* __restrict__ a, const float* __restrict__ X, float* __restrict__ Y) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    float acc[PMAX] = {};
+    for (int k = rowptr[i]; k < rowptr[i + 1]; k++) {
+      const float v = a[k];
+      const float* xr = X + (long)colidx[k] * P;
+#pragma unroll
+      for (int p = 0; p < PMAX; p++)
+        if (p < P) acc[p] += v * xr[p];
+    }
+#pragma unroll
+    for (int p = 0; p < PMAX; p++)
+      if (p < P) Y[i * P + p] = acc[p];
+  }
+}
+
+// Y = L X (rows of L) or Y = L^T X (columns of L, through the L^T index).
+__global__ void k_spmm_l(int n, int P, const int* __restrict__ ptr, const int* __restrict__ idx,
+                         const int* __restrict__ other, const float* __restrict__ lval, int transpose,
+                         const float* __restrict__ X, float* __restrict__ Y) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    float acc[PMAX] = {};
+    for (int t = ptr[i]; t < ptr[i + 1]; t++) {
+      const int q = transpose ? idx[t] : t;    // L entry
+      const int j = other[q];                  // its column (L) or row (L^T)
+      const float v = lval[q];
+#pragma unroll
+      for (int p = 0; p < PMAX; p++)
+        if (p < P) acc[p] += v * X[(long)j * P + p];
+    }
+#pragma unroll
+    for (int p = 0; p < PMAX; p++)
+      if (p < P) Y[i * P + p] = acc[p];
+  }
+}
+
+// G = 2 (W - Z) / (nP) and the loss sum((W - Z)^2) / (nP) (double atomics
+// of per-CTA sums).
+__global__ void __launch_bounds__(NT) k_residual(long len, float scale, const float* __restrict__ W,
+                                                const float* __restrict__ Z, float* __restrict__ G,
+                                                double* __restrict__ loss) {
+  __shared__ double red[NT / kWarp];
+  double acc = 0;
+  for (long t = blockIdx.x * (long)NT + threadIdx.x; t < len; t += (long)gridDim.x * NT) {
+    const float r = W[t] - Z[t];
+    G[t] = 2.f * r * scale;
+    acc += (double)r * r;
+  }
+  acc = tbsla_gpu::block_sum<NT>(acc, red);
+  if (threadIdx.x == 0) atomicAdd(loss, acc * scale);
+}
+
+// dL_q = sum_p G_ip V_jp + U_ip GV_jp for L entry q = (i, j).
+__global__ void k_dl(long nl, int P, const int* __restrict__ lrow, const int* __restrict__ lcol,
+                     const float* __restrict__ G, const float* __restrict__ V, const float* __restrict__ U,
+                     const float* __restrict__ GV, float* __restrict__ dl) {
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < nl; q += (long)gridDim.x * blockDim.x) {
+    const long i = lrow[q], j = lcol[q];
+    float acc = 0.f;
+    for (int p = 0; p < P; p++) acc += G[i * P + p] * V[j * P + p] + U[i * P + p] * GV[j * P + p];
+    dl[q] = acc;
+  }
+}
+
+// Gaussian probes (Box-Muller over a counter-based SplitMix64 stream).
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+__global__ void k_gauss(long len, unsigned long long seed, float* __restrict__ Z) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < len; t += (long)gridDim.x * blockDim.x) {
+    const unsigned long long r = mix64(seed * 0x100000001b3ull + (unsigned long long)t);
+    const float u1 = ((r >> 40) + 0.5f) * (1.f / 16777216.f);
+    const float u2 = ((r & 0xffffff) + 0.5f) * (1.f / 16777216.f);
+    Z[t] = sqrtf(-2.f * logf(u1)) * cospif(2.f * u2);
+  }
+}
+
+// ---- device kernels: backward --------------------------------------------------------
+
+// Head, row side: dL -> parameter gradients of the head, and dh_i
+// (written, not added: the first contribution to dh).
+__global__ void __launch_bounds__(NT) k_head_bwd(int n, const int* __restrict__ lrowptr,
+                                                const int* __restrict__ lcol, const int* __restrict__ lsrc,
+                                                const float* __restrict__ e, const float* __restrict__ s,
+                                                const float* __restrict__ w, const float* __restrict__ h,
+                                                const float* __restrict__ dl, const float* __restrict__ xi,
+                                                float* __restrict__ dh, float* __restrict__ grad) {
+  __shared__ float part[NT / kWarp][2 * H + 3];
+  const int f = threadIdx.x & 31, wi = threadIdx.x / kWarp;
+  const float we = w[OFF_WE + f], wd = w[OFF_WD + f];
+  float gwe = 0.f, gwd = 0.f, gce = 0.f, gbe = 0.f, gbd = 0.f;
+  for (long i = warp_id(); i < n; i += warp_count()) {
+    const float hi = h[i * H + f], si = s[i];
+    const int q0 = lrowptr[i], q1 = lrowptr[i + 1] - 1;
+    float d = 0.f;
+    for (int q = q0; q < q1; q++) {
+      const float dO = si * dl[q];
+      const float hj = h[(long)lcol[q] * H + f];
+      gwe += dO * hi * hj;
+      gce += dO * e[lsrc[q]];
+      gbe += dO;
+      d += dO * we * hj;
+    }
+    const float dxi = si * dl[q1] * sigmoid(xi[i]);
+    gwd += dxi * hi;
+    gbd += dxi;
+    dh[i * H + f] = d + dxi * wd;
+  }
+  part[wi][f] = gwe;
+  part[wi][H + f] = gwd;
+  if (f == 0) {
+    part[wi][2 * H] = gce;
+    part[wi][2 * H + 1] = gbe;
+    part[wi][2 * H + 2] = gbd;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < 2 * H + 3; c += NT) {
+    float acc = 0.f;
+    for (int v = 0; v < NT / kWarp; v++) acc += part[v][c];
+    const int dst = c < H ? OFF_WE + c : c < 2 * H ? OFF_WD + c - H : c == 2 * H ? OFF_CE : c == 2 * H + 1 ? OFF_BE : OFF_BD;
+    atomicAdd(grad + dst, acc);
+  }
+}
+
+// Head, column side: dh_j += sum over strictly lower entries (i, j) of
+// s_i dL_ij w_e * h_i.
+__global__ void __launch_bounds__(NT) k_head_bwd_cols(int n, const int* __restrict__ trowptr,
+                                                     const int* __restrict__ tidx, const int* __restrict__ lrow,
+                                                     const float* __restrict__ s, const float* __restrict__ w,
+                                                     const float* __restrict__ h, const float* __restrict__ dl,
+                                                     float* __restrict__ dh) {
+  const int f = threadIdx.x & 31;
+  const float we = w[OFF_WE + f];
+  for (long j = warp_id(); j < n; j += warp_count()) {
+    float d = 0.f;
+    for (int t = trowptr[j]; t < trowptr[j + 1]; t++) {
+      const int q = tidx[t];
+      const int i = lrow[q];
+      if (i == j) continue;  // the diagonal was handled on the row side
+      d += s[i] * dl[q] * we * h[(long)i * H + f];
+    }
+    dh[j * H + f] += d;
+  }
+}
+
+// Message layer backward for h_out = h + relu(W [h; m] + b):
+//   dz = dh_out * (z > 0);  dW += dz [h; m]^T;  db += dz;
+//   dh_in = dh_out + (W^T dz)[:H] (in place);  dm = (W^T dz)[H:]
+__global__ void __launch_bounds__(NT) k_layer_bwd(int n, const float* __restrict__ w, const float* __restrict__ h,
+                                                 const float* __restrict__ m, const float* __restrict__ z,
+                                                 float* __restrict__ dh, float* __restrict__ dm,
+                                                 float* __restrict__ grad) {
+  __shared__ float wt[2 * H][H + 1];
+  __shared__ float gsum[2 * H * H + H];
+  for (int t = threadIdx.x; t < 2 * H * H; t += NT) wt[t % (2 * H)][t / (2 * H)] = w[t];
+  for (int t = threadIdx.x; t < 2 * H * H + H; t += NT) gsum[t] = 0.f;
+  __syncthreads();
+  const int o = threadIdx.x & 31;
+  float gw[2 * H];
+#pragma unroll
+  for (int k = 0; k < 2 * H; k++) gw[k] = 0.f;
+  float gb = 0.f;
+  for (long i = warp_id(); i < n; i += warp_count()) {
+    const float dz = z[i * H + o] > 0.f ? dh[i * H + o] : 0.f;
+    const float hi = h[i * H + o], mi = m[i * H + o];
+    float dhin = 0.f, dmin = 0.f;
+#pragma unroll
+    for (int k = 0; k < H; k++) {
+      gw[k] += dz * __shfl_sync(FULL, hi, k);
+      gw[H + k] += dz * __shfl_sync(FULL, mi, k);
+      const float dzk = __shfl_sync(FULL, dz, k);  // lane o gathers sum_k W[k][o] dz_k
+      dhin += wt[o][k] * dzk;
+      dmin += wt[H + o][k] * dzk;
+    }
+    gb += dz;
+    dh[i * H + o] += dhin;
+    dm[i * H + o] = dmin;
+  }
+#pragma unroll
+  for (int k = 0; k < 2 * H; k++) atomicAdd(&gsum[o * 2 * H + k], gw[k]);
+  atomicAdd(&gsum[2 * H * H + o], gb);
+  __syncthreads();
+  for (int t = threadIdx.x; t < 2 * H * H + H; t += NT) atomicAdd(grad + t, gsum[t]);
+}
+
+// Input layer backward: dW0 += dz0 x^T, db0 += dz0.
+__global__ void __launch_bounds__(NT) k_layer0_bwd(int n, const float* __restrict__ x, const float* __restrict__ z0,
+                                                  const float* __restrict__ dh, float* __restrict__ grad) {
+  __shared__ float gsum[H * F0 + H];
+  for (int t = threadIdx.x; t < H * F0 + H; t += NT) gsum[t] = 0.f;
+  __syncthreads();
+  const int o = threadIdx.x & 31;
+  float gw[F0] = {}, gb = 0.f;
+  for (long i = warp_id(); i < n; i += warp_count()) {
+    const float dz = z0[i * H + o] > 0.f ? dh[i * H + o] : 0.f;
+#pragma unroll
+    for (int k = 0; k < F0; k++) gw[k] += dz * x[i * F0 + k];
+    gb += dz;
+  }
+#pragma unroll
+  for (int k = 0; k < F0; k++) atomicAdd(&gsum[o * F0 + k], gw[k]);
+  atomicAdd(&gsum[H * F0 + o], gb);
+  __syncthreads();
+  for (int t = threadIdx.x; t < H * F0 + H; t += NT) atomicAdd(grad + OFF_W0 + t, gsum[t]);
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters; the forward copy is
+// the bfloat16 rounding of the result.
+__global__ void k_adam(int np, float* __restrict__ theta, const float* __restrict__ g, float* __restrict__ mo,
+                       float* __restrict__ ve, float* __restrict__ wq, float lr, float c1, float c2) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < np; t += gridDim.x * blockDim.x) {
+    const float gt = g[t];
+    const float m = b1 * mo[t] + (1.f - b1) * gt;
+    const float v = b2 * ve[t] + (1.f - b2) * gt * gt;
+    mo[t] = m;
+    ve[t] = v;
+    const float th = theta[t] - lr * (m / c1) / (sqrtf(v / c2) + eps);
+    theta[t] = th;
+    wq[t] = __bfloat162float(__float2bfloat16_rn(th));
+  }
+}
+
+// ---- host orchestration --------------------------------------------------------------
+
+#define MCK(call)                                               \
+  do {                                                          \
+    cudaError_t e_ = (call);                                    \
+    if (e_ != cudaSuccess) {                                    \
+      cudaGetLastError();                                       \
+      return e_ == cudaErrorMemoryAllocation ? TBSLA_ERR_ALLOC  \
+                                             : TBSLA_ERR_CUDA;  \
+    }                                                           \
+  } while (0)
+
+// A device buffer that grows on demand.
+template <class T>
+struct Grow {
+  T* p = nullptr;
+  size_t cap = 0;
+  int need(size_t n) {
+    if (n <= cap && p) return TBSLA_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    MCK(cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)));
+    cap = n;
+    return TBSLA_OK;
+  }
+  template <class V>
+  int put(const std::vector<V>& v, cudaStream_t s) {
+    int st = need(v.size());
+    if (st) return st;
+    if (!v.empty()) MCK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    return TBSLA_OK;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Device copy of a graph plus the activations and probe blocks of one pass.
+struct Work {
+  int n = 0, P = 0;
+  long nnz = 0, nl = 0;
+  Grow<int> rowptr, colidx, lrowptr, lcol, lsrc, lrow, trowptr, tidx;
+  Grow<float> aval, e, s, x, lval, xi, dl;
+  Grow<float> h[NL + 1], z[NL + 1], m[NL + 1], dh, dm;
+  Grow<float> Z, U, V, W, G, GV;
+  void release() {
+    for (auto* g : {&rowptr, &colidx, &lrowptr, &lcol, &lsrc, &lrow, &trowptr, &tidx}) g->release();
+    for (auto* g : {&aval, &e, &s, &x, &lval, &xi, &dl, &dh, &dm, &Z, &U, &V, &W, &G, &GV}) g->release();
+    for (int l = 0; l <= NL; l++) {
+      h[l].release();
+      z[l].release();
+      m[l].release();
+    }
+  }
+};
+
+int upload(const HostGraph& g, int P, Work* w, cudaStream_t s) {
+  int st;
+  w->n = g.n;
+  w->P = P;
+  w->nnz = (long)g.colidx.size();
+  w->nl = (long)g.lcol.size();
+  if ((st = w->rowptr.put(g.rowptr, s)) || (st = w->colidx.put(g.colidx, s)) || (st = w->aval.put(g.aval, s)) ||
+      (st = w->e.put(g.e, s)) || (st = w->s.put(g.s, s)) || (st = w->x.put(g.x, s)) ||
+      (st = w->lrowptr.put(g.lrowptr, s)) || (st = w->lcol.put(g.lcol, s)) || (st = w->lsrc.put(g.lsrc, s)) ||
+      (st = w->lrow.put(g.lrow, s)) || (st = w->trowptr.put(g.trowptr, s)) || (st = w->tidx.put(g.tidx, s)))
+    return st;
+  const size_t nh = (size_t)g.n * H, np = (size_t)g.n * std::max(P, 1);
+  for (int l = 0; l <= NL; l++)
+    if ((st = w->h[l].need(nh)) || (st = w->z[l].need(nh)) || (st = w->m[l].need(nh))) return st;
+  if ((st = w->dh.need(nh)) || (st = w->dm.need(nh)) || (st = w->lval.need(w->nl)) || (st = w->xi.need(g.n)) ||
+      (st = w->dl.need(w->nl)))
+    return st;
+  for (auto* b : {&w->Z, &w->U, &w->V, &w->W, &w->G, &w->GV})
+    if ((st = b->need(np))) return st;
+  return TBSLA_OK;
+}
+
+int warp_grid(long n) { return (int)std::max<long>(1, std::min<long>((n + NT / kWarp - 1) / (NT / kWarp), 152L * 8)); }
+int row_grid(long n) { return (int)std::max<long>(1, std::min<long>((n + NT - 1) / NT, 152L * 16)); }
+
+// Forward pass: activations and L values.
+int forward(const float* wq, Work& w, cudaStream_t s) {
+  const int n = w.n, gw = warp_grid(n);
+  k_layer0<<<gw, NT, 0, s>>>(n, w.x.p, wq, w.z[0].p, w.h[0].p);
+  for (int l = 1; l <= NL; l++) {
+    k_aggregate<<<gw, NT, 0, s>>>(n, w.rowptr.p, w.colidx.p, w.e.p, w.h[l - 1].p, w.m[l].p, 0);
+    k_layer<<<gw, NT, 0, s>>>(n, wq + off_layer(l), w.h[l - 1].p, w.m[l].p, w.z[l].p, w.h[l].p);
+  }
+  k_head<<<gw, NT, 0, s>>>(n, w.lrowptr.p, w.lcol.p, w.lsrc.p, w.e.p, w.s.p, wq, w.h[NL].p, w.lval.p, w.xi.p);
+  MCK(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+// Loss on the probes in w.Z and the gradient into grad (zeroed here).
+int backward(const float* wq, Work& w, double* dloss, float* grad, cudaStream_t s) {
+  const int n = w.n, P = w.P, gw = warp_grid(n), gr = row_grid(n);
+  const long len = (long)n * P;
+  k_spmm_a<<<gr, NT, 0, s>>>(n, P, w.rowptr.p, w.colidx.p, w.aval.p, w.Z.p, w.U.p);
+  k_spmm_l<<<gr, NT, 0, s>>>(n, P, w.trowptr.p, w.tidx.p, w.lrow.p, w.lval.p, 1, w.U.p, w.V.p);
+  k_spmm_l<<<gr, NT, 0, s>>>(n, P, w.lrowptr.p, nullptr, w.lcol.p, w.lval.p, 0, w.V.p, w.W.p);
+  MCK(cudaMemsetAsync(dloss, 0, sizeof(double), s));
+  k_residual<<<row_grid(len), NT, 0, s>>>(len, 1.f / (float)len, w.W.p, w.Z.p, w.G.p, dloss);
+  k_spmm_l<<<gr, NT, 0, s>>>(n, P, w.trowptr.p, w.tidx.p, w.lrow.p, w.lval.p, 1, w.G.p, w.GV.p);
+  k_dl<<<row_grid(w.nl), NT, 0, s>>>(w.nl, P, w.lrow.p, w.lcol.p, w.G.p, w.V.p, w.U.p, w.GV.p, w.dl.p);
+  MCK(cudaMemsetAsync(grad, 0, NPARAMS * sizeof(float), s));
+  k_head_bwd<<<gw, NT, 0, s>>>(n, w.lrowptr.p, w.lcol.p, w.lsrc.p, w.e.p, w.s.p, wq, w.h[NL].p, w.dl.p, w.xi.p,
+                               w.dh.p, grad);
+  k_head_bwd_cols<<<gw, NT, 0, s>>>(n, w.trowptr.p, w.tidx.p, w.lrow.p, w.s.p, wq, w.h[NL].p, w.dl.p, w.dh.p);
+  for (int l = NL; l >= 1; l--) {
+    k_layer_bwd<<<gw, NT, 0, s>>>(n, wq + off_layer(l), w.h[l - 1].p, w.m[l].p, w.z[l].p, w.dh.p, w.dm.p,
+                                  grad + off_layer(l));
+    k_aggregate<<<gw, NT, 0, s>>>(n, w.rowptr.p, w.colidx.p, w.e.p, w.dm.p, w.dh.p, 1);
+  }
+  k_layer0_bwd<<<gw, NT, 0, s>>>(n, w.x.p, w.z[0].p, w.dh.p, grad);
+  MCK(cudaGetLastError());
+  return TBSLA_OK;
+}
+
+float bf16_round(float v) {
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x7fffu + ((u >> 16) & 1u)) & 0xffff0000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
+}  // namespace
+
+struct tbsla_mpnn {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  float *theta = nullptr, *wq = nullptr, *grad = nullptr, *mo = nullptr, *ve = nullptr;
+  double* dloss = nullptr;
+  long step = 0;
+  Work work;
+  ~tbsla_mpnn() {
+    cudaSetDevice(device);
+    if (stream) cudaStreamSynchronize(stream);
+    work.release();
+    for (void* p : {(void*)theta, (void*)wq, (void*)grad, (void*)mo, (void*)ve, (void*)dloss})
+      if (p) cudaFree(p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  int set(const std::vector<float>& th) {
+    std::vector<float> q(th.size());
+    for (size_t k = 0; k < th.size(); k++) q[k] = bf16_round(th[k]);
+    MCK(cudaMemcpyAsync(theta, th.data(), NPARAMS * 4, cudaMemcpyHostToDevice, stream));
+    MCK(cudaMemcpyAsync(wq, q.data(), NPARAMS * 4, cudaMemcpyHostToDevice, stream));
+    MCK(cudaMemsetAsync(mo, 0, NPARAMS * 4, stream));
+    MCK(cudaMemsetAsync(ve, 0, NPARAMS * 4, stream));
+    MCK(cudaStreamSynchronize(stream));
+    step = 0;
+    return TBSLA_OK;
+  }
+};
+
+// ---- C ABI ---------------------------------------------------------------------------
+
+extern "C" {
+
+int tbsla_mpnn_create(tbsla_mpnn** out, unsigned long long seed) {
+  if (!out) return TBSLA_ERR_INVALID_ARG;
+  *out = nullptr;
+  int dev = 0;
+  int st = tbsla_impl::dev_ready(&dev);
+  if (st) return st;
+  auto* net = new (std::nothrow) tbsla_mpnn();
+  if (!net) return TBSLA_ERR_ALLOC;
+  net->device = dev;
+  cudaSetDevice(dev);
+  if (cudaStreamCreateWithFlags(&net->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&net->theta, NPARAMS * 4) != cudaSuccess || cudaMalloc(&net->wq, NPARAMS * 4) != cudaSuccess ||
+      cudaMalloc(&net->grad, NPARAMS * 4) != cudaSuccess || cudaMalloc(&net->mo, NPARAMS * 4) != cudaSuccess ||
+      cudaMalloc(&net->ve, NPARAMS * 4) != cudaSuccess || cudaMalloc(&net->dloss, 8) != cudaSuccess) {
+    cudaGetLastError();
+    delete net;
+    return TBSLA_ERR_ALLOC;
+  }
+  // He-scaled message layers, zero biases; the head starts at L = D^-1/2
+  // (Jacobi): w_e = c_e = b_e = w_d = 0 and softplus(b_d) = 1.
+  std::vector<float> th(NPARAMS, 0.f);
+  std::mt19937_64 rng(seed);
+  std::normal_distribution<float> n0(0.f, std::sqrt(2.f / F0)), nl(0.f, 0.5f * std::sqrt(2.f / (2 * H)));
+  for (int k = 0; k < H * F0; k++) th[OFF_W0 + k] = n0(rng);
+  for (int l = 1; l <= NL; l++)
+    for (int k = 0; k < 2 * H * H; k++) th[off_layer(l) + k] = nl(rng);
+  th[OFF_BD] = std::log(std::exp(1.f) - 1.f);
+  st = net->set(th);
+  if (st) {
+    delete net;
+    return st;
+  }
+  *out = net;
+  return TBSLA_OK;
+}
+
+int tbsla_mpnn_destroy(tbsla_mpnn* net) {
+  delete net;
+  return TBSLA_OK;
+}
+
+int tbsla_mpnn_params(const tbsla_mpnn* net, float* theta, int* nparams) {
+  if (!net) return TBSLA_ERR_INVALID_ARG;
+  if (nparams) *nparams = NPARAMS;
+  if (theta) {
+    cudaSetDevice(net->device);
+    MCK(cudaMemcpyAsync(theta, net->theta, NPARAMS * 4, cudaMemcpyDeviceToHost, net->stream));
+    MCK(cudaStreamSynchronize(net->stream));
+  }
+  return TBSLA_OK;
+}
+
+int tbsla_mpnn_set_params(tbsla_mpnn* net, const float* theta, int nparams) {
+  if (!net || !theta || nparams != NPARAMS) return TBSLA_ERR_INVALID_ARG;
+  cudaSetDevice(net->device);
+  return net->set(std::vector<float>(theta, theta + NPARAMS));
+}
+
+int tbsla_mpnn_loss_grad(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, const double* Z, double* loss,
+                         float* grad) {
+  if (!net || !A || nprobes < 1 || nprobes > PMAX || !Z) return TBSLA_ERR_INVALID_ARG;
+  HostGraph g;
+  int st = build_graph(A, &g);
+  if (st) return st;
+  cudaSetDevice(net->device);
+  cudaStream_t s = net->stream;
+  Work& w = net->work;
+  if ((st = upload(g, nprobes, &w, s))) return st;
+  std::vector<float> zf((size_t)g.n * nprobes);
+  for (size_t k = 0; k < zf.size(); k++) zf[k] = (float)Z[k];
+  MCK(cudaMemcpyAsync(w.Z.p, zf.data(), zf.size() * 4, cudaMemcpyHostToDevice, s));
+  if ((st = forward(net->wq, w, s)) || (st = backward(net->wq, w, net->dloss, net->grad, s))) return st;
+  double l = 0;
+  MCK(cudaMemcpyAsync(&l, net->dloss, 8, cudaMemcpyDeviceToHost, s));
+  if (grad) MCK(cudaMemcpyAsync(grad, net->grad, NPARAMS * 4, cudaMemcpyDeviceToHost, s));
+  MCK(cudaStreamSynchronize(s));
+  if (loss) *loss = l;
+  return TBSLA_OK;
+}
+
+int tbsla_mpnn_train_step(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, unsigned long long seed, float lr,
+                          double* loss) {
+  if (!net || !A || nprobes < 1 || nprobes > PMAX || !(lr > 0)) return TBSLA_ERR_INVALID_ARG;
+  HostGraph g;
+  int st = build_graph(A, &g);
+  if (st) return st;
+  cudaSetDevice(net->device);
+  cudaStream_t s = net->stream;
+  Work& w = net->work;
+  if ((st = upload(g, nprobes, &w, s))) return st;
+  const long len = (long)g.n * nprobes;
+  k_gauss<<<row_grid(len), NT, 0, s>>>(len, seed, w.Z.p);
+  if ((st = forward(net->wq, w, s)) || (st = backward(net->wq, w, net->dloss, net->grad, s))) return st;
+  net->step++;
+  const float c1 = 1.f - std::pow(0.9f, (float)net->step), c2 = 1.f - std::pow(0.999f, (float)net->step);
+  k_adam<<<(NPARAMS + NT - 1) / NT, NT, 0, s>>>(NPARAMS, net->theta, net->grad, net->mo, net->ve, net->wq, lr, c1,
+                                               c2);
+  MCK(cudaGetLastError());
+  double l = 0;
+  MCK(cudaMemcpyAsync(&l, net->dloss, 8, cudaMemcpyDeviceToHost, s));
+  MCK(cudaStreamSynchronize(s));
+  if (loss) *loss = l;
+  return TBSLA_OK;
+}
+
+int tbsla_mpnn_factor(tbsla_mpnn* net, const tbsla_matrix* A, tbsla_matrix* L) {
+  if (!net || !A || !L || L->format != TBSLA_CSR) return TBSLA_ERR_INVALID_ARG;
+  HostGraph g;
+  int st = build_graph(A, &g);
+  if (st) return st;
+  cudaSetDevice(net->device);
+  cudaStream_t s = net->stream;
+  Work& w = net->work;
+  if ((st = upload(g, 1, &w, s)) || (st = forward(net->wq, w, s))) return st;
+  std::vector<float> lv(w.nl);
+  MCK(cudaMemcpyAsync(lv.data(), w.lval.p, w.nl * 4, cudaMemcpyDeviceToHost, s));
+  MCK(cudaStreamSynchronize(s));
+  std::vector<double> vals(lv.begin(), lv.end());
+  tbsla_info I{};
+  I.n_row = I.n_col = I.ln_row = I.ln_col = g.n;
+  I.nnz = w.nl;
+  I.NR = I.NC = 1;
+  return tbsla_matrix_set_csr(L, &I, vals.data(), g.lrowptr.data(), g.lcol.data());
+}
+
+}  // extern "C"

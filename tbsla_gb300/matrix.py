@@ -381,6 +381,59 @@ class Batch:
             check(st, "batch_cg")
         return x, its, rr, st == L.OK
 
+    def set_factors(self, factors):
+        """Lower-triangular CSR factors L (one per system): cg(precond=2)
+        then applies z = L (L^T r)."""
+        self._factors = list(factors)
+        arr = (C.c_void_p * len(factors))(*[f._h.value for f in factors])
+        check(lib.tbsla_batch_set_factors(self._h, arr, len(factors)), "batch_set_factors")
+
+
+class MPNN:
+    """The learned preconditioner: a message-passing network that maps an SPD
+    CSR matrix A to a lower-triangular L on the pattern of tril(A), with
+    M^-1 = L L^T (tbsla_mpnn_*).  Untrained, L = D^-1/2 (Jacobi)."""
+
+    NPARAMS = 6467
+
+    def __init__(self, seed: int = 0):
+        h = C.c_void_p()
+        check(lib.tbsla_mpnn_create(C.byref(h), seed), "mpnn_create")
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            lib.tbsla_mpnn_destroy(h)
+            self._h = C.c_void_p()
+
+    def params(self) -> np.ndarray:
+        th = np.empty(self.NPARAMS, np.float32)
+        check(lib.tbsla_mpnn_params(self._h, th.ctypes.data_as(C.c_void_p), None), "mpnn_params")
+        return th
+
+    def set_params(self, theta):
+        th = np.ascontiguousarray(theta, np.float32)
+        check(lib.tbsla_mpnn_set_params(self._h, th.ctypes.data_as(C.c_void_p), len(th)), "mpnn_set_params")
+
+    def loss_grad(self, A, Z: np.ndarray):
+        Z = np.ascontiguousarray(Z, np.float64)
+        g = np.empty(self.NPARAMS, np.float32)
+        loss = C.c_double()
+        check(lib.tbsla_mpnn_loss_grad(self._h, A._h, Z.shape[1], Z.ctypes.data_as(C.c_void_p), C.byref(loss),
+                                       g.ctypes.data_as(C.c_void_p)), "mpnn_loss_grad")
+        return loss.value, g
+
+    def train_step(self, A, probes: int = 8, seed: int = 0, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        check(lib.tbsla_mpnn_train_step(self._h, A._h, probes, seed, lr, C.byref(loss)), "mpnn_train_step")
+        return loss.value
+
+    def factor(self, A):
+        Lm = MatrixCSR()
+        check(lib.tbsla_mpnn_factor(self._h, A._h, Lm._h), "mpnn_factor")
+        return Lm
+
 
 def fill_uniform(n: int, lo: float, hi: float, seed: int, out: np.ndarray | None = None) -> np.ndarray:
     out = np.empty(n) if out is None else _f64(out, "out")
@@ -392,5 +445,5 @@ def device_init(device: int = 0):
     check(lib.tbsla_device_init(device), "device_init")
 
 
-__all__ = ["Matrix", "MatrixCOO", "MatrixSCOO", "MatrixCSR", "MatrixELL", "MatrixDENSE", "FORMATS",
+__all__ = ["Matrix", "MatrixCOO", "MatrixSCOO", "MatrixCSR", "MatrixELL", "MatrixDENSE", "FORMATS", "MPNN",
            "fill_uniform", "device_init", "TbslaError"]

@@ -200,3 +200,34 @@ def test_oracle_pagerank_and_cg_fixed_points():
     b = T.fill_uniform(12 ** 3, -1.0, 1.0, 9)
     x, it, rr = oracle.cg(a["rowptr"], a["colidx"], a["values"], b, rel_tol=1e-8)
     assert rr <= 1e-8 and it > 5
+
+
+def test_mpnn_oracle_gradient_is_the_derivative_of_its_loss():
+    """The learned preconditioner's restated loss gradient (oracle/mpnn.py)
+    against central finite differences, bfloat16 rounding switched off."""
+    import tbsla_gb300 as T
+    import oracle.mpnn as M
+
+    m = T.MatrixCSR()
+    m.fill_diffusion7(5, 1.0, 3.0, 11)
+    a = m.arrays()
+    rng = np.random.default_rng(0)
+    th = M.unpack(M.init_params(1))
+    th["we"] = rng.normal(0, 0.3, M.H)
+    th["wd"] = rng.normal(0, 0.3, M.H)
+    th["ce"], th["be"] = -0.4, 0.05
+    theta = M.pack(th)
+    Z = rng.normal(size=(len(a["rowptr"]) - 1, 3))
+    keep = M.bf16
+    M.bf16 = lambda x: np.asarray(x, np.float64)
+    try:
+        _, g = M.loss_and_grad(theta, a["rowptr"], a["colidx"], a["values"], Z)
+        for k in rng.choice(M.NPARAMS, 30, replace=False):
+            tp, tm = theta.copy(), theta.copy()
+            tp[k] += 1e-6
+            tm[k] -= 1e-6
+            fd = (M.loss_and_grad(tp, a["rowptr"], a["colidx"], a["values"], Z)[0]
+                  - M.loss_and_grad(tm, a["rowptr"], a["colidx"], a["values"], Z)[0]) / 2e-6
+            assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(fd)), k
+    finally:
+        M.bf16 = keep
