@@ -49,6 +49,7 @@ def parse_args():
                    help="spmv: the large-SpMV headline; pagerank: the PageRank graph; cg: batched CG; "
                         "learned: learned-preconditioner PCG against Jacobi-PCG")
     p.add_argument("--train-systems", type=int, default=2000, help="learned: training systems (seeds 1000..)")
+    p.add_argument("--epochs", type=int, default=1, help="learned: passes over the training systems")
     p.add_argument("--eval-systems", type=int, default=32, help="learned: held-out systems (seeds 9000..)")
     p.add_argument("--eval-n", type=int, default=128, help="learned: held-out grid size n (n^3 unknowns)")
     p.add_argument("--n", type=int, default=None, help="rows (spmv: 2^24, pagerank: 2^22)")
@@ -605,12 +606,17 @@ def run_learned(a):
     net = T.MPNN(1)
     t0 = time.time()
     losses = []
+    total = a.train_systems * a.epochs
     with ThreadPoolExecutor(4) as pool:
-        futs = [pool.submit(system, int(sizes[k]), 1000 + k) for k in range(min(8, a.train_systems))]
-        for k in range(a.train_systems):
+        # systems are regenerated each epoch (same seeds) rather than held
+        def sub(k):
+            return pool.submit(system, int(sizes[k % a.train_systems]), 1000 + k % a.train_systems)
+
+        futs = [sub(k) for k in range(min(8, total))]
+        for k in range(total):
             A = futs[k].result()
-            if k + 8 < a.train_systems:
-                futs.append(pool.submit(system, int(sizes[k + 8]), 1000 + k + 8))
+            if k + 8 < total:
+                futs.append(sub(k + 8))
             losses.append(net.train_step(A, probes=8, seed=k, lr=1e-3))
             futs[k] = None
     t_train = time.time() - t0
@@ -650,7 +656,7 @@ def run_learned(a):
                    "unknowns_per_system": N, "rel_tol": 1e-8,
                    "step": "one batched PCG solve of the held-out systems (host call, wall clock)",
                    "parallelism": "1 GPU"},
-        "train": {"systems": a.train_systems, "seconds": round(t_train, 1),
+        "train": {"systems": a.train_systems, "epochs": a.epochs, "adam_steps": total, "seconds": round(t_train, 1),
                   "loss_first_50": float(np.mean(losses[:50])), "loss_last_50": float(np.mean(losses[-50:]))},
         "factor_seconds": round(t_factor, 2), "solvers": res, "clocks": clocks,
     }
