@@ -150,6 +150,11 @@ int tbsla_fill_uniform(double* out, long n, double lo, double hi, unsigned long 
  *      (MatrixCSR.cpp:49-96, MatrixELL.cpp:25-79, MatrixSCOO.cpp:75-101,
  *      MatrixDENSE.cpp:15-37) --------------------------------------------- */
 int tbsla_matrix_convert(tbsla_matrix** out, const tbsla_matrix* coo, int format);
+/* The same conversion with the (row, column) ordering of CSR / ELL done by a
+ * stable radix sort on the GPU (MatrixCSR.cpp:49-96 sorts on the host):
+ * identical arrays, TBSLA_ERR_NO_DEVICE without a GPU.  SCOO and DENSE are
+ * the host copy / scatter either way. */
+int tbsla_matrix_convert_device(tbsla_matrix** out, const tbsla_matrix* coo, int format);
 
 /* ---- binary I/O: write/read (e.g. MatrixCSR.cpp:236-295), the reference's
  *      wire format byte for byte --------------------------------------------- */

@@ -95,6 +95,7 @@ _SIGS = {
     "tbsla_matrix_fill_diffusion7": (I, [P, I, D, D, ULL]),
     "tbsla_fill_uniform": (I, [P, L, D, D, ULL]),
     "tbsla_matrix_convert": (I, [C.POINTER(P), P, I]),
+    "tbsla_matrix_convert_device": (I, [C.POINTER(P), P, I]),
     "tbsla_matrix_write": (I, [P, C.c_char_p, I]),
     "tbsla_matrix_read": (I, [P, C.c_char_p, L]),
     "tbsla_matrix_set_precision": (I, [P, I]),

@@ -197,19 +197,27 @@ int tbsla_fill_uniform(double* out, long n, double lo, double hi, unsigned long 
   return TBSLA_OK;
 }
 
-int tbsla_matrix_convert(tbsla_matrix** out, const tbsla_matrix* coo, int format) {
+static int convert(tbsla_matrix** out, const tbsla_matrix* coo, int format, bool device) {
   if (!out || !coo || coo->format != TBSLA_COO || !valid_format(format) || format == TBSLA_COO)
     return TBSLA_ERR_INVALID_ARG;
   auto* m = new (std::nothrow) tbsla_matrix();
   if (!m) return TBSLA_ERR_ALLOC;
   m->format = format;
-  int st = convert_from_coo(m, coo, format);
+  int st = convert_from_coo(m, coo, format, device);
   if (st) {
     delete m;
     return st;
   }
   *out = m;
   return TBSLA_OK;
+}
+
+int tbsla_matrix_convert(tbsla_matrix** out, const tbsla_matrix* coo, int format) {
+  return convert(out, coo, format, false);
+}
+
+int tbsla_matrix_convert_device(tbsla_matrix** out, const tbsla_matrix* coo, int format) {
+  return convert(out, coo, format, true);
 }
 
 int tbsla_matrix_write(const tbsla_matrix* m, const char* path, int append) {

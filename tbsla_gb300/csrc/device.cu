@@ -97,6 +97,7 @@ struct DeviceMatrix {
   unsigned* sell_counter = nullptr;
   double* colw = nullptr;  // PageRank: column sums of the stored values
   bool colw_ok = false;
+  double colw_s0 = 0, colw_m0 = 0;  // S and M of the start vector 1/n
   long nnz = 0;  // entries on the device
   int min_row = 0, max_row = -1;
   double* x = nullptr;
@@ -694,22 +695,24 @@ int column_weights(const tbsla_matrix* m, DeviceMatrix* d) {
   }
   int st = status_of(cudaMemcpyAsync(d->colw, w.data(), w.size() * 8, cudaMemcpyHostToDevice, d->stream));
   if (!st) st = status_of(cudaStreamSynchronize(d->stream));
-  if (!st) d->colw_ok = true;
-  return st;
-}
-
-// Scale and teleport weight of step 0 from x_0 = 1/n: S and M summed in
-// index order, as the oracle forms them.
-void initial_coefficients(const DeviceMatrix* d, int n, double beta, double x_init, double c[2]) {
-  std::vector<double> w(n);
-  cudaMemcpy(w.data(), d->colw, (size_t)n * 8, cudaMemcpyDeviceToHost);
+  if (st) return st;
+  // S and M of x_0 = 1/n, summed in index order as the oracle forms them
+  const double x_init = 1.0 / I.ln_row;
   double S = 0, M = 0;
-  for (int i = 0; i < n; i++) {
+  for (int i = 0; i < I.ln_row; i++) {
     S += x_init;
     M += w[i] * x_init;
   }
-  c[0] = 1.0 / S;
-  c[1] = 1.0 - beta * M * c[0];
+  d->colw_s0 = S;
+  d->colw_m0 = M;
+  d->colw_ok = true;
+  return TBSLA_OK;
+}
+
+// Scale and teleport weight of step 0 from x_0 = 1/n.
+void initial_coefficients(const DeviceMatrix* d, double beta, double c[2]) {
+  c[0] = 1.0 / d->colw_s0;
+  c[1] = 1.0 - beta * d->colw_m0 * c[0];
 }
 }  // namespace
 
@@ -744,7 +747,7 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
   }
   const double x_init = 1.0 / n;
   double c0[2];
-  initial_coefficients(d, n, beta, x_init, c0);
+  initial_coefficients(d, beta, c0);
   vec_fill(x0, x_init, n, s);
   cudaMemcpyAsync(coef, c0, 16, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
@@ -822,7 +825,7 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   }
   const double x_init = 1.0 / n;
   double cc[2];
-  initial_coefficients(d, n, beta, x_init, cc);
+  initial_coefficients(d, beta, cc);
   std::vector<double> c0(64, 0.0);
   for (int k = 0; k < nvec; k++) {
     c0[k] = cc[0];
@@ -953,6 +956,43 @@ int dev_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* tr
   if (best) *best = cand[bestk];
   ensure(m, &st);
   return st;
+}
+
+int dev_coo_order(const int* row, const int* col, long n, int n_row, int n_col, long* start, long* perm) {
+  int st = check_device();
+  if (st) return st;
+  if (n >= (1L << 31) - 1) return TBSLA_ERR_INVALID_ARG;
+  cudaSetDevice(g_device);
+  cudaStream_t s = nullptr;
+  int *drow = nullptr, *dcol = nullptr, *p0 = nullptr, *p1 = nullptr;
+  uint64_t *k0 = nullptr, *k1 = nullptr;
+  unsigned *cnt = nullptr, *scr = nullptr;
+  const size_t ns = std::max<size_t>(1, std::max(radix_scratch(n), scan_scratch((long)n_row + 1)));
+  auto cleanup = [&]() {
+    for (void* q : {(void*)drow, (void*)dcol, (void*)p0, (void*)p1, (void*)k0, (void*)k1, (void*)cnt, (void*)scr})
+      if (q) cudaFree(q);
+    if (s) cudaStreamDestroy(s);
+  };
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess || (st = dalloc(&drow, n)) ||
+      (st = dalloc(&dcol, n)) || (st = dalloc(&p0, n)) || (st = dalloc(&p1, n)) || (st = dalloc(&k0, n)) ||
+      (st = dalloc(&k1, n)) || (st = dalloc(&cnt, (size_t)n_row + 1)) || (st = dalloc(&scr, ns))) {
+    cleanup();
+    return st ? st : TBSLA_ERR_CUDA;
+  }
+  int alt = 0;
+  std::vector<int> hp(n);
+  std::vector<unsigned> hs((size_t)n_row + 1);
+  st = n ? status_of(cudaMemcpyAsync(drow, row, n * 4, cudaMemcpyHostToDevice, s)) : TBSLA_OK;
+  if (!st && n) st = status_of(cudaMemcpyAsync(dcol, col, n * 4, cudaMemcpyHostToDevice, s));
+  if (!st) st = status_of(coo_order(drow, dcol, n, n_row, n_col, k0, k1, p0, p1, cnt, scr, &alt, s));
+  if (!st && n) st = status_of(cudaMemcpyAsync(hp.data(), alt ? p1 : p0, n * 4, cudaMemcpyDeviceToHost, s));
+  if (!st) st = status_of(cudaMemcpyAsync(hs.data(), cnt, hs.size() * 4, cudaMemcpyDeviceToHost, s));
+  if (!st) st = status_of(cudaStreamSynchronize(s));
+  cleanup();
+  if (st) return st;
+  for (size_t i = 0; i < hs.size(); i++) start[i] = hs[i];
+  for (long k = 0; k < n; k++) perm[k] = hp[k];
+  return TBSLA_OK;
 }
 
 int dev_ready(int* device) {

@@ -36,6 +36,10 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
 int dev_cg(tbsla_matrix* m, const double* b, double* x, int max_it, double rel_tol, int precond,
            int refresh, int* iterations, double* rel_residual);
 
+// COO -> CSR ordering on the GPU: start[n_row + 1] row starts and perm[n]
+// the storage indices in (row, col) order, ties in storage order.
+int dev_coo_order(const int* row, const int* col, long n, int n_row, int n_col, long* start, long* perm);
+
 // Autotuner: times the CSR kernel configurations, keeps the fastest.
 int dev_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* trials, int max_trials,
                  int* ntrials);

@@ -4,6 +4,7 @@
 #include <numeric>
 #include <vector>
 
+#include "device.hpp"
 #include "matrix.hpp"
 
 namespace tbsla_impl {
@@ -93,7 +94,7 @@ int validate(const tbsla_matrix* m) {
 }
 
 // Converting constructors MatrixCSR/ELL/SCOO/DENSE(const MatrixCOO&).
-int convert_from_coo(tbsla_matrix* out, const tbsla_matrix* coo, int format) {
+int convert_from_coo(tbsla_matrix* out, const tbsla_matrix* coo, int format, bool device) {
   if (coo->format != TBSLA_COO) return TBSLA_ERR_INVALID_ARG;
   const tbsla_info& C = coo->info;
   long nnz = C.nnz;
@@ -138,18 +139,23 @@ int convert_from_coo(tbsla_matrix* out, const tbsla_matrix* coo, int format) {
   // stable sort by column inside each row.
   int n_row = C.n_row;
   std::vector<long> start(n_row + 1, 0);
-  for (long k = 0; k < nnz; k++) start[row[k] + 1]++;
-  for (int i = 0; i < n_row; i++) start[i + 1] += start[i];
   std::vector<long> perm(nnz);
-  {
-    std::vector<long> pos(start.begin(), start.end() - 1);
-    for (long k = 0; k < nnz; k++) perm[pos[row[k]]++] = k;
+  if (device) {  // the same order from a radix sort on the GPU (kernels/sort.cu)
+    int st = dev_coo_order(row, col, nnz, n_row, C.n_col, start.data(), perm.data());
+    if (st) return st;
+  } else {
+    for (long k = 0; k < nnz; k++) start[row[k] + 1]++;
+    for (int i = 0; i < n_row; i++) start[i + 1] += start[i];
+    {
+      std::vector<long> pos(start.begin(), start.end() - 1);
+      for (long k = 0; k < nnz; k++) perm[pos[row[k]]++] = k;
+    }
+    parallel_for(n_row, [&](long b, long e) {
+      for (long i = b; i < e; i++)
+        std::stable_sort(perm.begin() + start[i], perm.begin() + start[i + 1],
+                         [&](long a, long c) { return col[a] < col[c]; });
+    });
   }
-  parallel_for(n_row, [&](long b, long e) {
-    for (long i = b; i < e; i++)
-      std::stable_sort(perm.begin() + start[i], perm.begin() + start[i + 1],
-                       [&](long a, long c) { return col[a] < col[c]; });
-  });
 
   if (format == TBSLA_CSR) {  // MatrixCSR.cpp:62-95
     out->idx0.resize(n_row + 1);

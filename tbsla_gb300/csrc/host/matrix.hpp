@@ -107,7 +107,9 @@ int fill_diffusion7(tbsla_matrix* m, int n, double sigma, double corr_len,
 void fill_uniform(double* out, long n, double lo, double hi, unsigned long long seed);
 
 // Conversions (formats.cpp).
-int convert_from_coo(tbsla_matrix* out, const tbsla_matrix* coo, int format);
+// device: order the entries with the GPU radix sort instead of the host sort
+// (same result).
+int convert_from_coo(tbsla_matrix* out, const tbsla_matrix* coo, int format, bool device = false);
 
 // Binary I/O (io.cpp).
 int write_file(const tbsla_matrix* m, const char* path, bool append);

@@ -240,6 +240,22 @@ cudaError_t csr_col_sums(const double* vals, const int* rowptr, const int* colid
 // value /= s[col - f_col] where that is > 0.
 cudaError_t csr_normalize_cols(double* vals, const int* rowptr, const int* colidx, int n_row,
                                int f_col, const double* s, cudaStream_t st);
+// Stable LSD radix sort (8-bit digits) of (key, value) pairs over the low
+// `bits` key bits; the result is in the *_alt arrays when *result_in_alt.
+// scratch: radix_scratch(n) words.
+long radix_scratch(long n);
+cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* keys_alt, int* vals, int* vals_alt, long n, int bits,
+                             unsigned* scratch, int* result_in_alt, cudaStream_t s);
+// Exclusive scan in place; scratch: scan_scratch(n) words.
+long scan_scratch(long n);
+cudaError_t exclusive_scan(unsigned* a, long n, unsigned* scratch, cudaStream_t s);
+// COO -> CSR ordering: perm = the entries sorted by (row, col), ties in
+// storage order; rowcount (n_row + 1) becomes the row starts.  scratch:
+// max(radix_scratch(n), scan_scratch(n_row + 1)) words.
+cudaError_t coo_order(const int* row, const int* col, long n, int n_row, int n_col, uint64_t* keys,
+                      uint64_t* keys_alt, int* perm, int* perm_alt, unsigned* rowcount, unsigned* scratch,
+                      int* perm_in_alt, cudaStream_t s);
+
 // Narrowing copy of FP64 values to the storage precision.
 cudaError_t convert_values(const double* src, void* dst, int prec, long n, cudaStream_t s);
 // Row-major -> column-major transpose of ELL arrays.

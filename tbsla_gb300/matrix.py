@@ -37,14 +37,17 @@ class Matrix:
 
     FORMAT = -1
 
-    def __init__(self, coo: "MatrixCOO | None" = None, _handle=None):
+    def __init__(self, coo: "MatrixCOO | None" = None, _handle=None, device: bool = False):
+        """coo: converting constructor (MatrixCSR(const MatrixCOO&) ...);
+        device=True orders the entries with the GPU radix sort."""
         h = C.c_void_p()
         if _handle is not None:
             h = _handle
         elif coo is not None:
             if not isinstance(coo, MatrixCOO):
                 raise TypeError("conversion constructors take a MatrixCOO")
-            check(lib.tbsla_matrix_convert(C.byref(h), coo._h, self.FORMAT), "convert")
+            fn = lib.tbsla_matrix_convert_device if device else lib.tbsla_matrix_convert
+            check(fn(C.byref(h), coo._h, self.FORMAT), "convert")
         else:
             check(lib.tbsla_matrix_create(C.byref(h), self.FORMAT), "create")
         self._h = h
