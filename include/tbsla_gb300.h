@@ -264,6 +264,19 @@ int tbsla_normalize_cols(tbsla_matrix* m, const double* s);
 /* s <- column sums (zeroed first), then normalize_cols(s). */
 int tbsla_make_stochastic(tbsla_matrix* m, double* s);
 
+/* ---- SpMM and the sparse-softmax helpers, CSR only ---------------------------
+ * tbsla_dense_multiply: MatrixCSR::dense_multiply (MatrixCSR.cpp:1269-1281),
+ * C (n_row x cols_B, row-major) = A B with B (n_col x cols_B) indexed by
+ * the column as stored; C is overwritten.
+ * tbsla_get_row_max_abs: get_row_max_abs (:1283-1312), max |a_ij| per local
+ * row (0 for an empty row).
+ * tbsla_apply_exponential: apply_exponential (:1315-1334), every nonzero a_ij
+ * becomes exp(a_ij - max_abs[i]) (base <= 0) or base^(a_ij - max_abs[i]);
+ * no shift when max_abs is NULL. */
+int tbsla_dense_multiply(const tbsla_matrix* m, const double* B, double* C, int cols_B);
+int tbsla_get_row_max_abs(const tbsla_matrix* m, double* max_abs);
+int tbsla_apply_exponential(tbsla_matrix* m, const double* max_abs, int base);
+
 /* ---- PageRank (src/mpi/matrix/Matrix.cpp:540-602, 641-790), CSR only --------
  * A column-stochastic (zero columns = dangling nodes).  x_0 = 1/n and, with
  * each iterate normalised by its sum S_k before use,

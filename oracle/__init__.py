@@ -60,11 +60,13 @@ def ref() -> C.CDLL | None:
         for name in ("ref_delete", "ref_fill_cdiag", "ref_fill_cqmat", "ref_fill_random", "ref_info",
                      "ref_arrays", "ref_adopt", "ref_write", "ref_read", "ref_Ax", "ref_spmv",
                      "ref_a_axpx_", "ref_AAxpAx", "ref_AAxpAxpx", "ref_get_col_sums",
-                     "ref_normalize_cols"):
+                     "ref_normalize_cols", "ref_dense_multiply", "ref_row_max_abs", "ref_apply_exponential"):
             getattr(_r, name).restype = None if not name.endswith(("write", "read")) else I
         _r.ref_fill_cqmat.argtypes = [P, I, I, I, D, C.c_uint, I, I, I, I]
         _r.ref_fill_random.argtypes = [P, I, I, D, C.c_uint, I, I, I, I]
         _r.ref_adopt.argtypes = [P, P, L, P, P, P]
+        _r.ref_dense_multiply.argtypes = [P, P, P, I]
+        _r.ref_apply_exponential.argtypes = [P, P, I]
     return _r
 
 
@@ -181,6 +183,28 @@ def cg(rowptr, colidx, values, b, x0=None, max_iterations=10000, rel_tol=1e-8, d
     it = lib().orc_cg(I(n), _p(rowptr), _p(colidx), _p(values), _p(diag_inv), _p(b), _p(x),
                       I(max_iterations), D(rel_tol), C.byref(rr))
     return x, it, rr.value
+
+
+def csr_dense_multiply(rowptr, colidx, values, B):
+    n = len(rowptr) - 1
+    B = np.ascontiguousarray(B, np.float64)
+    cols = B.shape[1]
+    Cm = np.empty((n, cols))
+    lib().orc_csr_dense_multiply(I(n), _p(values), _p(rowptr), _p(colidx), _p(B), _p(Cm), I(cols))
+    return Cm
+
+
+def csr_row_max_abs(rowptr, values):
+    n = len(rowptr) - 1
+    out = np.empty(n)
+    lib().orc_csr_row_max_abs(I(n), _p(values), _p(rowptr), _p(out))
+    return out
+
+
+def csr_apply_exponential(rowptr, values, max_abs=None, base=-1):
+    v = np.array(values, np.float64)
+    lib().orc_csr_apply_exponential(I(len(rowptr) - 1), _p(v), _p(rowptr), _p(max_abs), I(base))
+    return v
 
 
 def bf16_round(a: np.ndarray) -> np.ndarray:

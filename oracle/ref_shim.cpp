@@ -255,4 +255,19 @@ void ref_normalize_cols(void* hp, double* s) {
   static_cast<Handle*>(hp)->m->normalize_cols(s);
 }
 
+// CSR only (MatrixCSR.cpp:1269-1334).
+void ref_dense_multiply(void* hp, const double* B, double* Cm, int cols) {
+  as<RCSR>(static_cast<Handle*>(hp))->dense_multiply(B, Cm, cols);
+}
+
+void ref_row_max_abs(void* hp, double* out) {
+  Quiet q;
+  as<RCSR>(static_cast<Handle*>(hp))->get_row_max_abs(out);
+}
+
+void ref_apply_exponential(void* hp, double* max_abs, int base) {
+  Quiet q;
+  as<RCSR>(static_cast<Handle*>(hp))->apply_exponential(max_abs, base);
+}
+
 }  // extern "C"

@@ -239,6 +239,49 @@ void orc_csr_normalize_cols(int ln_row, int f_col, long nnz, double* values,
     }
 }
 
+/* ---- SpMM and the sparse-softmax helpers (CSR) ---------------------------- */
+
+/* C = A B, MatrixCSR::dense_multiply (src/cpp/matrix/MatrixCSR.cpp:1269-1281):
+ * C zero-filled over n_row x cols_B, then C[i][k] += a_ij * B[colidx_j][k]
+ * in entry order (the column index is used as stored, without f_col). */
+void orc_csr_dense_multiply(int n_row, const double* values, const int* rowptr, const int* colidx,
+                            const double* B, double* Cm, int cols_B) {
+  for (long t = 0; t < (long)n_row * cols_B; t++) Cm[t] = 0.0;
+  for (int i = 0; i < n_row; i++)
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) {
+      const int col = colidx[j];
+      const double v = values[j];
+      for (int k = 0; k < cols_B; k++) Cm[(long)i * cols_B + k] += v * B[(long)col * cols_B + k];
+    }
+}
+
+/* max_abs[i] = max over the row's nonzero values of |a_ij| (0 for an empty
+ * row), MatrixCSR::get_row_max_abs (MatrixCSR.cpp:1283-1312). */
+void orc_csr_row_max_abs(int ln_row, const double* values, const int* rowptr, double* max_abs) {
+  for (int i = 0; i < ln_row; i++) {
+    double m = 0.0;
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) {
+      const double z = values[j];
+      if (z != 0 && fabs(z) > m) m = fabs(z);
+    }
+    max_abs[i] = m;
+  }
+}
+
+/* MatrixCSR::apply_exponential (MatrixCSR.cpp:1315-1334): every nonzero
+ * a_ij becomes exp(a_ij - max_abs[i]) (base <= 0) or base^(a_ij - max_abs[i]),
+ * without the shift when max_abs is NULL; zeros stay. */
+void orc_csr_apply_exponential(int ln_row, double* values, const int* rowptr, const double* max_abs,
+                               int base) {
+  for (int i = 0; i < ln_row; i++)
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) {
+      const double z = values[j];
+      if (z == 0) continue;
+      const double a = max_abs ? z - max_abs[i] : z;
+      values[j] = base <= 0 ? exp(a) : pow((double)base, a);
+    }
+}
+
 /* ---- PageRank --------------------------------------------------------- */
 
 /* Power iteration following src/mpi/matrix/Matrix.cpp:540-602 (loop),

@@ -51,6 +51,13 @@ void orc_csr_col_sums(int ln_row, int f_col, long nnz, const double* values,
 void orc_csr_normalize_cols(int ln_row, int f_col, long nnz, double* values,
                             const int* rowptr, const int* colidx, const double* s);
 
+/* ---- SpMM and sparse-softmax helpers (CSR) */
+void orc_csr_dense_multiply(int n_row, const double* values, const int* rowptr, const int* colidx,
+                            const double* B, double* Cm, int cols_B);
+void orc_csr_row_max_abs(int ln_row, const double* values, const int* rowptr, double* max_abs);
+void orc_csr_apply_exponential(int ln_row, double* values, const int* rowptr, const double* max_abs,
+                               int base);
+
 /* ---- PageRank / CG restatements (reference bugs fixed, see tbsla_oracle.c) */
 int orc_pagerank(int n, const int* rowptr, const int* colidx, const double* values,
                  const double* teleport, double beta, double epsilon, int max_iterations,

@@ -19,6 +19,8 @@ class MatrixCSR : public Matrix {
     double* page_rank(double beta, double epsilon, int max_iterations, int& nb_iterations_done);
     void CG(const double* b, double* x, int max_iterations, int& nb_iterations_done,
             double rel_tol = 1e-8, int precond = 0);
+    // C = A B (MatrixCSR.cpp:1269-1281), on the GPU
+    void dense_multiply(const double* B, double* C, int cols_B);
 };
 
 }}  // namespace tbsla::cpp

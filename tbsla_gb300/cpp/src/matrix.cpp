@@ -204,8 +204,10 @@ void Matrix::get_row_sums(double*) { throw GpuError(TBSLA_ERR_UNSUPPORTED, "get_
 void Matrix::normalize_rows(double*) { throw GpuError(TBSLA_ERR_UNSUPPORTED, "normalize_rows"); }
 void Matrix::get_col_sums(double* buffer) { check(tbsla_get_col_sums(h_, buffer), "get_col_sums"); }
 void Matrix::normalize_cols(double* s) { check(tbsla_normalize_cols(h_, s), "normalize_cols"); }
-void Matrix::get_row_max_abs(double*) { throw GpuError(TBSLA_ERR_UNSUPPORTED, "get_row_max_abs"); }
-void Matrix::apply_exponential(double*, int) { throw GpuError(TBSLA_ERR_UNSUPPORTED, "apply_exponential"); }
+void Matrix::get_row_max_abs(double* max_abs) { check(tbsla_get_row_max_abs(h_, max_abs), "get_row_max_abs"); }
+void Matrix::apply_exponential(double* max_abs, int base) {
+  check(tbsla_apply_exponential(h_, max_abs, base), "apply_exponential");
+}
 
 void Matrix::set_precision(int precision) { check(tbsla_matrix_set_precision(h_, precision), "set_precision"); }
 
@@ -314,6 +316,10 @@ void MatrixCSR::CG(const double* b, double* x, int max_iterations, int& nb_itera
   double rr = 0;
   int st = tbsla_cg(h_, b, x, max_iterations, rel_tol, precond, 50, &nb_iterations_done, &rr);
   if (st != TBSLA_OK && st != TBSLA_ERR_NOT_CONVERGED) check(st, "cg");
+}
+
+void MatrixCSR::dense_multiply(const double* B, double* C, int cols_B) {
+  check(tbsla_dense_multiply(h_, B, C, cols_B), "dense_multiply");
 }
 
 MatrixELL::MatrixELL() : Matrix(TBSLA_ELL) {}

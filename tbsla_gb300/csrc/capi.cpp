@@ -275,6 +275,22 @@ int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, i
   return TBSLA_OK;
 }
 
+int tbsla_dense_multiply(const tbsla_matrix* m, const double* B, double* C, int cols_B) {
+  if (!m || cols_B < 0 || (cols_B > 0 && (!B || !C))) return TBSLA_ERR_INVALID_ARG;
+  if (cols_B == 0) return TBSLA_OK;
+  return dev_dense_multiply(m, B, C, cols_B);
+}
+
+int tbsla_get_row_max_abs(const tbsla_matrix* m, double* max_abs) {
+  if (!m || !max_abs) return TBSLA_ERR_INVALID_ARG;
+  return dev_row_max_abs(m, max_abs);
+}
+
+int tbsla_apply_exponential(tbsla_matrix* m, const double* max_abs, int base) {
+  if (!m) return TBSLA_ERR_INVALID_ARG;
+  return dev_apply_exponential(m, max_abs, base);
+}
+
 int tbsla_matrix_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* trials, int max_trials,
                           int* ntrials) {
   if (!m || max_trials < 0 || (max_trials > 0 && !trials)) return TBSLA_ERR_INVALID_ARG;

@@ -652,6 +652,73 @@ int dev_make_stochastic(tbsla_matrix* m, double* s) {
   return dev_normalize_cols(m, s);
 }
 
+// ---- SpMM and the sparse-softmax helpers ---------------------------------------------
+
+int dev_dense_multiply(const tbsla_matrix* m, const double* B, double* Cm, int cols) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const tbsla_info& I = m->info;
+  const size_t nb = (size_t)I.n_col * cols, nc = (size_t)I.n_row * cols;
+  cudaStream_t s = d->stream;
+  double *db = nullptr, *dc = nullptr;
+  if ((st = dalloc(&db, std::max<size_t>(nb, 1))) || (st = dalloc(&dc, std::max<size_t>(nc, 1)))) {
+    cudaFree(db);
+    return st;
+  }
+  st = status_of(cudaMemcpyAsync(db, B, nb * 8, cudaMemcpyHostToDevice, s));
+  if (!st) st = status_of(cudaMemsetAsync(dc, 0, nc * 8, s));  // MatrixCSR.cpp:1270
+  if (!st) st = status_of(csr_dense_multiply(d->vals, d->prec, d->idx0, d->idx1, I.ln_row, db, cols, dc, s));
+  if (!st) st = status_of(cudaMemcpyAsync(Cm, dc, nc * 8, cudaMemcpyDeviceToHost, s));
+  if (!st) st = status_of(cudaStreamSynchronize(s));
+  cudaFree(db);
+  cudaFree(dc);
+  return st;
+}
+
+int dev_row_max_abs(const tbsla_matrix* m, double* max_abs) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const tbsla_info& I = m->info;
+  cudaStream_t s = d->stream;
+  if ((st = d->vec(&d->t, &d->t_len, std::max<size_t>(I.ln_row, 1)))) return st;
+  double* v64;
+  bool owned;
+  if ((st = values64(m, d, &v64, &owned))) return st;
+  st = status_of(csr_row_max_abs(v64, d->idx0, I.ln_row, d->t, s));
+  if (!st) st = status_of(cudaMemcpyAsync(max_abs, d->t, (size_t)I.ln_row * 8, cudaMemcpyDeviceToHost, s));
+  if (!st) st = status_of(cudaStreamSynchronize(s));
+  if (owned) cudaFree(v64);
+  return st;
+}
+
+int dev_apply_exponential(tbsla_matrix* m, const double* max_abs, int base) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const tbsla_info& I = m->info;
+  if (I.nnz == 0) return TBSLA_OK;
+  cudaStream_t str = d->stream;
+  if ((st = d->vec(&d->t, &d->t_len, std::max<size_t>(I.ln_row, 1)))) return st;
+  if (max_abs) TRY(cudaMemcpyAsync(d->t, max_abs, (size_t)I.ln_row * 8, cudaMemcpyHostToDevice, str));
+  double* v64;
+  bool owned;
+  if ((st = values64(m, d, &v64, &owned))) return st;
+  TRY(csr_apply_exponential(v64, d->idx0, I.ln_row, max_abs ? d->t : nullptr, base, str));
+  // keep the host arrays (the reference layout) in step with the device
+  TRY(cudaMemcpyAsync(m->values.data(), v64, d->nnz * 8, cudaMemcpyDeviceToHost, str));
+  if (owned) TRY(convert_values(v64, d->vals, d->prec, d->nnz, str));
+  if (d->algo == 2 && d->svals) TRY(sell_fill(sell_args(m, d), str));
+  d->colw_ok = false;
+  TRY(cudaStreamSynchronize(str));
+  if (owned) cudaFree(v64);
+  return TBSLA_OK;
+}
+
 // ---- PageRank ------------------------------------------------------------------------
 
 namespace {

@@ -28,6 +28,11 @@ int dev_col_sums(tbsla_matrix* m, double* s, bool zero_first);
 int dev_normalize_cols(tbsla_matrix* m, const double* s);
 int dev_make_stochastic(tbsla_matrix* m, double* s);
 
+// MatrixCSR::dense_multiply, get_row_max_abs, apply_exponential (host buffers).
+int dev_dense_multiply(const tbsla_matrix* m, const double* B, double* C, int cols);
+int dev_row_max_abs(const tbsla_matrix* m, double* max_abs);
+int dev_apply_exponential(tbsla_matrix* m, const double* max_abs, int base);
+
 int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* result,
                   int* iterations, double* error);
 int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double beta, double eps,

@@ -256,6 +256,17 @@ cudaError_t coo_order(const int* row, const int* col, long n, int n_row, int n_c
                       uint64_t* keys_alt, int* perm, int* perm_alt, unsigned* rowcount, unsigned* scratch,
                       int* perm_in_alt, cudaStream_t s);
 
+// C = A B (MatrixCSR::dense_multiply): B (rows indexed by the stored
+// column) and C row-major with k columns; C rows [0, n_row) written.
+cudaError_t csr_dense_multiply(const void* vals, int prec, const int* rowptr, const int* colidx, int n_row,
+                               const double* B, int k, double* Cm, cudaStream_t s);
+// out[i] = max_j |a_ij| (0 for an empty row).
+cudaError_t csr_row_max_abs(const double* vals, const int* rowptr, int n_row, double* out, cudaStream_t s);
+// a_ij <- exp(a_ij - max_abs[i]) (base <= 0) or base^(a_ij - max_abs[i]) for
+// every nonzero a_ij; no shift when max_abs is null.
+cudaError_t csr_apply_exponential(double* vals, const int* rowptr, int n_row, const double* max_abs, int base,
+                                  cudaStream_t s);
+
 // Narrowing copy of FP64 values to the storage precision.
 cudaError_t convert_values(const double* src, void* dst, int prec, long n, cudaStream_t s);
 // Row-major -> column-major transpose of ELL arrays.

@@ -267,6 +267,23 @@ class MatrixCSR(Matrix):
     def set_sell_params(self, short_thr: int = 64, long_thr: int = 64, sigma: int = 16384, col_block: int = 0):
         check(lib.tbsla_matrix_set_sell_params(self._h, short_thr, long_thr, sigma, col_block), "set_sell_params")
 
+    # ---- SpMM / sparse softmax (MatrixCSR.cpp:1269-1334) ---------------------
+    def dense_multiply(self, B: np.ndarray) -> np.ndarray:
+        B = np.ascontiguousarray(B, np.float64)
+        Cm = np.empty((self.get_n_row(), B.shape[1]))
+        check(lib.tbsla_dense_multiply(self._h, _ptr(B), _ptr(Cm), B.shape[1]), "dense_multiply")
+        return Cm
+
+    def get_row_max_abs(self) -> np.ndarray:
+        out = np.empty(self.info()["ln_row"])
+        check(lib.tbsla_get_row_max_abs(self._h, _ptr(out)), "get_row_max_abs")
+        return out
+
+    def apply_exponential(self, max_abs: np.ndarray | None = None, base: int = -1):
+        mx = None if max_abs is None else _f64(max_abs, "max_abs")
+        check(lib.tbsla_apply_exponential(self._h, _ptr(mx) if mx is not None else None, base),
+              "apply_exponential")
+
     # project generators
     def fill_uniform_rows(self, n, k, seed):
         check(lib.tbsla_matrix_fill_uniform_rows(self._h, n, k, seed), "fill_uniform_rows")

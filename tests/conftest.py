@@ -39,7 +39,7 @@ def golden():
     def load(name):
         return np.load(os.path.join(GOLDEN, name))
 
-    return {n: load(n + ".npz") for n in ("gen", "ops", "files", "cfg1")}
+    return {n: load(n + ".npz") for n in ("gen", "ops", "files", "cfg1", "spmm")}
 
 
 META = "n_row n_col ln_row ln_col f_row f_col pr pc NR NC max_col".split()

@@ -278,10 +278,47 @@ def cfg1(R):
     np.savez_compressed(os.path.join(OUT, "cfg1.npz"), **out)
 
 
+def spmm(R):
+    """dense_multiply, get_row_max_abs and apply_exponential of the
+    reference's MatrixCSR (MatrixCSR.cpp:1269-1334) on cqmat / cdiag /
+    random matrices."""
+    out = {}
+    fills = {"cqmat": lambda h: R.L.ref_fill_cqmat(h, 40, 40, 6, 0.4, 2, 0, 0, 1, 1),
+             "cdiag": lambda h: R.L.ref_fill_cdiag(h, 40, 40, 3, 0, 0, 1, 1),
+             "random": lambda h: R.L.ref_fill_random(h, 60, 50, 0.1, 3, 0, 0, 1, 1)}
+    rng = np.random.default_rng(11)
+    for key, fill in fills.items():
+        h = R.new(2)
+        fill(h)
+        i = R.info(h)
+        for cols in (1, 5, 33):
+            B = rng.uniform(-1, 1, (i["n_col"], cols))
+            Cm = np.full((i["n_row"], cols), 7.0)
+            R.L.ref_dense_multiply(h, C.c_void_p(B.ctypes.data), C.c_void_p(Cm.ctypes.data), cols)
+            out[f"{key}/B{cols}"] = B
+            out[f"{key}/C{cols}"] = Cm
+        mx = np.zeros(i["ln_row"])
+        R.L.ref_row_max_abs(h, C.c_void_p(mx.ctypes.data))
+        out[f"{key}/max_abs"] = mx
+        R.L.ref_delete(h)
+        for tag, use_max, base in (("exp_max", True, -1), ("exp", False, -1), ("pow2_max", True, 2)):
+            h = R.new(2)
+            fill(h)
+            R.L.ref_apply_exponential(h, C.c_void_p(mx.ctypes.data) if use_max else None, base)
+            out[f"{key}/{tag}"] = R.arrays(h, 2)["values"]
+            R.L.ref_delete(h)
+    np.savez_compressed(os.path.join(OUT, "spmm.npz"), **out)
+
+
 if __name__ == "__main__":
     R = Ref()
+    if len(sys.argv) > 1:  # only the named fixtures
+        for name in sys.argv[1:]:
+            globals()[name](R)
+        raise SystemExit(0)
     print("gen", gen(R))
     ops(R)
     files(R)
     cfg1(R)
+    spmm(R)
     print("done")

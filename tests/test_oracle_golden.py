@@ -231,3 +231,28 @@ def test_mpnn_oracle_gradient_is_the_derivative_of_its_loss():
             assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(fd)), k
     finally:
         M.bf16 = keep
+
+
+SPMM_FILLS = {"cqmat": lambda m: m.fill_cqmat(40, 40, 6, 0.4, 2), "cdiag": lambda m: m.fill_cdiag(40, 40, 3),
+              "random": lambda m: m.fill_random(60, 50, 0.1, 3)}
+
+
+def test_oracle_spmm_and_softmax_helpers(golden):
+    """dense_multiply, get_row_max_abs and apply_exponential restated, bit
+    for bit against the reference's MatrixCSR (tests/golden/spmm.npz)."""
+    import tbsla_gb300 as T
+
+    g = golden["spmm"]
+    for key, fill in SPMM_FILLS.items():
+        m = T.MatrixCSR()
+        fill(m)
+        a = m.arrays()
+        for cols in (1, 5, 33):
+            Cm = oracle.csr_dense_multiply(a["rowptr"], a["colidx"], a["values"], g[f"{key}/B{cols}"])
+            assert np.array_equal(Cm, g[f"{key}/C{cols}"]), (key, cols)
+        mx = oracle.csr_row_max_abs(a["rowptr"], a["values"])
+        assert np.array_equal(mx, g[f"{key}/max_abs"]), key
+        for tag, use_max, base in (("exp_max", True, -1), ("exp", False, -1), ("pow2_max", True, 2)):
+            v = oracle.csr_apply_exponential(a["rowptr"], a["values"], mx if use_max else None, base)
+            end = int(a["rowptr"][-1])  # CSR fill_cqmat over-counts nnz; the arrays end at rowptr[n]
+            assert np.array_equal(v[:end], g[f"{key}/{tag}"]), (key, tag)
