@@ -52,6 +52,8 @@ def parse_args():
     p.add_argument("--epochs", type=int, default=1, help="learned: passes over the training systems")
     p.add_argument("--eval-systems", type=int, default=32, help="learned: held-out systems (seeds 9000..)")
     p.add_argument("--eval-n", type=int, default=128, help="learned: held-out grid size n (n^3 unknowns)")
+    p.add_argument("--factor-prec", choices=["f32", "bf16"], default="bf16",
+                   help="learned: storage precision of the factor L")
     p.add_argument("--n", type=int, default=None, help="rows (spmv: 2^24, pagerank: 2^22)")
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
@@ -631,7 +633,7 @@ def run_learned(a):
     for name, pre in (("jacobi_pcg", 1), ("learned_pcg", 2)):
         bt = T.Batch(held, T.F32)
         if pre == 2:
-            bt.set_factors(factors)
+            bt.set_factors(factors, T.BF16 if a.factor_prec == "bf16" else T.F32)
         bt.cg(rhs, max_iterations=20, rel_tol=1e-8, precond=pre, refresh=50, graph_iters=10)  # warm-up
         if pre == 2:
             clk.start()
@@ -653,7 +655,7 @@ def run_learned(a):
         "scaling": "weak", "vs_baseline": None, "dtype": "bf16 weights / f32 network; f32 values, f64 vectors",
         "data": "synthetic: seeded diffusion systems (train seeds 1000.., held-out 9000..)",
         "config": {"workload": f"learned_pcg_mpnn3x32_train{a.train_systems}_n32to64_eval{a.eval_systems}x{a.eval_n}^3",
-                   "unknowns_per_system": N, "rel_tol": 1e-8,
+                   "unknowns_per_system": N, "rel_tol": 1e-8, "factor_storage": a.factor_prec,
                    "step": "one batched PCG solve of the held-out systems (host call, wall clock)",
                    "parallelism": "1 GPU"},
         "train": {"systems": a.train_systems, "epochs": a.epochs, "adam_steps": total, "seconds": round(t_train, 1),

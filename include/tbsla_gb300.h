@@ -330,9 +330,12 @@ int tbsla_batch_cg(tbsla_batch* b, const double* rhs, double* x, int max_iterati
                    double* rel_residual);
 /* Factored preconditioner M^-1 = L L^T for every system of the batch (L:
  * lower-triangular CSR handles, one per system, same sizes), used by
- * tbsla_batch_cg with precond = 2.  Values are stored in the batch's
- * precision. */
-int tbsla_batch_set_factors(tbsla_batch* b, tbsla_matrix* const* factors, int nsys);
+ * tbsla_batch_cg with precond = 2.  Values are stored in `precision`
+ * (TBSLA_F64 / F32 / BF16); M stays SPD whatever the rounding, since it is
+ * L L^T of the rounded L with a positive diagonal.  z = L (L^T r) is
+ * computed in FP32 arithmetic on r rounded to FP32; r.z and the CG vectors
+ * stay FP64. */
+int tbsla_batch_set_factors(tbsla_batch* b, tbsla_matrix* const* factors, int nsys, int precision);
 
 /* ---- learned preconditioner (no reference counterpart) ------------------------
  * A message-passing network over the pattern of an SPD CSR matrix A that

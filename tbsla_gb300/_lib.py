@@ -109,7 +109,7 @@ _SIGS = {
     "tbsla_batch_destroy": (I, [P]),
     "tbsla_batch_rows": (I, [P, IP, C.POINTER(L)]),
     "tbsla_batch_cg": (I, [P, P, P, I, D, I, I, I, IP, DP]),
-    "tbsla_batch_set_factors": (I, [P, C.POINTER(P), I]),
+    "tbsla_batch_set_factors": (I, [P, C.POINTER(P), I, I]),
     "tbsla_mpnn_create": (I, [C.POINTER(P), ULL]),
     "tbsla_mpnn_destroy": (I, [P]),
     "tbsla_mpnn_params": (I, [P, P, IP]),

@@ -63,7 +63,8 @@ struct tbsla_batch {
   // factored preconditioner L L^T (block-diagonal over the systems)
   int *lrowptr = nullptr, *lcolidx = nullptr, *trowptr = nullptr, *tcolidx = nullptr;
   void *lvals = nullptr, *tvals = nullptr;
-  double* t = nullptr;
+  int lprec = TBSLA_F64;
+  float *rf = nullptr, *tf = nullptr;
   double *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
   double* scal = nullptr;
   int *status = nullptr, *iters = nullptr;
@@ -76,7 +77,7 @@ struct tbsla_batch {
     if (stream) cudaStreamSynchronize(stream);
     if (graph) cudaGraphExecDestroy(graph);
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
-                  scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, t};
+                  scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf};
     for (void* v : ps)
       if (v) cudaFree(v);
     if (vals && vals != vals64) cudaFree(vals);
@@ -108,7 +109,9 @@ struct tbsla_batch {
     c.tcolidx = f ? tcolidx : nullptr;
     c.lvals = f ? lvals : nullptr;
     c.tvals = f ? tvals : nullptr;
-    c.t = f ? t : nullptr;
+    c.lprec = lprec;
+    c.rf = f ? rf : nullptr;
+    c.tf = f ? tf : nullptr;
     c.b = b;
     c.x = x;
     c.r = r;
@@ -271,9 +274,10 @@ int tbsla_batch_destroy(tbsla_batch* b) {
   return TBSLA_OK;
 }
 
-int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int nsys) {
+int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int nsys, int precision) {
   using namespace tbsla_impl;
-  if (!B || !factors || nsys != B->nsys) return TBSLA_ERR_INVALID_ARG;
+  if (!B || !factors || nsys != B->nsys || precision < TBSLA_F64 || precision > TBSLA_BF16)
+    return TBSLA_ERR_INVALID_ARG;
   // L concatenated block-diagonally, and L^T built by a counting sort
   std::vector<int> rp(B->n + 1, 0), ci;
   std::vector<double> va;
@@ -310,18 +314,20 @@ int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int ns
   cudaSetDevice(B->device);
   cudaStream_t st = B->stream;
   for (void* p : {(void*)B->lrowptr, (void*)B->lcolidx, (void*)B->trowptr, (void*)B->tcolidx, B->lvals, B->tvals,
-                  (void*)B->t})
+                  (void*)B->rf, (void*)B->tf})
     if (p) cudaFree(p);
   B->lrowptr = B->lcolidx = B->trowptr = B->tcolidx = nullptr;
   B->lvals = B->tvals = nullptr;
-  B->t = nullptr;
+  B->rf = B->tf = nullptr;
   double* tmp = nullptr;
-  const size_t es = B->prec == TBSLA_F64 ? 8 : B->prec == TBSLA_F32 ? 4 : 2;
+  const size_t es = precision == TBSLA_F64 ? 8 : precision == TBSLA_F32 ? 4 : 2;
+  B->lprec = precision;
   CK(alloc(&B->lrowptr, rp.size()));
   CK(alloc(&B->lcolidx, std::max<size_t>(ci.size(), 1)));
   CK(alloc(&B->trowptr, trp.size()));
   CK(alloc(&B->tcolidx, std::max<size_t>(tci.size(), 1)));
-  CK(alloc(&B->t, B->n));
+  CK(alloc(&B->rf, B->n));
+  CK(alloc(&B->tf, B->n));
   CK(cudaMalloc(&B->lvals, std::max<size_t>(nl, 1) * es));
   CK(cudaMalloc(&B->tvals, std::max<size_t>(nl, 1) * es));
   CK(alloc(&tmp, std::max<size_t>(nl, 1) * 2));
@@ -331,8 +337,8 @@ int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int ns
   CK(cudaMemcpyAsync(B->tcolidx, tci.data(), tci.size() * 4, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(tmp, va.data(), nl * 8, cudaMemcpyHostToDevice, st));
   CK(cudaMemcpyAsync(tmp + nl, tva.data(), nl * 8, cudaMemcpyHostToDevice, st));
-  CK(convert_values(tmp, B->lvals, B->prec, nl, st));
-  CK(convert_values(tmp + nl, B->tvals, B->prec, nl, st));
+  CK(convert_values(tmp, B->lvals, precision, nl, st));
+  CK(convert_values(tmp + nl, B->tvals, precision, nl, st));
   CK(cudaStreamSynchronize(st));
   cudaFree(tmp);
   if (B->graph_pre == 2) B->graph_pre = -1;  // recapture with the new arrays

@@ -39,9 +39,11 @@ struct EpiResidual {
   double* r;
   double* z;  // nullptr when unpreconditioned
   const double* dinv;
+  float* rf;  // factored preconditioner: r in FP32
   __device__ __forceinline__ void emit(int row, double s, double* red) const {
     const double ri = b[row] - s;
     r[row] = ri;
+    if (rf) rf[row] = (float)ri;
     const double zi = dinv ? dinv[row] * ri : ri;
     if (dinv) z[row] = zi;
     red[0] = fma_rn(ri, ri, red[0]);
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(NT) k_cg_residual(CgBatch c, int mask) {
   if (!((mask >> c.status[sys]) & 1)) return;
   const uint64_t pol = policy_evict_first();
   CsrArgs a{c.vals64, kF64, c.rowptr, c.colidx, c.blocks, c.nblocks, 0, c.items};
-  EpiResidual epi{c.b, c.r, c.dinv ? c.z : nullptr, c.dinv};
+  EpiResidual epi{c.b, c.r, c.dinv ? c.z : nullptr, c.dinv, c.lrowptr ? c.rf : nullptr};
   double red[2] = {0, 0};
   csr_block<double, ITEMS>(a, b, c.x, epi, red, stage, sm, pol);
   const double rr = block_sum<NT>(red[0], sm.red);
@@ -105,6 +107,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(CgBatch c) {
       c.z[i] = zi;
     }
     if (!c.lrowptr) rz = fma_rn(ri, zi, rz);  // factored: r.z comes with z
+    else c.rf[i] = (float)ri;
     rr = fma_rn(ri, ri, rr);
   }
   rz = block_sum<NT>(rz, red_s);
@@ -177,30 +180,44 @@ __global__ void __launch_bounds__(NT) k_cg_restart(CgBatch c, int all) {
   for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = z[i];
 }
 
-// out = M in over the chunks of the masked systems, M = L or L^T in CSR
-// (values in V); with `acc`, acc[sys] += r . out per chunk.
+__device__ __forceinline__ float to_f32(double v) { return (float)v; }
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// tf = L^T rf over the chunks of the masked systems (FP32 arithmetic).
 template <class V>
-__global__ void __launch_bounds__(NT) k_cg_factor(CgBatch c, int mask, const int* __restrict__ rp,
-                                                 const int* __restrict__ ci, const void* vals,
-                                                 const double* __restrict__ in, double* __restrict__ out,
-                                                 double* acc) {
+__global__ void __launch_bounds__(NT) k_cg_factor_t(CgBatch c, int mask) {
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  if (!((mask >> c.status[sys]) & 1)) return;
+  const V* v = static_cast<const V*>(c.tvals);
+  const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+    float s = 0.f;
+    for (int k = c.trowptr[i]; k < c.trowptr[i + 1]; k++) s = fmaf(to_f32(v[k]), c.rf[c.tcolidx[k]], s);
+    c.tf[i] = s;
+  }
+}
+
+// z = L tf (FP32 arithmetic, stored in FP64) and acc[sys] += r . z (FP64).
+template <class V>
+__global__ void __launch_bounds__(NT) k_cg_factor_l(CgBatch c, int mask, double* acc) {
   __shared__ double red_s[NT / kWarp];
   const int ch = blockIdx.x;
   const int sys = c.chunk_sys[ch];
   if (!((mask >> c.status[sys]) & 1)) return;
-  const V* v = static_cast<const V*>(vals);
+  const V* v = static_cast<const V*>(c.lvals);
   const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
   double d = 0;
   for (int i = r0 + threadIdx.x; i < r1; i += NT) {
-    double s = 0;
-    for (int k = rp[i]; k < rp[i + 1]; k++) s = fma_rn(widen(v[k]), in[ci[k]], s);
-    out[i] = s;
-    if (acc) d = fma_rn(c.r[i], s, d);
+    float s = 0.f;
+    for (int k = c.lrowptr[i]; k < c.lrowptr[i + 1]; k++) s = fmaf(to_f32(v[k]), c.tf[c.lcolidx[k]], s);
+    const double zi = widen(s);
+    c.z[i] = zi;
+    d = fma_rn(c.r[i], zi, d);
   }
-  if (acc) {
-    d = block_sum<NT>(d, red_s);
-    if (threadIdx.x == 0) atomicAdd(acc + sys, d);
-  }
+  d = block_sum<NT>(d, red_s);
+  if (threadIdx.x == 0) atomicAdd(acc + sys, d);
 }
 
 __global__ void k_cg_activate(CgBatch c) {
@@ -309,14 +326,14 @@ cudaError_t cg_restart(const CgBatch& c, bool all, cudaStream_t s) {
 
 template <class V>
 cudaError_t factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s) {
-  k_cg_factor<V><<<c.nchunks, NT, 0, s>>>(c, mask, c.trowptr, c.tcolidx, c.tvals, c.r, c.t, nullptr);
-  k_cg_factor<V><<<c.nchunks, NT, 0, s>>>(c, mask, c.lrowptr, c.lcolidx, c.lvals, c.t, c.z, acc);
+  k_cg_factor_t<V><<<c.nchunks, NT, 0, s>>>(c, mask);
+  k_cg_factor_l<V><<<c.nchunks, NT, 0, s>>>(c, mask, acc);
   return cudaGetLastError();
 }
 
 cudaError_t cg_factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s) {
   if (!c.lrowptr || c.nchunks == 0) return cudaSuccess;
-  switch (c.prec) {
+  switch (c.lprec) {
     case kF64: return factor_apply<double>(c, mask, acc, s);
     case kF32: return factor_apply<float>(c, mask, acc, s);
     case kBF16: return factor_apply<__nv_bfloat16>(c, mask, acc, s);

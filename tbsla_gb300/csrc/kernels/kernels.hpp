@@ -178,10 +178,12 @@ struct CgBatch {
   int nchunks;
   const double* dinv;  // Jacobi: 1/diag(A); nullptr = unpreconditioned
   // factored preconditioner z = L (L^T r) (nullptr lrowptr = none): L and
-  // L^T as CSR, values in `prec`; t = L^T r
+  // L^T as CSR, values in `lprec`, applied in FP32 arithmetic: rf = fp32(r),
+  // tf = L^T rf, z = fp64(L tf)
   const int *lrowptr, *lcolidx, *trowptr, *tcolidx;
   const void *lvals, *tvals;
-  double* t;
+  int lprec;
+  float *rf, *tf;
   const double* b;
   double *x, *r, *z, *p, *q;  // z == r when unpreconditioned
   // per-system scalars (rrt: squared FP64 true residual of the last check)

@@ -401,12 +401,12 @@ class Batch:
             check(st, "batch_cg")
         return x, its, rr, st == L.OK
 
-    def set_factors(self, factors):
-        """Lower-triangular CSR factors L (one per system): cg(precond=2)
-        then applies z = L (L^T r)."""
+    def set_factors(self, factors, precision=L.F32):
+        """Lower-triangular CSR factors L (one per system), stored in
+        `precision`: cg(precond=2) then applies z = L (L^T r)."""
         self._factors = list(factors)
         arr = (C.c_void_p * len(factors))(*[f._h.value for f in factors])
-        check(lib.tbsla_batch_set_factors(self._h, arr, len(factors)), "batch_set_factors")
+        check(lib.tbsla_batch_set_factors(self._h, arr, len(factors), precision), "batch_set_factors")
 
 
 class MPNN:

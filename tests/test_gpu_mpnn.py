@@ -74,10 +74,10 @@ def test_untrained_factor_is_jacobi(gpu):
     assert np.allclose(ratio, ratio[0], rtol=1e-6) and abs(ratio[0] - 1) < 1e-2
 
 
-def _solve(T, systems, factors, precond):
+def _solve(T, systems, factors, precond, factor_prec=None):
     bt = T.Batch(systems, T.F32)
     if factors is not None:
-        bt.set_factors(factors)
+        bt.set_factors(factors, T.F32 if factor_prec is None else factor_prec)
     rhs = np.concatenate([T.fill_uniform(len(s.arrays()["rowptr"]) - 1, -1.0, 1.0, 70 + i)
                           for i, s in enumerate(systems)])
     x, its, rr, ok = bt.cg(rhs, max_iterations=5000, rel_tol=1e-8, precond=precond, refresh=50, graph_iters=10)
@@ -103,5 +103,9 @@ def test_factored_pcg_converges_and_training_beats_jacobi(gpu):
     assert np.mean(losses[-24:]) < 0.8 * np.mean(losses[:24])
     held = [diffusion(T, 14, 9000 + i) for i in range(4)]
     its_j = _solve(T, held, None, 1)
-    its_l = _solve(T, held, [net.factor(A) for A in held], 2)
+    factors = [net.factor(A) for A in held]
+    its_l = _solve(T, held, factors, 2)
     assert its_l.mean() < its_j.mean(), (its_l, its_j)
+    # bfloat16 factor storage: still SPD, still converges to the FP64 bar
+    its_b = _solve(T, held, factors, 2, T.BF16)
+    assert its_b.mean() < its_j.mean(), (its_b, its_j)
