@@ -174,7 +174,7 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
 /* CSR SpMV kernel: TBSLA_CSR_SELL (default; sliced-ELL device layout,
  * slices of 32 lanes over rows of similar length, see
  * tbsla_matrix_set_sell_params; `items` = steps per lane in flight, 4/8/16,
- * or 0 for 8, 16 past 2^23 columns), TBSLA_CSR_MERGE (merge-path split,
+ * 0 = 8), TBSLA_CSR_MERGE (merge-path split,
  * `items` row ends + entries per thread, 4/8/16, 0 = 8) or
  * TBSLA_CSR_ROWBLOCK (row-block adaptive, see
  * tbsla_matrix_set_csr_tile; `items` unused).  Changing the kernel or the

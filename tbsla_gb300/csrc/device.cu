@@ -244,9 +244,9 @@ SellArgs sell_args(const tbsla_matrix* m, const DeviceMatrix* d) {
   a.f_col = m->info.f_col;
   a.svals = d->svals;
   a.scols = d->scols;
-  // automatic: 8 steps in flight while x stays in L2, 16 when most gathers
-  // go to HBM and more of them must be in flight
-  a.unroll = m->sell_unroll > 0 ? m->sell_unroll : (m->info.ln_col > (1 << 23) ? 16 : 8);
+  // automatic: 8 steps in flight (the column blocks keep x in L2, where
+  // 16 costs more in occupancy than it gains in latency)
+  a.unroll = m->sell_unroll > 0 ? m->sell_unroll : 8;
   a.nblocks = (int)d->sell.size();
   a.blocks = d->sell.data();
   return a;

@@ -60,7 +60,7 @@ struct tbsla_matrix {
   int sell_short = 64;     // sliced ELL: rows up to this length, one lane each, sorted per window
   int sell_long = 64;      // longer rows: fewest lanes keeping a slice this many steps wide
   int sell_sigma = 16384;  // window of consecutive rows sorted together
-  int sell_unroll = 0;     // steps per lane in flight (0: 8, or 16 past 2^23 columns)
+  int sell_unroll = 0;     // steps per lane in flight (0: 8)
   int sell_colblock = 0;   // columns per block (0: 8,388,608 = 64 MiB of x)
   int device = 0;
   mutable tbsla_impl::DeviceMatrix* dev = nullptr;

@@ -55,6 +55,9 @@ __global__ void __launch_bounds__(NT) k_csr_spmv(CsrArgs a, const double* __rest
 // t * tele_i and t = 1 - (beta * M) * s, M = sum_j w_j x_j (w = column sums
 // of A as stored), so that y sums to 1.  Reductions: L1 change, sum y and
 // sum w y (the next step's S and M).
+// Four FP64 operations per row (GB300's FP64 pipe is the epilogue's
+// bound): yn = fma(beta s, sum, c), the change fma(-x, s, yn), S += yn,
+// M = fma(w, yn, M).
 struct EpiPageRank {
   double* y;
   const double* x;
@@ -63,10 +66,10 @@ struct EpiPageRank {
   double beta, s, t, c_uniform;
   __device__ __forceinline__ void emit(int row, double sum, double* red) const {
     const double c = tele ? mul_rn(t, tele[row]) : c_uniform;
-    const double yn = add_rn(mul_rn(mul_rn(beta, sum), s), c);
-    red[0] = add_rn(red[0], fabs(yn - mul_rn(x[row], s)));
+    const double yn = fma_rn(mul_rn(beta, s), sum, c);
+    red[0] = add_rn(red[0], fabs(fma_rn(-x[row], s, yn)));
     red[1] = add_rn(red[1], yn);
-    red[2] = add_rn(red[2], mul_rn(colw[row], yn));
+    red[2] = fma_rn(colw[row], yn, red[2]);
     y[row] = yn;
   }
 };
