@@ -73,6 +73,15 @@ def parse_args():
     return a
 
 
+def launches_per_step(a, n: int) -> int:
+    """Kernel launches of one SpMV: one per column block (sliced ELL), the
+    tile pass and the carry pass (merge path), or one (row blocks)."""
+    if a.algo == "sell":
+        cb = int(a.sell.split(",")[3]) or 8388608
+        return -(-n // cb)
+    return 2 if a.algo == "merge" else 1
+
+
 def algorithmic_bytes(n: int, nnz: int, s_v: int) -> int:
     return nnz * (s_v + 4) + 4 * (n + 1) + 8 * n + 8 * n
 
@@ -368,7 +377,7 @@ def run_ours(a):
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_val, "unit": "GB/s", "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n,
                 "ms_per_step": statistics.mean(e2e) * 1e3},
-        "gpu_launches": a.steps,
+        "gpu_launches": a.steps * launches_per_step(a, n),
         "clocks": clocks,
         "extra": extra,
     }

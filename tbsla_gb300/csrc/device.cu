@@ -2,7 +2,10 @@
 //
 // HBM layout per format (built once by dev_upload, dropped on host mutation):
 //   CSR   rowptr int32[ln_row+1], colidx int32[nnz], values V[nnz],
-//         row-block partition int32[nblocks+1]
+//         row-block partition int32[nblocks+1], merge-path tile starts and
+//         carries, and (default kernel) the sliced-ELL copy: per column
+//         block a plan (slice descriptors, lane words) and the step-major
+//         values / columns
 //   ELL   columns int32[max_col*ln_row] and values V[max_col*ln_row],
 //         slot-major (transposed from the reference's row-major)
 //   COO/  rows, cols int32[nnz] and values V[nnz], stably sorted by row
@@ -85,7 +88,7 @@ struct DeviceMatrix {
   int* blocks = nullptr;  // CSR row-block partition
   int nblocks = 0;
   int items = 8;
-  int algo = 0;            // CSR: 0 merge path, 1 row blocks
+  int algo = 0;            // CSR: 0 merge path, 1 row blocks, 2 sliced ELL
   int* coord = nullptr;    // CSR merge path: first row of each tile
   int* carry_row = nullptr;
   double* carry_val = nullptr;
