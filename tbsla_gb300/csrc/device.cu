@@ -307,9 +307,10 @@ int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
     cudaGetLastError();
     return TBSLA_ERR_ALLOC;
   }
-  if ((st = dalloc(&d->scols, std::max<size_t>(len, 1))) || (st = dalloc(&d->sell_counter, 2))) return st;
+  if ((st = dalloc(&d->scols, std::max<size_t>(len, 1))) || (st = dalloc(&d->sell_counter, kSellCounterWords)))
+    return st;
   d->bytes += len * (prec_size(d->prec) + 4);
-  TRY(cudaMemsetAsync(d->sell_counter, 0, 2 * sizeof(unsigned), d->stream));
+  TRY(cudaMemsetAsync(d->sell_counter, 0, kSellCounterWords * sizeof(unsigned), d->stream));
   TRY(sell_fill(sell_args(m, d), d->stream));
   return TBSLA_OK;
 }

@@ -105,9 +105,10 @@ struct SellArgs {
 };
 // Fills the slice arrays of every block from the CSR device arrays.
 cudaError_t sell_fill(const SellArgs& a, cudaStream_t s);
-// y = A x, one launch per column block; counter: 2 unsigned of zeroed
-// scratch, reset by each launch; a set *done (device) makes the launches
-// no-ops.
+// y = A x, one launch per column block; counter: kSellCounterWords
+// unsigned of zeroed scratch, reset by each launch; a set *done (device)
+// makes the launches no-ops.
+constexpr int kSellCounterWords = 1024;
 cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s,
                       const int* done = nullptr);
 

@@ -117,6 +117,32 @@ __device__ __forceinline__ Lane slice_lane(const SellPlan& p, const int4& d, int
   return l;
 }
 
+// Work claims of k_sell, spread over kQueues counters kQueueStride words
+// (256 bytes) apart: one counter drew every warp's atomic to a single L2
+// slice, which then ran at its tag-lookup limit and delayed the gathers
+// that live in that slice.  Queue q hands out items q, q + kQueues, ...; a
+// warp starts on queue (its index mod kQueues) and moves on to the next
+// queue when its own runs dry.  Lane 0 holds the state.
+constexpr int kQueues = 8, kQueueStride = 64;
+static_assert(kQueues * kQueueStride + 1 <= kSellCounterWords, "counter scratch");
+struct Claims {
+  unsigned* counter;
+  int nitems;
+  int q;     // queue the next ticket is drawn from
+  int left;  // queues not yet visited
+  __device__ __forceinline__ int ticket() { return (int)atomicAdd(counter + q * kQueueStride, 1u); }
+  // item of ticket t, drawn from queue q; past the end of q, the next queues
+  __device__ __forceinline__ int resolve(int t) {
+    int it = q + kQueues * t;
+    while (it >= nitems && left > 0) {
+      q = (q + 1) % kQueues;
+      left--;
+      it = q + kQueues * ticket();
+    }
+    return it;
+  }
+};
+
 // One column block: y = A_block x (block 0) or y += A_block x (later blocks,
 // whose plans leave out the rows without entries in the block).
 template <class V, int U>
@@ -125,18 +151,19 @@ __global__ void __launch_bounds__(NT) k_sell(SellPlan p, const V* __restrict__ s
                                             double* __restrict__ y, unsigned* __restrict__ counter,
                                             const int* __restrict__ done) {
   // a set done flag (an iteration that has converged) makes the launch a
-  // no-op; no warp has touched the counter then
+  // no-op; no warp has touched the counters then
   if (done && *(volatile const int*)done) return;
   const int lane = threadIdx.x & 31;
   const int nitems = p.nslices;
   const uint64_t pol = policy_evict_first();
   // Two items are claimed ahead, and the descriptor of the next one is
-  // loaded while the current one runs, so neither the work counter's
+  // loaded while the current one runs, so neither the work counters'
   // atomics nor the descriptor loads sit on the critical path.
+  Claims cl{counter, nitems, (int)((blockIdx.x * (NT / 32) + (threadIdx.x >> 5)) % kQueues), kQueues - 1};
   int cur = 0, nxt = 0;
   if (lane == 0) {
-    cur = (int)atomicAdd(counter, 1u);
-    nxt = (int)atomicAdd(counter, 1u);
+    cur = cl.resolve(cl.ticket());
+    nxt = cl.resolve(cl.ticket());
   }
   cur = __shfl_sync(FULL, cur, 0);
   nxt = __shfl_sync(FULL, nxt, 0);
@@ -148,7 +175,7 @@ __global__ void __launch_bounds__(NT) k_sell(SellPlan p, const V* __restrict__ s
   }
   while (cur < nitems) {
     int after = 0;
-    if (lane == 0) after = (int)atomicAdd(counter, 1u);
+    if (lane == 0) after = cl.ticket();
     int4 dn = make_int4(0, 0, 0, 0);
     int mn = -1;
     if (nxt < nitems) {
@@ -161,18 +188,19 @@ __global__ void __launch_bounds__(NT) k_sell(SellPlan p, const V* __restrict__ s
     double acc = slice_rows<V, U>(sv, sc, (long)d.x * 32 + lane, l.steps, d.y, x, f_col, pol);
     for (int o = (1 << d.z) >> 1; o > 0; o >>= 1) acc = add_rn(acc, __shfl_xor_sync(FULL, acc, o));
     if (head) y[l.row] = accumulate ? add_rn(y0, acc) : acc;
+    if (lane == 0) after = cl.resolve(after);
     cur = nxt;
     nxt = __shfl_sync(FULL, after, 0);
     d = dn;
     meta = mn;
   }
-  // The last warp to finish resets the work counter for the next launch:
+  // The last warp to finish resets the work counters for the next launch:
   // every warp's claims were answered before it counts itself out here.
   if (lane == 0) {
     const unsigned total = gridDim.x * (NT / 32);
-    if (atomicAdd(counter + 1, 1u) == total - 1) {
-      counter[0] = 0;
-      counter[1] = 0;
+    if (atomicAdd(counter + kQueues * kQueueStride, 1u) == total - 1) {
+      for (int q = 0; q < kQueues; q++) counter[q * kQueueStride] = 0;
+      counter[kQueues * kQueueStride] = 0;
     }
   }
 }
