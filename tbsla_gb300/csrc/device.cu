@@ -98,6 +98,8 @@ struct DeviceMatrix {
   void* svals = nullptr;
   int* scols = nullptr;
   unsigned* sell_counter = nullptr;
+  cudaStream_t xstream = nullptr;   // host entry point: x of column blocks 1.. copied here
+  std::vector<cudaEvent_t> xready;  // [block]: that block's x has arrived
   double* colw = nullptr;  // PageRank: column sums of the stored values
   bool colw_ok = false;
   double colw_s0 = 0, colw_m0 = 0;  // S and M of the start vector 1/n
@@ -125,6 +127,9 @@ struct DeviceMatrix {
     for (SellPlan& p : sell)
       for (void* q : {(void*)p.slice, (void*)p.lane, (void*)p.lane_len})
         if (q) cudaFree(q);
+    for (cudaEvent_t e : xready)
+      if (e) cudaEventDestroy(e);
+    if (xstream) cudaStreamDestroy(xstream);
     if (stream) cudaStreamDestroy(stream);
   }
 
@@ -513,6 +518,44 @@ int dev_bytes(const tbsla_matrix* m, size_t* bytes) {
   return TBSLA_OK;
 }
 
+namespace {
+// Host entry point of the sliced-ELL kernel with column blocks: x of block 0
+// goes over on the matrix stream, x of the later blocks on a second stream,
+// and each later block's launch waits only for its own part of x, so those
+// copies run under the earlier blocks' launches (the host link moves about
+// 0.2 TB/s each way; the first block's launch takes longer than the next
+// block's 64 MiB of x).  Results are those of dev_ax's plain path.
+int ax_host_blocks(const tbsla_matrix* m, DeviceMatrix* d, double* r, const double* v, int vect_incr,
+                   bool zero_first) {
+  const size_t nx = in_len(m), ny = out_len(m);
+  const int P = (int)d->sell.size();
+  cudaStream_t s = d->stream;
+  if (!d->xstream) TRY(cudaStreamCreateWithFlags(&d->xstream, cudaStreamNonBlocking));
+  while ((int)d->xready.size() < P + 1) {
+    cudaEvent_t e = nullptr;
+    TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    d->xready.push_back(e);
+  }
+  // the copies into d->x start after the matrix stream's earlier work
+  TRY(cudaEventRecord(d->xready[P], s));
+  TRY(cudaStreamWaitEvent(d->xstream, d->xready[P], 0));
+  for (int b = 0; b < P; b++) {
+    const size_t lo = std::min<size_t>((size_t)d->sell[b].col_lo, nx);
+    const size_t hi = b == P - 1 ? nx : std::min<size_t>((size_t)d->sell[b].col_hi, nx);
+    cudaStream_t cs = b == 0 ? s : d->xstream;
+    if (hi > lo) TRY(cudaMemcpyAsync(d->x + lo, v + lo, (hi - lo) * sizeof(double), cudaMemcpyHostToDevice, cs));
+    if (b > 0) TRY(cudaEventRecord(d->xready[b], d->xstream));
+  }
+  if (zero_first) TRY(cudaMemsetAsync(d->y, 0, ny * sizeof(double), s));
+  SellArgs a = sell_args(m, d);
+  a.ready = d->xready.data();
+  TRY(sell_spmv(a, d->x, d->y, d->sell_counter, s));
+  (void)vect_incr;
+  if (ny) TRY(cudaMemcpyAsync(r, d->y, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
+  return status_of(cudaStreamSynchronize(s));
+}
+}  // namespace
+
 int dev_ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr, bool zero_first,
            bool host, void* stream) {
   int st;
@@ -527,6 +570,8 @@ int dev_ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr, boo
   size_t nx = in_len(m), ny = out_len(m);
   if ((st = d->vec(&d->x, &d->x_len, nx)) || (st = d->vec(&d->y, &d->y_len, ny))) return st;
   cudaStream_t s = d->stream;
+  if (m->format == TBSLA_CSR && d->algo == 2 && d->sell.size() > 1 && nx && !skips_empty(m))
+    return ax_host_blocks(m, d, r, v, vect_incr, zero_first);
   if (nx) TRY(cudaMemcpyAsync(d->x, v, nx * sizeof(double), cudaMemcpyHostToDevice, s));
   if (zero_first) TRY(cudaMemsetAsync(d->y, 0, ny * sizeof(double), s));
   else if (accumulates(m->format) && ny) TRY(cudaMemcpyAsync(d->y, r, ny * sizeof(double), cudaMemcpyHostToDevice, s));

@@ -102,6 +102,9 @@ struct SellArgs {
   int unroll;               // steps per lane in flight: 4, 8 or 16
   int nblocks;              // column blocks
   const SellPlan* blocks;   // host array of plans holding device pointers
+  // optional, per block: the launch of block b > 0 waits for ready[b]
+  // (its part of x arriving on another stream)
+  const cudaEvent_t* ready = nullptr;
 };
 // Fills the slice arrays of every block from the CSR device arrays.
 cudaError_t sell_fill(const SellArgs& a, cudaStream_t s);

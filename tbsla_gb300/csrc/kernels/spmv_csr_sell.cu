@@ -254,6 +254,10 @@ cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* coun
   const int grid = std::max(1, sms * std::max(1, per));
   for (int b = 0; b < a.nblocks; b++) {
     const SellPlan& p = a.blocks[b];
+    if (a.ready && b > 0) {
+      cudaError_t e = cudaStreamWaitEvent(s, a.ready[b], 0);
+      if (e != cudaSuccess) return e;
+    }
     if (p.nslices == 0) continue;
     k_sell<V, U><<<grid, NT, 0, s>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
                                      counter, done);

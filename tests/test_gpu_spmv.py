@@ -283,6 +283,31 @@ def test_device_pointer_entry_points(gpu):
     assert torch.equal(zt, yt)
 
 
+def test_host_entry_with_column_blocks_equals_device_entry(gpu):
+    """The host entry point copies x of column blocks 1.. on a second
+    stream, under the earlier blocks' launches: the result equals the
+    device-pointer entry point's bit for bit, on repeated calls, for Ax and
+    for spmv, with 2 and with 7 column blocks."""
+    import torch
+
+    T = gpu
+    n = 1 << 17
+    m = powerlaw(T, n, seed=12)
+    for cb in (70000, 20000):
+        m.set_sell_params(64, 64, 16384, cb)
+        xt = torch.from_numpy(T.fill_uniform(n, -1.0, 1.0, cb)).cuda()
+        yt = torch.zeros(n, dtype=torch.float64, device="cuda")
+        m.Ax_device(yt, xt)
+        torch.cuda.synchronize()
+        ref = yt.cpu().numpy()
+        x = xt.cpu().numpy()
+        for _ in range(2):
+            y = np.full(n, 5.0)
+            m.Ax(y, x)
+            assert np.array_equal(y, ref), cb
+            assert np.array_equal(m.spmv(x), ref), cb
+
+
 def test_composite_ops_match_reference(gpu, golden):
     T = gpu
     ops = golden["ops"]
