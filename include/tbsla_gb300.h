@@ -168,6 +168,12 @@ int tbsla_matrix_set_precision(tbsla_matrix* m, int precision);
 int tbsla_matrix_upload(tbsla_matrix* m);
 /* Device bytes held by the handle's matrix copy. */
 int tbsla_matrix_device_bytes(const tbsla_matrix* m, size_t* bytes);
+/* Kernel launches one Ax / spmv makes on the device copy (builds it if
+ * needed): one per sliced-ELL plan (a column block, the last of several
+ * split in two by rows), two for the merge path, one otherwise, none for an
+ * empty matrix.  No counterpart in the reference (a property of this
+ * implementation's kernels). */
+int tbsla_matrix_kernel_launches(const tbsla_matrix* m, int* launches);
 /* CSR: block budget of the row-block partition (nnz per block, multiple of
  * 256, default 2048); changing it rebuilds the partition. */
 int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);

@@ -101,6 +101,7 @@ _SIGS = {
     "tbsla_matrix_set_precision": (I, [P, I]),
     "tbsla_matrix_upload": (I, [P]),
     "tbsla_matrix_device_bytes": (I, [P, C.POINTER(C.c_size_t)]),
+    "tbsla_matrix_kernel_launches": (I, [P, IP]),
     "tbsla_matrix_set_csr_tile": (I, [P, I]),
     "tbsla_matrix_set_csr_algorithm": (I, [P, I, I]),
     "tbsla_matrix_set_sell_params": (I, [P, I, I, I, I]),

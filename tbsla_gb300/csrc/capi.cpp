@@ -249,6 +249,11 @@ int tbsla_matrix_device_bytes(const tbsla_matrix* m, size_t* bytes) {
   return dev_bytes(m, bytes);
 }
 
+int tbsla_matrix_kernel_launches(const tbsla_matrix* m, int* launches) {
+  if (!m || !launches) return TBSLA_ERR_INVALID_ARG;
+  return dev_launches(m, launches);
+}
+
 int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block) {
   if (!m || nnz_per_block < 256 || nnz_per_block > 4096 || nnz_per_block % 256 != 0)
     return TBSLA_ERR_INVALID_ARG;

@@ -98,6 +98,9 @@ struct DeviceMatrix {
   void* svals = nullptr;
   int* scols = nullptr;
   unsigned* sell_counter = nullptr;
+  int sell_parts = 1;  // trailing plans that split the last column block by rows
+  cudaStream_t side = nullptr;  // least priority: the last row part runs here
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   cudaStream_t xstream = nullptr;   // host entry point: x of column blocks 1.. copied here
   std::vector<cudaEvent_t> xready;  // [block]: that block's x has arrived
   double* colw = nullptr;  // PageRank: column sums of the stored values
@@ -129,6 +132,9 @@ struct DeviceMatrix {
         if (q) cudaFree(q);
     for (cudaEvent_t e : xready)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {fork_ev, join_ev})
+      if (e) cudaEventDestroy(e);
+    if (side) cudaStreamDestroy(side);
     if (xstream) cudaStreamDestroy(xstream);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -257,6 +263,10 @@ SellArgs sell_args(const tbsla_matrix* m, const DeviceMatrix* d) {
   a.unroll = m->sell_unroll > 0 ? m->sell_unroll : 8;
   a.nblocks = (int)d->sell.size();
   a.blocks = d->sell.data();
+  a.parts = d->sell_parts;
+  a.side = d->side;
+  a.fork = d->fork_ev;
+  a.join = d->join_ev;
   return a;
 }
 
@@ -286,14 +296,29 @@ int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
         }
     });
   }
+  // With column blocks, the last block is planned in kRowParts parts by
+  // rows: after a part's launch its rows of y are final, so the host entry
+  // point copies them out while the next part runs.
+  const int R = P > 1 ? kRowParts : 1;
   long steps = 0;
-  d->sell.assign(P, SellPlan{});
+  d->sell.assign(P - 1 + R, SellPlan{});
   int st = TBSLA_OK;
-  for (int k = 0; k < P && !st; k++) {
+  std::vector<int> part;
+  for (int k = 0; k < P - 1 + R && !st; k++) {
+    const int blk = std::min(k, P - 1), r = k - blk;
+    const int* L = lens.data() + (size_t)blk * n;
+    const int r0 = (int)((long)n * r / R), r1 = (int)((long)n * (r + 1) / R);
+    if (R > 1 && blk == P - 1) {
+      part.assign(n, 0);
+      std::copy(L + r0, L + r1, part.begin() + r0);
+      L = part.data();
+    }
     SellPlan hp;
-    sell_plan_build(lens.data() + (size_t)k * n, n, m->sell_short, m->sell_long, m->sell_sigma, k > 0, steps, &hp);
-    hp.col_lo = k * W;
-    hp.col_hi = k == P - 1 ? INT_MAX : (k + 1) * W;
+    sell_plan_build(L, n, m->sell_short, m->sell_long, m->sell_sigma, blk > 0, steps, &hp);
+    hp.col_lo = blk * W;
+    hp.col_hi = blk == P - 1 ? INT_MAX : (blk + 1) * W;
+    hp.row_lo = blk == P - 1 ? r0 : 0;
+    hp.row_hi = blk == P - 1 ? r1 : n;
     SellPlan& dp = d->sell[k];
     dp = hp;
     dp.slice = nullptr;
@@ -305,6 +330,14 @@ int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
     if (!st) st = status_of(cudaStreamSynchronize(d->stream));  // host plan arrays are freed next
     sell_plan_free(&hp);
     steps += dp.sell_len / 32;
+  }
+  d->sell_parts = R;
+  if (!st && R > 1 && !d->side) {
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    st = status_of(cudaStreamCreateWithPriority(&d->side, cudaStreamNonBlocking, least));
+    if (!st) st = status_of(cudaEventCreateWithFlags(&d->fork_ev, cudaEventDisableTiming));
+    if (!st) st = status_of(cudaEventCreateWithFlags(&d->join_ev, cudaEventDisableTiming));
   }
   if (st) return st;
   const size_t len = (size_t)steps * 32;
@@ -322,7 +355,11 @@ int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
 
 int build(const tbsla_matrix* m, DeviceMatrix* d) {
   const tbsla_info& I = m->info;
-  TRY(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+  // the matrix's own stream at the greatest priority, so that work forked
+  // onto a least-priority side stream only fills its tails
+  int least = 0, greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&least, &greatest);
+  TRY(cudaStreamCreateWithPriority(&d->stream, cudaStreamNonBlocking, greatest));
   switch (m->format) {
     case TBSLA_CSR: {
       if (I.nnz == 0) return TBSLA_OK;
@@ -518,40 +555,79 @@ int dev_bytes(const tbsla_matrix* m, size_t* bytes) {
   return TBSLA_OK;
 }
 
+int dev_launches(const tbsla_matrix* m, int* launches) {
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  int k = 0;
+  if (skips_empty(m))
+    k = 0;
+  else if (m->format == TBSLA_COO || m->format == TBSLA_SCOO)
+    k = d->nnz > 0;
+  else if (m->format != TBSLA_CSR)
+    k = 1;
+  else if (d->algo == 2)
+    for (const SellPlan& p : d->sell) k += p.nslices > 0;
+  else
+    k = d->algo == 1 ? 1 : 2;
+  *launches = k;
+  return TBSLA_OK;
+}
+
 namespace {
-// Host entry point of the sliced-ELL kernel with column blocks: x of block 0
-// goes over on the matrix stream, x of the later blocks on a second stream,
-// and each later block's launch waits only for its own part of x, so those
-// copies run under the earlier blocks' launches (the host link moves about
-// 0.2 TB/s each way; the first block's launch takes longer than the next
-// block's 64 MiB of x).  Results are those of dev_ax's plain path.
+// Host entry point of the sliced-ELL kernel with column blocks.  The host
+// link of a GB300 moves about 0.2 TB/s each way, so the copies are hidden
+// under launches where the data allows:
+// - x of block 0 goes over on the matrix stream, x of the later blocks on a
+//   second stream, and each later launch waits only for its own part of x;
+// - the last block runs in parts by rows; once a part's launch ends its
+//   rows of y are final and go back on the second stream while the next
+//   part runs.
+// Results are those of dev_ax's plain path.
 int ax_host_blocks(const tbsla_matrix* m, DeviceMatrix* d, double* r, const double* v, int vect_incr,
                    bool zero_first) {
-  const size_t nx = in_len(m), ny = out_len(m);
-  const int P = (int)d->sell.size();
+  (void)vect_incr;  // CSR ignores it (MatrixCSR.cpp:209-233)
+  const size_t nx = in_len(m);
+  const int NP = (int)d->sell.size(), parts = d->sell_parts;
   cudaStream_t s = d->stream;
   if (!d->xstream) TRY(cudaStreamCreateWithFlags(&d->xstream, cudaStreamNonBlocking));
-  while ((int)d->xready.size() < P + 1) {
+  // [0, NP): x of plan b has arrived; [NP, 2 NP): plan b launched; 2 NP: start
+  while ((int)d->xready.size() < 2 * NP + 1) {
     cudaEvent_t e = nullptr;
     TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     d->xready.push_back(e);
   }
+  cudaEvent_t* ev = d->xready.data();
   // the copies into d->x start after the matrix stream's earlier work
-  TRY(cudaEventRecord(d->xready[P], s));
-  TRY(cudaStreamWaitEvent(d->xstream, d->xready[P], 0));
-  for (int b = 0; b < P; b++) {
-    const size_t lo = std::min<size_t>((size_t)d->sell[b].col_lo, nx);
-    const size_t hi = b == P - 1 ? nx : std::min<size_t>((size_t)d->sell[b].col_hi, nx);
-    cudaStream_t cs = b == 0 ? s : d->xstream;
-    if (hi > lo) TRY(cudaMemcpyAsync(d->x + lo, v + lo, (hi - lo) * sizeof(double), cudaMemcpyHostToDevice, cs));
-    if (b > 0) TRY(cudaEventRecord(d->xready[b], d->xstream));
+  TRY(cudaEventRecord(ev[2 * NP], s));
+  TRY(cudaStreamWaitEvent(d->xstream, ev[2 * NP], 0));
+  for (int b = 0; b < NP; b++) {
+    const SellPlan& p = d->sell[b];
+    if (b == 0 || p.col_lo != d->sell[b - 1].col_lo) {
+      const size_t lo = std::min<size_t>((size_t)p.col_lo, nx);
+      const size_t hi = p.col_hi == INT_MAX ? nx : std::min<size_t>((size_t)p.col_hi, nx);
+      if (hi > lo)
+        TRY(cudaMemcpyAsync(d->x + lo, v + lo, (hi - lo) * sizeof(double), cudaMemcpyHostToDevice,
+                            b == 0 ? s : d->xstream));
+    }
+    if (b > 0) TRY(cudaEventRecord(ev[b], d->xstream));
   }
-  if (zero_first) TRY(cudaMemsetAsync(d->y, 0, ny * sizeof(double), s));
+  if (zero_first) TRY(cudaMemsetAsync(d->y, 0, out_len(m) * sizeof(double), s));
+  std::vector<cudaEvent_t> after(NP, nullptr);
+  for (int b = NP - parts; b < NP - 1; b++) after[b] = ev[NP + b];
   SellArgs a = sell_args(m, d);
-  a.ready = d->xready.data();
+  a.ready = ev;
+  a.after = after.data();
   TRY(sell_spmv(a, d->x, d->y, d->sell_counter, s));
-  (void)vect_incr;
-  if (ny) TRY(cudaMemcpyAsync(r, d->y, ny * sizeof(double), cudaMemcpyDeviceToHost, s));
+  for (int b = NP - parts; b < NP; b++) {
+    const SellPlan& p = d->sell[b];
+    const size_t n = (size_t)(p.row_hi - p.row_lo);
+    cudaStream_t cs = b < NP - 1 ? d->xstream : s;
+    if (b < NP - 1) TRY(cudaStreamWaitEvent(cs, ev[NP + b], 0));
+    if (n) TRY(cudaMemcpyAsync(r + p.row_lo, d->y + p.row_lo, n * sizeof(double), cudaMemcpyDeviceToHost, cs));
+  }
+  TRY(cudaEventRecord(ev[2 * NP], d->xstream));
+  TRY(cudaStreamWaitEvent(s, ev[2 * NP], 0));
   return status_of(cudaStreamSynchronize(s));
 }
 }  // namespace

@@ -16,6 +16,7 @@ int dev_host_free(void* p);
 
 int dev_upload(const tbsla_matrix* m);
 int dev_bytes(const tbsla_matrix* m, size_t* bytes);
+int dev_launches(const tbsla_matrix* m, int* launches);
 
 // Ax / spmv.  host = true: r and v are host pointers, copied in and out.
 int dev_ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr, bool zero_first,

@@ -84,7 +84,10 @@ struct SellPlan {
   int* lane = nullptr;         // [32 * nslices]: base >= 0: (row - base) << 8 | len;
                                // base = -1: row; -1 for an unused lane
   int* lane_len = nullptr;     // [32 * nwide]: the row's entries in the block
+  int row_lo = 0, row_hi = 0;  // rows the plan may hold (a part of the last block: its rows)
 };
+// Parts by rows of the last column block (when there are several blocks).
+constexpr int kRowParts = 2;
 // Host: plan of one column block from its per-row entry counts L[n]
 // (arrays allocated with new[]); rows with no entry are left out when
 // skip_empty; step offsets start at step0.
@@ -102,16 +105,26 @@ struct SellArgs {
   int unroll;               // steps per lane in flight: 4, 8 or 16
   int nblocks;              // column blocks
   const SellPlan* blocks;   // host array of plans holding device pointers
-  // optional, per block: the launch of block b > 0 waits for ready[b]
-  // (its part of x arriving on another stream)
+  // optional, per plan: the launch of plan b > 0 waits for ready[b] (its
+  // part of x arriving on another stream), and after[b], when not null, is
+  // recorded once plan b is launched
   const cudaEvent_t* ready = nullptr;
+  const cudaEvent_t* after = nullptr;
+  // Row parts: the last `parts` plans split the last column block by rows.
+  // They do not depend on one another, so with a side stream the last part
+  // runs there (forked after the earlier blocks, joined back before
+  // sell_spmv returns) and its CTAs fill the tail of the part before it.
+  int parts = 1;
+  cudaStream_t side = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
 };
 // Fills the slice arrays of every block from the CSR device arrays.
 cudaError_t sell_fill(const SellArgs& a, cudaStream_t s);
-// y = A x, one launch per column block; counter: kSellCounterWords
-// unsigned of zeroed scratch, reset by each launch; a set *done (device)
-// makes the launches no-ops.
-constexpr int kSellCounterWords = 1024;
+// y = A x, one launch per plan; counter: kSellCounterWords unsigned of
+// zeroed scratch (a region per launch that may run at once), reset by each
+// launch; a set *done (device) makes the launches no-ops.
+constexpr int kSellCounterRegion = 1024;
+constexpr int kSellCounterWords = 2 * kSellCounterRegion;
 cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s,
                       const int* done = nullptr);
 

@@ -124,7 +124,7 @@ __device__ __forceinline__ Lane slice_lane(const SellPlan& p, const int4& d, int
 // warp starts on queue (its index mod kQueues) and moves on to the next
 // queue when its own runs dry.  Lane 0 holds the state.
 constexpr int kQueues = 8, kQueueStride = 64;
-static_assert(kQueues * kQueueStride + 1 <= kSellCounterWords, "counter scratch");
+static_assert(kQueues * kQueueStride + 1 <= kSellCounterRegion, "counter scratch");
 struct Claims {
   unsigned* counter;
   int nitems;
@@ -252,16 +252,27 @@ cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* coun
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V, U>, NT, 0);
   const int grid = std::max(1, sms * std::max(1, per));
+  const bool fork = a.side && a.parts > 1 && a.nblocks >= a.parts;
   for (int b = 0; b < a.nblocks; b++) {
     const SellPlan& p = a.blocks[b];
-    if (a.ready && b > 0) {
-      cudaError_t e = cudaStreamWaitEvent(s, a.ready[b], 0);
-      if (e != cudaSuccess) return e;
+    const bool on_side = fork && b == a.nblocks - 1;
+    cudaStream_t ls = on_side ? a.side : s;
+    cudaError_t e = cudaSuccess;
+    if (fork && b == a.nblocks - a.parts) e = cudaEventRecord(a.fork, s);
+    if (e == cudaSuccess && on_side) e = cudaStreamWaitEvent(ls, a.fork, 0);
+    if (e == cudaSuccess && a.ready && b > 0) e = cudaStreamWaitEvent(ls, a.ready[b], 0);
+    if (e == cudaSuccess && p.nslices > 0) {
+      k_sell<V, U><<<grid, NT, 0, ls>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
+                                        counter + (on_side ? kSellCounterRegion : 0), done);
+      e = cudaGetLastError();
     }
-    if (p.nslices == 0) continue;
-    k_sell<V, U><<<grid, NT, 0, s>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
-                                     counter, done);
-    cudaError_t e = cudaGetLastError();
+    // recorded for an empty plan too: the event then marks the earlier plans
+    if (e == cudaSuccess && a.after && a.after[b]) e = cudaEventRecord(a.after[b], ls);
+    if (e != cudaSuccess) return e;
+  }
+  if (fork) {
+    cudaError_t e = cudaEventRecord(a.join, a.side);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, a.join, 0);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;

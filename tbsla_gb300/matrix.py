@@ -116,6 +116,12 @@ class Matrix:
         check(lib.tbsla_matrix_device_bytes(self._h, C.byref(b)), "device_bytes")
         return b.value
 
+    def kernel_launches(self) -> int:
+        """Kernel launches one Ax makes on the device copy."""
+        k = C.c_int()
+        check(lib.tbsla_matrix_kernel_launches(self._h, C.byref(k)), "kernel_launches")
+        return k.value
+
     # ---- SpMV (Matrix.hpp:14-15) --------------------------------------------------------
     def Ax(self, r: np.ndarray, v: np.ndarray, vect_incr: int = 0):
         _f64(r, "r"), _f64(v, "v")

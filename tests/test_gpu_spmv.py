@@ -285,9 +285,10 @@ def test_device_pointer_entry_points(gpu):
 
 def test_host_entry_with_column_blocks_equals_device_entry(gpu):
     """The host entry point copies x of column blocks 1.. on a second
-    stream, under the earlier blocks' launches: the result equals the
-    device-pointer entry point's bit for bit, on repeated calls, for Ax and
-    for spmv, with 2 and with 7 column blocks."""
+    stream under the earlier blocks' launches, and y back part by part as
+    the last block's row parts finish: the result equals the device-pointer
+    entry point's bit for bit, on repeated calls, for Ax and for spmv, with
+    2 and with 7 column blocks."""
     import torch
 
     T = gpu
@@ -306,6 +307,12 @@ def test_host_entry_with_column_blocks_equals_device_entry(gpu):
             m.Ax(y, x)
             assert np.array_equal(y, ref), cb
             assert np.array_equal(m.spmv(x), ref), cb
+    # one launch per plan: 7 column blocks, the last one in two row parts
+    assert m.kernel_launches() == 8
+    m.set_sell_params(64, 64, 16384, 0)
+    assert m.kernel_launches() == 1
+    m.set_algorithm(m.MERGE, 8)
+    assert m.kernel_launches() == 2
 
 
 def test_composite_ops_match_reference(gpu, golden):
