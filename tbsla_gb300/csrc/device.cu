@@ -114,6 +114,8 @@ struct DeviceMatrix {
   size_t y_len = 0;
   double* t = nullptr;
   size_t t_len = 0;
+  double* pr_ctl = nullptr;  // PageRank: coefficients [0, 4) and flags (2 int) at [4]
+  size_t pr_ctl_len = 0;
   // persistent-kernel control and reduction scratch
   unsigned* counter = nullptr;
   double* partials = nullptr;
@@ -123,7 +125,7 @@ struct DeviceMatrix {
   ~DeviceMatrix() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
-    for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t,
+    for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t, (void*)pr_ctl,
                     (void*)counter, (void*)partials, (void*)result, (void*)coord, (void*)carry_row,
                     (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)colw})
       if (p) cudaFree(p);
@@ -919,24 +921,20 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
   if (st) return st;
   const int n = I.n_row;
   cudaStream_t s = d->stream;
-  double *x0 = nullptr, *x1 = nullptr, *coef = nullptr;
-  int* flags = nullptr;  // [0] done, [1] iterations
   // the sliced-ELL kernel (FP64-efficient on skewed rows) with a separate
   // epilogue pass, or the row-block kernel with the epilogue fused
   const bool sell = d->algo == 2;
   int sms = 152;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device);
   int grid = sell ? 8 * sms : (I.nnz > 0 ? csr_pagerank_grid(d->items, d->prec) : 1);
-  auto cleanup = [&]() {
-    for (void* p : {(void*)x0, (void*)x1, (void*)coef, (void*)flags})
-      if (p) cudaFree(p);
-  };
-  if ((st = dalloc(&x0, n)) || (st = dalloc(&x1, n)) || (st = dalloc(&coef, 4)) ||
-      (st = dalloc(&flags, 2)) || (st = d->ctl(3, grid)) || (st = column_weights(m, d)) ||
-      (sell && (st = d->vec(&d->t, &d->t_len, (size_t)n)))) {
-    cleanup();
+  // the two iterates and the control words stay with the device copy, so
+  // repeated solves allocate (and synchronise on frees) nothing
+  if ((st = d->vec(&d->x, &d->x_len, (size_t)n)) || (st = d->vec(&d->y, &d->y_len, (size_t)n)) ||
+      (st = d->vec(&d->pr_ctl, &d->pr_ctl_len, 8)) || (st = d->ctl(3, grid)) || (st = column_weights(m, d)) ||
+      (sell && (st = d->vec(&d->t, &d->t_len, (size_t)n))))
     return st;
-  }
+  double *x0 = d->x, *x1 = d->y, *coef = d->pr_ctl;
+  int* flags = reinterpret_cast<int*>(d->pr_ctl + 4);  // [0] done, [1] iterations
   const double x_init = 1.0 / n;
   double c0[2];
   initial_coefficients(d, beta, c0);
@@ -961,16 +959,11 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
       } else if (I.nnz > 0) {
         e = csr_pagerank_step(a, even ? x0 : x1, even ? x1 : x0, p, ctl, grid, s);
       }
-      if (e != cudaSuccess) {
-        cleanup();
-        return I.nnz > 0 ? status_of(e) : TBSLA_ERR_BAD_MATRIX;
-      }
+      if (e != cudaSuccess) return I.nnz > 0 ? status_of(e) : TBSLA_ERR_BAD_MATRIX;
     }
     if (cudaMemcpyAsync(hflags, flags, 2 * sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess) {
-      cleanup();
+        cudaStreamSynchronize(s) != cudaSuccess)
       return TBSLA_ERR_CUDA;
-    }
   }
   const int iters = hflags[1];
   double* fin = (iters % 2 == 1) ? x1 : x0;
@@ -982,7 +975,6 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
   double herr = 0;
   if (!st) st = status_of(cudaMemcpyAsync(&herr, d->result, 8, cudaMemcpyDeviceToHost, s));
   if (!st) st = status_of(cudaStreamSynchronize(s));
-  cleanup();
   if (st) return st;
   if (iterations) *iterations = iters;
   if (error) *error = herr;

@@ -307,9 +307,18 @@ class MatrixCSR(Matrix):
         check(lib.tbsla_matrix_fill_diffusion7(self._h, n, sigma, corr_len, seed), "fill_diffusion7")
 
     # PageRank / CG
-    def page_rank(self, beta=0.85, epsilon=1e-10, max_iterations=1000):
+    def page_rank(self, beta=0.85, epsilon=1e-10, max_iterations=1000, out: np.ndarray | None = None):
+        """PageRank vector of this column-stochastic matrix.  out: an
+        optional float64 array of n entries that receives the result
+        (repeated solves then reuse one host buffer instead of faulting in
+        a fresh one each call)."""
         n = self.get_n_row()
-        x = np.empty(n)
+        if out is None:
+            x = np.empty(n)
+        else:
+            x = out
+            if x.dtype != np.float64 or x.shape != (n,) or not x.flags.c_contiguous:
+                raise ValueError("out must be a contiguous float64 array of n entries")
         it = C.c_int()
         err = C.c_double()
         st = lib.tbsla_page_rank(self._h, beta, epsilon, max_iterations, _ptr(x), C.byref(it), C.byref(err))

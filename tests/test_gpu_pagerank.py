@@ -42,6 +42,13 @@ def test_make_stochastic_and_pagerank(gpu, prec):
     # the oracle run to convergence stops within one iteration of the GPU
     _, it_conv, _ = oracle.pagerank(a["rowptr"], a["colidx"], vals, 0.85, 1e-10, 500)
     assert abs(it_conv - it) <= 1
+    # repeated solves into one caller buffer: the same vector (the iterates
+    # are kept with the device copy between solves)
+    buf = np.full(n, 7.0)
+    for _ in range(2):
+        y, it2, _, ok2 = g.page_rank(0.85, 1e-10, 500, out=buf)
+        assert y is buf and ok2 and it2 == it
+        assert np.array_equal(buf, x)
 
 
 def test_pagerank_iteration_limit(gpu):
