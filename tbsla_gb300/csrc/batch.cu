@@ -64,6 +64,8 @@ struct tbsla_batch {
   int *lrowptr = nullptr, *lcolidx = nullptr, *trowptr = nullptr, *tcolidx = nullptr;
   void *lvals = nullptr, *tvals = nullptr;
   int lprec = TBSLA_F64;
+  short *ldelta = nullptr, *tdelta = nullptr;  // ELL form (lslots > 0)
+  int lslots = 0, tslots = 0;
   float *rf = nullptr, *tf = nullptr;
   double *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
   double* scal = nullptr;
@@ -77,7 +79,8 @@ struct tbsla_batch {
     if (stream) cudaStreamSynchronize(stream);
     if (graph) cudaGraphExecDestroy(graph);
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
-                  scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf};
+                  scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf,
+                  ldelta, tdelta};
     for (void* v : ps)
       if (v) cudaFree(v);
     if (vals && vals != vals64) cudaFree(vals);
@@ -110,6 +113,10 @@ struct tbsla_batch {
     c.lvals = f ? lvals : nullptr;
     c.tvals = f ? tvals : nullptr;
     c.lprec = lprec;
+    c.ldelta = f ? ldelta : nullptr;
+    c.tdelta = f ? tdelta : nullptr;
+    c.lslots = f ? lslots : 0;
+    c.tslots = f ? tslots : 0;
     c.rf = f ? rf : nullptr;
     c.tf = f ? tf : nullptr;
     c.b = b;
@@ -311,34 +318,79 @@ int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int ns
       tci[q] = (int)i;
       tva[q] = va[k];
     }
+  // ELL form of L and of L^T when every row has at most 8 entries, every
+  // column lies within 32767 of its row and the padding stays under half
+  // the entries (stencil-pattern factors: 4 entries per row)
+  std::vector<short> ld, td;
+  std::vector<double> lv, tv;
+  auto ell = [&](const std::vector<int>& r, const std::vector<int>& c, const std::vector<double>& v, int* slots,
+                 std::vector<short>& d, std::vector<double>& e) {
+    const long n = B->n;
+    int K = 0;
+    for (long i = 0; i < n; i++) K = std::max(K, r[i + 1] - r[i]);
+    if (K == 0 || K > 8 || (long)K * n > nl + nl / 2) return false;
+    d.assign((size_t)K * n, 0);
+    e.assign((size_t)K * n, 0.0);
+    for (long i = 0; i < n; i++)
+      for (int j = r[i]; j < r[i + 1]; j++) {
+        const long delta = (long)c[j] - i;
+        if (delta < -32767 || delta > 32767) return false;
+        const size_t o = (size_t)(j - r[i]) * n + i;
+        d[o] = (short)delta;
+        e[o] = v[j];
+      }
+    *slots = K;
+    return true;
+  };
+  int lk = 0, tk = 0;
+  const bool use_ell = nl > 0 && ell(rp, ci, va, &lk, ld, lv) && ell(trp, tci, tva, &tk, td, tv);
   cudaSetDevice(B->device);
   cudaStream_t st = B->stream;
   for (void* p : {(void*)B->lrowptr, (void*)B->lcolidx, (void*)B->trowptr, (void*)B->tcolidx, B->lvals, B->tvals,
-                  (void*)B->rf, (void*)B->tf})
+                  (void*)B->rf, (void*)B->tf, (void*)B->ldelta, (void*)B->tdelta})
     if (p) cudaFree(p);
   B->lrowptr = B->lcolidx = B->trowptr = B->tcolidx = nullptr;
   B->lvals = B->tvals = nullptr;
   B->rf = B->tf = nullptr;
+  B->ldelta = B->tdelta = nullptr;
+  B->lslots = B->tslots = 0;
   double* tmp = nullptr;
   const size_t es = precision == TBSLA_F64 ? 8 : precision == TBSLA_F32 ? 4 : 2;
   B->lprec = precision;
-  CK(alloc(&B->lrowptr, rp.size()));
-  CK(alloc(&B->lcolidx, std::max<size_t>(ci.size(), 1)));
-  CK(alloc(&B->trowptr, trp.size()));
-  CK(alloc(&B->tcolidx, std::max<size_t>(tci.size(), 1)));
   CK(alloc(&B->rf, B->n));
   CK(alloc(&B->tf, B->n));
-  CK(cudaMalloc(&B->lvals, std::max<size_t>(nl, 1) * es));
-  CK(cudaMalloc(&B->tvals, std::max<size_t>(nl, 1) * es));
-  CK(alloc(&tmp, std::max<size_t>(nl, 1) * 2));
-  CK(cudaMemcpyAsync(B->lrowptr, rp.data(), rp.size() * 4, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(B->lcolidx, ci.data(), ci.size() * 4, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(B->trowptr, trp.data(), trp.size() * 4, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(B->tcolidx, tci.data(), tci.size() * 4, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(tmp, va.data(), nl * 8, cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(tmp + nl, tva.data(), nl * 8, cudaMemcpyHostToDevice, st));
-  CK(convert_values(tmp, B->lvals, precision, nl, st));
-  CK(convert_values(tmp + nl, B->tvals, precision, nl, st));
+  if (use_ell) {
+    const size_t nle = lv.size(), nte = tv.size();
+    CK(alloc(&B->ldelta, nle));
+    CK(alloc(&B->tdelta, nte));
+    CK(cudaMalloc(&B->lvals, nle * es));
+    CK(cudaMalloc(&B->tvals, nte * es));
+    CK(alloc(&tmp, nle + nte));
+    CK(cudaMemcpyAsync(B->ldelta, ld.data(), nle * 2, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B->tdelta, td.data(), nte * 2, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tmp, lv.data(), nle * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tmp + nle, tv.data(), nte * 8, cudaMemcpyHostToDevice, st));
+    CK(convert_values(tmp, B->lvals, precision, (long)nle, st));
+    CK(convert_values(tmp + nle, B->tvals, precision, (long)nte, st));
+    B->lslots = lk;
+    B->tslots = tk;
+  } else {
+    CK(alloc(&B->lrowptr, rp.size()));
+    CK(alloc(&B->lcolidx, std::max<size_t>(ci.size(), 1)));
+    CK(alloc(&B->trowptr, trp.size()));
+    CK(alloc(&B->tcolidx, std::max<size_t>(tci.size(), 1)));
+    CK(cudaMalloc(&B->lvals, std::max<size_t>(nl, 1) * es));
+    CK(cudaMalloc(&B->tvals, std::max<size_t>(nl, 1) * es));
+    CK(alloc(&tmp, std::max<size_t>(nl, 1) * 2));
+    CK(cudaMemcpyAsync(B->lrowptr, rp.data(), rp.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B->lcolidx, ci.data(), ci.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B->trowptr, trp.data(), trp.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B->tcolidx, tci.data(), tci.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tmp, va.data(), nl * 8, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(tmp + nl, tva.data(), nl * 8, cudaMemcpyHostToDevice, st));
+    CK(convert_values(tmp, B->lvals, precision, nl, st));
+    CK(convert_values(tmp + nl, B->tvals, precision, nl, st));
+  }
   CK(cudaStreamSynchronize(st));
   cudaFree(tmp);
   if (B->graph_pre == 2) B->graph_pre = -1;  // recapture with the new arrays
@@ -355,7 +407,7 @@ int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets) {
 int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterations, double rel_tol,
                    int precond, int refresh, int graph_iters, int* iterations, double* rel_residual) {
   if (!B || !rhs || !x || max_iterations < 0 || rel_tol < 0 || precond < 0 || precond > 2 || refresh < 0 ||
-      (precond == 2 && !B->lrowptr))
+      (precond == 2 && !B->rf))
     return TBSLA_ERR_INVALID_ARG;
   cudaSetDevice(B->device);
   const int K = graph_iters > 0 ? graph_iters : 10;

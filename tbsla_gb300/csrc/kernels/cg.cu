@@ -76,14 +76,14 @@ __global__ void __launch_bounds__(NT) k_cg_residual(CgBatch c, int mask) {
   if (!((mask >> c.status[sys]) & 1)) return;
   const uint64_t pol = policy_evict_first();
   CsrArgs a{c.vals64, kF64, c.rowptr, c.colidx, c.blocks, c.nblocks, 0, c.items};
-  EpiResidual epi{c.b, c.r, c.dinv ? c.z : nullptr, c.dinv, c.lrowptr ? c.rf : nullptr};
+  EpiResidual epi{c.b, c.r, c.dinv ? c.z : nullptr, c.dinv, c.rf};
   double red[2] = {0, 0};
   csr_block<double, ITEMS>(a, b, c.x, epi, red, stage, sm, pol);
   const double rr = block_sum<NT>(red[0], sm.red);
   const double rz = block_sum<NT>(red[1], sm.red);
   if (threadIdx.x == 0) {
     atomicAdd(c.rrt + sys, rr);
-    if (!c.lrowptr) atomicAdd(c.rz + sys, rz);  // factored: r.z comes with z
+    if (!c.rf) atomicAdd(c.rz + sys, rz);  // factored: r.z comes with z
   }
 }
 
@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(NT) k_cg_update(CgBatch c) {
       zi = c.dinv[i] * ri;
       c.z[i] = zi;
     }
-    if (!c.lrowptr) rz = fma_rn(ri, zi, rz);  // factored: r.z comes with z
+    if (!c.rf) rz = fma_rn(ri, zi, rz);  // factored: r.z comes with z
     else c.rf[i] = (float)ri;
     rr = fma_rn(ri, ri, rr);
   }
@@ -220,6 +220,53 @@ __global__ void __launch_bounds__(NT) k_cg_factor_l(CgBatch c, int mask, double*
   if (threadIdx.x == 0) atomicAdd(acc + sys, d);
 }
 
+// The same two passes over the ELL form: slot k of row i is its k-th entry
+// (same FP32 operations in the same order as the CSR passes; a padded slot
+// adds 0 * x[i]).  No row pointer, 2-byte column offsets, every load of a
+// slot coalesced.  One row per thread at a time keeps the registers low and
+// the SM full of rows in flight, which is what hides the dependent gathers.
+template <class V>
+__global__ void __launch_bounds__(NT) k_cg_factor_t_ell(CgBatch c, int mask) {
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  if (!((mask >> c.status[sys]) & 1)) return;
+  const V* v = static_cast<const V*>(c.tvals);
+  const long n = c.n;
+  const int K = c.tslots, r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+    float s = 0.f;
+    for (int k = 0; k < K; k++) {
+      const long o = k * n + i;
+      s = fmaf(to_f32(v[o]), c.rf[i + c.tdelta[o]], s);
+    }
+    c.tf[i] = s;
+  }
+}
+
+template <class V>
+__global__ void __launch_bounds__(NT) k_cg_factor_l_ell(CgBatch c, int mask, double* acc) {
+  __shared__ double red_s[NT / kWarp];
+  const int ch = blockIdx.x;
+  const int sys = c.chunk_sys[ch];
+  if (!((mask >> c.status[sys]) & 1)) return;
+  const V* v = static_cast<const V*>(c.lvals);
+  const long n = c.n;
+  const int K = c.lslots, r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+  double d = 0;
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) {
+    float s = 0.f;
+    for (int k = 0; k < K; k++) {
+      const long o = k * n + i;
+      s = fmaf(to_f32(v[o]), c.tf[i + c.ldelta[o]], s);
+    }
+    const double zi = widen(s);
+    c.z[i] = zi;
+    d = fma_rn(c.r[i], zi, d);
+  }
+  d = block_sum<NT>(d, red_s);
+  if (threadIdx.x == 0) atomicAdd(acc + sys, d);
+}
+
 __global__ void k_cg_activate(CgBatch c) {
   for (int s = threadIdx.x; s < c.nsys; s += blockDim.x)
     if (c.status[s] == kRestart) c.status[s] = kActive;
@@ -310,7 +357,7 @@ cudaError_t cg_true_residual(const CgBatch& c, int mask, bool init, cudaStream_t
     e = c.items == 4 ? launch_res<4>(c, mask, s) : launch_res<8>(c, mask, s);
     if (e != cudaSuccess) return e;
   }
-  if (c.lrowptr) {  // z = L L^T r, rz = r.z of the masked systems
+  if (c.rf) {  // z = L L^T r, rz = r.z of the masked systems
     e = cg_factor_apply(c, mask, c.rz, s);
     if (e != cudaSuccess) return e;
   }
@@ -326,13 +373,18 @@ cudaError_t cg_restart(const CgBatch& c, bool all, cudaStream_t s) {
 
 template <class V>
 cudaError_t factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s) {
-  k_cg_factor_t<V><<<c.nchunks, NT, 0, s>>>(c, mask);
-  k_cg_factor_l<V><<<c.nchunks, NT, 0, s>>>(c, mask, acc);
+  if (c.lslots > 0) {
+    k_cg_factor_t_ell<V><<<c.nchunks, NT, 0, s>>>(c, mask);
+    k_cg_factor_l_ell<V><<<c.nchunks, NT, 0, s>>>(c, mask, acc);
+  } else {
+    k_cg_factor_t<V><<<c.nchunks, NT, 0, s>>>(c, mask);
+    k_cg_factor_l<V><<<c.nchunks, NT, 0, s>>>(c, mask, acc);
+  }
   return cudaGetLastError();
 }
 
 cudaError_t cg_factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s) {
-  if (!c.lrowptr || c.nchunks == 0) return cudaSuccess;
+  if (!c.rf || c.nchunks == 0) return cudaSuccess;
   switch (c.lprec) {
     case kF64: return factor_apply<double>(c, mask, acc, s);
     case kF32: return factor_apply<float>(c, mask, acc, s);

@@ -200,7 +200,12 @@ struct CgBatch {
   const int *lrowptr, *lcolidx, *trowptr, *tcolidx;
   const void *lvals, *tvals;
   int lprec;
-  float *rf, *tf;
+  // ELL form of L and L^T (lslots > 0; then no CSR arrays): slot-major
+  // values [slot * n + i] and column offsets from the row as int16, padded
+  // with value 0 at offset 0
+  const short *ldelta, *tdelta;
+  int lslots, tslots;
+  float *rf, *tf;  // set for a factored run
   const double* b;
   double *x, *r, *z, *p, *q;  // z == r when unpreconditioned
   // per-system scalars (rrt: squared FP64 true residual of the last check)

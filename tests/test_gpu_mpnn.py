@@ -109,3 +109,42 @@ def test_factored_pcg_converges_and_training_beats_jacobi(gpu):
     # bfloat16 factor storage: still SPD, still converges to the FP64 bar
     its_b = _solve(T, held, factors, 2, T.BF16)
     assert its_b.mean() < its_j.mean(), (its_b, its_j)
+
+
+def test_factor_layouts_agree(gpu):
+    """Factors of at most 8 entries per row are applied from an ELL copy
+    (2-byte column offsets, no row pointer), longer ones from CSR.  The same
+    factor padded with explicit zeros past 8 entries per row takes the CSR
+    path: the same preconditioner (a zero product leaves an FP32 sum
+    unchanged), so both solves reach the FP64-verified 1e-8 residual in the
+    same number of iterations, to within the one that the order of the FP64
+    atomic dot products can move."""
+    T = gpu
+    systems = [diffusion(T, 11 + i, 60 + i) for i in range(3)]
+    short, padded = [], []
+    for A in systems:
+        a = A.arrays()
+        n = len(a["rowptr"]) - 1
+        rp, ci, va = [0], [], []
+        rp9, ci9, va9 = [0], [], []
+        for i in range(n):
+            cols = a["colidx"][a["rowptr"][i]:a["rowptr"][i + 1]]
+            vals = a["values"][a["rowptr"][i]:a["rowptr"][i + 1]]
+            d = vals[cols == i][0]
+            row = {int(c): (-0.1 * v / d if c != i else 1 / np.sqrt(d)) for c, v in zip(cols, vals) if c <= i}
+            for c in sorted(row):
+                ci.append(c)
+                va.append(row[c])
+            rp.append(len(ci))
+            for c in range(max(0, i - 7), i):
+                row.setdefault(c, 0.0)
+            for c in sorted(row):
+                ci9.append(c)
+                va9.append(row[c])
+            rp9.append(len(ci9))
+        short.append(T.MatrixCSR.from_arrays(n, n, np.array(rp, np.int32), np.array(ci, np.int32), np.array(va)))
+        padded.append(T.MatrixCSR.from_arrays(n, n, np.array(rp9, np.int32), np.array(ci9, np.int32),
+                                              np.array(va9)))
+    its_short = _solve(T, systems, short, 2, T.F32)
+    its_padded = _solve(T, systems, padded, 2, T.F32)
+    assert np.abs(np.asarray(its_short) - np.asarray(its_padded)).max() <= 1
