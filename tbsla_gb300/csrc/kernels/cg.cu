@@ -223,43 +223,52 @@ __global__ void __launch_bounds__(NT) k_cg_factor_l(CgBatch c, int mask, double*
 // The same two passes over the ELL form: slot k of row i is its k-th entry
 // (same FP32 operations in the same order as the CSR passes; a padded slot
 // adds 0 * x[i]).  No row pointer, 2-byte column offsets, every load of a
-// slot coalesced.  One row per thread at a time keeps the registers low and
-// the SM full of rows in flight, which is what hides the dependent gathers.
-template <class V>
+// slot coalesced.  The slots are unrolled up to KMAX (4, or 8 for longer
+// rows), so a row's offset and value loads go out together and then its
+// gathers: two memory latencies per row instead of two per slot.  One row
+// per thread at a time keeps the registers low and the SM full of rows.
+template <class V, int KMAX>
+__device__ __forceinline__ float ell_row(const V* __restrict__ v, const short* __restrict__ dl,
+                                         const float* __restrict__ x, long n, int K, int i) {
+  short d[KMAX];
+  V a[KMAX];
+#pragma unroll
+  for (int k = 0; k < KMAX; k++) {
+    const long o = k * n + i;
+    d[k] = k < K ? dl[o] : (short)0;
+    a[k] = k < K ? v[o] : V(0.0f);
+  }
+  float g[KMAX];
+#pragma unroll
+  for (int k = 0; k < KMAX; k++) g[k] = k < K ? x[i + d[k]] : 0.f;
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < KMAX; k++)
+    if (k < K) s = fmaf(to_f32(a[k]), g[k], s);
+  return s;
+}
+
+template <class V, int KMAX>
 __global__ void __launch_bounds__(NT) k_cg_factor_t_ell(CgBatch c, int mask) {
   const int ch = blockIdx.x;
   const int sys = c.chunk_sys[ch];
   if (!((mask >> c.status[sys]) & 1)) return;
-  const V* v = static_cast<const V*>(c.tvals);
-  const long n = c.n;
+  const V* __restrict__ v = static_cast<const V*>(c.tvals);
   const int K = c.tslots, r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
-  for (int i = r0 + threadIdx.x; i < r1; i += NT) {
-    float s = 0.f;
-    for (int k = 0; k < K; k++) {
-      const long o = k * n + i;
-      s = fmaf(to_f32(v[o]), c.rf[i + c.tdelta[o]], s);
-    }
-    c.tf[i] = s;
-  }
+  for (int i = r0 + threadIdx.x; i < r1; i += NT) c.tf[i] = ell_row<V, KMAX>(v, c.tdelta, c.rf, c.n, K, i);
 }
 
-template <class V>
+template <class V, int KMAX>
 __global__ void __launch_bounds__(NT) k_cg_factor_l_ell(CgBatch c, int mask, double* acc) {
   __shared__ double red_s[NT / kWarp];
   const int ch = blockIdx.x;
   const int sys = c.chunk_sys[ch];
   if (!((mask >> c.status[sys]) & 1)) return;
-  const V* v = static_cast<const V*>(c.lvals);
-  const long n = c.n;
+  const V* __restrict__ v = static_cast<const V*>(c.lvals);
   const int K = c.lslots, r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
   double d = 0;
   for (int i = r0 + threadIdx.x; i < r1; i += NT) {
-    float s = 0.f;
-    for (int k = 0; k < K; k++) {
-      const long o = k * n + i;
-      s = fmaf(to_f32(v[o]), c.tf[i + c.ldelta[o]], s);
-    }
-    const double zi = widen(s);
+    const double zi = widen(ell_row<V, KMAX>(v, c.ldelta, c.tf, c.n, K, i));
     c.z[i] = zi;
     d = fma_rn(c.r[i], zi, d);
   }
@@ -373,9 +382,12 @@ cudaError_t cg_restart(const CgBatch& c, bool all, cudaStream_t s) {
 
 template <class V>
 cudaError_t factor_apply(const CgBatch& c, int mask, double* acc, cudaStream_t s) {
-  if (c.lslots > 0) {
-    k_cg_factor_t_ell<V><<<c.nchunks, NT, 0, s>>>(c, mask);
-    k_cg_factor_l_ell<V><<<c.nchunks, NT, 0, s>>>(c, mask, acc);
+  if (c.lslots > 0 && c.lslots <= 4 && c.tslots <= 4) {
+    k_cg_factor_t_ell<V, 4><<<c.nchunks, NT, 0, s>>>(c, mask);
+    k_cg_factor_l_ell<V, 4><<<c.nchunks, NT, 0, s>>>(c, mask, acc);
+  } else if (c.lslots > 0) {
+    k_cg_factor_t_ell<V, 8><<<c.nchunks, NT, 0, s>>>(c, mask);
+    k_cg_factor_l_ell<V, 8><<<c.nchunks, NT, 0, s>>>(c, mask, acc);
   } else {
     k_cg_factor_t<V><<<c.nchunks, NT, 0, s>>>(c, mask);
     k_cg_factor_l<V><<<c.nchunks, NT, 0, s>>>(c, mask, acc);

@@ -113,38 +113,34 @@ def test_factored_pcg_converges_and_training_beats_jacobi(gpu):
 
 def test_factor_layouts_agree(gpu):
     """Factors of at most 8 entries per row are applied from an ELL copy
-    (2-byte column offsets, no row pointer), longer ones from CSR.  The same
-    factor padded with explicit zeros past 8 entries per row takes the CSR
-    path: the same preconditioner (a zero product leaves an FP32 sum
+    (2-byte column offsets, no row pointer; kernels unrolled for 4 or 8
+    slots), longer ones from CSR.  The same factor padded with explicit
+    zeros to 6 and to 11 entries per row takes the 8-slot ELL and the CSR
+    paths: the same preconditioner (a zero product leaves an FP32 sum
     unchanged), so both solves reach the FP64-verified 1e-8 residual in the
     same number of iterations, to within the one that the order of the FP64
     atomic dot products can move."""
     T = gpu
     systems = [diffusion(T, 11 + i, 60 + i) for i in range(3)]
-    short, padded = [], []
+    # zeros added at the columns i - z, 0 < z <= pad: none (ELL, 4 slots),
+    # 2 (ELL, up to 6 slots), 7 (CSR, up to 11 entries per row)
+    layouts = {0: [], 2: [], 7: []}
     for A in systems:
         a = A.arrays()
         n = len(a["rowptr"]) - 1
-        rp, ci, va = [0], [], []
-        rp9, ci9, va9 = [0], [], []
-        for i in range(n):
-            cols = a["colidx"][a["rowptr"][i]:a["rowptr"][i + 1]]
-            vals = a["values"][a["rowptr"][i]:a["rowptr"][i + 1]]
-            d = vals[cols == i][0]
-            row = {int(c): (-0.1 * v / d if c != i else 1 / np.sqrt(d)) for c, v in zip(cols, vals) if c <= i}
-            for c in sorted(row):
-                ci.append(c)
-                va.append(row[c])
-            rp.append(len(ci))
-            for c in range(max(0, i - 7), i):
-                row.setdefault(c, 0.0)
-            for c in sorted(row):
-                ci9.append(c)
-                va9.append(row[c])
-            rp9.append(len(ci9))
-        short.append(T.MatrixCSR.from_arrays(n, n, np.array(rp, np.int32), np.array(ci, np.int32), np.array(va)))
-        padded.append(T.MatrixCSR.from_arrays(n, n, np.array(rp9, np.int32), np.array(ci9, np.int32),
-                                              np.array(va9)))
-    its_short = _solve(T, systems, short, 2, T.F32)
-    its_padded = _solve(T, systems, padded, 2, T.F32)
-    assert np.abs(np.asarray(its_short) - np.asarray(its_padded)).max() <= 1
+        for pad, out in layouts.items():
+            rp, ci, va = [0], [], []
+            for i in range(n):
+                cols = a["colidx"][a["rowptr"][i]:a["rowptr"][i + 1]]
+                vals = a["values"][a["rowptr"][i]:a["rowptr"][i + 1]]
+                d = vals[cols == i][0]
+                row = {int(c): (-0.1 * v / d if c != i else 1 / np.sqrt(d)) for c, v in zip(cols, vals) if c <= i}
+                for c in range(max(0, i - pad), i):
+                    row.setdefault(c, 0.0)
+                for c in sorted(row):
+                    ci.append(c)
+                    va.append(row[c])
+                rp.append(len(ci))
+            out.append(T.MatrixCSR.from_arrays(n, n, np.array(rp, np.int32), np.array(ci, np.int32), np.array(va)))
+    its = [np.asarray(_solve(T, systems, f, 2, T.F32)) for f in layouts.values()]
+    assert max(np.abs(its[0] - i).max() for i in its[1:]) <= 1
