@@ -315,6 +315,42 @@ def test_host_entry_with_column_blocks_equals_device_entry(gpu):
     assert m.kernel_launches() == 2
 
 
+def test_column_blocks_with_empty_parts(gpu):
+    """Column blocks whose last block has entries only in the first half of
+    the rows (its second row part is empty), or none at all: host and device
+    entry points still equal the oracle, on repeated calls."""
+    import torch
+
+    T = gpu
+    n = 50_000
+    rng = np.random.default_rng(17)
+    for case in ("upper-half", "none"):
+        rows, cols = [], []
+        for i in range(n):
+            k = int(rng.integers(1, 9))
+            hi = n if (case == "upper-half" and i < n // 2) else 30_000
+            c = np.unique(rng.integers(0, hi, k))
+            rows += [i] * len(c)
+            cols += list(c)
+        rows = np.array(rows)
+        rp = np.concatenate([[0], np.cumsum(np.bincount(rows, minlength=n))]).astype(np.int32)
+        ci = np.array(cols, np.int32)
+        va = rng.uniform(-1, 1, len(ci))
+        m = T.MatrixCSR.from_arrays(n, n, rp, ci, va)
+        m.set_sell_params(64, 64, 16384, 40_000)  # blocks [0, 40000), [40000, n)
+        x = rng.uniform(0, 1, n)
+        ref = oracle.csr_ax(rp, ci, va, x)
+        scale = oracle.csr_absrow(rp, ci, va, x)
+        for _ in range(2):
+            y = np.full(n, 3.0)
+            m.Ax(y, x)
+            assert oracle.rel_err_normalized(y, ref, scale) <= TOL, case
+        yt = torch.full((n,), 3.0, dtype=torch.float64, device="cuda")
+        m.Ax_device(yt, torch.from_numpy(x).cuda())
+        torch.cuda.synchronize()
+        assert np.array_equal(yt.cpu().numpy(), y), case
+
+
 def test_composite_ops_match_reference(gpu, golden):
     T = gpu
     ops = golden["ops"]
