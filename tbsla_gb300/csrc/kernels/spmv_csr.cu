@@ -149,6 +149,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
   const bool active = lane < nvec;
   const double sc = active ? p.coef_in[lane] : 0.0;        // 1 / sum of the vector
   const double tc = active ? p.coef_in[kWarp + lane] : 0.0;  // teleport weight
+  const double bsc = mul_rn(p.beta, sc);
   double err = 0, sum = 0, dsum = 0;  // L1 change, sum y, sum w y
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm)) {
     const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
@@ -186,10 +187,12 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
       }
       if (active) {
         const size_t o = (size_t)row * nvec + lane;
-        const double yn = add_rn(mul_rn(mul_rn(p.beta, acc), sc), mul_rn(tc, T[o]));
-        err = add_rn(err, fabs(yn - mul_rn(X[o], sc)));
+        // the single-vector epilogue's operations (EpiPageRank), per column:
+        // six FP64 instructions per row and vector
+        const double yn = fma_rn(bsc, acc, mul_rn(tc, T[o]));
+        err = add_rn(err, fabs(fma_rn(-X[o], sc, yn)));
         sum = add_rn(sum, yn);
-        dsum = add_rn(dsum, mul_rn(p.colw[row], yn));
+        dsum = fma_rn(p.colw[row], yn, dsum);
         Y[o] = yn;
       }
     }
