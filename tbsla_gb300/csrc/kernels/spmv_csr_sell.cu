@@ -68,13 +68,42 @@ __device__ __forceinline__ double steps_k(const V* __restrict__ sv, const int* _
 
 // Sum of one lane's `steps` entries of a slice `width` steps wide (width is
 // warp-uniform, so every branch below is too and no DFMA is issued past it).
+// With FP64 values, full groups of U steps are software-pipelined on the
+// column stream: the next group's column indices are loaded while the
+// current group's gathers are in flight, so a group waits for one memory
+// latency (the gathers), not for two (the columns, then the gathers).  It
+// costs 9 registers (FP64: 71 -> 80, still 3 CTAs per SM; FP32 values would
+// drop from 4 CTAs per SM to 3, which loses more than the overlap gains).
 template <class V, int U>
 __device__ __forceinline__ double slice_rows(const V* __restrict__ sv, const int* __restrict__ sc, long off,
                                              int steps, int width, const double* __restrict__ x, int f_col,
                                              uint64_t pol) {
   double acc = 0;
   int j = 0;
-  for (; j + U <= width; j += U) acc = steps_k<V, U>(sv, sc, off, j, steps, x, f_col, pol, acc);
+  if (sizeof(V) != 8) {
+    for (; j + U <= width; j += U) acc = steps_k<V, U>(sv, sc, off, j, steps, x, f_col, pol, acc);
+  } else if (U <= width) {
+    int cn[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) cn[u] = u < steps ? ld_stream(sc + off + (long)u * 32, pol) : f_col;
+    for (; j + U <= width; j += U) {
+      V v[U];
+      double xv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const bool live = j + u < steps;
+        xv[u] = live ? ld_gather(x + cn[u] - f_col) : 0.0;
+        v[u] = live ? ld_stream(sv + off + (long)(j + u) * 32, pol) : V(0.0f);
+      }
+      const bool more = j + 2 * U <= width;
+#pragma unroll
+      for (int u = 0; u < U; u++)
+        cn[u] = (more && j + U + u < steps) ? ld_stream(sc + off + (long)(j + U + u) * 32, pol) : f_col;
+      __syncwarp();
+#pragma unroll
+      for (int u = 0; u < U; u++) acc = fma_rn(widen(v[u]), xv[u], acc);
+    }
+  }
   // remainder (< U steps) in binary pieces
   if (U > 8 && j + 8 <= width) {
     acc = steps_k<V, 8>(sv, sc, off, j, steps, x, f_col, pol, acc);
