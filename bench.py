@@ -45,8 +45,9 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["spmv", "pagerank", "cg", "learned"], default="spmv",
-                   help="spmv: the large-SpMV headline; pagerank: the PageRank graph; cg: batched CG; "
+    p.add_argument("--workload", choices=["spmv", "small", "pagerank", "cg", "learned"], default="spmv",
+                   help="spmv: the large-SpMV headline; small: the 10^4-row matrix in every format and the "
+                        "2000^2 DENSE GEMV; pagerank: the PageRank graph; cg: batched CG; "
                         "learned: learned-preconditioner PCG against Jacobi-PCG")
     p.add_argument("--train-systems", type=int, default=2000, help="learned: training systems (seeds 1000..)")
     p.add_argument("--epochs", type=int, default=1, help="learned: passes over the training systems")
@@ -424,6 +425,128 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+def run_small(a):
+    """The reference's CPU-runnable workload: n = 10^4 rows, column i plus 9
+    uniform columns per row, U[-1,1) values, x U[0,1), seed 0, as COO, SCOO,
+    CSR and ELL, and a 2000 x 2000 DENSE GEMV; 100 Ax per format as in the
+    reference perf app (tbsla_perf.cpp:101-106).  Everything fits L2, so the
+    time is launch and latency: per format, device microseconds per Ax over
+    100 back-to-back launches on one stream and over the same 100 launches
+    replayed from a CUDA graph (CUDA events), and per host call through
+    tbsla_Ax with pinned buffers (x in, y out, synchronised).  CPU baseline:
+    the oracle's restatement of each format's loop, one host thread."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import oracle
+    import tbsla_gb300 as T
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    T.device_init(local)
+    n, reps = 10_000, 100
+    csr = T.MatrixCSR()
+    csr.fill_uniform_rows(n, 10, 0)
+    a0 = csr.arrays()
+    nnz = int(a0["rowptr"][-1])
+    x = T.fill_uniform(n, 0.0, 1.0, 0)
+    rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(a0["rowptr"]))
+    coo = T.MatrixCOO.from_arrays(n, n, rows, a0["colidx"], a0["values"])
+    ell = T.MatrixELL(coo)
+    dense = T.MatrixDENSE()
+    dense.fill_dense_uniform(2000, 2000, 0)
+    xd = T.fill_uniform(2000, 0.0, 1.0, 0)
+    max_col = ell.info()["max_col"]
+    # algorithmic bytes per Ax (values, indices, x once, y)
+    cases = {"COO": (coo, x, nnz * 16 + 16 * n), "SCOO": (T.MatrixSCOO(coo), x, nnz * 16 + 16 * n),
+             "CSR": (csr, x, nnz * 12 + 4 * (n + 1) + 16 * n), "ELL": (ell, x, n * max_col * 12 + 16 * n),
+             "DENSE": (dense, xd, 8 * 2000 * 2000 + 16 * 2000)}
+    ae = ell.arrays()
+    ad = dense.arrays()
+    cpu = {"COO": lambda: oracle.coo_ax(n, rows, a0["colidx"], a0["values"], x),
+           "SCOO": lambda: oracle.scoo_ax(n, 0, 0, rows, a0["colidx"], a0["values"], x),
+           "CSR": lambda: oracle.csr_ax(a0["rowptr"], a0["colidx"], a0["values"], x),
+           "ELL": lambda: oracle.ell_ax(ae["values"], ae["columns"], n, max_col, x),
+           "DENSE": lambda: oracle.dense_ax(ad["values"], 2000, 2000, xd)}
+    s = torch.cuda.Stream()
+    out = {}
+    launches = 0
+    clk = Clocks(local)
+    clk.start()
+    for name, (m, xv, B) in cases.items():
+        m.upload()
+        nr = m.info()["ln_row"] if name != "COO" else m.info()["n_row"]
+        xt = torch.from_numpy(xv).cuda()
+        yt = torch.zeros(nr, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            for _ in range(a.warmup):
+                m.Ax_device(yt, xt, stream=s)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(reps):
+                m.Ax_device(yt, xt, stream=s)
+            e1.record(s)
+        s.synchronize()
+        stream_us = e0.elapsed_time(e1) * 1e3 / reps
+        launches += reps * m.kernel_launches()
+        graph_us = None
+        try:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=s):
+                for _ in range(reps):
+                    m.Ax_device(yt, xt, stream=s)
+            g.replay()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(s):
+                e0.record(s)
+                g.replay()
+                e1.record(s)
+            s.synchronize()
+            graph_us = e0.elapsed_time(e1) * 1e3 / reps
+        except RuntimeError as err:  # a capture the library refused: report it
+            graph_us = f"not captured: {err}"[:120]
+        hx, hy = C.c_void_p(), C.c_void_p()
+        T.check(T.lib.tbsla_host_alloc(C.byref(hx), len(xv) * 8))
+        T.check(T.lib.tbsla_host_alloc(C.byref(hy), nr * 8))
+        np.ctypeslib.as_array(C.cast(hx, C.POINTER(C.c_double)), shape=(len(xv),))[:] = xv
+        for _ in range(a.warmup):
+            T.check(T.lib.tbsla_Ax(m._h, hy, hx, 0))
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            T.check(T.lib.tbsla_Ax(m._h, hy, hx, 0))
+        host_us = (time.perf_counter() - t0) * 1e6 / reps
+        T.lib.tbsla_host_free(hx)
+        T.lib.tbsla_host_free(hy)
+        t0 = time.perf_counter()
+        for _ in range(10):
+            cpu[name]()
+        cpu_us = (time.perf_counter() - t0) * 1e6 / 10
+        out[name] = {"device_us": stream_us, "graph_us": graph_us, "host_call_us": host_us,
+                     "GB/s_device": B / (stream_us * 1e-6) / 1e9, "bytes_per_ax": B, "cpu_oracle_us": cpu_us}
+    clocks = clk.stop()
+    csr_us = out["CSR"]["device_us"]
+    line = {
+        "metric": "SpMV time per Ax, 10^4-row matrix (CSR; every format in `formats`)", "value": csr_us,
+        "unit": "us", "n_gpus": ws, "steps": reps, "warmup": a.warmup, "ms_per_step": csr_us * 1e-3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: the reference's own generator recipe (seed 0), no dataset",
+        "config": {"workload": "spmv_uniform_rows_n10000_k10_all_formats_dense2000_f64", "n": n, "nnz": nnz,
+                   "reps": reps, "l2": "resident (1.4 MB): launch and latency bound", "parallelism": "1 GPU"},
+        "formats": out,
+        "cpu_baseline": {"value": out["CSR"]["cpu_oracle_us"], "unit": "us", "cores": 1, "kind": "port",
+                         "sample": "10 Ax of each format through the oracle's C loops"},
+        "e2e": {"value": out["CSR"]["host_call_us"], "unit": "us", "h2d_bytes_per_step": 8 * n,
+                "d2h_bytes_per_step": 8 * n},
+        "gpu_launches": launches, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_pagerank(a):
     """The PageRank workload: preferential-attachment graph, n = 2^22 nodes,
     Zipf(2.1) out-degrees of mean 16, 5% dangling, seed 2; column-stochastic
@@ -672,6 +795,8 @@ if __name__ == "__main__":
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "small":
+        run_small(args)
     elif args.workload == "pagerank":
         run_pagerank(args)
     elif args.workload == "cg":

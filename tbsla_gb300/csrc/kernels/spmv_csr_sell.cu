@@ -286,12 +286,16 @@ cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* coun
     const SellPlan& p = a.blocks[b];
     const bool on_side = fork && b == a.nblocks - 1;
     cudaStream_t ls = on_side ? a.side : s;
+    // a small plan gets about one warp per slice, not the whole resident
+    // grid (whose warps would mostly find no work and then all count out on
+    // one atomic)
+    const int pg = std::min(grid, std::max(1, (p.nslices + NT / 32 - 1) / (NT / 32)));
     cudaError_t e = cudaSuccess;
     if (fork && b == a.nblocks - a.parts) e = cudaEventRecord(a.fork, s);
     if (e == cudaSuccess && on_side) e = cudaStreamWaitEvent(ls, a.fork, 0);
     if (e == cudaSuccess && a.ready && b > 0) e = cudaStreamWaitEvent(ls, a.ready[b], 0);
     if (e == cudaSuccess && p.nslices > 0) {
-      k_sell<V, U><<<grid, NT, 0, ls>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
+      k_sell<V, U><<<pg, NT, 0, ls>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
                                         counter + (on_side ? kSellCounterRegion : 0), done);
       e = cudaGetLastError();
     }
