@@ -63,10 +63,10 @@ struct EpiPageRank {
   const double* x;
   const double* colw;
   const double* tele;
-  double beta, s, t, c_uniform;
+  double bs, s, t, c_uniform;  // bs = beta * s, formed once per thread
   __device__ __forceinline__ void emit(int row, double sum, double* red) const {
     const double c = tele ? mul_rn(t, tele[row]) : c_uniform;
-    const double yn = fma_rn(mul_rn(beta, s), sum, c);
+    const double yn = fma_rn(bs, sum, c);
     red[0] = add_rn(red[0], fabs(fma_rn(-x[row], s, yn)));
     red[1] = add_rn(red[1], yn);
     red[2] = fma_rn(colw[row], yn, red[2]);
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   if (*(volatile int*)p.done) return;  // converged in an earlier launch: no-op
   const uint64_t pol = policy_evict_first();
   const double s = p.coef_in[0], t = p.coef_in[1];
-  EpiPageRank epi{y, x, p.colw, p.tele, p.beta, s, t, t / p.n_nodes};
+  EpiPageRank epi{y, x, p.colw, p.tele, mul_rn(p.beta, s), s, t, t / p.n_nodes};
   double red[3] = {0, 0, 0};
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm))
     csr_block<V, ITEMS>(a, b, x, epi, red, stage, sm, pol);
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(NT) k_pagerank_epilogue(const double* __restri
   __shared__ Smem sm;
   if (*(volatile int*)p.done) return;
   const double s = p.coef_in[0], tw = p.coef_in[1];
-  EpiPageRank epi{y, x, p.colw, p.tele, p.beta, s, tw, tw / p.n_nodes};
+  EpiPageRank epi{y, x, p.colw, p.tele, mul_rn(p.beta, s), s, tw, tw / p.n_nodes};
   double red[3] = {0, 0, 0};
   for (long i = blockIdx.x * (long)NT + threadIdx.x; i < n; i += (long)gridDim.x * NT)
     epi.emit((int)i, t[i], red);
