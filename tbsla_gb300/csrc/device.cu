@@ -99,8 +99,9 @@ struct DeviceMatrix {
   int* scols = nullptr;
   unsigned* sell_counter = nullptr;
   int sell_parts = 1;  // trailing plans that split the last column block by rows
-  cudaStream_t side = nullptr;  // least priority: the last row part runs here
-  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  std::vector<cudaStream_t> side;  // row parts 1..: falling priorities
+  cudaEvent_t fork_ev = nullptr;
+  std::vector<cudaEvent_t> join_ev;
   cudaStream_t xstream = nullptr;   // host entry point: x of column blocks 1.. copied here
   std::vector<cudaEvent_t> xready;  // [block]: that block's x has arrived
   double* colw = nullptr;  // PageRank: column sums of the stored values
@@ -134,9 +135,11 @@ struct DeviceMatrix {
         if (q) cudaFree(q);
     for (cudaEvent_t e : xready)
       if (e) cudaEventDestroy(e);
-    for (cudaEvent_t e : {fork_ev, join_ev})
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    for (cudaEvent_t e : join_ev)
       if (e) cudaEventDestroy(e);
-    if (side) cudaStreamDestroy(side);
+    for (cudaStream_t q : side)
+      if (q) cudaStreamDestroy(q);
     if (xstream) cudaStreamDestroy(xstream);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -266,9 +269,9 @@ SellArgs sell_args(const tbsla_matrix* m, const DeviceMatrix* d) {
   a.nblocks = (int)d->sell.size();
   a.blocks = d->sell.data();
   a.parts = d->sell_parts;
-  a.side = d->side;
+  a.side = d->side.empty() ? nullptr : d->side.data();
   a.fork = d->fork_ev;
-  a.join = d->join_ev;
+  a.join = d->join_ev.empty() ? nullptr : d->join_ev.data();
   return a;
 }
 
@@ -334,12 +337,19 @@ int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
     steps += dp.sell_len / 32;
   }
   d->sell_parts = R;
-  if (!st && R > 1 && !d->side) {
+  if (!st && R > 1 && d->side.empty()) {
+    // part k on priority greatest + k (numerically larger = lower), at most
+    // the least priority; the matrix stream has the greatest
     int least = 0, greatest = 0;
     cudaDeviceGetStreamPriorityRange(&least, &greatest);
-    st = status_of(cudaStreamCreateWithPriority(&d->side, cudaStreamNonBlocking, least));
+    d->side.assign(R - 1, nullptr);
+    d->join_ev.assign(R - 1, nullptr);
+    for (int k = 1; k < R && !st; k++) {
+      const int prio = std::min(least, greatest + k);
+      st = status_of(cudaStreamCreateWithPriority(&d->side[k - 1], cudaStreamNonBlocking, prio));
+      if (!st) st = status_of(cudaEventCreateWithFlags(&d->join_ev[k - 1], cudaEventDisableTiming));
+    }
     if (!st) st = status_of(cudaEventCreateWithFlags(&d->fork_ev, cudaEventDisableTiming));
-    if (!st) st = status_of(cudaEventCreateWithFlags(&d->join_ev, cudaEventDisableTiming));
   }
   if (st) return st;
   const size_t len = (size_t)steps * 32;

@@ -111,12 +111,14 @@ struct SellArgs {
   const cudaEvent_t* ready = nullptr;
   const cudaEvent_t* after = nullptr;
   // Row parts: the last `parts` plans split the last column block by rows.
-  // They do not depend on one another, so with a side stream the last part
-  // runs there (forked after the earlier blocks, joined back before
-  // sell_spmv returns) and its CTAs fill the tail of the part before it.
+  // They do not depend on one another, so with side streams part k >= 1
+  // runs on side[k - 1] (forked after the earlier blocks, joined back
+  // before sell_spmv returns); the side streams have falling priorities,
+  // so each part's CTAs fill the tail of the part before it.
   int parts = 1;
-  cudaStream_t side = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr;
+  const cudaStream_t* side = nullptr;  // [parts - 1]
+  cudaEvent_t fork = nullptr;
+  const cudaEvent_t* join = nullptr;   // [parts - 1]
 };
 // Fills the slice arrays of every block from the CSR device arrays.
 cudaError_t sell_fill(const SellArgs& a, cudaStream_t s);
@@ -124,7 +126,7 @@ cudaError_t sell_fill(const SellArgs& a, cudaStream_t s);
 // zeroed scratch (a region per launch that may run at once), reset by each
 // launch; a set *done (device) makes the launches no-ops.
 constexpr int kSellCounterRegion = 1024;
-constexpr int kSellCounterWords = 2 * kSellCounterRegion;
+constexpr int kSellCounterWords = kRowParts * kSellCounterRegion;
 cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* counter, cudaStream_t s,
                       const int* done = nullptr);
 

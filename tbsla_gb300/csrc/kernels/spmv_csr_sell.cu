@@ -282,32 +282,34 @@ cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* coun
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V, U>, NT, 0);
   const int grid = std::max(1, sms * std::max(1, per));
   const bool fork = a.side && a.parts > 1 && a.nblocks >= a.parts;
+  const int first_part = a.nblocks - a.parts;
   for (int b = 0; b < a.nblocks; b++) {
     const SellPlan& p = a.blocks[b];
-    const bool on_side = fork && b == a.nblocks - 1;
-    cudaStream_t ls = on_side ? a.side : s;
+    const int k = fork && b >= first_part ? b - first_part : 0;  // row part (0: matrix stream)
+    cudaStream_t ls = k > 0 ? a.side[k - 1] : s;
     // a small plan gets about one warp per slice, not the whole resident
     // grid (whose warps would mostly find no work and then all count out on
     // one atomic)
     const int pg = std::min(grid, std::max(1, (p.nslices + NT / 32 - 1) / (NT / 32)));
     cudaError_t e = cudaSuccess;
-    if (fork && b == a.nblocks - a.parts) e = cudaEventRecord(a.fork, s);
-    if (e == cudaSuccess && on_side) e = cudaStreamWaitEvent(ls, a.fork, 0);
+    if (fork && b == first_part) e = cudaEventRecord(a.fork, s);
+    if (e == cudaSuccess && k > 0) e = cudaStreamWaitEvent(ls, a.fork, 0);
     if (e == cudaSuccess && a.ready && b > 0) e = cudaStreamWaitEvent(ls, a.ready[b], 0);
     if (e == cudaSuccess && p.nslices > 0) {
       k_sell<V, U><<<pg, NT, 0, ls>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
-                                        counter + (on_side ? kSellCounterRegion : 0), done);
+                                      counter + k * kSellCounterRegion, done);
       e = cudaGetLastError();
     }
     // recorded for an empty plan too: the event then marks the earlier plans
     if (e == cudaSuccess && a.after && a.after[b]) e = cudaEventRecord(a.after[b], ls);
+    if (e == cudaSuccess && k > 0) e = cudaEventRecord(a.join[k - 1], ls);
     if (e != cudaSuccess) return e;
   }
-  if (fork) {
-    cudaError_t e = cudaEventRecord(a.join, a.side);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, a.join, 0);
-    if (e != cudaSuccess) return e;
-  }
+  if (fork)
+    for (int k = 1; k < a.parts; k++) {
+      cudaError_t e = cudaStreamWaitEvent(s, a.join[k - 1], 0);
+      if (e != cudaSuccess) return e;
+    }
   return cudaSuccess;
 }
 
