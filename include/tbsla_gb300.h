@@ -278,10 +278,16 @@ int tbsla_make_stochastic(tbsla_matrix* m, double* s);
  * row (0 for an empty row).
  * tbsla_apply_exponential: apply_exponential (:1315-1334), every nonzero a_ij
  * becomes exp(a_ij - max_abs[i]) (base <= 0) or base^(a_ij - max_abs[i]);
- * no shift when max_abs is NULL. */
+ * no shift when max_abs is NULL.
+ * tbsla_get_row_sums: get_row_sums (:1147-1164), s[i] = sum of local row i
+ * in entry order (s has ln_row entries).
+ * tbsla_normalize_rows: normalize_rows (:1177-1190), a_ij /= s[i], or 0
+ * where s[i] = 0 (the reference's safeguard). */
 int tbsla_dense_multiply(const tbsla_matrix* m, const double* B, double* C, int cols_B);
 int tbsla_get_row_max_abs(const tbsla_matrix* m, double* max_abs);
 int tbsla_apply_exponential(tbsla_matrix* m, const double* max_abs, int base);
+int tbsla_get_row_sums(const tbsla_matrix* m, double* s);
+int tbsla_normalize_rows(tbsla_matrix* m, const double* s);
 
 /* ---- PageRank (src/mpi/matrix/Matrix.cpp:540-602, 641-790), CSR only --------
  * A column-stochastic (zero columns = dangling nodes).  x_0 = 1/n and, with

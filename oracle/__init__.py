@@ -60,7 +60,8 @@ def ref() -> C.CDLL | None:
         for name in ("ref_delete", "ref_fill_cdiag", "ref_fill_cqmat", "ref_fill_random", "ref_info",
                      "ref_arrays", "ref_adopt", "ref_write", "ref_read", "ref_Ax", "ref_spmv",
                      "ref_a_axpx_", "ref_AAxpAx", "ref_AAxpAxpx", "ref_get_col_sums",
-                     "ref_normalize_cols", "ref_dense_multiply", "ref_row_max_abs", "ref_apply_exponential"):
+                     "ref_normalize_cols", "ref_dense_multiply", "ref_row_max_abs", "ref_apply_exponential",
+                     "ref_row_sums", "ref_normalize_rows"):
             getattr(_r, name).restype = None if not name.endswith(("write", "read")) else I
         _r.ref_fill_cqmat.argtypes = [P, I, I, I, D, C.c_uint, I, I, I, I]
         _r.ref_fill_random.argtypes = [P, I, I, D, C.c_uint, I, I, I, I]
@@ -199,6 +200,19 @@ def csr_row_max_abs(rowptr, values):
     out = np.empty(n)
     lib().orc_csr_row_max_abs(I(n), _p(values), _p(rowptr), _p(out))
     return out
+
+
+def csr_row_sums(rowptr, values):
+    n = len(rowptr) - 1
+    out = np.empty(n)
+    lib().orc_csr_row_sums(I(n), _p(values), _p(rowptr), _p(out))
+    return out
+
+
+def csr_normalize_rows(rowptr, values, s):
+    v = np.array(values, np.float64)
+    lib().orc_csr_normalize_rows(I(len(rowptr) - 1), _p(v), _p(rowptr), _p(np.ascontiguousarray(s, np.float64)))
+    return v
 
 
 def csr_apply_exponential(rowptr, values, max_abs=None, base=-1):

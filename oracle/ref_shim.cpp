@@ -265,6 +265,16 @@ void ref_row_max_abs(void* hp, double* out) {
   as<RCSR>(static_cast<Handle*>(hp))->get_row_max_abs(out);
 }
 
+void ref_row_sums(void* hp, double* out) {
+  Quiet q;
+  as<RCSR>(static_cast<Handle*>(hp))->get_row_sums(out);
+}
+
+void ref_normalize_rows(void* hp, double* s) {
+  Quiet q;
+  as<RCSR>(static_cast<Handle*>(hp))->normalize_rows(s);
+}
+
 void ref_apply_exponential(void* hp, double* max_abs, int base) {
   Quiet q;
   as<RCSR>(static_cast<Handle*>(hp))->apply_exponential(max_abs, base);

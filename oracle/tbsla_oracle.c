@@ -268,6 +268,23 @@ void orc_csr_row_max_abs(int ln_row, const double* values, const int* rowptr, do
   }
 }
 
+/* s[i] = sum of row i's values in entry order, MatrixCSR::get_row_sums
+ * (MatrixCSR.cpp:1147-1164). */
+void orc_csr_row_sums(int ln_row, const double* values, const int* rowptr, double* s) {
+  for (int i = 0; i < ln_row; i++) {
+    double sum = 0.0;
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) sum += values[j];
+    s[i] = sum;
+  }
+}
+
+/* a_ij /= s[i], or 0 where s[i] == 0, MatrixCSR::normalize_rows
+ * (MatrixCSR.cpp:1177-1190). */
+void orc_csr_normalize_rows(int ln_row, double* values, const int* rowptr, const double* s) {
+  for (int i = 0; i < ln_row; i++)
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) values[j] = s[i] != 0 ? values[j] / s[i] : 0.0;
+}
+
 /* MatrixCSR::apply_exponential (MatrixCSR.cpp:1315-1334): every nonzero
  * a_ij becomes exp(a_ij - max_abs[i]) (base <= 0) or base^(a_ij - max_abs[i]),
  * without the shift when max_abs is NULL; zeros stay. */

@@ -55,6 +55,8 @@ void orc_csr_normalize_cols(int ln_row, int f_col, long nnz, double* values,
 void orc_csr_dense_multiply(int n_row, const double* values, const int* rowptr, const int* colidx,
                             const double* B, double* Cm, int cols_B);
 void orc_csr_row_max_abs(int ln_row, const double* values, const int* rowptr, double* max_abs);
+void orc_csr_row_sums(int ln_row, const double* values, const int* rowptr, double* s);
+void orc_csr_normalize_rows(int ln_row, double* values, const int* rowptr, const double* s);
 void orc_csr_apply_exponential(int ln_row, double* values, const int* rowptr, const double* max_abs,
                                int base);
 

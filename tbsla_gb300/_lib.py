@@ -131,6 +131,8 @@ _SIGS = {
     "tbsla_make_stochastic": (I, [P, P]),
     "tbsla_dense_multiply": (I, [P, P, P, I]),
     "tbsla_get_row_max_abs": (I, [P, P]),
+    "tbsla_get_row_sums": (I, [P, P]),
+    "tbsla_normalize_rows": (I, [P, P]),
     "tbsla_apply_exponential": (I, [P, P, I]),
     "tbsla_page_rank": (I, [P, D, D, I, P, IP, DP]),
     "tbsla_page_rank_batched": (I, [P, I, P, D, D, I, P, IP]),

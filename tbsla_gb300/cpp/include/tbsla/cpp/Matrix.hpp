@@ -11,10 +11,13 @@
 //  - NUMAinit() builds the device copy (the GPU analogue of first-touch
 //    placement);
 //  - get_vectorization() names the CUDA target;
-//  - get_row_sums / normalize_rows / fill_brain (attention and brain-model
-//    helpers, not on the SpMV / PageRank / CG path) raise
-//    GpuError(TBSLA_ERR_UNSUPPORTED); get_row_max_abs / apply_exponential
-//    (CSR) and MatrixCSR::dense_multiply run on the GPU.
+//  - fill_brain (the brain-model generator, not on the SpMV / PageRank / CG
+//    path) raises GpuError(TBSLA_ERR_UNSUPPORTED); the sparse-softmax
+//    helpers get_row_sums / normalize_rows / get_row_max_abs /
+//    apply_exponential and MatrixCSR::dense_multiply run on the GPU for CSR
+//    (other formats raise TBSLA_ERR_UNSUPPORTED);
+//  - get_row_sums / normalize_rows do not print the reference's progress
+//    lines.
 #ifndef TBSLA_GB300_CPP_MATRIX
 #define TBSLA_GB300_CPP_MATRIX
 

@@ -200,8 +200,8 @@ void Matrix::fill_brain(int, int, int*, std::vector<std::vector<double> >,
   throw GpuError(TBSLA_ERR_UNSUPPORTED, "fill_brain");
 }
 
-void Matrix::get_row_sums(double*) { throw GpuError(TBSLA_ERR_UNSUPPORTED, "get_row_sums"); }
-void Matrix::normalize_rows(double*) { throw GpuError(TBSLA_ERR_UNSUPPORTED, "normalize_rows"); }
+void Matrix::get_row_sums(double* buffer) { check(tbsla_get_row_sums(h_, buffer), "get_row_sums"); }
+void Matrix::normalize_rows(double* s) { check(tbsla_normalize_rows(h_, s), "normalize_rows"); }
 void Matrix::get_col_sums(double* buffer) { check(tbsla_get_col_sums(h_, buffer), "get_col_sums"); }
 void Matrix::normalize_cols(double* s) { check(tbsla_normalize_cols(h_, s), "normalize_cols"); }
 void Matrix::get_row_max_abs(double* max_abs) { check(tbsla_get_row_max_abs(h_, max_abs), "get_row_max_abs"); }

@@ -291,6 +291,16 @@ int tbsla_get_row_max_abs(const tbsla_matrix* m, double* max_abs) {
   return dev_row_max_abs(m, max_abs);
 }
 
+int tbsla_get_row_sums(const tbsla_matrix* m, double* s) {
+  if (!m || !s) return TBSLA_ERR_INVALID_ARG;
+  return dev_row_sums(m, s);
+}
+
+int tbsla_normalize_rows(tbsla_matrix* m, const double* s) {
+  if (!m || !s) return TBSLA_ERR_INVALID_ARG;
+  return dev_normalize_rows(m, s);
+}
+
 int tbsla_apply_exponential(tbsla_matrix* m, const double* max_abs, int base) {
   if (!m) return TBSLA_ERR_INVALID_ARG;
   return dev_apply_exponential(m, max_abs, base);

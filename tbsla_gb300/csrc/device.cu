@@ -783,6 +783,53 @@ int dev_normalize_cols(tbsla_matrix* m, const double* s) {
   return TBSLA_OK;
 }
 
+int dev_row_sums(const tbsla_matrix* m, double* s) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const tbsla_info& I = m->info;
+  if (I.ln_row <= 0) return TBSLA_OK;
+  if (I.nnz == 0) {  // MatrixCSR.cpp:1152-1154: zeroed, nothing to add
+    std::memset(s, 0, sizeof(double) * I.ln_row);
+    return TBSLA_OK;
+  }
+  cudaStream_t str = d->stream;
+  if ((st = d->vec(&d->t, &d->t_len, (size_t)I.ln_row))) return st;
+  double* v64;
+  bool owned;
+  if ((st = values64(m, d, &v64, &owned))) return st;
+  st = status_of(csr_row_sums(v64, d->idx0, I.ln_row, d->t, str));
+  if (!st) st = status_of(cudaMemcpyAsync(s, d->t, (size_t)I.ln_row * 8, cudaMemcpyDeviceToHost, str));
+  if (!st) st = status_of(cudaStreamSynchronize(str));
+  if (owned) cudaFree(v64);
+  return st;
+}
+
+int dev_normalize_rows(tbsla_matrix* m, const double* s) {
+  if (m->format != TBSLA_CSR) return TBSLA_ERR_UNSUPPORTED;
+  int st;
+  DeviceMatrix* d = ensure(m, &st);
+  if (st) return st;
+  const tbsla_info& I = m->info;
+  if (I.nnz == 0 || I.ln_row <= 0) return TBSLA_OK;
+  cudaStream_t str = d->stream;
+  if ((st = d->vec(&d->t, &d->t_len, (size_t)I.ln_row))) return st;
+  TRY(cudaMemcpyAsync(d->t, s, (size_t)I.ln_row * 8, cudaMemcpyHostToDevice, str));
+  double* v64;
+  bool owned;
+  if ((st = values64(m, d, &v64, &owned))) return st;
+  TRY(csr_normalize_rows(v64, d->idx0, I.ln_row, d->t, str));
+  // keep the host arrays (the reference layout) in step with the device
+  TRY(cudaMemcpyAsync(m->values.data(), v64, d->nnz * 8, cudaMemcpyDeviceToHost, str));
+  if (owned) TRY(convert_values(v64, d->vals, d->prec, d->nnz, str));
+  if (d->algo == 2 && d->svals) TRY(sell_fill(sell_args(m, d), str));  // slice copy
+  d->colw_ok = false;
+  TRY(cudaStreamSynchronize(str));
+  if (owned) cudaFree(v64);
+  return TBSLA_OK;
+}
+
 int dev_make_stochastic(tbsla_matrix* m, double* s) {
   int st = dev_col_sums(m, s, true);
   if (st) return st;

@@ -32,6 +32,9 @@ int dev_make_stochastic(tbsla_matrix* m, double* s);
 // MatrixCSR::dense_multiply, get_row_max_abs, apply_exponential (host buffers).
 int dev_dense_multiply(const tbsla_matrix* m, const double* B, double* C, int cols);
 int dev_row_max_abs(const tbsla_matrix* m, double* max_abs);
+// MatrixCSR::get_row_sums / normalize_rows (host buffers).
+int dev_row_sums(const tbsla_matrix* m, double* s);
+int dev_normalize_rows(tbsla_matrix* m, const double* s);
 int dev_apply_exponential(tbsla_matrix* m, const double* max_abs, int base);
 
 int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* result,

@@ -288,6 +288,9 @@ cudaError_t csr_dense_multiply(const void* vals, int prec, const int* rowptr, co
                                const double* B, int k, double* Cm, cudaStream_t s);
 // out[i] = max_j |a_ij| (0 for an empty row).
 cudaError_t csr_row_max_abs(const double* vals, const int* rowptr, int n_row, double* out, cudaStream_t s);
+// Row sums in entry order (FP64 values) and a_ij / s_i (0 where s_i = 0).
+cudaError_t csr_row_sums(const double* vals, const int* rowptr, int n_row, double* out, cudaStream_t s);
+cudaError_t csr_normalize_rows(double* vals, const int* rowptr, int n_row, const double* sums, cudaStream_t s);
 // a_ij <- exp(a_ij - max_abs[i]) (base <= 0) or base^(a_ij - max_abs[i]) for
 // every nonzero a_ij; no shift when max_abs is null.
 cudaError_t csr_apply_exponential(double* vals, const int* rowptr, int n_row, const double* max_abs, int base,

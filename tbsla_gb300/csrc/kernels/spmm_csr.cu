@@ -7,6 +7,9 @@
 // one coalesced load of a B row segment and one FMA per lane, in entry
 // order.  csr_row_max_abs / csr_apply_exponential replace get_row_max_abs
 // (:1283-1312) and apply_exponential (:1315-1334): one warp per row.
+// csr_row_sums / csr_normalize_rows replace get_row_sums (:1147-1164: each
+// row summed in entry order, so one thread per row) and normalize_rows
+// (:1177-1190: a_ij / s_i, or 0 where s_i = 0; one warp per row).
 #include <algorithm>
 
 #include "common.cuh"
@@ -67,6 +70,24 @@ __global__ void __launch_bounds__(NT) k_apply_exp(double* __restrict__ vals, con
   }
 }
 
+__global__ void __launch_bounds__(NT) k_row_sums(const double* __restrict__ vals, const int* __restrict__ rowptr,
+                                                int n_row, double* __restrict__ out) {
+  for (long i = (long)blockIdx.x * NT + threadIdx.x; i < n_row; i += (long)gridDim.x * NT) {
+    double sum = 0;
+    for (int j = rowptr[i]; j < rowptr[i + 1]; j++) sum = add_rn(sum, vals[j]);
+    out[i] = sum;
+  }
+}
+
+__global__ void __launch_bounds__(NT) k_normalize_rows(double* __restrict__ vals, const int* __restrict__ rowptr,
+                                                      int n_row, const double* __restrict__ s) {
+  const int lane = threadIdx.x & 31;
+  for (long i = warp_id(); i < n_row; i += warp_count()) {
+    const double si = s[i];
+    for (int j = rowptr[i] + lane; j < rowptr[i + 1]; j += kWarp) vals[j] = si != 0 ? vals[j] / si : 0.0;
+  }
+}
+
 int warp_grid(long rows) { return (int)std::max<long>(1, std::min<long>((rows + 7) / 8, 152L * 16)); }
 
 }  // namespace
@@ -97,6 +118,19 @@ cudaError_t csr_apply_exponential(double* vals, const int* rowptr, int n_row, co
                                   cudaStream_t s) {
   if (n_row <= 0) return cudaSuccess;
   k_apply_exp<<<warp_grid(n_row), NT, 0, s>>>(vals, rowptr, n_row, max_abs, base);
+  return cudaGetLastError();
+}
+
+cudaError_t csr_row_sums(const double* vals, const int* rowptr, int n_row, double* out, cudaStream_t s) {
+  if (n_row <= 0) return cudaSuccess;
+  const int g = (int)std::max<long>(1, std::min<long>((n_row + NT - 1) / NT, 152L * 16));
+  k_row_sums<<<g, NT, 0, s>>>(vals, rowptr, n_row, out);
+  return cudaGetLastError();
+}
+
+cudaError_t csr_normalize_rows(double* vals, const int* rowptr, int n_row, const double* sums, cudaStream_t s) {
+  if (n_row <= 0) return cudaSuccess;
+  k_normalize_rows<<<warp_grid(n_row), NT, 0, s>>>(vals, rowptr, n_row, sums);
   return cudaGetLastError();
 }
 

@@ -285,6 +285,16 @@ class MatrixCSR(Matrix):
         check(lib.tbsla_get_row_max_abs(self._h, _ptr(out)), "get_row_max_abs")
         return out
 
+    def get_row_sums(self, s: np.ndarray | None = None) -> np.ndarray:
+        """Row sums in entry order (MatrixCSR::get_row_sums)."""
+        out = np.empty(self.info()["ln_row"]) if s is None else s
+        check(lib.tbsla_get_row_sums(self._h, _ptr(out)), "get_row_sums")
+        return out
+
+    def normalize_rows(self, s: np.ndarray):
+        """a_ij /= s[i], 0 where s[i] = 0 (MatrixCSR::normalize_rows)."""
+        check(lib.tbsla_normalize_rows(self._h, _ptr(_f64(s, "s"))), "normalize_rows")
+
     def apply_exponential(self, max_abs: np.ndarray | None = None, base: int = -1):
         mx = None if max_abs is None else _f64(max_abs, "max_abs")
         check(lib.tbsla_apply_exponential(self._h, _ptr(mx) if mx is not None else None, base),

@@ -279,9 +279,9 @@ def cfg1(R):
 
 
 def spmm(R):
-    """dense_multiply, get_row_max_abs and apply_exponential of the
-    reference's MatrixCSR (MatrixCSR.cpp:1269-1334) on cqmat / cdiag /
-    random matrices."""
+    """dense_multiply, get_row_max_abs, apply_exponential, get_row_sums and
+    normalize_rows of the reference's MatrixCSR (MatrixCSR.cpp:1147-1190,
+    1269-1334) on cqmat / cdiag / random matrices."""
     out = {}
     fills = {"cqmat": lambda h: R.L.ref_fill_cqmat(h, 40, 40, 6, 0.4, 2, 0, 0, 1, 1),
              "cdiag": lambda h: R.L.ref_fill_cdiag(h, 40, 40, 3, 0, 0, 1, 1),
@@ -305,6 +305,23 @@ def spmm(R):
             h = R.new(2)
             fill(h)
             R.L.ref_apply_exponential(h, C.c_void_p(mx.ctypes.data) if use_max else None, base)
+            out[f"{key}/{tag}"] = R.arrays(h, 2)["values"]
+            R.L.ref_delete(h)
+        h = R.new(2)
+        fill(h)
+        rs = np.zeros(i["ln_row"])
+        R.L.ref_row_sums(h, C.c_void_p(rs.ctypes.data))
+        out[f"{key}/row_sums"] = rs
+        R.L.ref_delete(h)
+        # normalize_rows by the row sums, and by sums with every third one
+        # zero (the reference's safeguard sets those rows to 0)
+        rz = rs.copy()
+        rz[::3] = 0
+        for tag, sv in (("norm_rows", rs), ("norm_rows_zero", rz)):
+            h = R.new(2)
+            fill(h)
+            sv = np.ascontiguousarray(sv)
+            R.L.ref_normalize_rows(h, C.c_void_p(sv.ctypes.data))
             out[f"{key}/{tag}"] = R.arrays(h, 2)["values"]
             R.L.ref_delete(h)
     np.savez_compressed(os.path.join(OUT, "spmm.npz"), **out)

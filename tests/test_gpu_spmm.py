@@ -1,8 +1,8 @@
 """CSR dense_multiply (SpMM) and the sparse-softmax helpers on the GPU
 against the reference's recordings (tests/golden/spmm.npz) and the oracle:
 SpMM within the FP64 bar (one fused multiply-add per product, the reference
-rounds the product first), row maxima exact, exponentials within 2 ulp of
-the host libm."""
+rounds the product first), row maxima, row sums and row normalisation
+exact, exponentials within 2 ulp of the host libm."""
 import numpy as np
 import pytest
 
@@ -42,6 +42,21 @@ def test_against_reference_recordings(gpu, golden):
             v = e.arrays()["values"][:end]
             ref = g[f"{key}/{tag}"]
             assert np.allclose(v, ref, rtol=5e-16, atol=0), (key, tag)
+        # row sums in entry order and the division: bit for bit, including
+        # the rows whose sum is given as 0 (set to 0)
+        rs = m.get_row_sums()
+        assert np.array_equal(rs, g[f"{key}/row_sums"]), key
+        rz = rs.copy()
+        rz[::3] = 0
+        for tag, sv in (("norm_rows", rs), ("norm_rows_zero", rz)):
+            e = T.MatrixCSR()
+            fill(e)
+            e.normalize_rows(sv)
+            assert np.array_equal(e.arrays()["values"][:end], g[f"{key}/{tag}"][:end]), (key, tag)
+            x = np.linspace(0.5, 1.5, e.info()["n_col"])
+            ea = e.arrays()
+            assert np.allclose(e.spmv(x), oracle.csr_ax(ea["rowptr"], ea["colidx"], ea["values"], x),
+                               rtol=1e-13, atol=1e-300), (key, tag)  # device copy refreshed
 
 
 @pytest.mark.parametrize("prec", ["f64", "f32"])

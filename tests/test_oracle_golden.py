@@ -238,8 +238,9 @@ SPMM_FILLS = {"cqmat": lambda m: m.fill_cqmat(40, 40, 6, 0.4, 2), "cdiag": lambd
 
 
 def test_oracle_spmm_and_softmax_helpers(golden):
-    """dense_multiply, get_row_max_abs and apply_exponential restated, bit
-    for bit against the reference's MatrixCSR (tests/golden/spmm.npz)."""
+    """dense_multiply, get_row_max_abs, apply_exponential, get_row_sums and
+    normalize_rows restated, bit for bit against the reference's MatrixCSR
+    (tests/golden/spmm.npz)."""
     import tbsla_gb300 as T
 
     g = golden["spmm"]
@@ -256,3 +257,11 @@ def test_oracle_spmm_and_softmax_helpers(golden):
             v = oracle.csr_apply_exponential(a["rowptr"], a["values"], mx if use_max else None, base)
             end = int(a["rowptr"][-1])  # CSR fill_cqmat over-counts nnz; the arrays end at rowptr[n]
             assert np.array_equal(v[:end], g[f"{key}/{tag}"]), (key, tag)
+        rs = oracle.csr_row_sums(a["rowptr"], a["values"])
+        assert np.array_equal(rs, g[f"{key}/row_sums"]), key
+        end = int(a["rowptr"][-1])
+        rz = rs.copy()
+        rz[::3] = 0
+        for tag, sv in (("norm_rows", rs), ("norm_rows_zero", rz)):
+            v = oracle.csr_normalize_rows(a["rowptr"], a["values"], sv)
+            assert np.array_equal(v[:end], g[f"{key}/{tag}"][:end]), (key, tag)
