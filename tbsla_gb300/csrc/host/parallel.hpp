@@ -31,4 +31,22 @@ void parallel_for(long n, F fn) {
   for (auto& x : th) x.join();
 }
 
+// The same over n heavy items (each worth thousands of elements, e.g. a
+// window of rows to sort): split across threads whenever n > 1.
+template <class F>
+void parallel_for_items(long n, F fn) {
+  const int nt = (int)std::min<long>(host_threads(), n);
+  if (nt <= 1) {
+    fn(0L, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt);
+  for (int t = 0; t < nt; t++) {
+    long b = n * t / nt, e = n * (t + 1) / nt;
+    th.emplace_back([=] { fn(b, e); });
+  }
+  for (auto& x : th) x.join();
+}
+
 }  // namespace tbsla_impl

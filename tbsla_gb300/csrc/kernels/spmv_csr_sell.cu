@@ -341,7 +341,7 @@ cudaError_t launch_u(const SellArgs& a, const double* x, double* y, unsigned* co
 
 void sell_plan_build(const int* L, int n, int sthr, int lthr, int sigma, bool skip_empty, long step0,
                      SellPlan* p) {
-  using tbsla_impl::parallel_for;
+  using tbsla_impl::parallel_for_items;
   *p = SellPlan{};
   p->n = n;
   sthr = std::max(1, std::min(sthr, 255));
@@ -396,7 +396,7 @@ void sell_plan_build(const int* L, int n, int sthr, int lthr, int sigma, bool sk
   // Short rows: one lane each, sorted by length within windows.
   const int nwin = (n + sigma - 1) / sigma;
   std::vector<std::vector<int>> win(nwin);
-  parallel_for(nwin, [&](long b, long e) {
+  parallel_for_items(nwin, [&](long b, long e) {
     for (long w = b; w < e; w++) {
       const int r0 = (int)(w * sigma), r1 = (int)std::min<long>((w + 1) * (long)sigma, n);
       auto& v = win[w];
@@ -411,7 +411,7 @@ void sell_plan_build(const int* L, int n, int sthr, int lthr, int sigma, bool sk
   const long nshort = first[nwin];
   desc.resize(nwide + nshort);
   meta.resize(32 * (nwide + nshort));
-  parallel_for(nwin, [&](long b, long e) {
+  parallel_for_items(nwin, [&](long b, long e) {
     for (long w = b; w < e; w++) {
       const auto& v = win[w];
       const int base = (int)(w * sigma);
