@@ -191,13 +191,16 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
 int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items);
 /* Sliced-ELL layout: the columns are split into blocks of at most
  * col_block columns (0 = 8,388,608, i.e. 64 MiB of FP64 x, about what L2
- * keeps for gathers), processed one launch each, the first writing r and the
- * others adding to it.  Within a block, rows of at most short_thr (1..255) entries take one
+ * keeps for gathers), processed one launch each (the last of several in two
+ * parts by rows), the first writing r and the others adding to it.  Within
+ * a block, rows of at most short_thr (0..255) entries take one
  * lane each and are sorted by length within windows of `sigma` (32..2^23)
  * consecutive rows; longer rows take the fewest lanes (a power of two up to
  * 32) that keep their slice at most long_thr steps wide and are sorted by
- * length over the whole block (defaults 64, 64, 16384, 0).  Changing them
- * rebuilds the device copy. */
+ * length over the whole block (defaults 0, 0, 16384, 0; a threshold of 0
+ * is automatic: 64, or 128 when there are several column blocks, whose
+ * per-block row lengths are about halved).  Changing them rebuilds the
+ * device copy. */
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block);
 
 /* One CSR kernel configuration and its measured time. */

@@ -266,7 +266,7 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block) {
 }
 
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block) {
-  if (!m || short_thr < 1 || short_thr > 255 || long_thr < 1 || sigma < 32 || sigma > (1 << 23) ||
+  if (!m || short_thr < 0 || short_thr > 255 || long_thr < 0 || sigma < 32 || sigma > (1 << 23) ||
       col_block < 0)
     return TBSLA_ERR_INVALID_ARG;
   if (m->sell_short != short_thr || m->sell_long != long_thr || m->sell_sigma != sigma ||

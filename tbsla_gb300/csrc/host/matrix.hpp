@@ -57,8 +57,9 @@ struct tbsla_matrix {
   int csr_tile = 2048;     // row-block budget (entries per block)
   int csr_algo = 2;        // 0: merge path, 1: row blocks, 2: sliced ELL (default)
   int merge_items = 8;     // merge path: items per thread
-  int sell_short = 64;     // sliced ELL: rows up to this length, one lane each, sorted per window
-  int sell_long = 64;      // longer rows: fewest lanes keeping a slice this many steps wide
+  int sell_short = 0;      // sliced ELL: rows up to this length, one lane each, sorted per window
+                           // (0: 64, or 128 with several column blocks)
+  int sell_long = 0;       // longer rows: fewest lanes keeping a slice this many steps wide (0: as short)
   int sell_sigma = 16384;  // window of consecutive rows sorted together
   int sell_unroll = 0;     // steps per lane in flight (0: 8)
   int sell_colblock = 0;   // columns per block (0: 8,388,608 = 64 MiB of x)

@@ -270,7 +270,9 @@ class MatrixCSR(Matrix):
         check(lib.tbsla_matrix_autotune(self._h, reps, C.byref(best), trials, max_trials, C.byref(nt)), "autotune")
         return best.as_dict(), [trials[i].as_dict() for i in range(nt.value)]
 
-    def set_sell_params(self, short_thr: int = 64, long_thr: int = 64, sigma: int = 16384, col_block: int = 0):
+    def set_sell_params(self, short_thr: int = 0, long_thr: int = 0, sigma: int = 16384, col_block: int = 0):
+        """Sliced-ELL layout thresholds (0: automatic), window and column
+        block (0: 8,388,608 columns)."""
         check(lib.tbsla_matrix_set_sell_params(self._h, short_thr, long_thr, sigma, col_block), "set_sell_params")
 
     # ---- SpMM / sparse softmax (MatrixCSR.cpp:1269-1334) ---------------------

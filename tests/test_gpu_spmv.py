@@ -147,7 +147,8 @@ def powerlaw(T, n, seed=5, **kw):
     return m
 
 
-CSR_KERNELS = [("sell", (64, 64, 16384, 8, 0)), ("sell", (4, 3, 64, 4, 50000)),
+CSR_KERNELS = [("sell", (64, 64, 16384, 8, 0)), ("sell", (0, 0, 16384, 8, 0)), ("sell", (0, 0, 16384, 8, 50000)),
+               ("sell", (4, 3, 64, 4, 50000)),
                ("sell", (255, 1000, 1 << 20, 16, 100000)), ("sell", (128, 128, 16384, 16, 4096)),
                ("merge", 4), ("merge", 8), ("merge", 16), ("rowblock", 1024), ("rowblock", 2048),
                ("rowblock", 4096)]

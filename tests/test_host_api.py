@@ -191,6 +191,13 @@ def test_bad_arguments():
         T.MatrixCOO().fill_powerlaw if False else T.MatrixDENSE().fill_dense_uniform(0, 4, 1)
     h = C.c_void_p()
     assert T.lib.tbsla_matrix_create(C.byref(h), 7) == L.ERR_INVALID_ARG
+    # sliced-ELL thresholds: 0 (automatic) .. 255; negative rejected
+    m = T.MatrixCSR()
+    m.set_sell_params(0, 0, 16384, 0)
+    m.set_sell_params(255, 1000, 32, 1)
+    for bad in ((-1, 0, 16384, 0), (256, 0, 16384, 0), (0, -1, 16384, 0), (0, 0, 16, 0), (0, 0, 16384, -1)):
+        with pytest.raises(T.TbslaError):
+            m.set_sell_params(*bad)
 
 
 @pytest.mark.skipif(has_gpu(), reason="checks the no-device status on a host without a GPU")
