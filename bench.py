@@ -60,8 +60,8 @@ def parse_args():
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
     p.add_argument("--algo", choices=["sell", "merge", "rowblock"], default="sell")
     p.add_argument("--sell", type=str, default="0,0,16384,0",
-                   help="sliced-ELL kernel: short_thr,long_thr,sigma,col_block (thresholds 0: 64, or 128 with "
-                        "several column blocks; col_block 0: 2^23 columns)")
+                   help="sliced-ELL kernel: short_thr,long_thr,sigma,col_block (thresholds 0: 128 for FP64 values "
+                        "with several column blocks, else 64; col_block 0: 2^23 columns)")
     p.add_argument("--items", type=int, default=0,
                    help="merge: items per thread (0 = 8); sell: steps per lane in flight (0 = automatic)")
     p.add_argument("--no-forms", action="store_true", help="skip the FP32 / BF16 side measurements")
@@ -359,7 +359,7 @@ def run_ours(a):
                    "format": "CSR", "n": n, "nnz": nnz, "value_dtype": a.prec, "x_y_dtype": "f64",
                    "bytes_per_step": B, "csr_kernel": a.algo, "autotune": tuned,
                    "work_split": {"merge": f"{a.items} items/thread", "rowblock": f"{a.tile} nnz/block",
-                                  "sell": f"one lane per row <= {a.sell.split(',')[0] if a.sell.split(',')[0] != '0' else 'auto (64, or 128 with column blocks)'} sorted per "
+                                  "sell": f"one lane per row <= {a.sell.split(',')[0] if a.sell.split(',')[0] != '0' else 'auto (128 for FP64 with column blocks, else 64)'} sorted per "
                                           f"{a.sell.split(',')[2]}-row window, else 2..32 lanes per row, slices "
                                           f"<= {a.sell.split(',')[1]} steps; {a.items or 'automatic'} steps/lane in flight; "
                                           f"column blocks of {int(a.sell.split(',')[3]) or 8388608} columns"}[a.algo],

@@ -198,8 +198,8 @@ int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items);
  * consecutive rows; longer rows take the fewest lanes (a power of two up to
  * 32) that keep their slice at most long_thr steps wide and are sorted by
  * length over the whole block (defaults 0, 0, 16384, 0; a threshold of 0
- * is automatic: 64, or 128 when there are several column blocks, whose
- * per-block row lengths are about halved).  Changing them rebuilds the
+ * is automatic: 128 for FP64 values with several column blocks, whose
+ * per-block row lengths are about halved, else 64).  Changing them rebuilds the
  * device copy. */
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block);
 

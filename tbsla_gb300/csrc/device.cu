@@ -307,10 +307,11 @@ int build_sell(const tbsla_matrix* m, DeviceMatrix* d) {
   const int R = P > 1 ? kRowParts : 1;
   // automatic thresholds: with several column blocks a row's entries are
   // spread over the blocks, so the per-block lengths the thresholds act on
-  // are about halved and the thresholds double (measured at n = 2^24: 128 /
-  // 128 is 1.6% faster than 64 / 64 there, and 64 / 64 is best with one
-  // block)
-  const int sthr = m->sell_short > 0 ? m->sell_short : (P > 1 ? 128 : 64);
+  // are about halved; for FP64 values (whose kernel keeps the next group's
+  // columns in flight) doubling the thresholds then pays: at n = 2^24 128 /
+  // 128 is 2.4% faster than 64 / 64.  With one block, or FP32 / BF16 values,
+  // 64 / 64 measured best.
+  const int sthr = m->sell_short > 0 ? m->sell_short : (P > 1 && d->prec == TBSLA_F64 ? 128 : 64);
   const int lthr = m->sell_long > 0 ? m->sell_long : sthr;
   long steps = 0;
   d->sell.assign(P - 1 + R, SellPlan{});

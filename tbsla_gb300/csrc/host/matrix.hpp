@@ -58,7 +58,7 @@ struct tbsla_matrix {
   int csr_algo = 2;        // 0: merge path, 1: row blocks, 2: sliced ELL (default)
   int merge_items = 8;     // merge path: items per thread
   int sell_short = 0;      // sliced ELL: rows up to this length, one lane each, sorted per window
-                           // (0: 64, or 128 with several column blocks)
+                           // (0: 128 for FP64 values with several column blocks, else 64)
   int sell_long = 0;       // longer rows: fewest lanes keeping a slice this many steps wide (0: as short)
   int sell_sigma = 16384;  // window of consecutive rows sorted together
   int sell_unroll = 0;     // steps per lane in flight (0: 8)
