@@ -66,7 +66,7 @@ struct tbsla_batch {
   int lprec = TBSLA_F64;
   short *ldelta = nullptr, *tdelta = nullptr;  // ELL form (lslots > 0)
   int lslots = 0, tslots = 0;
-  float *rf = nullptr, *tf = nullptr;
+  float *rf = nullptr, *tf = nullptr, *zf = nullptr;
   double *b = nullptr, *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
   double* scal = nullptr;
   int *status = nullptr, *iters = nullptr;
@@ -80,7 +80,7 @@ struct tbsla_batch {
     if (graph) cudaGraphExecDestroy(graph);
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
                   scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf,
-                  ldelta, tdelta};
+                  ldelta, tdelta, zf};
     for (void* v : ps)
       if (v) cudaFree(v);
     if (vals && vals != vals64) cudaFree(vals);
@@ -118,6 +118,7 @@ struct tbsla_batch {
     c.lslots = f ? lslots : 0;
     c.tslots = f ? tslots : 0;
     c.rf = f ? rf : nullptr;
+    c.zf = f ? zf : nullptr;
     c.tf = f ? tf : nullptr;
     c.b = b;
     c.x = x;
@@ -347,11 +348,11 @@ int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int ns
   cudaSetDevice(B->device);
   cudaStream_t st = B->stream;
   for (void* p : {(void*)B->lrowptr, (void*)B->lcolidx, (void*)B->trowptr, (void*)B->tcolidx, B->lvals, B->tvals,
-                  (void*)B->rf, (void*)B->tf, (void*)B->ldelta, (void*)B->tdelta})
+                  (void*)B->rf, (void*)B->tf, (void*)B->zf, (void*)B->ldelta, (void*)B->tdelta})
     if (p) cudaFree(p);
   B->lrowptr = B->lcolidx = B->trowptr = B->tcolidx = nullptr;
   B->lvals = B->tvals = nullptr;
-  B->rf = B->tf = nullptr;
+  B->rf = B->tf = B->zf = nullptr;
   B->ldelta = B->tdelta = nullptr;
   B->lslots = B->tslots = 0;
   double* tmp = nullptr;
@@ -359,6 +360,7 @@ int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int ns
   B->lprec = precision;
   CK(alloc(&B->rf, B->n));
   CK(alloc(&B->tf, B->n));
+  CK(alloc(&B->zf, B->n));
   if (use_ell) {
     const size_t nle = lv.size(), nte = tv.size();
     CK(alloc(&B->ldelta, nle));

@@ -138,9 +138,13 @@ __global__ void __launch_bounds__(NT) k_cg_direction(CgBatch c) {
   const int sys = c.chunk_sys[ch];
   if (c.status[sys] != kActive) return;
   const double beta = c.beta[sys];
-  const double* z = c.z;
   const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
-  for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = fma_rn(beta, c.p[i], z[i]);
+  if (c.zf) {
+    for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = fma_rn(beta, c.p[i], (double)c.zf[i]);
+  } else {
+    const double* z = c.z;
+    for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = fma_rn(beta, c.p[i], z[i]);
+  }
 }
 
 // Zero the true-residual accumulators of the masked systems.
@@ -175,9 +179,13 @@ __global__ void __launch_bounds__(NT) k_cg_restart(CgBatch c, int all) {
   const int ch = blockIdx.x;
   const int sys = c.chunk_sys[ch];
   if (!all && c.status[sys] != kRestart) return;
-  const double* z = c.z;
   const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
-  for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = z[i];
+  if (c.zf) {
+    for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = (double)c.zf[i];
+  } else {
+    const double* z = c.z;
+    for (int i = r0 + threadIdx.x; i < r1; i += NT) c.p[i] = z[i];
+  }
 }
 
 __device__ __forceinline__ float to_f32(double v) { return (float)v; }
@@ -199,7 +207,7 @@ __global__ void __launch_bounds__(NT) k_cg_factor_t(CgBatch c, int mask) {
   }
 }
 
-// z = L tf (FP32 arithmetic, stored in FP64) and acc[sys] += r . z (FP64).
+// z = L tf (FP32 arithmetic, stored in FP32: zf) and acc[sys] += r . z (FP64).
 template <class V>
 __global__ void __launch_bounds__(NT) k_cg_factor_l(CgBatch c, int mask, double* acc) {
   __shared__ double red_s[NT / kWarp];
@@ -213,7 +221,7 @@ __global__ void __launch_bounds__(NT) k_cg_factor_l(CgBatch c, int mask, double*
     float s = 0.f;
     for (int k = c.lrowptr[i]; k < c.lrowptr[i + 1]; k++) s = fmaf(to_f32(v[k]), c.tf[c.lcolidx[k]], s);
     const double zi = widen(s);
-    c.z[i] = zi;
+    c.zf[i] = s;
     d = fma_rn(c.r[i], zi, d);
   }
   d = block_sum<NT>(d, red_s);
@@ -268,9 +276,9 @@ __global__ void __launch_bounds__(NT) k_cg_factor_l_ell(CgBatch c, int mask, dou
   const int K = c.lslots, r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
   double d = 0;
   for (int i = r0 + threadIdx.x; i < r1; i += NT) {
-    const double zi = widen(ell_row<V, KMAX>(v, c.ldelta, c.tf, c.n, K, i));
-    c.z[i] = zi;
-    d = fma_rn(c.r[i], zi, d);
+    const float zs = ell_row<V, KMAX>(v, c.ldelta, c.tf, c.n, K, i);
+    c.zf[i] = zs;
+    d = fma_rn(c.r[i], widen(zs), d);
   }
   d = block_sum<NT>(d, red_s);
   if (threadIdx.x == 0) atomicAdd(acc + sys, d);

@@ -208,6 +208,7 @@ struct CgBatch {
   const short *ldelta, *tdelta;
   int lslots, tslots;
   float *rf, *tf;  // set for a factored run
+  float* zf;       // factored run: z in FP32 (computed in FP32, so exactly)
   const double* b;
   double *x, *r, *z, *p, *q;  // z == r when unpreconditioned
   // per-system scalars (rrt: squared FP64 true residual of the last check)
