@@ -219,6 +219,50 @@ def cpu_reference_time(arrays, x, n, nnz, seconds: float, reps_min: int = 2, rep
     return kind, times, y
 
 
+def gather_ceiling(m, x, s, flush, ms_spmv: float, warmup: int) -> dict:
+    """The x-gather part of the SpMV alone, as a measured ceiling for its
+    access pattern: torch.index_select (a library gather kernel) over the
+    matrix's own column indices, one column block of 2^23 columns at a time
+    as the sliced-ELL launches walk them, L2 flushed before each block, CUDA
+    events.  It moves an index (4 B) in and an entry (8 B) out per gather,
+    where the SpMV streams a value and a column (12 B) per entry."""
+    import numpy as np
+    import torch
+
+    a = m.arrays()
+    rp, ci = a["rowptr"], a["colidx"]
+    nnz = int(rp[-1])
+    xt = torch.from_numpy(x).cuda()
+    cb = 8388608
+    blocks = []
+    for lo in range(0, len(x), cb):
+        c = ci[:nnz]
+        sel = c[(c >= lo) & (c < lo + cb)]
+        blocks.append(torch.from_numpy(np.ascontiguousarray(sel)).cuda())
+    outs = [torch.empty(len(b), dtype=torch.float64, device="cuda") for b in blocks]
+    torch.cuda.synchronize()
+    times = []
+    with torch.cuda.stream(s):
+        for rep in range(warmup + 3):
+            t = 0.0
+            for b, o in zip(blocks, outs):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                torch.index_select(xt, 0, b, out=o)
+                e1.record(s)
+                s.synchronize()
+                t += e0.elapsed_time(e1)
+            if rep >= warmup:
+                times.append(t)
+    ms = statistics.median(times)
+    del blocks, outs
+    torch.cuda.empty_cache()
+    return {"gathers": nnz, "ms": ms, "gathers_per_s": nnz / (ms * 1e-3),
+            "spmv_gathers_per_s": nnz / (ms_spmv * 1e-3), "spmv_fraction_of_ceiling": ms / ms_spmv,
+            "kernel": "torch.index_select over the column indices, per column block, L2 flushed"}
+
+
 def run_ours(a):
     import ctypes as C
 
@@ -317,6 +361,8 @@ def run_ours(a):
     extra = {"gflops": 2 * nnz / (ms_step * 1e-3) / 1e9, "gen_s": round(t_gen, 2), "upload_s": round(t_up, 2),
              "step_ms_min": min(step_ms), "step_ms_max": max(step_ms),
              "device_bytes": m.device_bytes()}
+    if a.algo == "sell" and a.prec == "f64" and ws == 1:
+        extra["gather_ceiling"] = gather_ceiling(m, x, s, flush, ms_step, a.warmup)
     if not a.no_forms and a.prec == "f64":
         for name, pv, sv in (("f32", T.F32, 4), ("bf16", T.BF16, 2)):
             m.set_precision(pv)
