@@ -177,14 +177,16 @@ int tbsla_matrix_kernel_launches(const tbsla_matrix* m, int* launches);
 /* CSR: block budget of the row-block partition (nnz per block, multiple of
  * 256, default 2048); changing it rebuilds the partition. */
 int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block);
-/* CSR SpMV kernel: TBSLA_CSR_SELL (default; sliced-ELL device layout,
- * slices of 32 lanes over rows of similar length, see
- * tbsla_matrix_set_sell_params; `items` = steps per lane in flight, 4/8/16,
- * 0 = 8), TBSLA_CSR_MERGE (merge-path split,
+/* CSR SpMV kernel: TBSLA_CSR_AUTO (default: row blocks below 2^19 stored
+ * entries, where one short launch is latency-bound, else sliced ELL),
+ * TBSLA_CSR_SELL (sliced-ELL device layout, slices of 32 lanes over rows of
+ * similar length, see tbsla_matrix_set_sell_params; `items` = steps per
+ * lane in flight, 4/8/16, 0 = 8), TBSLA_CSR_MERGE (merge-path split,
  * `items` row ends + entries per thread, 4/8/16, 0 = 8) or
  * TBSLA_CSR_ROWBLOCK (row-block adaptive, see
  * tbsla_matrix_set_csr_tile; `items` unused).  Changing the kernel or the
  * merge split rebuilds the device copy. */
+#define TBSLA_CSR_AUTO (-1)
 #define TBSLA_CSR_MERGE 0
 #define TBSLA_CSR_ROWBLOCK 1
 #define TBSLA_CSR_SELL 2

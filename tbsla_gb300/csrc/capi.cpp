@@ -313,7 +313,7 @@ int tbsla_matrix_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_t
 }
 
 int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items) {
-  if (!m || algorithm < TBSLA_CSR_MERGE || algorithm > TBSLA_CSR_SELL ||
+  if (!m || algorithm < TBSLA_CSR_AUTO || algorithm > TBSLA_CSR_SELL ||
       (algorithm != TBSLA_CSR_ROWBLOCK && items != 0 && items != 4 && items != 8 && items != 16))
     return TBSLA_ERR_INVALID_ARG;
   if (algorithm == TBSLA_CSR_MERGE && items == 0) items = 8;

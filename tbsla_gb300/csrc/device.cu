@@ -398,9 +398,13 @@ int build(const tbsla_matrix* m, DeviceMatrix* d) {
       delete[] blocks;
       if (st) return st;
       // merge-path tiles and their carry scratch
-      d->algo = m->csr_algo;
-      d->merge_items = m->merge_items;
       const long enz = end - rp[0];
+      // automatic kernel: row blocks for small matrices, whose SpMV is one
+      // short launch where the sliced-ELL kernel's chain of dependent loads
+      // per slice shows (10^5 entries: 6.2 against 10.3 us); the sliced-ELL
+      // kernel from 2^19 entries on (10^7: 48 against 107 us)
+      d->algo = m->csr_algo >= 0 ? m->csr_algo : (enz < (1L << 19) ? TBSLA_CSR_ROWBLOCK : TBSLA_CSR_SELL);
+      d->merge_items = m->merge_items;
       d->ntiles = merge_tiles(I.ln_row, enz, d->merge_items);
       if ((st = dalloc(&d->coord, (size_t)d->ntiles + 1)) || (st = dalloc(&d->carry_row, (size_t)d->ntiles)) ||
           (st = dalloc(&d->carry_val, (size_t)d->ntiles)))

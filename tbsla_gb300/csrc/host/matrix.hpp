@@ -55,7 +55,7 @@ struct tbsla_matrix {
   tbsla_impl::Buf<int> idx0, idx1;
   int precision = TBSLA_F64;
   int csr_tile = 2048;     // row-block budget (entries per block)
-  int csr_algo = 2;        // 0: merge path, 1: row blocks, 2: sliced ELL (default)
+  int csr_algo = -1;       // -1: automatic (default), 0: merge path, 1: row blocks, 2: sliced ELL
   int merge_items = 8;     // merge path: items per thread
   int sell_short = 0;      // sliced ELL: rows up to this length, one lane each, sorted per window
                            // (0: 128 for FP64 values with several column blocks, else 64)

@@ -256,7 +256,7 @@ class MatrixCSR(Matrix):
     def set_tile(self, nnz_per_block: int):
         check(lib.tbsla_matrix_set_csr_tile(self._h, nnz_per_block), "set_csr_tile")
 
-    MERGE, ROWBLOCK, SELL = 0, 1, 2
+    AUTO, MERGE, ROWBLOCK, SELL = -1, 0, 1, 2
 
     def set_algorithm(self, algorithm: int, items: int = 0):
         check(lib.tbsla_matrix_set_csr_algorithm(self._h, algorithm, items), "set_csr_algorithm")

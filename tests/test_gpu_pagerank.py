@@ -60,6 +60,7 @@ def test_pagerank_with_column_blocks(gpu):
     g = graph(T, n, seed=6)
     g.make_stochastic(np.zeros(n))
     g.set_precision(T.F32)
+    g.set_algorithm(g.SELL)
     x1, it1, _, ok1 = g.page_rank(0.85, 1e-10, 500)
     g.set_sell_params(64, 64, 16384, 9000)  # four column blocks, the last in two row parts
     assert g.kernel_launches() == 3 + 2

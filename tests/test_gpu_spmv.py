@@ -295,6 +295,7 @@ def test_host_entry_with_column_blocks_equals_device_entry(gpu):
     T = gpu
     n = 1 << 17
     m = powerlaw(T, n, seed=12)
+    m.set_algorithm(m.SELL)
     for cb in (70000, 20000):
         m.set_sell_params(64, 64, 16384, cb)
         xt = torch.from_numpy(T.fill_uniform(n, -1.0, 1.0, cb)).cuda()
@@ -338,6 +339,7 @@ def test_column_blocks_with_empty_parts(gpu):
         ci = np.array(cols, np.int32)
         va = rng.uniform(-1, 1, len(ci))
         m = T.MatrixCSR.from_arrays(n, n, rp, ci, va)
+        m.set_algorithm(m.SELL)
         m.set_sell_params(64, 64, 16384, 40_000)  # blocks [0, 40000), [40000, n)
         x = rng.uniform(0, 1, n)
         ref = oracle.csr_ax(rp, ci, va, x)

@@ -191,6 +191,13 @@ def test_bad_arguments():
         T.MatrixCOO().fill_powerlaw if False else T.MatrixDENSE().fill_dense_uniform(0, 4, 1)
     h = C.c_void_p()
     assert T.lib.tbsla_matrix_create(C.byref(h), 7) == L.ERR_INVALID_ARG
+    # CSR kernel: -1 (automatic) .. 2
+    m = T.MatrixCSR()
+    for algo in (m.AUTO, m.MERGE, m.ROWBLOCK, m.SELL):
+        m.set_algorithm(algo)
+    for bad in (-2, 3):
+        with pytest.raises(T.TbslaError):
+            m.set_algorithm(bad)
     # sliced-ELL thresholds: 0 (automatic) .. 255; negative rejected
     m = T.MatrixCSR()
     m.set_sell_params(0, 0, 16384, 0)
