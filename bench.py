@@ -407,7 +407,8 @@ def run_ours(a):
                    "work_split": {"merge": f"{a.items} items/thread", "rowblock": f"{a.tile} nnz/block",
                                   "sell": f"one lane per row <= {a.sell.split(',')[0] if a.sell.split(',')[0] != '0' else 'auto (128 for FP64 with column blocks, else 64)'} sorted per "
                                           f"{a.sell.split(',')[2]}-row window, else 2..32 lanes per row, slices "
-                                          f"<= {a.sell.split(',')[1]} steps; {a.items or 'automatic'} steps/lane in flight; "
+                                          f"<= {a.sell.split(',')[1] if a.sell.split(',')[1] != '0' else 'the same'} steps; "
+                                          f"{a.items or 'automatic'} steps/lane in flight; "
                                           f"column blocks of {int(a.sell.split(',')[3]) or 8388608} columns"}[a.algo],
                    "l2": "flushed (256 MB write) between steps; inputs 3.2+ GB > L2",
                    "parallelism": f"replicas x{ws}"},
