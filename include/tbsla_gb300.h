@@ -232,6 +232,13 @@ int tbsla_matrix_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_t
 int tbsla_Ax(const tbsla_matrix* m, double* r, const double* v, int vect_incr);
 /* r <- A v into a zero-filled r (the reference returns a new[] array). */
 int tbsla_spmv(const tbsla_matrix* m, double* r, const double* v, int vect_incr);
+/* The same on device pointers r and v, enqueued on `stream` (a
+ * cudaStream_t; NULL = the handle's own stream) and not waited for.  Work the
+ * call forks onto the handle's internal streams (the second row part of a
+ * blocked sliced-ELL layout) is joined back into `stream` before it returns,
+ * so everything enqueued on `stream` afterwards sees r complete.  One call
+ * at a time per handle: the internal streams, events and work counters are
+ * the handle's. */
 int tbsla_Ax_device(const tbsla_matrix* m, double* r, const double* v, int vect_incr,
                     void* stream);
 int tbsla_spmv_device(const tbsla_matrix* m, double* r, const double* v, int vect_incr,
