@@ -666,6 +666,7 @@ def run_pagerank(a):
         "cpu_baseline": {"value": b_it * ito / to / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
                          "sample": f"oracle PageRank, {ito} iterations on the same FP32-rounded graph"},
         "batched": {"nvec": 32, "iterations": itb, "converged": bool(okb), "ms": tb * 1e3,
+                    "arithmetic": "double-float (float pairs) products and sums (compensated, Dot2), FP64 reductions",
                     "GB/s": b_itb * itb / tb / 1e9, "bytes_per_iteration": b_itb},
         "clocks": clocks, "gpu_launches": it,
     }

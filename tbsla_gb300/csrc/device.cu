@@ -1063,16 +1063,20 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   const int n = I.n_row;
   const size_t nn = (size_t)n * nvec;
   cudaStream_t s = d->stream;
-  double *X0 = nullptr, *X1 = nullptr, *T = nullptr, *coef = nullptr;
+  // FP32 / BF16 values: the iterates, teleport vectors and column sums in
+  // double-float (float pairs, the bytes of FP64), products and sums on the
+  // FP32 pipe; FP64 values keep FP64 arithmetic
+  const bool df = d->prec != TBSLA_F64;
+  double *X0 = nullptr, *X1 = nullptr, *T = nullptr, *coef = nullptr, *W = nullptr;
   int* flags = nullptr;
   int grid = csr_pagerank_batched_grid(d->prec);
   auto cleanup = [&]() {
-    for (void* p : {(void*)X0, (void*)X1, (void*)T, (void*)coef, (void*)flags})
+    for (void* p : {(void*)X0, (void*)X1, (void*)T, (void*)coef, (void*)flags, (void*)W})
       if (p) cudaFree(p);
   };
   if ((st = dalloc(&X0, nn)) || (st = dalloc(&X1, nn)) || (st = dalloc(&T, nn)) ||
       (st = dalloc(&coef, 128)) || (st = dalloc(&flags, 2)) || (st = d->ctl(96, grid)) ||
-      (st = column_weights(m, d))) {
+      (st = column_weights(m, d)) || (df && (st = dalloc(&W, (size_t)n)))) {
     cleanup();
     return st;
   }
@@ -1088,6 +1092,11 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   cudaMemcpyAsync(T, tele, nn * 8, cudaMemcpyHostToDevice, s);
   cudaMemcpyAsync(coef, c0.data(), 64 * 8, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
+  if (df && ((st = status_of(f64_to_df(X0, X0, (long)nn, s))) || (st = status_of(f64_to_df(T, T, (long)nn, s))) ||
+             (st = status_of(f64_to_df(d->colw, W, (long)n, s))))) {
+    cleanup();
+    return st;
+  }
   CsrArgs a = csr_args(m, d);
   PageRankArgs p{beta, (double)n, eps, nullptr, d->colw, coef, coef + 64, flags, flags + 1};
   Ctl ctl{d->counter, d->partials, d->result};
@@ -1098,7 +1107,8 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
       const bool even = (launched % 2) == 0;
       p.coef_in = coef + (even ? 0 : 64);
       p.coef_out = coef + (even ? 64 : 0);
-      cudaError_t e = csr_pagerank_batched_step(a, n, nvec, even ? X0 : X1, even ? X1 : X0, T, p, ctl, grid, s);
+      cudaError_t e = df ? csr_pagerank_batched_df_step(a, nvec, even ? X0 : X1, even ? X1 : X0, T, W, p, ctl, grid, s)
+                         : csr_pagerank_batched_step(a, n, nvec, even ? X0 : X1, even ? X1 : X0, T, p, ctl, grid, s);
       if (e != cudaSuccess) {
         cleanup();
         return status_of(e);
@@ -1112,6 +1122,14 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   }
   const int iters = hflags[1];
   double* fin = (iters % 2 == 1) ? X1 : X0;
+  if (df) {  // to FP64 in the other iterate's storage
+    double* out = (iters % 2 == 1) ? X0 : X1;
+    if ((st = status_of(df_to_f64(fin, out, (long)nn, s)))) {
+      cleanup();
+      return st;
+    }
+    fin = out;
+  }
   double* sums = d->result + 128;
   st = status_of(mat_colsum(fin, n, nvec, d->partials, sums, s));
   if (!st) st = status_of(mat_scale_cols(fin, n, nvec, sums, s));

@@ -161,6 +161,15 @@ cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
 // result[k] = L1 change, result[nvec + k] = S', result[2 nvec + k] = M';
 // the last CTA writes coef_out[k], coef_out[32 + k] and sets *done when
 // every column's change is < eps.
+// The same in double-float (pairs of floats h + l, about 46 bits) for FP32 /
+// BF16 values: X, Y, T (n x nvec) and W (the column sums, n) are float2
+// arrays of the same byte size as FP64 ones; reductions are FP64.
+cudaError_t csr_pagerank_batched_df_step(const CsrArgs& a, int nvec, const void* X, void* Y, const void* T,
+                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s);
+// FP64 <-> double-float (float2) conversions, element by element (the
+// destination may be the source's own storage).
+cudaError_t f64_to_df(const double* src, void* dst, long n, cudaStream_t s);
+cudaError_t df_to_f64(const void* src, double* dst, long n, cudaStream_t s);
 cudaError_t csr_pagerank_batched_step(const CsrArgs& a, int n_row, int nvec, const double* X,
                                       double* Y, const double* T, const PageRankArgs& p,
                                       Ctl ctl, int grid, cudaStream_t s);

@@ -131,6 +131,196 @@ __global__ void __launch_bounds__(NT) k_pagerank_epilogue(const double* __restri
   });
 }
 
+// The end of a batched PageRank step: per-column CTA sums over warps (in
+// warp order), per-CTA partials, and the last CTA's sums in CTA order
+// (deterministic), coefficients of the next step and the done flag.
+__device__ __forceinline__ void batched_finish(double err, double sum, double dsum, int nvec,
+                                               double (*s_red)[3 * kWarp], Smem& sm, const PageRankArgs& p,
+                                               Ctl ctl) {
+  const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  s_red[warp][lane] = err;
+  s_red[warp][kWarp + lane] = sum;
+  s_red[warp][2 * kWarp + lane] = dsum;
+  __syncthreads();
+  if (threadIdx.x < 3 * kWarp) {
+    double acc = 0;
+    for (int w = 0; w < NT / kWarp; w++) acc = add_rn(acc, s_red[w][threadIdx.x]);
+    ctl.partials[(size_t)blockIdx.x * 3 * kWarp + threadIdx.x] = acc;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned t = atomicAdd(ctl.counter + 1, 1u);
+    sm.flag = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!sm.flag) return;
+  __threadfence();
+  if (threadIdx.x < 3 * kWarp) {
+    double acc = 0;
+#pragma unroll 8
+    for (int i = 0; i < (int)gridDim.x; i++)
+      acc = add_rn(acc, __ldcg(ctl.partials + (size_t)i * 3 * kWarp + threadIdx.x));
+    s_red[0][threadIdx.x] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int all = 1;
+    for (int k = 0; k < nvec; k++) {
+      const double e = s_red[0][k], sm_ = s_red[0][kWarp + k], d = s_red[0][2 * kWarp + k];
+      ctl.result[k] = e;
+      ctl.result[nvec + k] = sm_;
+      ctl.result[2 * nvec + k] = d;
+      const double s1 = 1.0 / sm_;
+      p.coef_out[k] = s1;
+      p.coef_out[kWarp + k] = teleport_weight(p.beta, s1, d);
+      if (!(e < p.eps)) all = 0;
+    }
+    *p.iters += 1;
+    if (all) *p.done = 1;
+    ctl.counter[0] = 0;
+    ctl.counter[1] = 0;
+    __threadfence();
+  }
+}
+
+
+// Double-float arithmetic: a value is the unevaluated sum h + l of two
+// floats (about 46 significant bits; Dekker 1971, TwoSum after Knuth).  The
+// batched PageRank with FP32 / BF16 values uses it: its FP64 multiply-adds
+// held GB300's narrow FP64 pipe 80% busy, and FP32 runs 64 times faster.
+// Every step is a round-to-nearest intrinsic, so nothing is contracted or
+// reassociated.
+struct DF {
+  float h, l;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  DF s = two_sum(a.h, b.h);
+  const DF t = two_sum(a.l, b.l);
+  s = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
+  return fast_two_sum(s.h, __fadd_rn(s.l, t.l));
+}
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float pr = __fmul_rn(a.h, b.h);
+  const float e = __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.l, __fmaf_rn(a.h, b.h, -pr)));
+  return fast_two_sum(pr, e);
+}
+// One term of a compensated dot product (Ogita, Rump and Oishi 2005,
+// Dot2): sum s plus error c gathers a (xh + xl), with the product's and the
+// sum's rounding errors carried exactly into c; the row's value is s + c.
+__device__ __forceinline__ void dot2_step(float& s, float& c, float a, DF x) {
+  const float pr = __fmul_rn(a, x.h);
+  const float e1 = __fmaf_rn(a, x.h, -pr);
+  const DF t = two_sum(s, pr);
+  s = t.h;
+  c = __fmaf_rn(a, x.l, __fadd_rn(c, __fadd_rn(e1, t.l)));
+}
+__device__ __forceinline__ DF df_neg(DF a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ DF df_of(double d) {
+  const float h = __double2float_rn(d);
+  return {h, __double2float_rn(d - (double)h)};
+}
+__device__ __forceinline__ double df_val(DF a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ DF df_ld(const float2* p) {
+  const float2 v = *p;
+  return {v.x, v.y};
+}
+__device__ __forceinline__ float as_f32(float v) { return v; }
+__device__ __forceinline__ float as_f32(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// The batched step in double-float, for FP32 / BF16 values (exact in one
+// float): X, Y, T and the column sums w are stored as float pairs; each
+// lane sums its row's products a_ij X[j, k] in entry order as a compensated
+// dot product (Dot2: about twice FP32 precision), and the epilogue forms the single-vector epilogue's quantities (y = beta s acc +
+// t T, |y - x s|, y, w y) in the same arithmetic.  The CTA and grid
+// reductions run in FP64 (batched_finish).
+template <class V>
+__global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int nvec, const float2* __restrict__ X,
+                                                               float2* __restrict__ Y, const float2* __restrict__ T,
+                                                               const float2* __restrict__ W, PageRankArgs p,
+                                                               Ctl ctl) {
+  __shared__ Smem sm;
+  __shared__ double s_red[NT / kWarp][3 * kWarp];
+  if (*(volatile int*)p.done) return;
+  const uint64_t pol = policy_evict_first();
+  const V* vals = static_cast<const V*>(a.vals);
+  const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
+  const bool active = lane < nvec;
+  const double scd = active ? p.coef_in[lane] : 0.0;
+  const DF sc = df_of(scd), tc = df_of(active ? p.coef_in[kWarp + lane] : 0.0), bsc = df_of(mul_rn(p.beta, scd));
+  DF err{0.f, 0.f}, sum{0.f, 0.f}, dsum{0.f, 0.f};
+  for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm)) {
+    const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
+    for (int row = r0 + warp; row < r1; row += NT / kWarp) {
+      const int s = a.rowptr[row], e = a.rowptr[row + 1];
+      float as = 0.f, ac = 0.f;  // compensated sum of the row's products
+      for (int base = s; base < e; base += kWarp) {
+        const int j = base + lane;
+        int c = 0;
+        float v = 0.f;
+        if (j < e) {
+          c = ld_stream(a.colidx + j, pol);
+          v = as_f32(ld_stream(vals + j, pol));
+        }
+        const int m = min(kWarp, e - base);
+        // 8 entries' gathers of X in flight, then their products added in
+        // entry order; a short tail runs as a masked batch (a dead slot adds
+        // 0 * 0, which leaves s and c as they are), so a row of a few
+        // entries waits for one gather latency, not one per entry
+        for (int t = 0; t < m; t += 8) {
+          DF xv[8];
+          float vv[8];
+#pragma unroll
+          for (int u = 0; u < 8; u++) {
+            const bool live = t + u < m;
+            const int ct = __shfl_sync(0xffffffffu, c, (t + u) & (kWarp - 1));
+            const float vu = __shfl_sync(0xffffffffu, v, (t + u) & (kWarp - 1));
+            vv[u] = live ? vu : 0.f;
+            xv[u] = (active && live) ? df_ld(X + (size_t)(ct - a.f_col) * nvec + lane) : DF{0.f, 0.f};
+          }
+#pragma unroll
+          for (int u = 0; u < 8; u++) dot2_step(as, ac, vv[u], xv[u]);
+        }
+      }
+      if (active) {
+        const DF acc = fast_two_sum(as, ac);
+        const size_t o = (size_t)row * nvec + lane;
+        const DF yn = df_add(df_mul(bsc, acc), df_mul(tc, df_ld(T + o)));
+        DF dx = df_add(yn, df_neg(df_mul(df_ld(X + o), sc)));
+        if (dx.h < 0) dx = df_neg(dx);
+        err = df_add(err, dx);
+        sum = df_add(sum, yn);
+        dsum = df_add(dsum, df_mul(df_ld(W + row), yn));
+        Y[o] = make_float2(yn.h, yn.l);
+      }
+    }
+  }
+  batched_finish(df_val(err), df_val(sum), df_val(dsum), nvec, s_red, sm, p, ctl);
+}
+
+__global__ void k_f64_to_df(const double* src, float2* dst, long n) {  // may run in place
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const DF v = df_of(src[i]);
+    dst[i] = make_float2(v.h, v.l);
+  }
+}
+
+__global__ void k_df_to_f64(const float2* src, double* dst, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const float2 v = src[i];
+    dst[i] = (double)v.x + (double)v.y;
+  }
+}
+
 // Batched personalised PageRank: lanes of a warp are the nvec vectors; the
 // warps of the CTA take the rows of a block in turn.  Each lane sums its
 // row's products in entry order.
@@ -197,51 +387,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
       }
     }
   }
-  // per-column CTA sums over warps, in warp order
-  s_red[warp][lane] = err;
-  s_red[warp][kWarp + lane] = sum;
-  s_red[warp][2 * kWarp + lane] = dsum;
-  __syncthreads();
-  if (threadIdx.x < 3 * kWarp) {
-    double acc = 0;
-    for (int w = 0; w < NT / kWarp; w++) acc = add_rn(acc, s_red[w][threadIdx.x]);
-    ctl.partials[(size_t)blockIdx.x * 3 * kWarp + threadIdx.x] = acc;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned t = atomicAdd(ctl.counter + 1, 1u);
-    sm.flag = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!sm.flag) return;
-  __threadfence();
-  if (threadIdx.x < 3 * kWarp) {
-    double acc = 0;
-#pragma unroll 8
-    for (int i = 0; i < (int)gridDim.x; i++)
-      acc = add_rn(acc, __ldcg(ctl.partials + (size_t)i * 3 * kWarp + threadIdx.x));
-    s_red[0][threadIdx.x] = acc;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int all = 1;
-    for (int k = 0; k < nvec; k++) {
-      const double e = s_red[0][k], sm_ = s_red[0][kWarp + k], d = s_red[0][2 * kWarp + k];
-      ctl.result[k] = e;
-      ctl.result[nvec + k] = sm_;
-      ctl.result[2 * nvec + k] = d;
-      const double s1 = 1.0 / sm_;
-      p.coef_out[k] = s1;
-      p.coef_out[kWarp + k] = teleport_weight(p.beta, s1, d);
-      if (!(e < p.eps)) all = 0;
-    }
-    *p.iters += 1;
-    if (all) *p.done = 1;
-    ctl.counter[0] = 0;
-    ctl.counter[1] = 0;
-    __threadfence();
-  }
+  batched_finish(err, sum, dsum, nvec, s_red, sm, p, ctl);
 }
 
 template <class K>
@@ -344,10 +490,37 @@ int csr_pagerank_grid(int items, int prec) {
 int csr_pagerank_batched_grid(int prec) {
   switch (prec) {
     case kF64: return resident_grid(k_csr_pagerank_batched<double>);
-    case kF32: return resident_grid(k_csr_pagerank_batched<float>);
-    case kBF16: return resident_grid(k_csr_pagerank_batched<__nv_bfloat16>);
+    case kF32: return resident_grid(k_csr_pagerank_batched_df<float>);
+    case kBF16: return resident_grid(k_csr_pagerank_batched_df<__nv_bfloat16>);
   }
   return 152;
+}
+
+cudaError_t csr_pagerank_batched_df_step(const CsrArgs& a, int nvec, const void* X, void* Y, const void* T,
+                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s) {
+  if (nvec < 1 || nvec > kWarp) return cudaErrorInvalidValue;
+  const float2 *x = static_cast<const float2*>(X), *t = static_cast<const float2*>(T),
+               *w = static_cast<const float2*>(W);
+  float2* y = static_cast<float2*>(Y);
+  switch (a.prec) {
+    case kF32: k_csr_pagerank_batched_df<float><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
+    case kBF16: k_csr_pagerank_batched_df<__nv_bfloat16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t f64_to_df(const double* src, void* dst, long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_f64_to_df<<<(int)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, s>>>(src, static_cast<float2*>(dst), n);
+  return cudaGetLastError();
+}
+
+cudaError_t df_to_f64(const void* src, double* dst, long n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_df_to_f64<<<(int)std::min<long>((n + 255) / 256, 152L * 16), 256, 0, s>>>(static_cast<const float2*>(src), dst,
+                                                                           n);
+  return cudaGetLastError();
 }
 
 cudaError_t csr_spmv(const CsrArgs& a, const double* x, double* y, cudaStream_t s) {
