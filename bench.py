@@ -35,6 +35,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+SMS = 152  # GB300 streaming multiprocessors
 METRIC = "SpMV HBM GB/s (% peak); CG time-to-1e-8 residual: learned vs Jacobi PCG, 1 GB300"
 PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "csr_spmv_powerlaw_n16M_fp64.md")
 
@@ -45,9 +46,10 @@ def parse_args():
     p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["spmv", "small", "pagerank", "cg", "learned"], default="spmv",
+    p.add_argument("--workload", choices=["spmv", "small", "formats", "pagerank", "cg", "learned"], default="spmv",
                    help="spmv: the large-SpMV headline; small: the 10^4-row matrix in every format and the "
-                        "2000^2 DENSE GEMV; pagerank: the PageRank graph; cg: batched CG; "
+                        "2000^2 DENSE GEMV; formats: every format at n = 2^22 rows and a 32768 x 16384 DENSE "
+                        "GEMV; pagerank: the PageRank graph; cg: batched CG; "
                         "learned: learned-preconditioner PCG against Jacobi-PCG")
     p.add_argument("--train-systems", type=int, default=2000, help="learned: training systems (seeds 1000..)")
     p.add_argument("--epochs", type=int, default=1, help="learned: passes over the training systems")
@@ -55,7 +57,8 @@ def parse_args():
     p.add_argument("--eval-n", type=int, default=128, help="learned: held-out grid size n (n^3 unknowns)")
     p.add_argument("--factor-prec", choices=["f32", "bf16"], default="bf16",
                    help="learned: storage precision of the factor L")
-    p.add_argument("--n", type=int, default=None, help="rows (spmv: 2^24, pagerank: 2^22)")
+    p.add_argument("--n", type=int, default=None, help="rows (spmv: 2^24, pagerank and formats: 2^22)")
+    p.add_argument("--formats", type=str, default="coo,scoo,csr,ell,dense", help="formats: which formats to run")
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
     p.add_argument("--algo", choices=["sell", "merge", "rowblock"], default="sell")
@@ -71,7 +74,7 @@ def parse_args():
     a = p.parse_args()
     a.warmup = max(a.warmup, 3)
     if a.n is None:
-        a.n = 1 << 22 if a.workload == "pagerank" else 1 << 24
+        a.n = 1 << 22 if a.workload in ("pagerank", "formats") else 1 << 24
     return a
 
 
@@ -595,6 +598,164 @@ def run_small(a):
         print(json.dumps(line), flush=True)
 
 
+def run_formats(a):
+    """Every format past L2: the reference's row recipe (column i plus 9
+    uniform columns per row, U[-1,1) values, x U[0,1), seed 0) at n = 2^22
+    rows (41.9 M entries; x = 32 MiB stays in L2 once read, so each kernel
+    streams its own arrays) as COO, SCOO, CSR and ELL, and a 32768 x 16384
+    DENSE GEMV (4.3 GB), all FP64.  Per format: device time per Ax (CUDA
+    events on the launching stream, L2 flushed before each step, median),
+    algorithmic bytes / time against the measured HBM copy bandwidth, and a
+    host call through tbsla_Ax with pinned buffers (x in, y out).  CPU
+    baseline: the oracle's loop for each format (CSR on all host threads,
+    the others on one)."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import oracle
+    import tbsla_gb300 as T
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    T.device_init(local)
+    want = [f.strip().upper() for f in a.formats.split(",")]
+    n = a.n
+    dm, dk = 32768, 16384
+    csr = T.MatrixCSR()
+    csr.fill_uniform_rows(n, 10, 0)
+    a0 = csr.arrays()
+    nnz = int(a0["rowptr"][-1])
+    x = T.fill_uniform(n, 0.0, 1.0, 0)
+    rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(a0["rowptr"]))
+    builders = {
+        "COO": lambda: T.MatrixCOO.from_arrays(n, n, rows, a0["colidx"], a0["values"]),
+        "SCOO": lambda: T.MatrixSCOO(T.MatrixCOO.from_arrays(n, n, rows, a0["colidx"], a0["values"])),
+        "CSR": lambda: csr,
+        "ELL": lambda: T.MatrixELL(T.MatrixCOO.from_arrays(n, n, rows, a0["colidx"], a0["values"])),
+    }
+    # algorithmic bytes per Ax: the stored arrays once, x once, y once
+    sparse_bytes = {"COO": nnz * 16 + 16 * n, "SCOO": nnz * 16 + 16 * n,
+                    "CSR": nnz * 12 + 4 * (n + 1) + 16 * n, "ELL": nnz * 12 + 16 * n}
+    peak, peak_kind = peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    s = torch.cuda.Stream()
+    out = {}
+    launches = 0
+    clk = Clocks(local)
+    clk.start()
+    for name in ("COO", "SCOO", "CSR", "ELL", "DENSE"):
+        if name not in want:
+            continue
+        if name == "DENSE":
+            m = T.MatrixDENSE()
+            m.fill_dense_uniform(dm, dk, 0)
+            xv = T.fill_uniform(dk, 0.0, 1.0, 0)
+            nr, B = dm, 8 * dm * dk + 8 * dk + 8 * dm
+        else:
+            m = builders[name]()
+            xv, nr, B = x, n, sparse_bytes[name]
+            if name == "ELL":
+                assert m.info()["max_col"] == 10
+        m.upload()
+        xt = torch.from_numpy(xv).cuda()
+        yt = torch.zeros(nr, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        times = []
+        with torch.cuda.stream(s):
+            for step in range(a.warmup + a.steps):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                m.Ax_device(yt, xt, stream=s)
+                e1.record(s)
+                s.synchronize()
+                if step >= a.warmup:
+                    times.append(e0.elapsed_time(e1))
+        launches += a.steps * m.kernel_launches()
+        ms = statistics.median(times)
+        hx, hy = C.c_void_p(), C.c_void_p()
+        T.check(T.lib.tbsla_host_alloc(C.byref(hx), len(xv) * 8))
+        T.check(T.lib.tbsla_host_alloc(C.byref(hy), nr * 8))
+        np.ctypeslib.as_array(C.cast(hx, C.POINTER(C.c_double)), shape=(len(xv),))[:] = xv
+        for _ in range(a.warmup):
+            T.check(T.lib.tbsla_Ax(m._h, hy, hx, 0))
+        host = []
+        for _ in range(a.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            T.check(T.lib.tbsla_Ax(m._h, hy, hx, 0))
+            host.append(time.perf_counter() - t0)
+        T.lib.tbsla_host_free(hx)
+        T.lib.tbsla_host_free(hy)
+        cpu_s = None
+        if a.cpu_seconds > 0:
+            if name == "DENSE":
+                ad = m.arrays()
+                run = lambda: oracle.dense_ax(ad["values"], dm, dk, xv, threads=True)  # noqa: E731
+            elif name == "CSR":
+                run = lambda: oracle.csr_ax(a0["rowptr"], a0["colidx"], a0["values"], x, threads=True)  # noqa: E731
+            elif name == "ELL":
+                ae = m.arrays()
+                run = lambda: oracle.ell_ax(ae["values"], ae["columns"], n, 10, x)  # noqa: E731
+            elif name == "COO":
+                run = lambda: oracle.coo_ax(n, rows, a0["colidx"], a0["values"], x)  # noqa: E731
+            else:
+                run = lambda: oracle.scoo_ax(n, 0, 0, rows, a0["colidx"], a0["values"], x)  # noqa: E731
+            t0 = time.perf_counter()
+            run()
+            cpu_s = time.perf_counter() - t0
+        # FP64 instructions per entry: one fused multiply-add (ELL: a rounded
+        # product and an add, for the reference's rounding); gathers: one x
+        # entry per stored entry (DENSE reads x in order, from L1)
+        entries = dm * dk if name == "DENSE" else nnz
+        out[name] = {"device_ms": ms, "GB/s": B / (ms * 1e-3) / 1e9, "frac_of_peak": B / (ms * 1e-3) / 1e9 / peak,
+                     "fp64_ops": entries * (2 if name == "ELL" else 1), "gathers": 0 if name == "DENSE" else nnz,
+                     "bytes_per_ax": B, "host_call_ms": statistics.median(host) * 1e3,
+                     "cpu_oracle_ms": None if cpu_s is None else cpu_s * 1e3,
+                     "cpu_threads": (os.cpu_count() if name in ("CSR", "DENSE") else 1)}
+        del m, xt, yt
+        torch.cuda.empty_cache()
+    clocks = clk.stop()
+    # Floors per Ax: HBM (algorithmic bytes at the measured copy bandwidth),
+    # the FP64 pipe (2 lanes per cycle per SM: one warp instruction per 16
+    # cycles) and the L1->L2 request rate of the x gathers (one request per
+    # gather, about one per SM cycle), at the SM clock sampled during the run.
+    f_sm = (clocks.get("sm_mhz") or 2070.0) * 1e6
+    for v in out.values():
+        fl = {"hbm": v["bytes_per_ax"] / (peak * 1e9) * 1e3, "fp64_pipe": v["fp64_ops"] / (SMS * 2 * f_sm) * 1e3,
+              "gather_requests": v["gathers"] / (SMS * f_sm) * 1e3}
+        bound = max(fl, key=fl.get)
+        v["floors_ms"] = fl
+        v["bound"] = bound
+        v["frac_of_bound"] = fl[bound] / v["device_ms"]
+    head = "CSR" if "CSR" in out else next(iter(out))
+    h = out[head]
+    line = {
+        "metric": "SpMV HBM GB/s (% peak) per format, x L2-resident", "value": h["GB/s"], "unit": "GB/s",
+        "n_gpus": ws, "steps": a.steps, "warmup": a.warmup, "ms_per_step": h["device_ms"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: the reference's row recipe (seed 0) at n = 2^22, no dataset",
+        "config": {"workload": f"spmv_uniform_rows_n{n}_k10_formats_dense{dm}x{dk}_f64", "n": n, "nnz": nnz,
+                   "head_format": head, "l2": "flushed (256 MB write) before each step; arrays > L2",
+                   "parallelism": "1 GPU"},
+        "formats": out,
+        "roofline": {"bound": "hbm", "achieved": h["GB/s"], "peak": peak, "unit": "GB/s",
+                     "frac": h["GB/s"] / peak, "peak_source": peak_kind, "traffic": None},
+        "cpu_baseline": {"value": (h["bytes_per_ax"] / (h["cpu_oracle_ms"] * 1e-3) / 1e9
+                                   if h["cpu_oracle_ms"] else None), "unit": "GB/s",
+                         "cores": h["cpu_threads"], "kind": "port",
+                         "sample": f"one Ax of the {head} matrix through the oracle's loop"},
+        "e2e": {"value": h["bytes_per_ax"] / (h["host_call_ms"] * 1e-3) / 1e9, "unit": "GB/s",
+                "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n, "ms_per_step": h["host_call_ms"]},
+        "gpu_launches": launches, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def run_pagerank(a):
     """The PageRank workload: preferential-attachment graph, n = 2^22 nodes,
     Zipf(2.1) out-degrees of mean 16, 5% dangling, seed 2; column-stochastic
@@ -846,6 +1007,8 @@ if __name__ == "__main__":
         run_reference(args)
     elif args.workload == "small":
         run_small(args)
+    elif args.workload == "formats":
+        run_formats(args)
     elif args.workload == "pagerank":
         run_pagerank(args)
     elif args.workload == "cg":

@@ -16,6 +16,7 @@ namespace tbsla_gpu {
 namespace {
 
 constexpr int NT = 256;
+constexpr int kDenseU = 4;  // 16-byte loads in flight per thread, CTA-per-row kernel
 
 __device__ __forceinline__ double2 ld_stream2(const double* p, uint64_t pol) {
   double2 v;
@@ -46,6 +47,59 @@ __global__ void __launch_bounds__(NT) k_dense(const V* __restrict__ A, int ln_ro
     for (; j < ln_col; j += kWarp) acc = fma_rn(widen(ld_stream(a + j, pol)), __ldg(x + j), acc);
     acc = warp_sum(acc);
     if (lane == 0) y[row] = add_rn(y[row], acc);
+  }
+}
+
+// FP64 rows of at least 2*NT*U columns with 16-byte aligned starts: one CTA
+// per row (launched with a CTA per row; the loop also accepts fewer CTAs),
+// every thread with U 16-byte loads in flight.
+// A warp per row leaves the last round of rows to a fraction of the warps
+// (32768 rows over 9728 warps: 4 rounds for some, 3 for the rest); a CTA per
+// row spreads each row over the whole CTA and the rows over 8x fewer
+// workers, so the last round is a small share of the launch.  Partial sums:
+// warp butterfly, then the NT/32 warp sums in a fixed order (a double-
+// buffered slot per row parity, one barrier per row).
+template <int U>
+__global__ void __launch_bounds__(NT) k_dense_rows_f64x2(const double* __restrict__ A, int ln_row,
+                                                        int ln_col, const double* __restrict__ x,
+                                                        double* __restrict__ y) {
+  __shared__ double s_part[2][NT / kWarp];
+  const int lane = threadIdx.x % kWarp, warp = threadIdx.x / kWarp;
+  const uint64_t pol = policy_evict_first();
+  const int half = ln_col / 2;
+  const double2* x2 = reinterpret_cast<const double2*>(x);
+  int parity = 0;
+  for (int row = blockIdx.x; row < ln_row; row += gridDim.x, parity ^= 1) {
+    const double* a = A + (size_t)row * ln_col;
+    double acc0 = 0, acc1 = 0;
+    int j = threadIdx.x;
+    for (; j + (U - 1) * NT < half; j += U * NT) {
+      double2 av[U], bv[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) av[u] = ld_stream2(a + 2 * (j + u * NT), pol);
+#pragma unroll
+      for (int u = 0; u < U; u++) bv[u] = __ldg(x2 + j + u * NT);
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        acc0 = fma_rn(av[u].x, bv[u].x, acc0);
+        acc1 = fma_rn(av[u].y, bv[u].y, acc1);
+      }
+    }
+    for (; j < half; j += NT) {
+      const double2 a0 = ld_stream2(a + 2 * j, pol);
+      const double2 b0 = __ldg(x2 + j);
+      acc0 = fma_rn(a0.x, b0.x, acc0);
+      acc1 = fma_rn(a0.y, b0.y, acc1);
+    }
+    const double w = warp_sum(add_rn(acc0, acc1));
+    if (lane == 0) s_part[parity][warp] = w;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0;
+#pragma unroll
+      for (int i = 0; i < NT / kWarp; i++) t = add_rn(t, s_part[parity][i]);
+      y[row] = add_rn(y[row], t);
+    }
   }
 }
 
@@ -178,7 +232,10 @@ cudaError_t dense_gemv(const void* vals, int prec, int ln_row, int ln_col, const
   const int grid = (int)std::min<long>(((long)ln_row + NT / kWarp - 1) / (NT / kWarp), 152L * 8);
   switch (prec) {
     case kF64:
-      if (ln_col % 2 == 0 && ((uintptr_t)vals % 16) == 0 && ((uintptr_t)x % 16) == 0)
+      if (ln_col % 2 == 0 && ln_col >= 2 * NT * kDenseU && ((uintptr_t)vals % 16) == 0 && ((uintptr_t)x % 16) == 0)
+        k_dense_rows_f64x2<kDenseU><<<ln_row, NT, 0, s>>>(  // a CTA per row, scheduled as CTAs retire
+            static_cast<const double*>(vals), ln_row, ln_col, x, y);
+      else if (ln_col % 2 == 0 && ((uintptr_t)vals % 16) == 0 && ((uintptr_t)x % 16) == 0)
         k_dense_f64x2<<<grid, NT, 0, s>>>(static_cast<const double*>(vals), ln_row, ln_col, x, y);
       else
         k_dense<double><<<grid, NT, 0, s>>>(static_cast<const double*>(vals), ln_row, ln_col, x, y);

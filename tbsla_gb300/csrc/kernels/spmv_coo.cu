@@ -5,17 +5,26 @@
 // r[row + row_off] += values * v[col + col_off] for every triplet, where the
 // reference uses an OpenMP array reduction (one private copy of r per
 // thread).  Here the triplets are stably sorted by row once at upload, and
-// each CTA reduces a tile of 256*ITEMS consecutive triplets by key:
-//  1. striped, coalesced loads of (row, col, value); products with the
-//     gathered x staged in shared memory;
-//  2. each thread scans its ITEMS consecutive products; a block-wide
-//     segmented scan of the per-thread (has-segment-start, tail-sum) pairs
-//     gives every thread the partial sum carried into its range;
-//  3. each segment is written once by the thread that sees its end: a
-//     segment that starts and ends inside the tile owns its row outright
-//     (plain read-modify-write), while the tile's first and last segments may
-//     continue in the neighbouring tiles and are added with FP64 atomics.
-// No per-thread copy of r, no atomics except at tile boundaries.
+// every warp reduces chunks of 32*U consecutive triplets by key on its own
+// (no shared memory, no block barrier):
+//  1. lane l owns triplets base + l*U .. base + l*U + U-1 and reads them
+//     with 16-byte vector loads (rows, columns, values), which across the
+//     warp cover consecutive addresses; all x gathers are issued before any
+//     arithmetic;
+//  2. each lane sums its own U products in order, closing a segment at each
+//     row change (a segment that starts and ends inside the lane is final
+//     there); one segmented scan across the 32 lanes (shuffles) then gives
+//     each lane the sum of the segment running into it;
+//  3. each finished segment is added to r with one FP64 reduction (no
+//     returned value, so the warp never waits on it); a row whose triplets
+//     cross a chunk boundary gets one addition per chunk.
+// Each product is added with one fused multiply-add (GB300 retires one
+// warp-wide FP64 instruction per 16 cycles per SM, and a separate multiply
+// and add per triplet kept that pipe 77% busy); the reference rounds the
+// product first, so sums differ from its loop by that rounding only.
+#include <algorithm>
+#include <cstring>
+
 #include "common.cuh"
 #include "kernels.hpp"
 
@@ -25,103 +34,120 @@ namespace {
 
 constexpr int NT = 256;
 
-template <class V, int ITEMS>
+__device__ __forceinline__ uint4 ld_stream_v4(const void* p, uint64_t pol) {
+  uint4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
+  return v;
+}
+
+// U consecutive elements of type T from a 16-byte aligned address.
+template <class T, int U>
+__device__ __forceinline__ void ld_run(T (&out)[U], const T* p, uint64_t pol) {
+  static_assert(U * sizeof(T) % 16 == 0, "runs are whole 16-byte vectors");
+  constexpr int NV = U * (int)sizeof(T) / 16;
+  uint4 w[NV];
+#pragma unroll
+  for (int i = 0; i < NV; i++) w[i] = ld_stream_v4(reinterpret_cast<const uint4*>(p) + i, pol);
+  memcpy(out, w, sizeof(out));
+}
+
+template <class V, int U, bool VEC>
 __global__ void __launch_bounds__(NT) k_coo(const int* __restrict__ rows, const int* __restrict__ cols,
                                            const V* __restrict__ vals, long nnz, int row_off,
                                            int col_off, const double* __restrict__ x,
                                            double* __restrict__ y) {
-  constexpr int TILE = NT * ITEMS;
-  __shared__ double s_prod[TILE];
-  __shared__ int s_row[TILE];
-  __shared__ int s_wf[NT / kWarp];
-  __shared__ double s_wv[NT / kWarp];
-  __shared__ int s_first_head;
-  const int tid = threadIdx.x, lane = tid % kWarp, warp = tid / kWarp;
-  const long base = (long)blockIdx.x * TILE;
-  const int cnt = (int)min((long)TILE, nnz - base);
+  constexpr long CH = (long)kWarp * U;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x % kWarp;
+  const long gw = ((long)blockIdx.x * NT + threadIdx.x) / kWarp;
+  const long nw = (long)gridDim.x * NT / kWarp;
   const uint64_t pol = policy_evict_first();
-  if (tid == 0) s_first_head = TILE;
-
-  int r[ITEMS], c[ITEMS];
-  V v[ITEMS];
+  for (long base = gw * CH; base < nnz; base += nw * CH) {
+    const long e0 = base + (long)lane * U;
+    int r[U], c[U];
+    V v[U];
+    if (VEC && e0 + U <= nnz) {
+      ld_run<int, U>(r, rows + e0, pol);
+      ld_run<int, U>(c, cols + e0, pol);
+      ld_run<V, U>(v, vals + e0, pol);
+    } else {
 #pragma unroll
-  for (int k = 0; k < ITEMS; k++) {
-    const int i = k * NT + tid;
-    if (i < cnt) {
-      r[k] = ld_stream(rows + base + i, pol);
-      c[k] = ld_stream(cols + base + i, pol);
-      v[k] = ld_stream(vals + base + i, pol);
+      for (int k = 0; k < U; k++) {
+        r[k] = -1;  // past the end: a row of its own, never written
+        c[k] = 0;
+        v[k] = V(0);
+        if (e0 + k < nnz) {
+          r[k] = ld_stream(rows + e0 + k, pol);
+          c[k] = ld_stream(cols + e0 + k, pol);
+          v[k] = ld_stream(vals + e0 + k, pol);
+        }
+      }
     }
-  }
+    double xg[U];
 #pragma unroll
-  for (int k = 0; k < ITEMS; k++) {
-    const int i = k * NT + tid;
-    if (i < cnt) {
-      s_row[i] = r[k];
-      s_prod[i] = mul_rn(widen(v[k]), ld_gather(x + c[k] + col_off));
-    }
-  }
-  __syncthreads();
+    for (int k = 0; k < U; k++) xg[k] = r[k] >= 0 ? ld_gather(x + c[k] + col_off) : 0.0;
 
-  // Per-thread pair (f, t): f = a segment starts inside [lo, hi) (at k > 0),
-  // t = sum of the products after the last such start (all of them if none).
-  const int lo = tid * ITEMS, hi = min(lo + ITEMS, cnt);
-  int f = 0;
-  double t = 0;
-  for (int k = lo; k < hi; k++) {
-    if (k > 0 && s_row[k] != s_row[k - 1]) {
-      if (!f) atomicMin(&s_first_head, k);
-      f = 1;
-      t = 0;
-    }
-    t = add_rn(t, s_prod[k]);
-  }
-  // Inclusive segmented scan over the warp: (fa,ta) then (fb,tb) combine to
-  // (fa|fb, fb ? tb : ta + tb).
-  int fi = f;
-  double ti = t;
+    // Row before this lane's first triplet (-2 at the chunk start: a new
+    // segment, which may continue a row of the previous chunk).
+    int prev = __shfl_up_sync(full, r[U - 1], 1);
+    if (lane == 0) prev = -2;
+    const int h0 = r[0] != prev;
+    // In-lane pass: first = sum up to the first row change after k = 0
+    // (the part of the lane's first segment), acc = the open tail.
+    double acc = mul_rn(widen(v[0]), xg[0]), first = 0;
+    int closed = 0;  // a row change after k = 0 was seen
 #pragma unroll
-  for (int o = 1; o < kWarp; o <<= 1) {
-    const int fu = __shfl_up_sync(0xffffffffu, fi, o);
-    const double tu = __shfl_up_sync(0xffffffffu, ti, o);
-    if (lane >= o) {
-      ti = fi ? ti : add_rn(tu, ti);
-      fi |= fu;
+    for (int k = 1; k < U; k++) {
+      if (r[k] != r[k - 1]) {
+        if (!closed) first = acc;
+        else if (r[k - 1] >= 0) atomicAdd(y + r[k - 1] + row_off, acc);
+        closed = 1;
+        acc = 0;
+      }
+      acc = fma_rn(widen(v[k]), xg[k], acc);
     }
-  }
-  if (lane == kWarp - 1) {
-    s_wf[warp] = fi;
-    s_wv[warp] = ti;
-  }
-  const int fl = __shfl_up_sync(0xffffffffu, fi, 1);
-  const double tl = __shfl_up_sync(0xffffffffu, ti, 1);
-  __syncthreads();
-  // Exclusive prefix for this thread: earlier warps, then earlier lanes.
-  double carry = 0;
-  for (int w = 0; w < warp; w++) carry = s_wf[w] ? s_wv[w] : add_rn(carry, s_wv[w]);
-  if (lane > 0) carry = fl ? tl : add_rn(carry, tl);
-  const int first_head = s_first_head;
-
-  double acc = carry;
-  for (int k = lo; k < hi; k++) {
-    if (k > 0 && s_row[k] != s_row[k - 1]) {
-      double* dst = y + (s_row[k - 1] + row_off);
-      if (k == first_head) atomicAdd(dst, acc);  // first segment: may span the previous tile
-      else *dst = add_rn(*dst, acc);              // interior segment: owned by this CTA
-      acc = 0;
+    // Segmented scan of (starts a segment, open tail sum) across lanes:
+    // (fa, ta) then (fb, tb) -> (fa | fb, fb ? tb : ta + tb).
+    int f = h0 | closed;
+    double t = acc;
+#pragma unroll
+    for (int o = 1; o < kWarp; o <<= 1) {
+      const double tu = __shfl_up_sync(full, t, o);
+      const int fu = __shfl_up_sync(full, f, o);
+      if (lane >= o) {
+        if (!f) t = add_rn(tu, t);
+        f |= fu;
+      }
     }
-    acc = add_rn(acc, s_prod[k]);
+    // Sum of the segment running into this lane: the inclusive value of lane - 1.
+    double in = __shfl_up_sync(full, t, 1);
+    if (lane == 0) in = 0;
+    if (h0) {
+      // the incoming segment ended at the previous lane's last triplet
+      if (lane > 0 && prev >= 0) atomicAdd(y + prev + row_off, in);
+      if (closed && r[0] >= 0) atomicAdd(y + r[0] + row_off, first);
+    } else if (closed && r[0] >= 0) {
+      atomicAdd(y + r[0] + row_off, add_rn(in, first));
+    }
+    // the chunk's last segment (it may continue in the next chunk)
+    if (lane == kWarp - 1 && r[U - 1] >= 0) atomicAdd(y + r[U - 1] + row_off, t);
   }
-  if (lo < cnt && hi == cnt) atomicAdd(y + (s_row[cnt - 1] + row_off), acc);  // last segment
 }
 
 template <class V>
 cudaError_t launch(const void* vals, const int* rows, const int* cols, long nnz, int row_off,
                    int col_off, const double* x, double* y, cudaStream_t s) {
-  constexpr int ITEMS = 8;
-  const long tiles = (nnz + NT * ITEMS - 1) / (NT * ITEMS);
-  k_coo<V, ITEMS><<<(unsigned)tiles, NT, 0, s>>>(rows, cols, static_cast<const V*>(vals), nnz,
-                                                 row_off, col_off, x, y);
+  constexpr int U = 8;
+  constexpr long per_cta = (long)NT / kWarp * kWarp * U;
+  const long grid = (nnz + per_cta - 1) / per_cta;  // one chunk per warp: the block scheduler balances
+  const bool vec = ((uintptr_t)rows % 16 == 0) && ((uintptr_t)cols % 16 == 0) && ((uintptr_t)vals % 16 == 0);
+  if (vec)
+    k_coo<V, U, true><<<(unsigned)grid, NT, 0, s>>>(rows, cols, static_cast<const V*>(vals), nnz, row_off,
+                                                    col_off, x, y);
+  else
+    k_coo<V, U, false><<<(unsigned)grid, NT, 0, s>>>(rows, cols, static_cast<const V*>(vals), nnz, row_off,
+                                                     col_off, x, y);
   return cudaGetLastError();
 }
 
