@@ -58,7 +58,8 @@ def parse_args():
     p.add_argument("--factor-prec", choices=["f32", "bf16"], default="bf16",
                    help="learned: storage precision of the factor L")
     p.add_argument("--n", type=int, default=None, help="rows (spmv: 2^24, pagerank and formats: 2^22)")
-    p.add_argument("--formats", type=str, default="coo,scoo,csr,ell,dense", help="formats: which formats to run")
+    p.add_argument("--formats", type=str, default="coo,scoo,csr,ell,dense,dense_f32,dense_bf16",
+                   help="formats: which formats to run (dense_f32 / dense_bf16: DENSE with narrow values)")
     p.add_argument("--prec", choices=["f64", "f32", "bf16"], default="f64")
     p.add_argument("--tile", type=int, default=2048, help="row-block kernel: entries per block")
     p.add_argument("--algo", choices=["sell", "merge", "rowblock"], default="sell")
@@ -603,7 +604,8 @@ def run_formats(a):
     uniform columns per row, U[-1,1) values, x U[0,1), seed 0) at n = 2^22
     rows (41.9 M entries; x = 32 MiB stays in L2 once read, so each kernel
     streams its own arrays) as COO, SCOO, CSR and ELL, and a 32768 x 16384
-    DENSE GEMV (4.3 GB), all FP64.  Per format: device time per Ax (CUDA
+    DENSE GEMV (4.3 GB), FP64, and the same GEMV with FP32 and BF16
+    values (double-float arithmetic).  Per format: device time per Ax (CUDA
     events on the launching stream, L2 flushed before each step, median),
     algorithmic bytes / time against the measured HBM copy bandwidth, and a
     host call through tbsla_Ax with pinned buffers (x in, y out).  CPU
@@ -645,14 +647,19 @@ def run_formats(a):
     launches = 0
     clk = Clocks(local)
     clk.start()
-    for name in ("COO", "SCOO", "CSR", "ELL", "DENSE"):
+    dense = None
+    for name in ("COO", "SCOO", "CSR", "ELL", "DENSE", "DENSE_F32", "DENSE_BF16"):
         if name not in want:
             continue
-        if name == "DENSE":
-            m = T.MatrixDENSE()
-            m.fill_dense_uniform(dm, dk, 0)
+        if name.startswith("DENSE"):
+            if dense is None:
+                dense = T.MatrixDENSE()
+                dense.fill_dense_uniform(dm, dk, 0)
+            m = dense
+            sv = {"DENSE": 8, "DENSE_F32": 4, "DENSE_BF16": 2}[name]
+            m.set_precision({8: T.F64, 4: T.F32, 2: T.BF16}[sv])
             xv = T.fill_uniform(dk, 0.0, 1.0, 0)
-            nr, B = dm, 8 * dm * dk + 8 * dk + 8 * dm
+            nr, B = dm, sv * dm * dk + 8 * dk + 8 * dm
         else:
             m = builders[name]()
             xv, nr, B = x, n, sparse_bytes[name]
@@ -691,7 +698,7 @@ def run_formats(a):
         T.lib.tbsla_host_free(hx)
         T.lib.tbsla_host_free(hy)
         cpu_s = None
-        if a.cpu_seconds > 0:
+        if a.cpu_seconds > 0 and name not in ("DENSE_F32", "DENSE_BF16"):
             if name == "DENSE":
                 ad = m.arrays()
                 run = lambda: oracle.dense_ax(ad["values"], dm, dk, xv, threads=True)  # noqa: E731
@@ -708,14 +715,18 @@ def run_formats(a):
             run()
             cpu_s = time.perf_counter() - t0
         # FP64 instructions per entry: one fused multiply-add (ELL: a rounded
-        # product and an add, for the reference's rounding); gathers: one x
-        # entry per stored entry (DENSE reads x in order, from L1)
-        entries = dm * dk if name == "DENSE" else nnz
+        # product and an add, for the reference's rounding; the narrow DENSE
+        # forms none: double-float on the FP32 pipes); gathers: one x entry
+        # per stored entry (DENSE reads x in order, from L1)
+        entries = dm * dk if name.startswith("DENSE") else nnz
+        f64 = 0 if name in ("DENSE_F32", "DENSE_BF16") else entries * (2 if name == "ELL" else 1)
         out[name] = {"device_ms": ms, "GB/s": B / (ms * 1e-3) / 1e9, "frac_of_peak": B / (ms * 1e-3) / 1e9 / peak,
-                     "fp64_ops": entries * (2 if name == "ELL" else 1), "gathers": 0 if name == "DENSE" else nnz,
+                     "fp64_ops": f64, "gathers": 0 if name.startswith("DENSE") else nnz,
                      "bytes_per_ax": B, "host_call_ms": statistics.median(host) * 1e3,
                      "cpu_oracle_ms": None if cpu_s is None else cpu_s * 1e3,
                      "cpu_threads": (os.cpu_count() if name in ("CSR", "DENSE") else 1)}
+        if name.startswith("DENSE"):
+            out[name]["launches_per_ax"] = m.kernel_launches()
         del m, xt, yt
         torch.cuda.empty_cache()
     clocks = clk.stop()

@@ -115,6 +115,9 @@ struct DeviceMatrix {
   size_t y_len = 0;
   double* t = nullptr;
   size_t t_len = 0;
+  bool dense_df = false;     // DENSE, FP32 / BF16 values within the double-float range
+  float* xdf = nullptr;      // DENSE double-float: x split into xh[ln_col], xl[ln_col]
+  int* df_flag = nullptr;    // DENSE double-float: x out of range in this call
   double* pr_ctl = nullptr;  // PageRank: coefficients [0, 4) and flags (2 int) at [4]
   size_t pr_ctl_len = 0;
   // persistent-kernel control and reduction scratch
@@ -128,7 +131,8 @@ struct DeviceMatrix {
     if (stream) cudaStreamSynchronize(stream);
     for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t, (void*)pr_ctl,
                     (void*)counter, (void*)partials, (void*)result, (void*)coord, (void*)carry_row,
-                    (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)colw})
+                    (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)colw, (void*)xdf,
+                    (void*)df_flag})
       if (p) cudaFree(p);
     for (SellPlan& p : sell)
       for (void* q : {(void*)p.slice, (void*)p.lane, (void*)p.lane_len})
@@ -465,9 +469,23 @@ int build(const tbsla_matrix* m, DeviceMatrix* d) {
     }
     case TBSLA_DENSE: {
       if (I.nnz == 0) return TBSLA_OK;
-      int st = upload_values(d, m->values.data(), (size_t)I.ln_row * I.ln_col);
+      const size_t n = (size_t)I.ln_row * I.ln_col;
+      int st = upload_values(d, m->values.data(), n);
       if (!st) st = status_of(cudaStreamSynchronize(d->stream));
-      return st;
+      if (st || d->prec == TBSLA_F64) return st;
+      // narrow values: the double-float GEMV when every value is in its range
+      if ((st = dalloc(&d->df_flag, 1))) return st;
+      bool ok = false;
+      TRY(dense_values_df_range(d->vals, d->prec, n, d->df_flag, &ok, d->stream));
+      if (ok) {
+        if (cudaMalloc(&d->xdf, (size_t)I.ln_col * 2 * sizeof(float)) != cudaSuccess) {
+          cudaGetLastError();
+          return TBSLA_ERR_ALLOC;
+        }
+        d->bytes += (size_t)I.ln_col * 2 * sizeof(float) + 4;
+        d->dense_df = true;
+      }
+      return TBSLA_OK;
     }
   }
   return TBSLA_ERR_INVALID_ARG;
@@ -558,6 +576,8 @@ int ax_device(const tbsla_matrix* m, DeviceMatrix* d, double* r, const double* v
                                 scoo ? -I.f_col : 0, v, r, s));
     }
     case TBSLA_DENSE:
+      if (d->dense_df)
+        return status_of(dense_gemv_df(d->vals, d->prec, I.ln_row, I.ln_col, v, d->xdf, d->df_flag, r, s));
       return status_of(dense_gemv(d->vals, d->prec, I.ln_row, I.ln_col, v, r, s));
   }
   return TBSLA_ERR_INVALID_ARG;
@@ -588,6 +608,8 @@ int dev_launches(const tbsla_matrix* m, int* launches) {
     k = 0;
   else if (m->format == TBSLA_COO || m->format == TBSLA_SCOO)
     k = d->nnz > 0;
+  else if (m->format == TBSLA_DENSE)
+    k = d->dense_df ? 2 : 1;  // double-float: the split of x, then the GEMV
   else if (m->format != TBSLA_CSR)
     k = 1;
   else if (d->algo == 2)

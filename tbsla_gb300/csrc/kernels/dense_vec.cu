@@ -9,6 +9,7 @@
 #include <algorithm>
 
 #include "common.cuh"
+#include "df.cuh"
 #include "kernels.hpp"
 
 namespace tbsla_gpu {
@@ -17,6 +18,10 @@ namespace {
 
 constexpr int NT = 256;
 constexpr int kDenseU = 4;  // 16-byte loads in flight per thread, CTA-per-row kernel
+// rows per CTA pass, double-float kernel; 2 (each xh / xl load serving two
+// rows) measured 0.366 / 0.329 ms against 0.362 / 0.321 ms with 1 (FP32 /
+// BF16 values, 32768 x 16384)
+constexpr int kDenseDfRows = 1;
 
 __device__ __forceinline__ double2 ld_stream2(const double* p, uint64_t pol) {
   double2 v;
@@ -99,6 +104,156 @@ __global__ void __launch_bounds__(NT) k_dense_rows_f64x2(const double* __restric
 #pragma unroll
       for (int i = 0; i < NT / kWarp; i++) t = add_rn(t, s_part[parity][i]);
       y[row] = add_rn(y[row], t);
+    }
+  }
+}
+
+// FP32 / BF16 values in double-float arithmetic.  Widening every value to
+// FP64 for one FP64 multiply-add kept the FP64 pipe as busy as the FP64
+// matrix does (0.99 ms for 537 M entries) although the bytes halve.  Here:
+//  * x is split once per call into floats xh = fl32(x), xl = fl32(x - xh),
+//    which hold x to 2^-48 relative, kept as two arrays;
+//  * each thread accumulates its columns with compensated Dot2 steps (the
+//    product's and the sum's rounding errors carried exactly into a second
+//    float), 4 columns per step: one load of values (16 bytes FP32, 8 bytes
+//    BF16) and one 16-byte load each of xh and xl, consecutive across the
+//    warp;
+//  * the thread pairs are summed across the warp in double-float (TwoSum-
+//    based additions), and the NT/32 warp values in FP64, in a fixed order
+//    (keeping the warp values in double-float up to one conversion per row,
+//    so that fewer FP64 instructions occupy the pipe, measured 2-6% slower).
+// The float arithmetic is exact only inside the float exponent range, so the
+// path needs every nonzero |x| and |a| in [2^-40, 2^40] (products within
+// [2^-80, 2^80], sums of up to 2^31 of them finite, error terms normal): the
+// values are checked once at upload, x by the split kernel on every call,
+// which sets *bad; a launch that reads *bad set runs every row in FP64, in the
+// same kernel (no host round trip).
+constexpr float kDfLo = 9.094947017729282e-13f;  // 2^-40
+constexpr float kDfHi = 1.099511627776e12f;      // 2^40
+
+__device__ __forceinline__ bool df_in_range(double v) {
+  const double a = fabs(v);
+  return a == 0.0 || (a >= (double)kDfLo && a <= (double)kDfHi);  // false for NaN
+}
+
+// xs[0, n) = xh, xs[n, 2n) = xl: separate arrays, so that the GEMV's lanes
+// read consecutive words of each.
+__global__ void k_df_split_x(const double* __restrict__ x, int n, float* __restrict__ xs,
+                             int* __restrict__ bad) {
+  int any = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float h = __double2float_rn(v);
+    xs[i] = h;
+    xs[n + i] = __double2float_rn(v - (double)h);
+    any |= !df_in_range(v);
+  }
+  if (__any_sync(0xffffffffu, any) && threadIdx.x % kWarp == 0) atomicOr(bad, 1);
+}
+
+template <class V>
+__global__ void k_df_range_vals(const V* __restrict__ a, size_t n, int* __restrict__ bad) {
+  int any = 0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    any |= !df_in_range(widen(a[i]));
+  if (__any_sync(0xffffffffu, any) && threadIdx.x % kWarp == 0) atomicOr(bad, 1);
+}
+
+template <class V, int VEC>
+__device__ __forceinline__ void ld_vals(float (&out)[VEC], const V* p, uint64_t pol) {
+  if constexpr (VEC == 1) {
+    if constexpr (sizeof(V) == 4) {
+      out[0] = ld_stream(reinterpret_cast<const float*>(p), pol);
+    } else {  // bfloat16: the high 16 bits of a float
+      const __nv_bfloat16 b = ld_stream(reinterpret_cast<const __nv_bfloat16*>(p), pol);
+      out[0] = __uint_as_float((unsigned)*reinterpret_cast<const unsigned short*>(&b) << 16);
+    }
+  } else if constexpr (sizeof(V) == 4) {  // 4 floats: one 16-byte load
+    static_assert(VEC == 4, "four values per lane");
+    uint4 w;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=r"(w.x), "=r"(w.y), "=r"(w.z), "=r"(w.w) : "l"(p), "l"(pol));
+    out[0] = __uint_as_float(w.x); out[1] = __uint_as_float(w.y);
+    out[2] = __uint_as_float(w.z); out[3] = __uint_as_float(w.w);
+  } else {  // 4 bfloat16 (the high 16 bits of a float): one 8-byte load
+    static_assert(VEC == 4, "four values per lane");
+    unsigned u0, u1;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+                 : "=r"(u0), "=r"(u1) : "l"(p), "l"(pol));
+    out[0] = __uint_as_float(u0 << 16); out[1] = __uint_as_float(u0 & 0xffff0000u);
+    out[2] = __uint_as_float(u1 << 16); out[3] = __uint_as_float(u1 & 0xffff0000u);
+  }
+}
+
+template <class V, int VEC, int R>
+__global__ void __launch_bounds__(NT) k_dense_rows_df(const V* __restrict__ A, int ln_row, int ln_col,
+                                                     const float* __restrict__ xs,
+                                                     const double* __restrict__ x,
+                                                     const int* __restrict__ bad, double* __restrict__ y) {
+  __shared__ double s_part[2][R][NT / kWarp];
+  const int lane = threadIdx.x % kWarp, warp = threadIdx.x / kWarp;
+  const uint64_t pol = policy_evict_first();
+  const bool fp64 = *bad != 0;
+  const int groups = ln_col / VEC;  // VEC divides ln_col
+  int parity = 0;
+  // R rows per pass share every load of xh / xl
+  for (int row0 = blockIdx.x * R; row0 < ln_row; row0 += gridDim.x * R, parity ^= 1) {
+    const int nr = min(R, ln_row - row0);
+    double w[R];
+    if (fp64) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        double acc = 0;
+        if (r < nr) {
+          const V* a = A + (size_t)(row0 + r) * ln_col;
+          for (int j = threadIdx.x; j < ln_col; j += NT) acc = fma_rn(widen(ld_stream(a + j, pol)), __ldg(x + j), acc);
+        }
+        w[r] = warp_sum(acc);
+      }
+    } else {
+      float sh[R], sc[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) sh[r] = sc[r] = 0.f;
+      for (int g = threadIdx.x; g < groups; g += NT) {
+        float xh[VEC], xl[VEC];
+        if constexpr (VEC == 4) {
+          const float4 h4 = __ldg(reinterpret_cast<const float4*>(xs) + g);
+          const float4 l4 = __ldg(reinterpret_cast<const float4*>(xs + ln_col) + g);
+          xh[0] = h4.x; xh[1] = h4.y; xh[2] = h4.z; xh[3] = h4.w;
+          xl[0] = l4.x; xl[1] = l4.y; xl[2] = l4.z; xl[3] = l4.w;
+        } else {
+          xh[0] = __ldg(xs + g);
+          xl[0] = __ldg(xs + ln_col + g);
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) {
+          if (r < nr) {
+            float av[VEC];
+            ld_vals<V, VEC>(av, A + (size_t)(row0 + r) * ln_col + (size_t)g * VEC, pol);
+#pragma unroll
+            for (int k = 0; k < VEC; k++) dot2_step(sh[r], sc[r], av[k], DF{xh[k], xl[k]});
+          }
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        DF t = two_sum(sh[r], sc[r]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+          t = df_add(t, DF{__shfl_xor_sync(0xffffffffu, t.h, o), __shfl_xor_sync(0xffffffffu, t.l, o)});
+        w[r] = lane == 0 ? df_val(t) : 0.0;
+      }
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int r = 0; r < R; r++) s_part[parity][r][warp] = w[r];
+    }
+    __syncthreads();
+    if (threadIdx.x < nr) {
+      double t = 0;
+#pragma unroll
+      for (int i = 0; i < NT / kWarp; i++) t = add_rn(t, s_part[parity][threadIdx.x][i]);
+      y[row0 + threadIdx.x] = add_rn(y[row0 + threadIdx.x], t);
     }
   }
 }
@@ -243,6 +398,45 @@ cudaError_t dense_gemv(const void* vals, int prec, int ln_row, int ln_col, const
     case kF32: k_dense<float><<<grid, NT, 0, s>>>(static_cast<const float*>(vals), ln_row, ln_col, x, y); break;
     case kBF16: k_dense<__nv_bfloat16><<<grid, NT, 0, s>>>(static_cast<const __nv_bfloat16*>(vals), ln_row, ln_col, x, y); break;
     default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t dense_values_df_range(const void* vals, int prec, size_t n, int* flag, bool* ok, cudaStream_t s) {
+  *ok = false;
+  if (prec == kF64 || n == 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
+  if (e) return e;
+  const int grid = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16));
+  if (prec == kF32) k_df_range_vals<float><<<grid, 256, 0, s>>>(static_cast<const float*>(vals), n, flag);
+  else k_df_range_vals<__nv_bfloat16><<<grid, 256, 0, s>>>(static_cast<const __nv_bfloat16*>(vals), n, flag);
+  int h = 1;
+  if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+      (e = cudaStreamSynchronize(s)))
+    return e;
+  *ok = h == 0;
+  return cudaSuccess;
+}
+
+cudaError_t dense_gemv_df(const void* vals, int prec, int ln_row, int ln_col, const double* x, float* xs,
+                          int* bad, double* y, cudaStream_t s) {
+  if (ln_row == 0 || ln_col == 0) return cudaSuccess;
+  if (prec == kF64) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+  if (e) return e;
+  k_df_split_x<<<std::min((ln_col + 255) / 256, 152 * 4), 256, 0, s>>>(x, ln_col, xs, bad);
+  // four values per lane when every row starts on a 16-byte boundary (xs from cudaMalloc)
+  const bool vec = (uintptr_t)vals % 16 == 0 && (uintptr_t)xs % 16 == 0 && ln_col % 4 == 0;
+  constexpr int R = kDenseDfRows;
+  const int grid = (ln_row + R - 1) / R;
+  if (prec == kF32) {
+    const float* a = static_cast<const float*>(vals);
+    if (vec) k_dense_rows_df<float, 4, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);
+    else k_dense_rows_df<float, 1, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);
+  } else {
+    const __nv_bfloat16* a = static_cast<const __nv_bfloat16*>(vals);
+    if (vec) k_dense_rows_df<__nv_bfloat16, 4, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);
+    else k_dense_rows_df<__nv_bfloat16, 1, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);
   }
   return cudaGetLastError();
 }

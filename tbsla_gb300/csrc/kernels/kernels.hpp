@@ -258,6 +258,14 @@ cudaError_t coo_spmv(const void* vals, int prec, const int* rows, const int* col
 // ---- DENSE (row-major GEMV, accumulating) -------------------------------------
 cudaError_t dense_gemv(const void* vals, int prec, int ln_row, int ln_col, const double* x,
                        double* y, cudaStream_t s);
+// FP32 / BF16 values in double-float arithmetic (FP32 pipes): x split into
+// xs[0, ln_col) = xh and xs[ln_col, 2 ln_col) = xl; *bad (device int) is cleared, then set by the
+// split when x leaves the [2^-40, 2^40] magnitude range, in which case the
+// same launch computes in FP64.  The values must have passed
+// dense_values_df_range, which checks them once (synchronises on s).
+cudaError_t dense_gemv_df(const void* vals, int prec, int ln_row, int ln_col, const double* x, float* xs,
+                          int* bad, double* y, cudaStream_t s);
+cudaError_t dense_values_df_range(const void* vals, int prec, size_t n, int* flag, bool* ok, cudaStream_t s);
 
 // ---- vector / preparation kernels ---------------------------------------------
 cudaError_t vec_add(double* y, const double* x, long n, cudaStream_t s);  // y += x

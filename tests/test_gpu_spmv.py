@@ -261,6 +261,46 @@ def test_precision_forms(gpu, prec):
         assert err <= bound * 1.01, (fmt, err)
 
 
+@pytest.mark.parametrize("prec", ["f32", "bf16"])
+def test_dense_narrow_values_double_float(gpu, prec):
+    """DENSE with FP32 / BF16 values computes in double-float arithmetic on
+    the FP32 pipes: within the FP64 tolerance of the oracle on the same
+    rounded values, for rows that take 16-byte value loads and rows that do
+    not.  x with an entry outside [2^-40, 2^40] makes the same launch compute
+    in FP64; values outside that range are found at upload and keep the
+    FP64 kernel (one launch instead of two)."""
+    T = gpu
+    rng = np.random.default_rng(31)
+    P = T.F32 if prec == "f32" else T.BF16
+
+    def rounded(v):
+        return v.astype(np.float32).astype(np.float64) if prec == "f32" else oracle.bf16_round(v)
+
+    for nr, nc in ((300, 4096), (257, 2001), (5, 8), (3, 1)):
+        vals = rng.uniform(-1, 1, nr * nc)
+        m = T.MatrixDENSE.from_arrays(nr, nc, vals)
+        m.set_precision(P)
+        assert m.kernel_launches() == 2
+        rv = rounded(vals)
+        xs = (rng.uniform(0, 1, nc), rng.uniform(-1, 1, nc) * 2.0 ** rng.integers(-30, 31, nc),
+              np.where(np.arange(nc) == nc // 2, 2.0 ** 50, rng.uniform(0, 1, nc)))
+        for x in xs:
+            y = np.full(nr, 0.25)
+            m.Ax(y, x)
+            ref = oracle.dense_ax(rv, nr, nc, x, np.full(nr, 0.25))
+            scale = np.abs(rv.reshape(nr, nc) * x).sum(1) + 0.25
+            assert oracle.rel_err_normalized(y, ref, scale) <= TOL, (nr, nc)
+    vals = rng.uniform(-1, 1, 64 * 64)
+    vals[5] = 2.0 ** -60
+    m = T.MatrixDENSE.from_arrays(64, 64, vals)
+    m.set_precision(P)
+    assert m.kernel_launches() == 1
+    x = rng.uniform(0, 1, 64)
+    rv = rounded(vals)
+    ref = oracle.dense_ax(rv, 64, 64, x)
+    assert oracle.rel_err_normalized(m.spmv(x), ref, np.abs(rv.reshape(64, 64) * x).sum(1)) <= TOL
+
+
 def test_device_pointer_entry_points(gpu):
     import torch
 
