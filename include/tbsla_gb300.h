@@ -55,8 +55,9 @@ extern "C" {
 #define TBSLA_DENSE 4
 
 #define TBSLA_F64 0  /* values stored as double on the device (default) */
-#define TBSLA_F32 1  /* values stored as float, products and sums in double */
-#define TBSLA_BF16 2 /* values stored as bfloat16, products and sums in double */
+#define TBSLA_F32 1  /* values stored as float, products and sums in double (DENSE Ax and
+                        batched PageRank: double-float, about 2^-48 relative) */
+#define TBSLA_BF16 2 /* values stored as bfloat16, products and sums as for TBSLA_F32 */
 
 typedef struct tbsla_matrix tbsla_matrix;
 
@@ -162,7 +163,11 @@ int tbsla_matrix_write(const tbsla_matrix* m, const char* path, int append);
 int tbsla_matrix_read(tbsla_matrix* m, const char* path, long offset);
 
 /* ---- device copy ------------------------------------------------------------- */
-/* Value storage precision of the device copy (TBSLA_F64 default). */
+/* Value storage precision of the device copy (TBSLA_F64 default).  DENSE
+ * with TBSLA_F32 / TBSLA_BF16 values computes Ax in double-float on the FP32
+ * pipes when every nonzero |value| is in [2^-40, 2^40] (checked when the
+ * device copy is built) and, per call, every nonzero |v| too (otherwise that
+ * call computes in FP64); results stay within the FP64 tolerance. */
 int tbsla_matrix_set_precision(tbsla_matrix* m, int precision);
 /* Builds the device copy now (otherwise built by the first compute call). */
 int tbsla_matrix_upload(tbsla_matrix* m);
