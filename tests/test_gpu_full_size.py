@@ -13,6 +13,7 @@ smaller tests:
   the same number of iterations; the 32 personalised vectors, two against
   the oracle's solve and all 32 through the fixed-point residual
   |F(x) - x|_1 of one oracle iteration F.
+* The 32768 x 16384 DENSE GEMV with FP64, FP32 and BF16 values.
 * Batched CG on the 64 diffusion systems of sizes 16, 24, ..., 96 (17.1 M
   unknowns, FP32 values, FP64 refresh every 50 iterations): every system's
   true residual, recomputed by the oracle in FP64, is at most 1e-8.
@@ -80,8 +81,8 @@ def test_spmv_powerlaw_full_size(gpu, big, prec):
 
 
 def test_coo_full_size(gpu, big):
-    """The same 268.7 M entries in COO (segmented reduction in tiles of
-    2048 entries; rows longer than a tile span several CTAs)."""
+    """The same 268.7 M entries in COO (segmented reduction in warp chunks
+    of 256 triplets; rows of up to 4096 entries span several chunks)."""
     T = gpu
     a, x, n = big["a"], big["x"], big["n"]
     rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(a["rowptr"]))
@@ -89,6 +90,29 @@ def test_coo_full_size(gpu, big):
     del rows
     y = coo.spmv(x)
     assert oracle.rel_err_normalized(y, big["ref"], big["scale"]) <= TOL
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32", "bf16"])
+def test_dense_gemv_full_size(gpu, prec):
+    """The 32768 x 16384 GEMV of the formats workload (4.3 GB of FP64
+    values): FP64 FMAs, or double-float for FP32 / BF16 values, every row
+    within 1e-13 of the oracle on the same rounded values."""
+    T = gpu
+    nr, nc = 32768, 16384
+    d = T.MatrixDENSE()
+    d.fill_dense_uniform(nr, nc, 0)
+    d.set_precision({"f64": T.F64, "f32": T.F32, "bf16": T.BF16}[prec])
+    vals = d.arrays()["values"]
+    if prec == "f32":
+        vals = vals.astype(np.float32).astype(np.float64)
+    elif prec == "bf16":
+        vals = oracle.bf16_round(vals)
+    x = T.fill_uniform(nc, 0.0, 1.0, 0)
+    y = d.spmv(x)
+    assert d.kernel_launches() == (1 if prec == "f64" else 2)
+    ref = oracle.dense_ax(vals, nr, nc, x, threads=True)
+    scale = oracle.dense_ax(np.abs(vals), nr, nc, x, threads=True)  # x >= 0: sum_j |a_ij x_j|
+    assert oracle.rel_err_normalized(y, ref, scale) <= TOL
 
 
 def pa_graph(T):
