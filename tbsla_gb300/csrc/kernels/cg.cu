@@ -56,8 +56,10 @@ struct EpiResidual {
 // and the warps' sums, all FP64) cost about as much FP64 pipe time per
 // 256-row block as the block's 7 multiply-adds per row.  64 diffusion
 // systems, Jacobi-PCG: 584-619 ms with one block per CTA, 558 ms with 4,
-// 547 ms with 8.
-constexpr int kDotBlocksPerCta = 8;
+// 547 ms with 8.  The kernel also serves the learned-preconditioner solve,
+// whose factor passes it does not shorten: the learned / Jacobi time ratio
+// on the 128^3 systems was 0.454-0.469 with 1, 0.467 with 4, 0.478 with 8.
+constexpr int kDotBlocksPerCta = 4;
 
 template <class V, int ITEMS>
 __global__ void __launch_bounds__(NT) k_cg_spmv_dot(CgBatch c) {
