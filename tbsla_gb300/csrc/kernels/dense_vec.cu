@@ -1,11 +1,14 @@
 // DENSE GEMV and the small vector / preparation kernels of the path.
 //
-// dense_gemv replaces tbsla::cpp::MatrixDENSE::Ax
+// dense_gemv and dense_gemv_df replace tbsla::cpp::MatrixDENSE::Ax
 // (src/cpp/matrix/MatrixDENSE.cpp:77-86): r_i += sum_j A_ij v_j on a
-// row-major ln_row x ln_col matrix.  One warp per row; lanes read the row with
-// 16-byte loads (pairs of doubles) where the row start is 16-byte aligned,
-// x comes through L1 (it is reused by every row), partial sums are combined
-// with a warp butterfly and added to r_i.
+// row-major ln_row x ln_col matrix.  FP64 values: a CTA per row for rows of
+// at least 2048 columns, a warp per row below; 16-byte loads (pairs of
+// doubles) where the row start is 16-byte aligned, x through L1 (every row
+// reuses it), one FP64 multiply-add per entry (GB300's FP64 pipe, not HBM,
+// bounds an FP64 GEMV), partial sums combined in a fixed order and added to
+// r_i.  FP32 / BF16 values: double-float arithmetic on the FP32 pipes
+// (dense_gemv_df, below).
 #include <algorithm>
 
 #include "common.cuh"
