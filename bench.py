@@ -435,20 +435,22 @@ def run_ours(a):
 
 
 def run_reference(a):
+    """The reference arm: the reference's CSR Ax loop (MatrixCSR.cpp:209-233,
+    schedule(static) over all host cores) on the same workload.  The matrix
+    and x come from the oracle's restatement of the library's generator, so
+    this process loads only oracle code (never the GPU library)."""
     ws, rank, local = dist()
     if rank != 0:
         return
-    import numpy as np
-
-    import tbsla_gb300 as T
+    import oracle
 
     n = a.n
-    m = T.MatrixCSR()
-    m.fill_powerlaw(n, 16.0, 2.0, 4096, 0.3, 1024, 1)
-    nnz = m.get_nnz()
-    arrays = m.arrays()
-    del m
-    x = T.fill_uniform(n, 0.0, 1.0, 1)
+    t0 = time.time()
+    rp, ci, va = oracle.gen_powerlaw(n, 16.0, 2.0, 4096, 0.3, 1024, 1)
+    x = oracle.gen_uniform(n, 0.0, 1.0, 1)
+    t_gen = time.time() - t0
+    nnz = int(rp[-1])
+    arrays = {"rowptr": rp, "colidx": ci, "values": va}
     B = algorithmic_bytes(n, nnz, 8)
     kind, _, _ = cpu_reference_time(arrays, x, n, nnz, 0.0, reps_min=a.warmup, reps_max=a.warmup)
     kind, times, _ = cpu_reference_time(arrays, x, n, nnz, 0.0, reps_min=a.steps, reps_max=a.steps)
@@ -469,7 +471,9 @@ def run_reference(a):
         "dtype": "f64",
         "data": "synthetic: seeded generator (power-law rows, seed 1), no dataset",
         "config": {"workload": f"csr_spmv_powerlaw_n{n}_mean16_zipf2_max4096_local30pct_f64", "format": "CSR",
-                   "n": n, "nnz": nnz, "bytes_per_step": B, "parallelism": "host cores (OpenMP)"},
+                   "n": n, "nnz": nnz, "bytes_per_step": B, "parallelism": "host cores (OpenMP)",
+                   "generator": "oracle restatement of the library's power-law generator (identical arrays)",
+                   "gen_s": round(t_gen, 2)},
         "cpu_baseline": {"value": val, "unit": "GB/s", "cores": os.cpu_count(), "kind": kind,
                          "sample": f"{a.steps} full CSR Ax steps of the workload after {a.warmup} warm-up"},
         "e2e": {"value": val, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

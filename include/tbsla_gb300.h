@@ -95,6 +95,11 @@ int tbsla_matrix_set_coo(tbsla_matrix* m, const tbsla_info* info, const double* 
                          const int* row, const int* col);
 int tbsla_matrix_set_csr(tbsla_matrix* m, const tbsla_info* info, const double* values,
                          const int* rowptr, const int* colidx);
+/* Appends one entry (row, col, value) to a COO / SCOO handle (nnz grows by
+ * one; indices as stored, i.e. global for SCOO blocks); replaces
+ * MatrixSCOO::push_back (src/cpp/include/tbsla/cpp/MatrixSCOO.hpp:25), which
+ * the reference declares but never defines. */
+int tbsla_matrix_push_back(tbsla_matrix* m, int row, int col, double value);
 int tbsla_matrix_set_ell(tbsla_matrix* m, const tbsla_info* info, const double* values,
                          const int* columns);
 int tbsla_matrix_set_dense(tbsla_matrix* m, const tbsla_info* info, const double* values);
@@ -258,9 +263,13 @@ int tbsla_spmv_device(const tbsla_matrix* m, double* r, const double* v, int vec
  * a loop that must not call the CUDA allocator -- and that cannot build a
  * handle, which copies the matrix and allocates per-matrix scratch.  The
  * merge-path kernel's scratch (tile starts and carries) lives in a fixed
- * 1.25 MiB device array inside the library, so n_row + nnz may not exceed
- * TBSLA_NOALLOC_MAX_ITEMS (TBSLA_ERR_INVALID_ARG otherwise).  The first call
- * on a device looks the array up and should come before any stream capture.
+ * device array inside the library of 1,048,832 bytes (about 1 MiB: 65,536
+ * FP64 carries, 65,536 int32 carry rows and 65,537 int32 tile starts),
+ * which every device that loads the library holds until exit, so n_row +
+ * nnz may not exceed TBSLA_NOALLOC_MAX_ITEMS (TBSLA_ERR_INVALID_ARG
+ * otherwise).  Each call looks the array's device address up; the first
+ * call on a device loads the library's module there and should come before
+ * any stream capture.
  * Calls that overlap in time share the array and race: serialise them.
  * Results equal tbsla_Ax_device on a handle set to TBSLA_CSR_MERGE with 8
  * items. */

@@ -36,6 +36,10 @@ def lib() -> C.CDLL:
         _o.orc_pagerank.restype = I
         _o.orc_cg.restype = I
         _o.orc_ell_max_col.restype = I
+        _o.orc_gen_powerlaw_rows.restype = L
+        _o.orc_gen_powerlaw_rows.argtypes = [I, D, D, I, C.c_ulonglong, P]
+        _o.orc_gen_powerlaw_entries.argtypes = [I, D, I, C.c_ulonglong, P, P, P]
+        _o.orc_gen_uniform.argtypes = [P, L, D, D, C.c_ulonglong]
     return _o
 
 
@@ -80,6 +84,27 @@ def csr_ax(rowptr, colidx, values, v, r=None, f_col=0, nnz=None, threads=False):
     fn = lib().orc_csr_ax_omp if threads else lib().orc_csr_ax
     fn(I(n), I(f_col), L(nnz), _p(values), _p(rowptr), _p(colidx), _p(v), _p(r))
     return r
+
+
+def gen_powerlaw(n, mean_len=16.0, zipf_s=2.0, max_len=4096, local_frac=0.3, band=1024, seed=1):
+    """The large-SpMV workload matrix as CSR arrays (rowptr, colidx, values),
+    restated from this library's generator so that the CPU baseline does not
+    load the library it is compared with."""
+    rowptr = np.zeros(n + 1, np.int32)
+    nnz = lib().orc_gen_powerlaw_rows(I(n), D(mean_len), D(zipf_s), I(max_len), C.c_ulonglong(seed), _p(rowptr))
+    if nnz < 0:
+        raise ValueError("bad power-law parameters")
+    colidx = np.empty(nnz, np.int32)
+    values = np.empty(nnz, np.float64)
+    lib().orc_gen_powerlaw_entries(I(n), D(local_frac), I(band), C.c_ulonglong(seed), _p(rowptr), _p(colidx),
+                                   _p(values))
+    return rowptr, colidx, values
+
+
+def gen_uniform(n, lo, hi, seed):
+    out = np.empty(n)
+    lib().orc_gen_uniform(_p(out), L(n), D(lo), D(hi), C.c_ulonglong(seed))
+    return out
 
 
 def csr_ax_f32(rowptr, colidx, values32, v, r=None, f_col=0):

@@ -9,9 +9,10 @@ Build recipe for the two CPU checkers:
 * ``oracle/_ref/libtbsla_ref.so``: the unmodified reference core
   (``src/cpp/matrix/*.cpp`` + ``src/cpp/utils/*.cpp``), compiled straight
   from where those sources lie in the reference tree, together with
-  ``ref_shim.cpp``.  Built only where the reference tree exists; it is used to
-  record the golden vectors under ``tests/golden/`` and to validate the
-  restatement.  Nothing is copied out of the reference tree.
+  ``ref_shim.cpp``.  Built only where the reference tree is named by the
+  environment variable ``TBSLA_REFERENCE_ROOT`` (the TBSLA source tree's
+  root); it is used to record the golden vectors under ``tests/golden/`` and
+  to validate the restatement.  Nothing is copied out of the reference tree.
 """
 from __future__ import annotations
 
@@ -21,7 +22,18 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("TBSLA_REFERENCE_ROOT", "/root/reference")
+
+
+def ref_root() -> str | None:
+    """The reference tree's root from TBSLA_REFERENCE_ROOT; None when unset.
+    A set variable that names no TBSLA tree is an error."""
+    root = os.environ.get("TBSLA_REFERENCE_ROOT")
+    if not root:
+        return None
+    if not os.path.isdir(os.path.join(root, "src", "cpp", "matrix")):
+        raise RuntimeError(f"TBSLA_REFERENCE_ROOT={root!r} holds no src/cpp/matrix: not a TBSLA source tree")
+    return root
+
 ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libtbsla_ref.so")
 
@@ -44,7 +56,10 @@ def build_oracle(force: bool = False) -> str:
 
 
 def reference_sources() -> list[str]:
-    cpp = os.path.join(REF_ROOT, "src", "cpp")
+    root = ref_root()
+    if root is None:
+        return []
+    cpp = os.path.join(root, "src", "cpp")
     return sorted(glob.glob(os.path.join(cpp, "matrix", "*.cpp")) +
                   glob.glob(os.path.join(cpp, "utils", "*.cpp")))
 
@@ -57,7 +72,7 @@ def build_reference(force: bool = False) -> str | None:
     shim = os.path.join(HERE, "ref_shim.cpp")
     if force or _newer(REF_SO, srcs + [shim]):
         os.makedirs(os.path.dirname(REF_SO), exist_ok=True)
-        inc = os.path.join(REF_ROOT, "src", "cpp", "include")
+        inc = os.path.join(ref_root(), "src", "cpp", "include")
         cmd = ["g++", "-O3", "-std=c++14", "-fopenmp", "-fPIC", "-shared", "-I", inc,
                *srcs, shim, "-o", REF_SO]
         subprocess.check_call(cmd)

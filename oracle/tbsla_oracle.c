@@ -433,3 +433,164 @@ int orc_cg(int n, const int* rowptr, const int* colidx, const double* values,
   free(ap);
   return it;
 }
+
+/* ---- workload generator: the power-law SpMV matrix ----------------------
+ * Not a reference function: a restatement of this library's own generator
+ * (fill_powerlaw / fill_uniform of its host code), so that the CPU baseline
+ * can build the large-SpMV matrix without loading the library it is timed
+ * against.  Rows draw their length from a truncated Zipf law rescaled to the
+ * requested mean (stochastic rounding), their columns (a share `local_frac`
+ * within +-band of the diagonal, the rest uniform) from a counter-based
+ * SplitMix64 hash of (seed, row, draw), so every row depends only on its
+ * index.  Compiled with -ffp-contract=off, as the library's host code is, the
+ * arrays are identical to the library's on every host. */
+#include <stdint.h>
+
+static uint64_t gen_mix64(uint64_t z) {
+  z += 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+static uint64_t gen_hash3(uint64_t seed, uint64_t a, uint64_t b) {
+  return gen_mix64(gen_mix64(seed ^ gen_mix64(a + 0x632BE59BD9B4E019ull)) + b);
+}
+static double gen_u01(uint64_t h) { return (double)(h >> 11) * 0x1.0p-53; }
+static double gen_um11(uint64_t h) { return 2.0 * gen_u01(h) - 1.0; }
+
+typedef struct {
+  double* cdf;
+  int kmax;
+  double mean;
+} gen_zipf;
+
+static void zipf_init(gen_zipf* z, double s, int kmax) {
+  z->cdf = (double*)malloc(sizeof(double) * (size_t)kmax);
+  z->kmax = kmax;
+  double tot = 0, m = 0;
+  for (int k = 1; k <= kmax; k++) {
+    double p = pow((double)k, -s);
+    tot += p;
+    m += k * p;
+    z->cdf[k - 1] = tot;
+  }
+  for (int k = 0; k < kmax; k++) z->cdf[k] /= tot;
+  z->mean = m / tot;
+}
+
+/* first index whose cdf exceeds u, plus one */
+static int zipf_draw(const gen_zipf* z, double u) {
+  int lo = 0, hi = z->kmax;
+  while (lo < hi) {
+    int mid = lo + (hi - lo) / 2;
+    if (z->cdf[mid] > u) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo + 1;
+}
+
+static long zipf_rescale(int k, double scale, double u, long lo, long kmax) {
+  double y = k * scale;
+  long r = (long)floor(y);
+  if (u < y - (double)r) r++;
+  if (r < lo) r = lo;
+  if (r > kmax) r = kmax;
+  return r;
+}
+
+static double zipf_mean_at(const gen_zipf* z, double sc, long lo, long kmax) {
+  double m = 0, prev = 0;
+  for (int k = 1; k <= z->kmax; k++) {
+    double v = (double)k * sc;
+    if (v < (double)lo) v = (double)lo;
+    if (v > (double)kmax) v = (double)kmax;
+    m += (z->cdf[k - 1] - prev) * v;
+    prev = z->cdf[k - 1];
+  }
+  return m;
+}
+
+static double zipf_scale_for(const gen_zipf* z, double target, long lo, long kmax) {
+  double a = 0, b = 2.0 * target / z->mean + 1.0;
+  while (zipf_mean_at(z, b, lo, kmax) < target && b < 1e9) b *= 2;
+  for (int it = 0; it < 200; it++) {
+    double c = 0.5 * (a + b);
+    if (zipf_mean_at(z, c, lo, kmax) < target) a = c;
+    else b = c;
+  }
+  return b;
+}
+
+static int cmp_int(const void* a, const void* b) {
+  int x = *(const int*)a, y = *(const int*)b;
+  return (x > y) - (x < y);
+}
+
+long orc_gen_powerlaw_rows(int n, double mean_len, double zipf_s, int max_len,
+                           unsigned long long seed, int* rowptr) {
+  if (n <= 0 || max_len <= 0 || max_len > n) return -1;
+  gen_zipf z;
+  zipf_init(&z, zipf_s, max_len);
+  const double scale = zipf_scale_for(&z, mean_len, 1, max_len);
+  rowptr[0] = 0;
+  long acc = 0;
+  for (long i = 0; i < n; i++) {
+    int k = zipf_draw(&z, gen_u01(gen_hash3(seed, 1, (uint64_t)i)));
+    acc += zipf_rescale(k, scale, gen_u01(gen_hash3(seed, 12, (uint64_t)i)), 1, max_len);
+    if (acc > 0x7fffffffL) {
+      free(z.cdf);
+      return -1;
+    }
+    rowptr[i + 1] = (int)acc;
+  }
+  free(z.cdf);
+  return acc;
+}
+
+void orc_gen_powerlaw_entries(int n, double local_frac, int band, unsigned long long seed,
+                              const int* rowptr, int* colidx, double* values) {
+#pragma omp parallel
+  {
+    int cap = 16;
+    int* cols = (int*)malloc(sizeof(int) * (size_t)cap);
+#pragma omp for schedule(dynamic, 4096)
+    for (long i = 0; i < n; i++) {
+      int L = rowptr[i + 1] - rowptr[i];
+      long lo = i - band < 0 ? 0 : i - band;
+      long hi = i + band > (long)n - 1 ? (long)n - 1 : i + band;
+      int want = L < n ? L : n;
+      if (want > cap) {
+        cap = want;
+        cols = (int*)realloc(cols, sizeof(int) * (size_t)cap);
+      }
+      int size = 0;
+      uint64_t t = 0;
+      while (size < want) {
+        int need = want - size;
+        for (int d = 0; d < need; d++) {
+          uint64_t h = gen_hash3(seed, 2 + (uint64_t)i * 2, t++);
+          int local = gen_u01(h) < local_frac;
+          uint64_t h2 = gen_hash3(seed, 3 + (uint64_t)i * 2, t);
+          long c = local ? lo + (long)(h2 % (uint64_t)(hi - lo + 1)) : (long)(h2 % (uint64_t)n);
+          cols[size++] = (int)c;
+        }
+        qsort(cols, (size_t)size, sizeof(int), cmp_int);
+        int u = 0;
+        for (int q = 0; q < size; q++)
+          if (q == 0 || cols[q] != cols[u - 1]) cols[u++] = cols[q];
+        size = u;
+      }
+      long p0 = rowptr[i];
+      for (int j = 0; j < want; j++) {
+        colidx[p0 + j] = cols[j];
+        values[p0 + j] = gen_um11(gen_hash3(seed ^ 0xC3C3C3C3ull, 4, (uint64_t)(p0 + j)));
+      }
+    }
+    free(cols);
+  }
+}
+
+void orc_gen_uniform(double* out, long n, double lo, double hi, unsigned long long seed) {
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < n; i++) out[i] = lo + (hi - lo) * gen_u01(gen_hash3(seed, 0x5eed, (uint64_t)i));
+}

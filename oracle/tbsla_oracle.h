@@ -68,6 +68,13 @@ int orc_cg(int n, const int* rowptr, const int* colidx, const double* values,
            const double* diag_inv, const double* b, double* x, int max_iterations,
            double rel_tol, double* rel_residual);
 
+/* ---- the power-law workload matrix (this library's generator, restated) */
+long orc_gen_powerlaw_rows(int n, double mean_len, double zipf_s, int max_len,
+                           unsigned long long seed, int* rowptr);
+void orc_gen_powerlaw_entries(int n, double local_frac, int band, unsigned long long seed,
+                              const int* rowptr, int* colidx, double* values);
+void orc_gen_uniform(double* out, long n, double lo, double hi, unsigned long long seed);
+
 #ifdef __cplusplus
 }
 #endif

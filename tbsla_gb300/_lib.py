@@ -82,6 +82,7 @@ _SIGS = {
     "tbsla_matrix_info": (I, [P, C.POINTER(Info)]),
     "tbsla_matrix_set_coo": (I, [P, C.POINTER(Info), P, P, P]),
     "tbsla_matrix_set_csr": (I, [P, C.POINTER(Info), P, P, P]),
+    "tbsla_matrix_push_back": (I, [P, I, I, D]),
     "tbsla_matrix_set_ell": (I, [P, C.POINTER(Info), P, P]),
     "tbsla_matrix_set_dense": (I, [P, C.POINTER(Info), P]),
     "tbsla_matrix_arrays": (I, [P, C.POINTER(P), C.POINTER(P), C.POINTER(P)]),

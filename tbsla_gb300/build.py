@@ -51,7 +51,7 @@ def _stale(target: str, deps: list[str]) -> bool:
 def _compile(src: str, hdr: list[str], verbose: bool) -> str:
     rel = os.path.relpath(src, PKG).replace(os.sep, "_")
     obj = os.path.join(BUILD, rel + ".o")
-    if not _stale(obj, [src] + hdr):
+    if not _stale(obj, [src, os.path.abspath(__file__)] + hdr):
         return obj
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC,
            "-I", os.path.join(PKG, "cpp", "include")]
@@ -62,7 +62,7 @@ def _compile(src: str, hdr: list[str], verbose: bool) -> str:
         if os.environ.get("TBSLA_PTXAS_VERBOSE"):
             cmd.insert(1, "-Xptxas=-v")
     else:
-        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function",
+        cmd = ["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-unused-function",
                "-I", os.path.join(_cuda_home(), "include"), *inc, "-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)

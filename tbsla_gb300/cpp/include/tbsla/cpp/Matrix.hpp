@@ -22,6 +22,7 @@
 #define TBSLA_GB300_CPP_MATRIX
 
 #include <cstddef>
+#include <fstream>
 #include <iostream>
 #include <stdexcept>
 #include <string>
@@ -56,6 +57,9 @@ class Matrix {
   void AAxpAx(double* r, double* v, double* buffer, int vect_incr = 0) const;
   void AAxpAxpx(double* r, double* v, double* buffer, int vect_incr = 0) const;
   double* a_axpx_(const double* v, int vect_incr = 0) const;
+  // Declared as in Matrix.hpp:20 of the reference, which defines it nowhere:
+  // a program that calls it links against neither library.
+  double*& saxpy(const double* x, double* y);
 
   int get_n_row() const { return info().n_row; }
   int get_n_col() const { return info().n_col; }

@@ -12,6 +12,16 @@ class MatrixCOO : public Matrix {
     MatrixCOO();
 
     MatrixCOO(int n_row, int n_col, long nnz, const double* values, const int* row, const int* col);
+    // MatrixCOO.hpp:13: the reference adopts the three pointers but leaves
+    // nnz uninitialised (MatrixCOO.cpp:45-65), so their length is unknown.
+    // Here the matrix is n_row x n_col with no entries and the arrays are
+    // neither read nor adopted: pass the length with the overload above.
+    MatrixCOO(int n_row, int n_col, double* values, int* row, int* col);
+    // MatrixCOO.hpp:14: n_values zero entries at (0, 0) (the reference's
+    // zero-filled arrays of that length).
+    MatrixCOO(int n_row, int n_col, long n_values);
+    // MatrixCOO.hpp:15: an n_row x n_col matrix with no entries.
+    MatrixCOO(int n_row, int n_col);
     const double* get_values() const;
     const int* get_row() const;
     const int* get_col() const;

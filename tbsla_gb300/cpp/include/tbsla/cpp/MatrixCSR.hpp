@@ -21,6 +21,8 @@ class MatrixCSR : public Matrix {
             double rel_tol = 1e-8, int precond = 0);
     // C = A B (MatrixCSR.cpp:1269-1281), on the GPU
     void dense_multiply(const double* B, double* C, int cols_B);
+    // MatrixCSR.hpp:33: base -1 (the default) is e^x
+    void apply_exponential(double* max_abs, int base = -1) override;
 };
 
 }}  // namespace tbsla::cpp

@@ -236,6 +236,21 @@ MatrixCOO::MatrixCOO(int n_row, int n_col, long nnz, const double* values, const
   tbsla_info i = square_info(n_row, n_col, nnz);
   check(tbsla_matrix_set_coo(h_, &i, values, row, col), "set_coo");
 }
+MatrixCOO::MatrixCOO(int n_row, int n_col, double*, int*, int*) : Matrix(TBSLA_COO) {
+  tbsla_info i = square_info(n_row, n_col, 0);
+  check(tbsla_matrix_set_coo(h_, &i, nullptr, nullptr, nullptr), "set_coo");
+}
+MatrixCOO::MatrixCOO(int n_row, int n_col, long n_values) : Matrix(TBSLA_COO) {
+  if (n_values < 0) throw GpuError(TBSLA_ERR_INVALID_ARG, "MatrixCOO");
+  std::vector<double> v((size_t)n_values, 0.0);
+  std::vector<int> z((size_t)n_values, 0);
+  tbsla_info i = square_info(n_row, n_col, n_values);
+  check(tbsla_matrix_set_coo(h_, &i, v.data(), z.data(), z.data()), "set_coo");
+}
+MatrixCOO::MatrixCOO(int n_row, int n_col) : Matrix(TBSLA_COO) {
+  tbsla_info i = square_info(n_row, n_col, 0);
+  check(tbsla_matrix_set_coo(h_, &i, nullptr, nullptr, nullptr), "set_coo");
+}
 const double* MatrixCOO::get_values() const {
   const double* v;
   check(tbsla_matrix_arrays(h_, &v, nullptr, nullptr), "arrays");
@@ -292,7 +307,15 @@ MatrixSCOO::MatrixSCOO(int n_row, int n_col, long nnz, const double* values, con
   check(tbsla_matrix_set_coo(h_, &i, values, row, col), "set_coo");
 }
 
+MatrixSCOO::MatrixSCOO(int n_row, int n_col, int) : MatrixSCOO(n_row, n_col) {}
+MatrixSCOO::MatrixSCOO(int n_row, int n_col) : Matrix(TBSLA_SCOO) {
+  tbsla_info i = square_info(n_row, n_col, 0);
+  check(tbsla_matrix_set_coo(h_, &i, nullptr, nullptr, nullptr), "set_coo");
+}
+void MatrixSCOO::push_back(int r, int c, double v) { check(tbsla_matrix_push_back(h_, r, c, v), "push_back"); }
+
 MatrixCSR::MatrixCSR() : Matrix(TBSLA_CSR) {}
+void MatrixCSR::apply_exponential(double* max_abs, int base) { Matrix::apply_exponential(max_abs, base); }
 MatrixCSR::MatrixCSR(const MatrixCOO& m) : Matrix(TBSLA_CSR, convert(m, TBSLA_CSR)) {}
 MatrixCSR::MatrixCSR(int n_row, int n_col, double* values, int* rowptr, int* colidx) : Matrix(TBSLA_CSR) {
   tbsla_info i = square_info(n_row, n_col, rowptr ? rowptr[n_row] : 0);

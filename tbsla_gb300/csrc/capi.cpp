@@ -88,6 +88,17 @@ int tbsla_matrix_set_coo(tbsla_matrix* m, const tbsla_info* info, const double* 
   return TBSLA_OK;
 }
 
+int tbsla_matrix_push_back(tbsla_matrix* m, int row, int col, double value) {
+  if (!m || (m->format != TBSLA_COO && m->format != TBSLA_SCOO)) return TBSLA_ERR_INVALID_ARG;
+  if ((size_t)m->info.nnz != m->values.size()) return TBSLA_ERR_BAD_MATRIX;
+  m->invalidate();
+  m->values.push(value);
+  m->idx0.push(row);
+  m->idx1.push(col);
+  m->info.nnz += 1;
+  return TBSLA_OK;
+}
+
 int tbsla_matrix_set_csr(tbsla_matrix* m, const tbsla_info* info, const double* values,
                          const int* rowptr, const int* colidx) {
   if (!m || m->format != TBSLA_CSR || !sane_info(info)) return TBSLA_ERR_INVALID_ARG;

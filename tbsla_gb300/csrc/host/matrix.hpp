@@ -18,10 +18,21 @@ namespace tbsla_impl {
 template <class T>
 struct Buf {
   std::unique_ptr<T[]> p;
-  size_t n = 0;
+  size_t n = 0, cap = 0;
   void resize(size_t k) {
     p.reset(k ? new T[k] : nullptr);
-    n = k;
+    n = cap = k;
+  }
+  // Appends one element, doubling the capacity when full (amortised O(1)).
+  void push(const T& v) {
+    if (n == cap) {
+      const size_t c = cap ? 2 * cap : 16;
+      std::unique_ptr<T[]> q(new T[c]);
+      if (n) std::memcpy(q.get(), p.get(), n * sizeof(T));
+      p = std::move(q);
+      cap = c;
+    }
+    p[n++] = v;
   }
   void assign(const T* src, size_t k) {
     resize(k);

@@ -337,15 +337,10 @@ __global__ void k_diag_inv(const int* __restrict__ rowptr, const int* __restrict
   }
 }
 
-template <class K>
-cudaError_t prepare(K kernel, size_t smem) {
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
 template <class V, int ITEMS>
 cudaError_t launch_dot(const CgBatch& c, cudaStream_t s) {
   constexpr size_t smem = stage_bytes<V, ITEMS>();
-  static cudaError_t ready = prepare(k_cg_spmv_dot<V, ITEMS>, smem);
+  cudaError_t ready = smem_opt_in<k_cg_spmv_dot<V, ITEMS>>(smem);
   if (ready != cudaSuccess) return ready;
   k_cg_spmv_dot<V, ITEMS><<<(c.nblocks + kDotBlocksPerCta - 1) / kDotBlocksPerCta, NT, smem, s>>>(c);
   return cudaGetLastError();
@@ -354,7 +349,7 @@ cudaError_t launch_dot(const CgBatch& c, cudaStream_t s) {
 template <int ITEMS>
 cudaError_t launch_res(const CgBatch& c, int mask, cudaStream_t s) {
   constexpr size_t smem = stage_bytes<double, ITEMS>();
-  static cudaError_t ready = prepare(k_cg_residual<ITEMS>, smem);
+  cudaError_t ready = smem_opt_in<k_cg_residual<ITEMS>>(smem);
   if (ready != cudaSuccess) return ready;
   k_cg_residual<ITEMS><<<c.nblocks, NT, smem, s>>>(c, mask);
   return cudaGetLastError();

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace tbsla_gpu {
 
 constexpr int kWarp = 32;
@@ -130,6 +132,23 @@ __device__ __forceinline__ double block_sum(double v, double* scratch) {
   }
   __syncthreads();
   return r;
+}
+
+// Opts `Kernel` in to `smem` bytes of dynamic shared memory on the current
+// device.  The attribute belongs to each device's context, so it is set once
+// per device ordinal and kernel instantiation (a bit per device; ordinals
+// past 63 set it on every call).
+template <auto Kernel>
+cudaError_t smem_opt_in(size_t smem) {
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const unsigned long long bit = dev >= 0 && dev < 64 ? 1ull << dev : 0ull;
+  if (bit && (done.load(std::memory_order_acquire) & bit)) return cudaSuccess;
+  e = cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && bit) done.fetch_or(bit, std::memory_order_acq_rel);
+  return e;
 }
 
 }  // namespace tbsla_gpu

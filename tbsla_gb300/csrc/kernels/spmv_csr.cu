@@ -346,16 +346,10 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched(CsrArgs a, int nvec
   batched_finish(err, sum, dsum, nvec, s_red, sm, p, ctl);
 }
 
-template <class K>
-cudaError_t prepare(K kernel, size_t smem) {
-  // opt in to more than 48 KB of dynamic shared memory where the stage needs it
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
 template <class V, int ITEMS>
 cudaError_t launch_spmv(const CsrArgs& a, const double* x, double* y, cudaStream_t s) {
   constexpr size_t smem = stage_bytes<V, ITEMS>();
-  static cudaError_t ready = prepare(k_csr_spmv<V, ITEMS>, smem);
+  cudaError_t ready = smem_opt_in<k_csr_spmv<V, ITEMS>>(smem);
   if (ready != cudaSuccess) return ready;
   k_csr_spmv<V, ITEMS><<<a.nblocks, NT, smem, s>>>(a, x, y);
   return cudaGetLastError();
@@ -375,7 +369,7 @@ template <class V, int ITEMS>
 cudaError_t launch_pr(const CsrArgs& a, const double* x, double* y, const PageRankArgs& p, Ctl c,
                       int grid, cudaStream_t s) {
   constexpr size_t smem = stage_bytes<V, ITEMS>();
-  static cudaError_t ready = prepare(k_csr_pagerank<V, ITEMS>, smem);
+  cudaError_t ready = smem_opt_in<k_csr_pagerank<V, ITEMS>>(smem);
   if (ready != cudaSuccess) return ready;
   k_csr_pagerank<V, ITEMS><<<grid, NT, smem, s>>>(a, x, y, p, c);
   return cudaGetLastError();
@@ -417,37 +411,37 @@ void csr_partition(const int* rowptr, int n_row, int tile, int** out, int* nbloc
 }
 
 namespace {
-template <class K>
-int resident_grid(K kernel, size_t smem = 0) {
+template <auto Kernel>
+int resident_grid(size_t smem = 0) {
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (smem) prepare(kernel, smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, NT, smem);
+  if (smem) smem_opt_in<Kernel>(smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, Kernel, NT, smem);
   return std::max(1, sms * std::max(1, per));
 }
 }  // namespace
 
 int csr_pagerank_grid(int items, int prec) {
   switch (prec * 100 + items) {
-    case kF64 * 100 + 4: return resident_grid(k_csr_pagerank<double, 4>, stage_bytes<double, 4>());
-    case kF64 * 100 + 8: return resident_grid(k_csr_pagerank<double, 8>, stage_bytes<double, 8>());
-    case kF64 * 100 + 16: return resident_grid(k_csr_pagerank<double, 16>, stage_bytes<double, 16>());
-    case kF32 * 100 + 4: return resident_grid(k_csr_pagerank<float, 4>, stage_bytes<float, 4>());
-    case kF32 * 100 + 8: return resident_grid(k_csr_pagerank<float, 8>, stage_bytes<float, 8>());
-    case kF32 * 100 + 16: return resident_grid(k_csr_pagerank<float, 16>, stage_bytes<float, 16>());
-    case kBF16 * 100 + 4: return resident_grid(k_csr_pagerank<__nv_bfloat16, 4>, stage_bytes<__nv_bfloat16, 4>());
-    case kBF16 * 100 + 8: return resident_grid(k_csr_pagerank<__nv_bfloat16, 8>, stage_bytes<__nv_bfloat16, 8>());
-    case kBF16 * 100 + 16: return resident_grid(k_csr_pagerank<__nv_bfloat16, 16>, stage_bytes<__nv_bfloat16, 16>());
+    case kF64 * 100 + 4: return resident_grid<k_csr_pagerank<double, 4>>(stage_bytes<double, 4>());
+    case kF64 * 100 + 8: return resident_grid<k_csr_pagerank<double, 8>>(stage_bytes<double, 8>());
+    case kF64 * 100 + 16: return resident_grid<k_csr_pagerank<double, 16>>(stage_bytes<double, 16>());
+    case kF32 * 100 + 4: return resident_grid<k_csr_pagerank<float, 4>>(stage_bytes<float, 4>());
+    case kF32 * 100 + 8: return resident_grid<k_csr_pagerank<float, 8>>(stage_bytes<float, 8>());
+    case kF32 * 100 + 16: return resident_grid<k_csr_pagerank<float, 16>>(stage_bytes<float, 16>());
+    case kBF16 * 100 + 4: return resident_grid<k_csr_pagerank<__nv_bfloat16, 4>>(stage_bytes<__nv_bfloat16, 4>());
+    case kBF16 * 100 + 8: return resident_grid<k_csr_pagerank<__nv_bfloat16, 8>>(stage_bytes<__nv_bfloat16, 8>());
+    case kBF16 * 100 + 16: return resident_grid<k_csr_pagerank<__nv_bfloat16, 16>>(stage_bytes<__nv_bfloat16, 16>());
   }
   return 152;
 }
 
 int csr_pagerank_batched_grid(int prec) {
   switch (prec) {
-    case kF64: return resident_grid(k_csr_pagerank_batched<double>);
-    case kF32: return resident_grid(k_csr_pagerank_batched_df<float>);
-    case kBF16: return resident_grid(k_csr_pagerank_batched_df<__nv_bfloat16>);
+    case kF64: return resident_grid<k_csr_pagerank_batched<double>>();
+    case kF32: return resident_grid<k_csr_pagerank_batched_df<float>>();
+    case kBF16: return resident_grid<k_csr_pagerank_batched_df<__nv_bfloat16>>();
   }
   return 152;
 }

@@ -25,7 +25,6 @@
 //      the carries, in tile order, to the rows they belong to.
 // Results are deterministic (no atomics).
 #include <algorithm>
-#include <mutex>
 
 #include "common.cuh"
 #include "kernels.hpp"
@@ -234,8 +233,7 @@ __global__ void k_merge_carries(const int* __restrict__ carry_row, const double*
 template <class V, int ITEMS>
 cudaError_t launch(const MergeArgs& a, const double* x, double* y, cudaStream_t s) {
   constexpr size_t smem = merge_smem<V, ITEMS>();
-  static cudaError_t ready =
-      cudaFuncSetAttribute(k_csr_merge<V, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t ready = smem_opt_in<k_csr_merge<V, ITEMS>>(smem);
   if (ready != cudaSuccess) return ready;
   k_csr_merge<V, ITEMS><<<(unsigned)a.ntiles, NT, smem, s>>>(
       static_cast<const V*>(a.vals), a.rowptr, a.colidx, a.n, a.nnz, a.f_col, a.coord, x, y, a.carry_row,
@@ -290,7 +288,9 @@ cudaError_t csr_merge_spmv(const MergeArgs& a, const double* x, double* y, cudaS
 // (an application whose memory pool owns the whole device, or a loop that
 // must not call the CUDA allocator).  The array serves up to
 // kNoAllocTiles tiles of 2048 merge items (n_row + nnz <= 134,217,728);
-// bigger inputs are rejected.  Every scratch word is written before it is
+// bigger inputs are rejected.  Its size is 65,536 FP64 carries + 65,536
+// int32 carry rows + 65,537 int32 tile starts = 1,048,580 bytes, rounded up
+// to 1,048,832 (about 1 MiB), held on every device that loads the library.  Every scratch word is written before it is
 // read within a call, so nothing needs clearing between calls.  Calls that
 // overlap in time (other streams, other host threads) share the array and
 // race: the caller serialises them.
@@ -301,26 +301,16 @@ constexpr size_t kNoAllocBytes =
     (size_t)kNoAllocTiles * sizeof(double) + (size_t)kNoAllocTiles * sizeof(int) + (kNoAllocTiles + 1) * sizeof(int);
 static __device__ __align__(256) unsigned char g_noalloc_scratch[(kNoAllocBytes + 255) / 256 * 256];
 
-constexpr int kNoAllocDevices = 64;
-std::mutex g_noalloc_mutex;
-void* g_noalloc_base[kNoAllocDevices] = {};
-
-// Device address of the scratch array on the current device, looked up once
-// per device (the first call on a device therefore belongs before any stream
-// capture).
+// Device address of the scratch array on the current device.  It is looked
+// up on every call (the lookup allocates nothing), so the address stays right
+// when a device was reset and the module reloaded at another address.  The
+// first lookup on a device loads the module there, so the first call on a
+// device belongs before any stream capture.
 cudaError_t noalloc_base(void** base) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kNoAllocDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_base[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return e;
-    g_noalloc_base[dev] = p;
-  }
-  *base = g_noalloc_base[dev];
+  *base = p;
   return cudaSuccess;
 }
 

@@ -226,6 +226,10 @@ class MatrixCOO(Matrix):
 class MatrixSCOO(Matrix):
     FORMAT = L.SCOO
 
+    def push_back(self, r: int, c: int, v: float):
+        """Appends the entry (r, c, v) (MatrixSCOO.hpp:25)."""
+        check(lib.tbsla_matrix_push_back(self._h, int(r), int(c), float(v)), "push_back")
+
     @classmethod
     def from_arrays(cls, info: dict, row, col, values):
         m = cls()

@@ -3,8 +3,9 @@
 // src/cpp/tests/test_Ax_cdiag.cpp (every format, filled directly and
 // converted from COO, shapes (10,10) (5,10) (10,5) c = 0..12 and (30,30)
 // (20,30) (30,20) c = 0..24 step 2), checked exactly against the closed form
-// of src/cpp/utils/array.cpp:17-30; plus spmv (new[] result), a_axpx_ and a
-// stream write/read round trip.  Exits non-zero on the first mismatch.
+// of src/cpp/utils/array.cpp:17-30; plus spmv (new[] result), a_axpx_, a
+// stream write/read round trip and SCOO blocks built by push_back.  Exits
+// non-zero on the first mismatch.
 #include <tbsla/cpp/MatrixCOO.hpp>
 #include <tbsla/cpp/MatrixCSR.hpp>
 #include <tbsla/cpp/MatrixDENSE.hpp>
@@ -78,6 +79,13 @@ static void test_cdiag(int nr, int nc, int c) {
   MatrixDENSE dense2;
   dense2.fill_cdiag(nr, nc, c);
   check(dense2, nr, nc, c, "DENSE");
+  // the same entries appended one by one (MatrixSCOO::push_back)
+  MatrixSCOO scoo3(nr, nc, (int)coo.get_nnz());
+  const double* cv = coo.get_values();
+  const int* cr = coo.get_row();
+  const int* cc = coo.get_col();
+  for (long k = 0; k < coo.get_nnz(); k++) scoo3.push_back(cr[k], cc[k], cv[k]);
+  check(scoo3, nr, nc, c, "SCOO(push_back)");
 }
 
 int main() {

@@ -19,7 +19,7 @@ records:
                 library's generators (seed 0), x = U[0,1) seed 0, plus
                 checksums of the generated arrays
 
-Usage: python tests/golden/make_golden.py
+Usage: TBSLA_REFERENCE_ROOT=<root of the TBSLA source tree> python tests/golden/make_golden.py
 """
 from __future__ import annotations
 
@@ -45,7 +45,7 @@ class Ref:
     def __init__(self):
         self.L = oracle.ref()
         if self.L is None:
-            raise SystemExit("reference tree not available: cannot record golden vectors")
+            raise SystemExit("reference core not available: set TBSLA_REFERENCE_ROOT to the TBSLA source tree")
 
     def new(self, fmt):
         return C.c_void_p(self.L.ref_new(fmt))

@@ -22,3 +22,15 @@ def test_reference_arm_prints_one_contract_line():
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_arm_loads_no_library_code():
+    """The reference arm must time the reference's loop with nothing of this
+    library in the process: no libtbsla_gb300.so mapped after a run."""
+    code = ("import runpy, sys; sys.argv = ['bench.py', '--impl', 'reference', '--n', '20000', '--steps', '1', "
+            "'--warmup', '1']; runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('LOADED' if 'libtbsla_gb300' in maps or 'libtbsla.so' in maps else 'CLEAN')")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert out.stdout.strip().splitlines()[-1] == "CLEAN"

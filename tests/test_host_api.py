@@ -248,3 +248,19 @@ def test_project_generators_are_deterministic():
     dense[rows, a7["colidx"]] = a7["values"]
     assert np.allclose(dense, dense.T)
     assert np.linalg.eigvalsh(dense).min() > 0
+
+
+@pytest.mark.parametrize("n,max_len,local,band,seed", [(1 << 18, 4096, 0.3, 1024, 1), (5000, 300, 0.6, 16, 7)])
+def test_oracle_powerlaw_generator_matches_library(n, max_len, local, band, seed):
+    """The CPU baseline builds the large-SpMV matrix with the oracle's
+    restatement of the library's power-law generator (so that it loads no
+    library code); both must give the same arrays."""
+    import oracle
+
+    rp, ci, va = oracle.gen_powerlaw(n, 16.0, 2.0, max_len, local, band, seed)
+    m = T.MatrixCSR()
+    m.fill_powerlaw(n, 16.0, 2.0, max_len, local, band, seed)
+    a = m.arrays()
+    assert np.array_equal(rp, a["rowptr"]) and np.array_equal(ci, a["colidx"])
+    assert np.array_equal(va, a["values"])
+    assert np.array_equal(oracle.gen_uniform(n, 0.0, 1.0, seed), T.fill_uniform(n, 0.0, 1.0, seed))

@@ -1,8 +1,10 @@
-"""The allocation-free CSR SpMV (tbsla_csr_Ax_device_noalloc) against the
-handle entry point tbsla_Ax_device with the same merge-path kernel: equal
-results on two calls in a row, no device memory taken by the second call,
-and inputs past the scratch limit rejected.  The file sorts last so that it
-also runs after every other GPU test."""
+"""The allocation-free CSR SpMV (tbsla_csr_Ax_device_noalloc), for callers
+that may not call the CUDA allocator on the call path: against the handle
+entry point tbsla_Ax_device with the same merge-path kernel (equal results
+on two calls in a row, no device memory taken by the second call), against
+the oracle's restatement of MatrixCSR::Ax (1e-13 of sum_j |a_ij x_j| per
+row), and inputs past the scratch limit rejected.  The file sorts last so
+that it also runs after every other GPU test."""
 import ctypes as C
 
 import numpy as np
@@ -46,6 +48,14 @@ def test_noalloc_matches_handle_entry_point(gpu):
         if k == 1:
             assert torch.cuda.mem_get_info()[0] == free[1]
     assert not torch.equal(ys[0], ys[1])
+    # pinned directly to the oracle as well, not only to the other entry point
+    import oracle
+
+    for k in range(2):
+        xk = xs[k].cpu().numpy()
+        ref = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], xk)
+        scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], xk)
+        assert oracle.rel_err_normalized(ys[k].cpu().numpy(), ref, scale) <= 1e-13, k
 
 
 def test_noalloc_rejects_inputs_past_the_limit(gpu):
