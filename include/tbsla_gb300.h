@@ -356,9 +356,14 @@ int tbsla_cg(tbsla_matrix* m, const double* b, double* x, int max_iterations, do
  * residual satisfies ||b - A x|| <= rel_tol ||b||; iterations[s] and
  * rel_residual[s] receive its count and final true relative residual.
  * precond: 0 none, 1 Jacobi, 2 the factors of tbsla_batch_set_factors
- * (z = L L^T r).  graph_iters: iterations captured per CUDA graph replay
- * (0: 10).  Returns TBSLA_ERR_NOT_CONVERGED if some system hit
- * max_iterations. */
+ * (z = L L^T r).  With FP32 / BF16 storage the iteration runs in FP32 as the
+ * inner solver of FP64 iterative refinement: every `refresh` iterations
+ * (and on apparent convergence) the correction is added to x in FP64, the
+ * FP64 true residual b - A x replaces r and the iteration restarts.
+ * graph_iters: iterations captured per CUDA graph replay of the
+ * multi-launch engine (0: 10); the persistent engine runs the whole solve in
+ * one launch.  Returns TBSLA_ERR_NOT_CONVERGED if some system hit
+ * max_iterations, TBSLA_ERR_TIMEOUT if a bounded device wait ran out. */
 typedef struct tbsla_batch tbsla_batch;
 int tbsla_batch_create(tbsla_batch** b, tbsla_matrix* const* systems, int nsys, int precision);
 int tbsla_batch_destroy(tbsla_batch* b);
@@ -366,6 +371,25 @@ int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets);
 int tbsla_batch_cg(tbsla_batch* b, const double* rhs, double* x, int max_iterations, double rel_tol,
                    int precond, int refresh, int graph_iters, int* iterations,
                    double* rel_residual);
+/* After the last tbsla_batch_cg, per system: fallback[s] = 0 when it ran
+ * with the preconditioner asked for, 1 when its factor failed the check made
+ * before the first iteration (a non-finite value or a diagonal entry <= 0)
+ * and it ran Jacobi-PCG instead, 2 when its factored iteration stopped making
+ * progress (a refinement cycle that did not lower the FP64 true residual, or
+ * r.z not positive and finite) and it continued with Jacobi-PCG;
+ * precond_used[s] = the preconditioner it ended with (0, 1, 2).  Either
+ * pointer may be NULL.  Plain Jacobi-PCG is the fallback of the factored
+ * preconditioner: the reference's CG (CG.cpp:32-73) has none. */
+int tbsla_batch_fallbacks(const tbsla_batch* b, int* fallback, int* precond_used);
+/* Bound, in nanoseconds, on one grid-wide wait of the persistent solver
+ * (default 2e9).  A wait that runs out ends that solve on the GPU with
+ * TBSLA_ERR_TIMEOUT; the batch stays usable. */
+int tbsla_batch_set_wait_limit(tbsla_batch* b, long long ns);
+/* The engine of the last tbsla_batch_cg: persistent = 1 when the whole solve
+ * was one cooperative launch (every system's entries on at most 8 diagonals,
+ * at most 256 systems, a factor, if used, on at most 8 diagonals), 0 for the
+ * multi-launch engine; graph = 1 when it was replayed from a CUDA graph. */
+int tbsla_batch_engine(const tbsla_batch* b, int* persistent, int* graph);
 /* Factored preconditioner M^-1 = L L^T for every system of the batch (L:
  * lower-triangular CSR handles, one per system, same sizes), used by
  * tbsla_batch_cg with precond = 2.  Values are stored in `precision`

@@ -112,6 +112,9 @@ _SIGS = {
     "tbsla_batch_rows": (I, [P, IP, C.POINTER(L)]),
     "tbsla_batch_cg": (I, [P, P, P, I, D, I, I, I, IP, DP]),
     "tbsla_batch_set_factors": (I, [P, C.POINTER(P), I, I]),
+    "tbsla_batch_fallbacks": (I, [P, IP, IP]),
+    "tbsla_batch_set_wait_limit": (I, [P, C.c_longlong]),
+    "tbsla_batch_engine": (I, [P, IP, IP]),
     "tbsla_mpnn_create": (I, [C.POINTER(P), ULL]),
     "tbsla_mpnn_destroy": (I, [P]),
     "tbsla_mpnn_params": (I, [P, P, IP]),

@@ -7,6 +7,19 @@
 // the row chunks of the vector kernels (neither crosses a system boundary,
 // each carries its system id), the Jacobi diagonal, six FP64 vectors (b, x,
 // r, z, p, q) and per-system scalars.
+//
+// Two engines solve a batch:
+//  - persistent (kernels/cg_dia.cu): when every system's entries lie on at
+//    most 8 diagonals (stencils) and there are at most 256 systems, the batch
+//    also holds A slot-major per diagonal (values in the storage precision
+//    and in FP64, a delta table per system), the FP32 Jacobi diagonal and
+//    eight solve vectors in the iteration precision (FP32 for FP32 / BF16
+//    storage); the whole solve is one cooperative launch, captured once in a
+//    CUDA graph and replayed.  A factored preconditioner on at most 8
+//    diagonals is kept the same way (slot 0 the diagonal).
+//  - multi-launch (kernels/cg.cu): any other batch, and factors that are not
+//    diagonal-structured: four to six launches per iteration, captured in
+//    graphs of `graph_iters` iterations.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -16,6 +29,7 @@
 #include <vector>
 
 #include "device.hpp"
+#include "host/parallel.hpp"
 #include "kernels/kernels.hpp"
 
 using namespace tbsla_gpu;
@@ -74,15 +88,49 @@ struct tbsla_batch {
   int graph_k = 0, graph_pre = -1, graph_max = -1;
   double graph_tol2 = -1;
 
+  // persistent engine (DIA layout)
+  bool dia = false;
+  int K = 0;                      // diagonal slots of A
+  std::vector<int> adelta_h;      // [nsys * kDiaMaxDiag]
+  int* adelta = nullptr;
+  long* sys_off = nullptr;
+  int* row_sys = nullptr;
+  void* avals_dia = nullptr;      // [K][n] storage precision
+  double* a64_dia = nullptr;      // [K][n]
+  float* dinv_f = nullptr;
+  bool dia_factor = false;        // the factor is held in DIA form
+  int KL = 0;
+  std::vector<int> fdelta_h;      // [nsys * kDiaMaxDiag] deltas of the factor's slots
+  int* fdelta = nullptr;
+  void* lvals_dia = nullptr;      // [KL][n] in lprec_dia
+  int lprec_dia = TBSLA_F32;
+  void *dv = nullptr, *r0 = nullptr, *r1 = nullptr, *p0 = nullptr, *p1 = nullptr, *q2 = nullptr,
+       *z2 = nullptr, *t2 = nullptr;
+  int *mode_d = nullptr, *fallback_d = nullptr;
+  double *relres_d = nullptr, *acc = nullptr;
+  unsigned* bar = nullptr;
+  long long wait_ns = 2000000000LL;  // bound on one grid-wide wait of the persistent kernel
+  int pgrid = 0;
+  cudaGraphExec_t pgraph = nullptr;
+  DiaCg pkey{};                   // the arguments the graph was captured with
+  bool pgraph_ok = false;
+  // last solve
+  std::vector<int> fallback_h, mode_h;
+  std::vector<int> factor_fb;     // per system: the factor failed the host check (multi-launch engine)
+  int last_engine = 0, last_graph = 0;
+
   ~tbsla_batch() {
     cudaSetDevice(device);
     if (stream) cudaStreamSynchronize(stream);
     if (graph) cudaGraphExecDestroy(graph);
+    if (pgraph) cudaGraphExecDestroy(pgraph);
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
                   scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf,
-                  ldelta, tdelta, zf};
+                  ldelta, tdelta, zf, adelta, sys_off, row_sys, a64_dia, dinv_f, fdelta, lvals_dia,
+                  dv, r0, r1, p0, p1, q2, z2, t2, mode_d, fallback_d, relres_d, acc, bar};
     for (void* v : ps)
       if (v) cudaFree(v);
+    if (avals_dia && avals_dia != (void*)a64_dia) cudaFree(avals_dia);
     if (vals && vals != vals64) cudaFree(vals);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -142,6 +190,105 @@ struct tbsla_batch {
 };
 
 namespace {
+
+
+// Diagonal structure of the concatenated CSR arrays: per system the sorted
+// distinct col - row values (at most kDiaMaxDiag), false when a system has
+// more, a row repeats a column, or the batch has more than kDiaMaxSys
+// systems.  Systems are scanned in parallel.
+bool dia_deltas(const tbsla_batch* B, const std::vector<int>& rp, const std::vector<int>& ci,
+                std::vector<int>* delta, int* K) {
+  const int nsys = B->nsys;
+  if (nsys > kDiaMaxSys) return false;
+  delta->assign((size_t)nsys * kDiaMaxDiag, 0);
+  std::vector<int> cnt(nsys, 0);
+  std::vector<char> ok(nsys, 1);
+  tbsla_impl::parallel_for_items(nsys, [&](long b, long e) {
+    for (long s = b; s < e; s++) {
+      int* ds = delta->data() + s * kDiaMaxDiag;
+      int c = 0, hint = 0;
+      for (long i = B->off[s]; i < B->off[s + 1] && ok[s]; i++) {
+        unsigned used = 0;
+        for (int q = rp[i]; q < rp[i + 1]; q++) {
+          const long d = (long)ci[q] - i;
+          int k = -1;
+          for (int t = 0; t < c; t++) {  // start at the slot after the last hit
+            const int u = (hint + t) % c;
+            if (ds[u] == d) {
+              k = u;
+              break;
+            }
+          }
+          if (k < 0) {
+            if (c == kDiaMaxDiag) {
+              ok[s] = 0;
+              break;
+            }
+            ds[c] = (int)d;
+            k = c++;
+          }
+          if (used & (1u << k)) {  // the row repeats a column
+            ok[s] = 0;
+            break;
+          }
+          used |= 1u << k;
+          hint = (k + 1) % std::max(c, 1);
+        }
+      }
+      std::sort(ds, ds + c);
+      cnt[s] = c;
+    }
+  });
+  *K = 0;
+  for (int s = 0; s < nsys; s++) {
+    if (!ok[s]) return false;
+    *K = std::max(*K, cnt[s]);
+  }
+  return *K > 0;
+}
+
+// The DIA copy of the batch and the persistent engine's vectors.
+int build_dia(tbsla_batch* B, const std::vector<int>& delta, int K) {
+  cudaStream_t st = B->stream;
+  const long n = B->n;
+  const int nsys = B->nsys;
+  std::vector<int> rsys(n);
+  tbsla_impl::parallel_for_items(nsys, [&](long b, long e) {
+    for (long s = b; s < e; s++)
+      for (long i = B->off[s]; i < B->off[s + 1]; i++) rsys[i] = (int)s;
+  });
+  CK(alloc(&B->adelta, delta.size()));
+  CK(alloc(&B->sys_off, B->off.size()));
+  CK(alloc(&B->row_sys, (size_t)n));
+  CK(cudaMemcpyAsync(B->adelta, delta.data(), delta.size() * 4, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(B->sys_off, B->off.data(), B->off.size() * 8, cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(B->row_sys, rsys.data(), (size_t)n * 4, cudaMemcpyHostToDevice, st));
+  CK(alloc(&B->a64_dia, (size_t)K * n));
+  CK(cudaMemsetAsync(B->a64_dia, 0, (size_t)K * n * 8, st));
+  CK(dia_fill(B->rowptr, B->colidx, B->vals64, B->row_sys, B->adelta, K, n, B->a64_dia, st));
+  if (B->prec == TBSLA_F64) {
+    B->avals_dia = B->a64_dia;
+  } else {
+    CK(cudaMalloc(&B->avals_dia, std::max<size_t>((size_t)K * n, 1) * (B->prec == TBSLA_F32 ? 4 : 2)));
+    CK(convert_values(B->a64_dia, B->avals_dia, B->prec, (long)K * n, st));
+  }
+  CK(alloc(&B->dinv_f, (size_t)n));
+  CK(dia_dinv(B->a64_dia, B->row_sys, B->adelta, K, n, B->dinv_f, st));
+  const size_t es = B->prec == TBSLA_F64 ? 8 : 4;
+  for (void** v : {&B->dv, &B->r0, &B->r1, &B->p0, &B->p1, &B->q2, &B->z2, &B->t2})
+    CK(cudaMalloc(v, std::max<size_t>((size_t)n, 1) * es));
+  CK(alloc(&B->mode_d, nsys));
+  CK(alloc(&B->fallback_d, nsys));
+  CK(alloc(&B->relres_d, nsys));
+  CK(alloc(&B->acc, (size_t)12 * nsys));
+  CK(alloc(&B->bar, 4));
+  B->adelta_h = delta;
+  B->K = K;
+  B->dia = true;
+  B->fallback_h.assign(nsys, 0);
+  B->mode_h.assign(nsys, 0);
+  return TBSLA_OK;
+}
 
 int build_batch(tbsla_batch* B, tbsla_matrix* const* sys, int nsys, int prec) {
   using namespace tbsla_impl;
@@ -223,6 +370,12 @@ int build_batch(tbsla_batch* B, tbsla_matrix* const* sys, int nsys, int prec) {
   CK(alloc(&B->scal, (size_t)kNScal * nsys));
   CK(alloc(&B->status, nsys));
   CK(alloc(&B->iters, nsys));
+  std::vector<int> delta;
+  int K = 0;
+  if (dia_deltas(B, rp, ci, &delta, &K)) {
+    int st2 = build_dia(B, delta, K);
+    if (st2) return st2;
+  }
   return st_of(cudaStreamSynchronize(st));
 }
 
@@ -249,6 +402,185 @@ int capture(tbsla_batch* B, const CgBatch& c, int K) {
   cudaError_t e = cudaGraphInstantiate(&B->graph, g, 0);
   cudaGraphDestroy(g);
   return st_of(e);
+}
+
+
+
+// A factor on at most kDiaMaxDiag diagonals per system, kept in DIA form for
+// the persistent engine (slot 0 the diagonal, then the other deltas in
+// descending order); TBSLA_ERR_UNSUPPORTED for any other factor.
+int set_dia_factor(tbsla_batch* B, const std::vector<int>& rp, const std::vector<int>& ci,
+                   const std::vector<double>& va, int precision) {
+  const int nsys = B->nsys;
+  const long n = B->n;
+  std::vector<int> delta((size_t)nsys * kDiaMaxDiag, 0);
+  int KL = 0;
+  for (int s = 0; s < nsys; s++) {
+    int* ds = delta.data() + (size_t)s * kDiaMaxDiag;
+    int c = 1;  // ds[0] = 0, the diagonal
+    for (long i = B->off[s]; i < B->off[s + 1]; i++) {
+      unsigned used = 0;
+      for (int q = rp[i]; q < rp[i + 1]; q++) {
+        const int d = ci[q] - (int)i;
+        int k = 0;
+        while (k < c && ds[k] != d) k++;
+        if (k == c) {
+          if (c == kDiaMaxDiag) return TBSLA_ERR_UNSUPPORTED;
+          ds[c++] = d;
+        }
+        if (used & (1u << k)) return TBSLA_ERR_UNSUPPORTED;  // repeated column
+        used |= 1u << k;
+      }
+    }
+    std::sort(ds + 1, ds + c, [](int a, int b) { return a > b; });
+    KL = std::max(KL, c);
+  }
+  cudaSetDevice(B->device);
+  cudaStream_t st = B->stream;
+  int *rp_d = nullptr, *ci_d = nullptr;
+  double *va_d = nullptr, *l64 = nullptr;
+  auto release = [&]() {
+    for (void* p : {(void*)rp_d, (void*)ci_d, (void*)va_d, (void*)l64})
+      if (p) cudaFree(p);
+  };
+  auto fail = [&](cudaError_t e) {
+    cudaStreamSynchronize(st);
+    release();
+    return st_of(e);
+  };
+  cudaError_t e;
+  if ((e = alloc(&rp_d, rp.size())) || (e = alloc(&ci_d, std::max<size_t>(ci.size(), 1))) ||
+      (e = alloc(&va_d, std::max<size_t>(va.size(), 1))) || (e = alloc(&l64, (size_t)KL * n)))
+    return fail(e);
+  if (B->lvals_dia) cudaFree(B->lvals_dia);
+  B->lvals_dia = nullptr;
+  if (!B->fdelta && (e = alloc(&B->fdelta, delta.size()))) return fail(e);
+  const int lprec = precision == TBSLA_BF16 ? TBSLA_BF16 : TBSLA_F32;
+  if ((e = cudaMalloc(&B->lvals_dia, std::max<size_t>((size_t)KL * n, 1) * (lprec == TBSLA_BF16 ? 2 : 4))) ||
+      (e = cudaMemcpyAsync(rp_d, rp.data(), rp.size() * 4, cudaMemcpyHostToDevice, st)) ||
+      (!ci.empty() && (e = cudaMemcpyAsync(ci_d, ci.data(), ci.size() * 4, cudaMemcpyHostToDevice, st))) ||
+      (!va.empty() && (e = cudaMemcpyAsync(va_d, va.data(), va.size() * 8, cudaMemcpyHostToDevice, st))) ||
+      (e = cudaMemcpyAsync(B->fdelta, delta.data(), delta.size() * 4, cudaMemcpyHostToDevice, st)) ||
+      (e = cudaMemsetAsync(l64, 0, (size_t)KL * n * 8, st)) ||
+      (e = dia_fill(rp_d, ci_d, va_d, B->row_sys, B->fdelta, KL, n, l64, st)) ||
+      (e = convert_values(l64, B->lvals_dia, lprec, (long)KL * n, st)) || (e = cudaStreamSynchronize(st)))
+    return fail(e);
+  release();
+  B->fdelta_h = delta;
+  B->KL = KL;
+  B->lprec_dia = lprec;
+  B->dia_factor = true;
+  return TBSLA_OK;
+}
+
+// The persistent engine: H2D of b, x and the per-system modes, then the
+// device part -- clearing the correction, accumulators and barrier words,
+// and the one cooperative launch -- replayed from a CUDA graph captured once
+// per argument set (a direct launch where capture is refused), then D2H of
+// x and the per-system results.
+int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, double rel_tol, int precond,
+              int refresh, int* iterations, double* rel_residual) {
+  cudaStream_t s = B->stream;
+  const int ns = B->nsys;
+  const long n = B->n;
+  const int lprec = precond == 2 ? B->lprec_dia : TBSLA_F32;
+  const int grid = cg_dia_grid(B->prec, lprec);
+  if (grid <= 0) return TBSLA_ERR_CUDA;
+  DiaCg c;
+  std::memset(&c, 0, sizeof c);  // padding too: the struct is the graph's cache key
+  c.nsys = ns;
+  c.n = n;
+  c.K = B->K;
+  c.KL = precond == 2 ? B->KL : 0;
+  c.sys_off = B->sys_off;
+  c.chunks = B->chunks;
+  c.chunk_sys = B->chunk_sys;
+  c.nchunks = B->nchunks;
+  c.adelta = B->adelta;
+  c.avals = B->avals_dia;
+  c.prec = B->prec;
+  c.a64 = B->a64_dia;
+  c.dinv = B->dinv_f;
+  c.ldelta = precond == 2 ? B->fdelta : nullptr;
+  c.lvals = precond == 2 ? B->lvals_dia : nullptr;
+  c.lprec = lprec;
+  c.b = B->b;
+  c.x = B->x;
+  c.d = B->dv;
+  c.r0 = B->r0;
+  c.r1 = B->r1;
+  c.p0 = B->p0;
+  c.p1 = B->p1;
+  c.q = B->q2;
+  c.z = B->z2;
+  c.t = B->t2;
+  c.mode = B->mode_d;
+  c.status = B->status;
+  c.iters = B->iters;
+  c.fallback = B->fallback_d;
+  c.relres = B->relres_d;
+  c.acc = B->acc;
+  c.bar = B->bar;
+  c.tol2 = rel_tol * rel_tol;
+  c.max_it = max_iterations;
+  c.refresh = B->prec != TBSLA_F64 ? refresh : 0;
+  c.wait_ns = B->wait_ns;
+  std::vector<int> mode(ns, precond);
+  CK(cudaMemcpyAsync(B->b, rhs, n * 8, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(B->x, x, n * 8, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(B->mode_d, mode.data(), ns * sizeof(int), cudaMemcpyHostToDevice, s));
+  const size_t es = B->prec == TBSLA_F64 ? 8 : 4;
+  auto enqueue = [&](cudaStream_t st) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(B->dv, 0, (size_t)n * es, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B->acc, 0, (size_t)12 * ns * 8, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B->bar, 0, 4 * sizeof(unsigned), st);
+    if (e == cudaSuccess) e = cg_dia_solve(c, grid, st);
+    return e;
+  };
+  if (!B->pgraph || std::memcmp(&B->pkey, &c, sizeof c) != 0) {
+    if (B->pgraph) cudaGraphExecDestroy(B->pgraph);
+    B->pgraph = nullptr;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      e = enqueue(s);
+      const cudaError_t e2 = cudaStreamEndCapture(s, &g);
+      if (e == cudaSuccess) e = e2;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&B->pgraph, g, 0);
+      if (g) cudaGraphDestroy(g);
+    }
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      if (B->pgraph) cudaGraphExecDestroy(B->pgraph);
+      B->pgraph = nullptr;
+    }
+    B->pkey = c;
+  }
+  if (B->pgraph) CK(cudaGraphLaunch(B->pgraph, s));
+  else CK(enqueue(s));
+  std::vector<int> st(ns), it(ns);
+  std::vector<double> rr(ns);
+  unsigned err[4] = {0, 0, 0, 0};
+  B->mode_h.assign(ns, 0);
+  B->fallback_h.assign(ns, 0);
+  CK(cudaMemcpyAsync(x, B->x, n * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(st.data(), B->status, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(it.data(), B->iters, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(rr.data(), B->relres_d, ns * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(B->mode_h.data(), B->mode_d, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(B->fallback_h.data(), B->fallback_d, ns * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(err, B->bar, sizeof err, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  B->last_engine = 1;
+  B->last_graph = B->pgraph ? 1 : 0;
+  if (err[2]) return TBSLA_ERR_TIMEOUT;
+  bool all = true;
+  for (int k = 0; k < ns; k++) {
+    if (iterations) iterations[k] = it[k];
+    if (rel_residual) rel_residual[k] = rr[k];
+    all &= st[k] == kDone;
+  }
+  return all ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
 }
 
 }  // namespace
@@ -306,6 +638,49 @@ int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int ns
       }
       rp[o + i + 1] = (int)ci.size();
     }
+  }
+  // Per system, the check the persistent engine makes on the device before
+  // its first iteration: every value finite, every diagonal entry > 0.
+  B->factor_fb.assign(nsys, 0);
+  for (int s = 0; s < nsys; s++)
+    for (long i = B->off[s]; i < B->off[s + 1] && !B->factor_fb[s]; i++) {
+      bool diag = false;
+      for (int k = rp[i]; k < rp[i + 1]; k++) {
+        if (!std::isfinite(va[k])) B->factor_fb[s] = kFallbackBadFactor;
+        if (ci[k] == i) diag = va[k] > 0;
+      }
+      if (!diag) B->factor_fb[s] = kFallbackBadFactor;
+    }
+  if (B->dia) {
+    const int st2 = set_dia_factor(B, rp, ci, va, precision);
+    if (st2 != TBSLA_ERR_UNSUPPORTED) return st2;
+  }
+  B->dia_factor = false;
+  if (std::count(B->factor_fb.begin(), B->factor_fb.end(), 0) != nsys) {
+    // the multi-launch engine runs a system whose factor failed the check
+    // with the Jacobi factor L = D^-1/2 (z = D^-1 r: Jacobi-PCG)
+    std::vector<double> dinv(B->n);
+    CK(cudaMemcpy(dinv.data(), B->dinv, B->n * 8, cudaMemcpyDeviceToHost));
+    std::vector<int> rp2(B->n + 1, 0), ci2;
+    std::vector<double> va2;
+    ci2.reserve(ci.size());
+    va2.reserve(va.size());
+    for (int s = 0; s < nsys; s++)
+      for (long i = B->off[s]; i < B->off[s + 1]; i++) {
+        if (B->factor_fb[s]) {
+          ci2.push_back((int)i);
+          va2.push_back(std::sqrt(dinv[i]));
+        } else {
+          for (int k = rp[i]; k < rp[i + 1]; k++) {
+            ci2.push_back(ci[k]);
+            va2.push_back(va[k]);
+          }
+        }
+        rp2[i + 1] = (int)ci2.size();
+      }
+    rp.swap(rp2);
+    ci.swap(ci2);
+    va.swap(va2);
   }
   const long nl = (long)ci.size();
   std::vector<int> trp(B->n + 1, 0), tci(nl);
@@ -409,9 +784,21 @@ int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets) {
 int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterations, double rel_tol,
                    int precond, int refresh, int graph_iters, int* iterations, double* rel_residual) {
   if (!B || !rhs || !x || max_iterations < 0 || rel_tol < 0 || precond < 0 || precond > 2 || refresh < 0 ||
-      (precond == 2 && !B->rf))
+      (precond == 2 && !B->rf && !B->dia_factor))
     return TBSLA_ERR_INVALID_ARG;
   cudaSetDevice(B->device);
+  if (B->dia && (precond != 2 || B->dia_factor))
+    return dia_solve(B, rhs, x, max_iterations, rel_tol, precond, refresh, iterations, rel_residual);
+  B->last_engine = 0;
+  B->last_graph = 1;
+  B->fallback_h.assign(B->nsys, 0);
+  B->mode_h.assign(B->nsys, precond);
+  if (precond == 2)
+    for (int k = 0; k < B->nsys && k < (int)B->factor_fb.size(); k++)
+      if (B->factor_fb[k]) {
+        B->fallback_h[k] = B->factor_fb[k];
+        B->mode_h[k] = 1;
+      }
   const int K = graph_iters > 0 ? graph_iters : 10;
   const double tol2 = rel_tol * rel_tol;
   const CgBatch c = B->view(precond, tol2, max_iterations);
@@ -485,6 +872,28 @@ int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterati
     all &= hs[k] == kDone;
   }
   return all ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
+}
+
+int tbsla_batch_fallbacks(const tbsla_batch* B, int* fallback, int* precond_used) {
+  if (!B) return TBSLA_ERR_INVALID_ARG;
+  for (int k = 0; k < B->nsys; k++) {
+    if (fallback) fallback[k] = k < (int)B->fallback_h.size() ? B->fallback_h[k] : 0;
+    if (precond_used) precond_used[k] = k < (int)B->mode_h.size() ? B->mode_h[k] : 0;
+  }
+  return TBSLA_OK;
+}
+
+int tbsla_batch_set_wait_limit(tbsla_batch* B, long long ns) {
+  if (!B || ns < 0) return TBSLA_ERR_INVALID_ARG;
+  B->wait_ns = ns;
+  return TBSLA_OK;
+}
+
+int tbsla_batch_engine(const tbsla_batch* B, int* persistent, int* graph) {
+  if (!B) return TBSLA_ERR_INVALID_ARG;
+  if (persistent) *persistent = B->last_engine;
+  if (graph) *graph = B->last_graph;
+  return TBSLA_OK;
 }
 
 }  // extern "C"

@@ -1,0 +1,686 @@
+// Persistent batched CG on diagonal-structured systems: the whole solve of
+// every system in a batch -- initial residual, iterations, periodic FP64
+// residual refinement, verification, fallback -- in ONE cooperative launch.
+//
+// Follows tbsla::mpi::Matrix::CG (src/mpi/matrix/CG.cpp:32-73) restated as
+// in kernels/cg.cu (q = A p, alpha = r.z / p.q, beta = r_new.z_new / r.z,
+// relative stop test confirmed on the FP64 true residual b - A x).
+//
+// Layout (DIA): a system whose entries lie on at most 8 diagonals (col - row
+// = delta, the same deltas on every row of the system: 7-point stencils have
+// 0, +-1, +-n, +-n^2) stores its values slot-major, a[k * n + i] = the entry
+// of row i on the system's k-th diagonal (0 where the row has none), with the
+// deltas in a per-system table.  Every "gather" of a neighbour is then a
+// shifted contiguous stream: coalesced, no column indices in memory.
+//
+// Precision: with FP32 / BF16 storage the iteration runs entirely in FP32
+// (vectors and arithmetic; reductions summed in FP32 per warp and FP64
+// across warps), as the inner solver of FP64 iterative refinement: every
+// `refresh` iterations, and whenever the recursive residual says converged,
+// x += d (the FP32 correction) in FP64, r = b - A64 x in FP64 from the FP64
+// values, and the iteration restarts from that residual.  GB300's FP64 pipe
+// retires about 2 multiply-adds per clock per SM against 128 in FP32, so
+// FP64 only where it decides the answer.  FP64 storage runs the same loop in
+// FP64 with no periodic refresh.
+//
+// Preconditioners, per system: 0 none, 1 Jacobi (z = D^-1 r, D^-1 in FP32),
+// 2 factored z = L (L^T r) with L lower-triangular on at most 8 diagonals
+// (stored in FP32 or BF16, applied in T arithmetic).  Mode 2 falls back to
+// Jacobi for the system (fallback code in its status) when its factor holds
+// a non-finite value or a diagonal entry <= 0 (checked before the first
+// iteration), when a refinement cycle does not lower its FP64 true residual,
+// or when r.z stops being positive and finite.
+//
+// One iteration, all systems at once, grid-wide barriers between phases:
+//   A   q = A p; p.q              (modes 0/1 form p = z + beta p_old on the
+//                                   fly and write it)
+//   B   modes 0/1: alpha; d += alpha p; r -= alpha q; z = M r; r.z, r.r
+//   B'  mode 2: the same r update, and t = L^T r_new formed from r_old and q
+//       at the row's upper neighbours (so no extra pass), r.z = t.t
+//   D   mode 2: z = L t, p = z + beta p
+// Jacobi costs two barriers per iteration, the factored form three.
+//
+// Per-system scalars are kept in shared memory by every CTA and updated
+// redundantly from the same global sums after each barrier, so no CTA waits
+// for another to publish them.  The sums rotate through three accumulator
+// slots: CTA 0 clears the slot two phases ahead, which no CTA reads or
+// writes at that time.
+//
+// Every grid-wide wait is bounded (`wait_ns`, globaltimer): a CTA whose wait
+// runs out sets the error word and returns, and every other CTA returns at
+// its next wait; the host then reports TBSLA_ERR_TIMEOUT.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.hpp"
+
+namespace tbsla_gpu {
+
+namespace {
+
+constexpr int PNT = 256;  // threads per CTA
+constexpr int KMAX = kDiaMaxDiag;
+
+// local states of a system
+enum { S_ACTIVE = 0, S_CHECK = 1, S_RESTART_F = 2, S_DONE = 3, S_STOPPED = 4 };
+
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+template <class T, class V>
+__device__ __forceinline__ T val(V v);
+template <>
+__device__ __forceinline__ float val<float, float>(float v) { return v; }
+template <>
+__device__ __forceinline__ float val<float, __nv_bfloat16>(__nv_bfloat16 v) { return __bfloat162float(v); }
+template <>
+__device__ __forceinline__ double val<double, double>(double v) { return v; }
+template <>
+__device__ __forceinline__ double val<double, float>(float v) { return widen(v); }
+template <>
+__device__ __forceinline__ double val<double, __nv_bfloat16>(__nv_bfloat16 v) { return widen(v); }
+
+__device__ __forceinline__ bool finite_v(float v) { return isfinite(v); }
+__device__ __forceinline__ bool finite_v(__nv_bfloat16 v) { return isfinite(__bfloat162float(v)); }
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier with a bounded wait.  bar[0] arrival count, bar[1]
+// generation, bar[2] error word.  Returns false when the grid must stop.
+__device__ bool grid_sync(unsigned* bar, unsigned& gen, long long wait_ns, int* s_stop) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned target = gen + 1;
+    __threadfence();
+    const unsigned arrived = atomicAdd(&bar[0], 1u);
+    if (arrived == gridDim.x - 1) {
+      atomicExch(&bar[0], 0u);
+      __threadfence();
+      atomicExch(&bar[1], target);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (ld_acquire(&bar[1]) != target) {
+        if (ld_acquire(&bar[2]) != 0u) break;
+        if ((long long)(global_ns() - t0) > wait_ns) {
+          atomicExch(&bar[2], 1u);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    gen = target;
+    __threadfence();
+    *s_stop = ld_acquire(&bar[2]) != 0u;
+  }
+  __syncthreads();
+  return !*s_stop;
+}
+
+// Sum of up to 3 per-thread partials over the CTA, added to acc[what * ns +
+// sys] (FP64 atomics).  Warps sum in T, the CTA in FP64.
+template <class T, int NV>
+__device__ __forceinline__ void cta_add(T (&v)[NV], double* s_red, double* acc, int ns, int sys) {
+#pragma unroll
+  for (int k = 0; k < NV; k++) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  }
+  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
+  if (l == 0) {
+#pragma unroll
+    for (int k = 0; k < NV; k++) s_red[k * (PNT / 32) + w] = (double)v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0;
+    for (int i = 0; i < PNT / 32; i++) s += s_red[threadIdx.x * (PNT / 32) + i];
+    atomicAdd(acc + threadIdx.x * ns + sys, s);
+  }
+  __syncthreads();
+}
+
+template <class T, class V, class LV>
+__global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
+  __shared__ double s_rz[kDiaMaxSys], s_alpha[kDiaMaxSys], s_beta[kDiaMaxSys], s_bb[kDiaMaxSys],
+      s_prev[kDiaMaxSys], s_rzj[kDiaMaxSys];
+  __shared__ int s_st[kDiaMaxSys], s_why[kDiaMaxSys], s_mode[kDiaMaxSys], s_it[kDiaMaxSys],
+      s_since[kDiaMaxSys], s_fb[kDiaMaxSys];
+  __shared__ double s_red[3 * (PNT / 32)];
+  __shared__ int s_stop;
+  const int ns = c.nsys;
+  const int tid = threadIdx.x;
+  const long n = c.n;
+  const V* __restrict__ A = static_cast<const V*>(c.avals);
+  const LV* __restrict__ Lv = static_cast<const LV*>(c.lvals);
+  T* __restrict__ D = static_cast<T*>(c.d);
+  T* const R0 = static_cast<T*>(c.r0);
+  T* const R1 = static_cast<T*>(c.r1);
+  T* const P0 = static_cast<T*>(c.p0);
+  T* const P1 = static_cast<T*>(c.p1);
+  // the buffer of parity k (selects, not an indexed array: no local memory)
+  auto R = [&](int k) { return (k & 1) ? R1 : R0; };
+  auto P = [&](int k) { return (k & 1) ? P1 : P0; };
+  T* __restrict__ Q = static_cast<T*>(c.q);
+  T* __restrict__ Z = static_cast<T*>(c.z);
+  T* __restrict__ Tt = static_cast<T*>(c.t);
+  const uint64_t pol = policy_evict_first();
+
+  for (int s = tid; s < ns; s += PNT) {
+    s_st[s] = S_CHECK;
+    s_why[s] = 0;
+    s_mode[s] = c.mode[s];
+    s_it[s] = 0;
+    s_since[s] = 0;
+    s_fb[s] = 0;
+    s_rz[s] = s_alpha[s] = s_beta[s] = s_bb[s] = s_rzj[s] = 0;
+    s_prev[s] = __longlong_as_double(0x7ff0000000000000ll);  // +inf
+  }
+  __syncthreads();
+
+  unsigned gen = 0;
+  int ph = 0;       // phases done: accumulator slot of the current phase = ph % 3
+  int g = 0;        // iteration parity of the R / P buffers
+  bool init = true;
+  auto slot = [&](int p) { return c.acc + (size_t)(p % 3) * 4 * ns; };
+  // clear the slot two phases ahead (CTA 0), then run `body`, then the barrier
+  auto clear_ahead = [&]() {
+    if (blockIdx.x == 0) {
+      double* a = slot(ph + 1);
+      for (int t = tid; t < 4 * ns; t += PNT) a[t] = 0.0;
+    }
+  };
+  auto any_state = [&](int st, int mode) {
+    int f = 0;
+    for (int s = tid; s < ns; s += PNT) f |= s_st[s] == st && (mode < 0 || s_mode[s] == mode);
+    return __syncthreads_or(f) != 0;
+  };
+
+  for (;;) {
+    // ================= refinement: systems in S_CHECK ======================
+    if (any_state(S_CHECK, -1)) {
+      // R1: x += d (FP64), d = 0; at the start, check the factors
+      clear_ahead();
+      {
+        double* acc = slot(ph);
+        for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+          const int s = c.chunk_sys[ch];
+          if (s_st[s] != S_CHECK) continue;
+          const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+          const bool chk = init && s_mode[s] == 2;
+          float bad[1] = {0.f};
+          for (int i = r0 + tid; i < r1; i += PNT) {
+            const double xi = c.x[i] + (double)D[i];
+            if (isfinite(xi)) c.x[i] = xi;  // a non-finite correction is dropped
+            D[i] = (T)0;
+            if (chk) {
+              for (int k = 0; k < c.KL; k++) {
+                const LV lv = Lv[(size_t)k * n + i];
+                if (!finite_v(lv)) bad[0] = 1.f;
+                if (k == 0 && !(to_f(lv) > 0.f)) bad[0] = 1.f;  // slot 0 is the diagonal
+              }
+            }
+          }
+          if (chk) cta_add<float, 1>(bad, s_red, acc, ns, s);
+        }
+      }
+      if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
+      {
+        const double* acc = slot(ph);
+        for (int s = tid; s < ns; s += PNT)
+          if (s_st[s] == S_CHECK && init && s_mode[s] == 2 && acc[s] > 0) {
+            s_mode[s] = 1;
+            s_fb[s] = kFallbackBadFactor;
+          }
+        ph++;
+      }
+      __syncthreads();
+      // R2: r = b - A64 x in FP64 (true residual), r.r; b.b at the start; the
+      // Jacobi (or identity) z and r.z for a restart; p_old = 0
+      clear_ahead();
+      {
+        double* acc = slot(ph);
+        T* Rn = R(g);
+        T* Po = P(g);
+        for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+          const int s = c.chunk_sys[ch];
+          if (s_st[s] != S_CHECK) continue;
+          const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+          const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
+          int dd[KMAX];
+#pragma unroll
+          for (int k = 0; k < KMAX; k++) dd[k] = k < c.K ? c.adelta[s * KMAX + k] : 0;
+          const bool ident = s_mode[s] == 0;
+          double part[3] = {0, 0, 0};
+          for (int i = r0 + tid; i < r1; i += PNT) {
+            double ax = 0;
+#pragma unroll
+            for (int k = 0; k < KMAX; k++) {
+              if (k < c.K) {
+                long j = i + dd[k];
+                j = j < lo ? lo : (j >= hi ? hi - 1 : j);
+                ax = fma_rn(ld_stream(c.a64 + (size_t)k * n + i, pol), c.x[j], ax);
+              }
+            }
+            const double bi = c.b[i];
+            const double ri = bi - ax;
+            part[0] = fma_rn(ri, ri, part[0]);
+            part[1] = fma_rn(bi, bi, part[1]);
+            const T rt = (T)ri;
+            Rn[i] = rt;
+            const T zi = ident ? rt : (T)c.dinv[i] * rt;
+            Z[i] = zi;
+            part[2] += (double)(rt * zi);
+            Po[i] = (T)0;
+          }
+          cta_add<double, 3>(part, s_red, acc, ns, s);
+        }
+      }
+      if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
+      {
+        const double* acc = slot(ph);
+        for (int s = tid; s < ns; s += PNT) {
+          if (s_st[s] != S_CHECK) continue;
+          const double rrt = acc[s];
+          if (init) s_bb[s] = acc[ns + s];
+          const double bb = s_bb[s];
+          if (blockIdx.x == 0) c.relres[s] = bb > 0 ? sqrt(rrt / bb) : sqrt(rrt);
+          if (rrt <= c.tol2 * bb) {
+            s_st[s] = S_DONE;
+          } else if (s_it[s] >= c.max_it) {
+            s_st[s] = S_STOPPED;
+          } else {
+            if (s_mode[s] == 2 && !init && !(rrt < s_prev[s])) {  // no progress over a cycle (or NaN)
+              s_mode[s] = 1;
+              s_fb[s] = kFallbackStagnation;
+            }
+            s_prev[s] = rrt;
+            s_rzj[s] = acc[2 * ns + s];
+            s_beta[s] = 0;
+            s_since[s] = 0;
+            if (s_mode[s] == 2) {
+              s_st[s] = S_RESTART_F;
+            } else {
+              s_rz[s] = s_rzj[s];
+              s_st[s] = S_ACTIVE;
+            }
+          }
+        }
+        ph++;
+        init = false;
+      }
+      __syncthreads();
+      if (any_state(S_RESTART_F, -1)) {
+        // R3: t = L^T r (FP32 / T arithmetic), r.z = t.t
+        clear_ahead();
+        {
+          double* acc = slot(ph);
+          const T* Rc = R(g);
+          for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+            const int s = c.chunk_sys[ch];
+            if (s_st[s] != S_RESTART_F) continue;
+            const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+            const long hi = c.sys_off[s + 1];
+            int ld[KMAX];
+#pragma unroll
+            for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
+            T part[1] = {(T)0};
+            for (int i = r0 + tid; i < r1; i += PNT) {
+              T t = (T)0;
+#pragma unroll
+              for (int k = 0; k < KMAX; k++) {
+                if (k < c.KL) {
+                  const long j = (long)i - ld[k];  // L_{j,i} sits on row j = i - delta
+                  if (j < hi) t += val<T, LV>(Lv[(size_t)k * n + j]) * Rc[j];
+                }
+              }
+              Tt[i] = t;
+              part[0] += t * t;
+            }
+            cta_add<T, 1>(part, s_red, acc, ns, s);
+          }
+        }
+        if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
+        {
+          const double* acc = slot(ph);
+          for (int s = tid; s < ns; s += PNT) {
+            if (s_st[s] != S_RESTART_F) continue;
+            const double rz = acc[s];
+            if (!(rz > 0) || !isfinite(rz)) {  // unusable factor: Jacobi from here
+              s_mode[s] = 1;
+              s_fb[s] = kFallbackStagnation;
+              s_rz[s] = s_rzj[s];
+              s_st[s] = S_ACTIVE;
+            } else {
+              s_rz[s] = rz;
+            }
+          }
+          ph++;
+        }
+        __syncthreads();
+        // R4: p = L t
+        clear_ahead();
+        {
+          T* Po = P(g);
+          for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+            const int s = c.chunk_sys[ch];
+            if (s_st[s] != S_RESTART_F) continue;
+            const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+            const long lo = c.sys_off[s];
+            int ld[KMAX];
+#pragma unroll
+            for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
+            for (int i = r0 + tid; i < r1; i += PNT) {
+              T z = (T)0;
+#pragma unroll
+              for (int k = 0; k < KMAX; k++) {
+                if (k < c.KL) {
+                  long j = (long)i + ld[k];
+                  j = j < lo ? lo : j;
+                  z += val<T, LV>(Lv[(size_t)k * n + i]) * Tt[j];
+                }
+              }
+              Po[i] = z;
+            }
+          }
+        }
+        if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
+        for (int s = tid; s < ns; s += PNT)
+          if (s_st[s] == S_RESTART_F) s_st[s] = S_ACTIVE;
+        ph++;
+        __syncthreads();
+      }
+    }
+    if (!any_state(S_ACTIVE, -1)) break;
+
+    // ================= one iteration =======================================
+    T* Pold = P(g);
+    T* Pnew = P(g + 1);
+    // A: q = A p, p.q
+    clear_ahead();
+    {
+      double* acc = slot(ph);
+      for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+        const int s = c.chunk_sys[ch];
+        if (s_st[s] != S_ACTIVE) continue;
+        const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+        const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
+        int dd[KMAX];
+#pragma unroll
+        for (int k = 0; k < KMAX; k++) dd[k] = k < c.K ? c.adelta[s * KMAX + k] : 0;
+        const bool fact = s_mode[s] == 2;
+        const T beta = (T)s_beta[s];
+        T part[1] = {(T)0};
+        for (int i = r0 + tid; i < r1; i += PNT) {
+          T a[KMAX];
+#pragma unroll
+          for (int k = 0; k < KMAX; k++) a[k] = k < c.K ? val<T, V>(ld_stream(A + (size_t)k * n + i, pol)) : (T)0;
+          T q = (T)0, pi;
+          if (fact) {
+#pragma unroll
+            for (int k = 0; k < KMAX; k++) {
+              if (k < c.K) {
+                long j = i + dd[k];
+                j = j < lo ? lo : (j >= hi ? hi - 1 : j);
+                q += a[k] * Pold[j];
+              }
+            }
+            pi = Pold[i];
+          } else {
+#pragma unroll
+            for (int k = 0; k < KMAX; k++) {
+              if (k < c.K) {
+                long j = i + dd[k];
+                j = j < lo ? lo : (j >= hi ? hi - 1 : j);
+                q += a[k] * (Z[j] + beta * Pold[j]);
+              }
+            }
+            pi = Z[i] + beta * Pold[i];
+            Pnew[i] = pi;
+          }
+          Q[i] = q;
+          part[0] += pi * q;
+        }
+        cta_add<T, 1>(part, s_red, acc, ns, s);
+      }
+    }
+    if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
+    {
+      const double* acc = slot(ph);
+      for (int s = tid; s < ns; s += PNT) {
+        if (s_st[s] != S_ACTIVE) continue;
+        const double pq = acc[s];
+        s_alpha[s] = pq != 0 && isfinite(pq) ? s_rz[s] / pq : 0.0;
+      }
+      ph++;
+    }
+    __syncthreads();
+    // B / B': residual update, preconditioner, r.z and r.r
+    clear_ahead();
+    {
+      double* acc = slot(ph);
+      const T* Ro = R(g);
+      T* Rn = R(g + 1);
+      for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+        const int s = c.chunk_sys[ch];
+        if (s_st[s] != S_ACTIVE) continue;
+        const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+        const T alpha = (T)s_alpha[s];
+        const int mode = s_mode[s];
+        T part[2] = {(T)0, (T)0};
+        if (mode == 2) {
+          const long hi = c.sys_off[s + 1];
+          int ld[KMAX];
+#pragma unroll
+          for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
+          for (int i = r0 + tid; i < r1; i += PNT) {
+            D[i] += alpha * Pold[i];
+            const T ri = Ro[i] - alpha * Q[i];
+            Rn[i] = ri;
+            part[1] += ri * ri;
+            T t = (T)0;
+#pragma unroll
+            for (int k = 0; k < KMAX; k++) {
+              if (k < c.KL) {
+                const long j = (long)i - ld[k];
+                if (j < hi) t += val<T, LV>(Lv[(size_t)k * n + j]) * (Ro[j] - alpha * Q[j]);
+              }
+            }
+            Tt[i] = t;
+            part[0] += t * t;
+          }
+        } else {
+          for (int i = r0 + tid; i < r1; i += PNT) {
+            D[i] += alpha * Pnew[i];
+            const T ri = Ro[i] - alpha * Q[i];
+            Rn[i] = ri;
+            const T zi = mode == 1 ? (T)c.dinv[i] * ri : ri;
+            Z[i] = zi;
+            part[0] += ri * zi;
+            part[1] += ri * ri;
+          }
+        }
+        cta_add<T, 2>(part, s_red, acc, ns, s);
+      }
+    }
+    if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
+    {
+      const double* acc = slot(ph);
+      for (int s = tid; s < ns; s += PNT) {
+        if (s_st[s] != S_ACTIVE) continue;
+        s_it[s]++;
+        s_since[s]++;
+        const double rzn = acc[s], rr = acc[ns + s];
+        s_beta[s] = s_rz[s] != 0 ? rzn / s_rz[s] : 0.0;
+        s_rz[s] = rzn;
+        if (rr <= c.tol2 * s_bb[s]) {
+          s_st[s] = S_CHECK;
+          s_why[s] = 1;
+        } else if (s_it[s] >= c.max_it) {
+          s_st[s] = S_CHECK;
+          s_why[s] = 3;
+        } else if (c.refresh > 0 && s_since[s] >= c.refresh) {
+          s_st[s] = S_CHECK;
+          s_why[s] = 2;
+        } else if (!(rzn > 0) || !isfinite(rzn) || !isfinite(rr)) {
+          s_st[s] = S_CHECK;  // breakdown: refine (and fall back if it does not help)
+          s_why[s] = 4;
+        }
+      }
+      ph++;
+    }
+    __syncthreads();
+    if (any_state(S_ACTIVE, 2)) {
+      // D: z = L t, p = z + beta p
+      clear_ahead();
+      for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+        const int s = c.chunk_sys[ch];
+        if (s_st[s] != S_ACTIVE || s_mode[s] != 2) continue;
+        const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+        const long lo = c.sys_off[s];
+        const T beta = (T)s_beta[s];
+        int ld[KMAX];
+#pragma unroll
+        for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
+        for (int i = r0 + tid; i < r1; i += PNT) {
+          T z = (T)0;
+#pragma unroll
+          for (int k = 0; k < KMAX; k++) {
+            if (k < c.KL) {
+              long j = (long)i + ld[k];
+              j = j < lo ? lo : j;
+              z += val<T, LV>(Lv[(size_t)k * n + i]) * Tt[j];
+            }
+          }
+          Pnew[i] = z + beta * Pold[i];
+        }
+      }
+      if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
+      ph++;
+    }
+    g++;
+  }
+
+  // results (CTA 0)
+  if (blockIdx.x == 0) {
+    for (int s = tid; s < ns; s += PNT) {
+      c.status[s] = s_st[s] == S_DONE ? kDone : kStopped;
+      c.iters[s] = s_it[s];
+      c.mode[s] = s_mode[s];
+      c.fallback[s] = s_fb[s];
+    }
+  }
+}
+
+// ---- layout builders ----------------------------------------------------------
+
+// a64[k * n + i] = entry of row i on diagonal k of its system (zeroed first by
+// the caller); one thread per row over the concatenated CSR arrays.
+__global__ void k_dia_fill(const int* __restrict__ rowptr, const int* __restrict__ colidx,
+                           const double* __restrict__ vals, const int* __restrict__ row_sys,
+                           const int* __restrict__ delta, int K, long n, double* __restrict__ out) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int s = row_sys[i];
+    for (int e = rowptr[i]; e < rowptr[i + 1]; e++) {
+      const long d = (long)colidx[e] - i;
+      for (int k = 0; k < K; k++)
+        if (delta[s * KMAX + k] == d) {
+          out[(size_t)k * n + i] = vals[e];
+          break;
+        }
+    }
+  }
+}
+
+// 1 / a_ii in FP32 (1 where the diagonal is missing or zero).
+__global__ void k_dia_dinv(const double* __restrict__ a64, const int* __restrict__ row_sys,
+                           const int* __restrict__ delta, int K, long n, float* __restrict__ dinv) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int s = row_sys[i];
+    double d = 0;
+    for (int k = 0; k < K; k++)
+      if (delta[s * KMAX + k] == 0) {  // the first slot of delta 0 (padding slots repeat it, zero-valued)
+        d = a64[(size_t)k * n + i];
+        break;
+      }
+    dinv[i] = d != 0 ? (float)(1.0 / d) : 1.f;
+  }
+}
+
+template <class T, class V, class LV>
+cudaError_t launch_persistent(const DiaCg& c, int grid, cudaStream_t s) {
+  void* args[] = {const_cast<DiaCg*>(&c)};
+  return cudaLaunchCooperativeKernel((const void*)k_cg_persistent<T, V, LV>, dim3(grid), dim3(PNT), args, 0, s);
+}
+
+template <class T, class V, class LV>
+int resident_grid() {
+  int dev = 0, sms = 0, per = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_persistent<T, V, LV>, PNT, 0) != cudaSuccess)
+    return 0;
+  return sms * per;
+}
+
+int variant(int prec, int lprec) {
+  const int l = lprec == kBF16 ? 1 : 0;  // factor values: bfloat16 or float
+  if (prec == kF64) return 0 + l;
+  if (prec == kF32) return 2 + l;
+  return 4 + l;
+}
+
+}  // namespace
+
+int cg_dia_grid(int prec, int lprec) {
+  switch (variant(prec, lprec)) {
+    case 0: return resident_grid<double, double, float>();
+    case 1: return resident_grid<double, double, __nv_bfloat16>();
+    case 2: return resident_grid<float, float, float>();
+    case 3: return resident_grid<float, float, __nv_bfloat16>();
+    case 4: return resident_grid<float, __nv_bfloat16, float>();
+    case 5: return resident_grid<float, __nv_bfloat16, __nv_bfloat16>();
+  }
+  return 0;
+}
+
+cudaError_t cg_dia_solve(const DiaCg& c, int grid, cudaStream_t s) {
+  switch (variant(c.prec, c.lprec)) {
+    case 0: return launch_persistent<double, double, float>(c, grid, s);
+    case 1: return launch_persistent<double, double, __nv_bfloat16>(c, grid, s);
+    case 2: return launch_persistent<float, float, float>(c, grid, s);
+    case 3: return launch_persistent<float, float, __nv_bfloat16>(c, grid, s);
+    case 4: return launch_persistent<float, __nv_bfloat16, float>(c, grid, s);
+    case 5: return launch_persistent<float, __nv_bfloat16, __nv_bfloat16>(c, grid, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t dia_fill(const int* rowptr, const int* colidx, const double* vals, const int* row_sys,
+                     const int* delta, int K, long n, double* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (int)std::min<long>((n + 255) / 256, 152L * 16);
+  k_dia_fill<<<grid, 256, 0, s>>>(rowptr, colidx, vals, row_sys, delta, K, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t dia_dinv(const double* a64, const int* row_sys, const int* delta, int K, long n, float* dinv,
+                     cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int grid = (int)std::min<long>((n + 255) / 256, 152L * 16);
+  k_dia_dinv<<<grid, 256, 0, s>>>(a64, row_sys, delta, K, n, dinv);
+  return cudaGetLastError();
+}
+
+}  // namespace tbsla_gpu

@@ -227,6 +227,51 @@ struct CgBatch {
   double tol2;
   int max_it;
 };
+// ---- persistent batched CG on diagonal-structured systems (cg_dia.cu) ----------
+constexpr int kDiaMaxDiag = 8;   // diagonals per system (A and L)
+constexpr int kDiaMaxSys = 256;  // systems per batch
+enum DiaFallback { kFallbackNone = 0, kFallbackBadFactor = 1, kFallbackStagnation = 2 };
+struct DiaCg {
+  int nsys;
+  long n;
+  int K, KL;              // diagonal slots of A and of L (batch-wide, zero-padded)
+  const long* sys_off;    // [nsys + 1] first row of each system
+  const int* chunks;      // [nchunks + 1] row bounds of the work chunks (never across systems)
+  const int* chunk_sys;   // [nchunks]
+  int nchunks;
+  const int* adelta;      // [nsys * kDiaMaxDiag] col - row of each slot of A (padding: 0, value 0)
+  const void* avals;      // [K][n] in `prec` (the iteration's A)
+  int prec;
+  const double* a64;      // [K][n] FP64 (true residual)
+  const float* dinv;      // [n] Jacobi
+  const int* ldelta;      // [nsys * kDiaMaxDiag] L's deltas (<= 0), slot 0 the diagonal
+  const void* lvals;      // [KL][n] in `lprec` (F32 or BF16)
+  int lprec;
+  const double* b;
+  double* x;
+  void *d, *r0, *r1, *p0, *p1, *q, *z, *t;  // FP32 (narrow storage) or FP64 vectors
+  int* mode;              // [nsys] in: preconditioner per system; out: the one it ended with
+  int* status;            // [nsys] out: kDone / kStopped
+  int* iters;             // [nsys] out
+  int* fallback;          // [nsys] out: DiaFallback
+  double* relres;         // [nsys] out: FP64 true relative residual at exit
+  double* acc;            // [3][4][nsys] rotating accumulator slots (zeroed before launch)
+  unsigned* bar;          // [4] grid barrier: count, generation, error (zeroed before launch)
+  double tol2;
+  int max_it;
+  int refresh;            // iterations per refinement cycle (narrow storage), 0 = never
+  long long wait_ns;      // bound on one grid-wide wait
+};
+// Co-resident CTAs of the persistent kernel for (prec, lprec) on this device.
+int cg_dia_grid(int prec, int lprec);
+// The whole batched solve, one cooperative launch of `grid` CTAs.
+cudaError_t cg_dia_solve(const DiaCg& c, int grid, cudaStream_t s);
+// out[k * n + i] = value of row i on slot k (zeroed by the caller).
+cudaError_t dia_fill(const int* rowptr, const int* colidx, const double* vals, const int* row_sys,
+                     const int* delta, int K, long n, double* out, cudaStream_t s);
+cudaError_t dia_dinv(const double* a64, const int* row_sys, const int* delta, int K, long n, float* dinv,
+                     cudaStream_t s);
+
 cudaError_t cg_spmv_dot(const CgBatch& c, cudaStream_t s);   // q = A p; pq += p.q
 cudaError_t cg_update(const CgBatch& c, cudaStream_t s);     // x += a p; r -= a q; z = M r; dots
 cudaError_t cg_scalars(const CgBatch& c, cudaStream_t s);    // beta, status, iteration counts

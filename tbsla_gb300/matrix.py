@@ -439,6 +439,29 @@ class Batch:
         arr = (C.c_void_p * len(factors))(*[f._h.value for f in factors])
         check(lib.tbsla_batch_set_factors(self._h, arr, len(factors), precision), "batch_set_factors")
 
+    def fallbacks(self):
+        """Per system after the last cg(): (fallback code, preconditioner
+        used at exit).  Codes: 0 none, 1 the factor failed its check and
+        Jacobi ran instead, 2 the factored iteration stalled and Jacobi took
+        over."""
+        ns = len(self.offsets) - 1
+        fb = np.zeros(ns, np.int32)
+        used = np.zeros(ns, np.int32)
+        check(lib.tbsla_batch_fallbacks(self._h, fb.ctypes.data_as(C.POINTER(C.c_int)),
+                                        used.ctypes.data_as(C.POINTER(C.c_int))), "batch_fallbacks")
+        return fb, used
+
+    def set_wait_limit(self, ns: int):
+        """Bound on one grid-wide wait of the persistent solver (ns)."""
+        check(lib.tbsla_batch_set_wait_limit(self._h, int(ns)), "batch_set_wait_limit")
+
+    def engine(self) -> dict:
+        """Engine of the last cg(): persistent (one cooperative launch) or
+        multi-launch, and whether a CUDA graph replayed it."""
+        p, g = C.c_int(), C.c_int()
+        check(lib.tbsla_batch_engine(self._h, C.byref(p), C.byref(g)), "batch_engine")
+        return {"persistent": bool(p.value), "graph": bool(g.value)}
+
 
 class MPNN:
     """The learned preconditioner: a message-passing network that maps an SPD

@@ -97,3 +97,73 @@ def test_start_vector_is_used(gpu):
     x, it, rr, ok = m.CG(b, rel_tol=1e-12)
     x2, it2, rr2, ok2 = m.CG(b, x=x.copy(), rel_tol=1e-6)
     assert ok2 and it2 == 0
+
+
+def test_persistent_engine_runs_the_whole_solve(gpu):
+    """Stencil systems take the persistent engine: one cooperative launch per
+    solve, replayed from a CUDA graph; results verified in FP64 on the host
+    for FP64 storage (FP64 iteration) and FP32 storage (FP32 iteration with
+    FP64 refinement), plain and Jacobi."""
+    T = gpu
+    sizes = [9, 13, 6, 17]
+    systems = [diffusion(T, s, 300 + i) for i, s in enumerate(sizes)]
+    rhs = np.concatenate([T.fill_uniform(s ** 3, -1.0, 1.0, 400 + i) for i, s in enumerate(sizes)])
+    for precision in (T.F64, T.F32):
+        batch = T.Batch(systems, precision)
+        off = batch.offsets
+        for precond in (0, 1):
+            for rep in range(2):  # the second solve replays the captured graph
+                x, its, rr, ok = batch.cg(rhs, max_iterations=4000, rel_tol=TOL, precond=precond, refresh=50)
+                assert ok and (rr <= TOL).all(), (precision, precond, its, rr)
+                eng = batch.engine()
+                assert eng["persistent"], eng
+                for k, m in enumerate(systems):
+                    xs, bs = x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]
+                    assert true_rel_residual(m, xs, bs) <= TOL, (k, precision, precond)
+                fb, used = batch.fallbacks()
+                assert (fb == 0).all() and (used == precond).all()
+
+
+def test_general_pattern_takes_multi_launch_engine(gpu):
+    """A matrix whose entries lie on more than 8 diagonals (here a random
+    symmetric pattern made diagonally dominant) keeps the multi-launch
+    engine and still reaches the FP64-verified tolerance."""
+    T = gpu
+    n = 3000
+    rng = np.random.default_rng(3)
+    rows = rng.integers(0, n, 12000)
+    cols = rng.integers(0, n, 12000)
+    vals = rng.uniform(-1, 0, 12000)
+    import scipy.sparse as sp
+
+    A = sp.coo_matrix((vals, (rows, cols)), shape=(n, n)).tocsr()
+    A = A + A.T
+    A = A + sp.diags(np.asarray(abs(A).sum(axis=1)).ravel() + 1.0)
+    A = A.tocsr()
+    A.sort_indices()
+    m = T.MatrixCSR.from_arrays(n, n, A.indptr.astype(np.int32), A.indices.astype(np.int32), A.data)
+    b = T.fill_uniform(n, -1.0, 1.0, 11)
+    batch = T.Batch([m], T.F64)
+    x, its, rr, ok = batch.cg(b, max_iterations=2000, rel_tol=TOL, precond=1)
+    assert ok and rr[0] <= TOL
+    assert not batch.engine()["persistent"]
+    assert true_rel_residual(m, x, b) <= TOL
+
+
+def test_bounded_wait_returns_timeout_status(gpu):
+    """Every grid-wide wait of the persistent kernel is bounded.  With a
+    limit of 0 ns the first wait runs out at once: the kernel returns, the
+    call reports TBSLA_ERR_TIMEOUT (nothing hangs), and the next solve with
+    the default limit on the same batch succeeds."""
+    T = gpu
+    systems = [diffusion(T, 10, 500 + i) for i in range(3)]
+    rhs = np.concatenate([T.fill_uniform(1000, -1.0, 1.0, 600 + i) for i in range(3)])
+    batch = T.Batch(systems, T.F32)
+    batch.set_wait_limit(0)
+    with pytest.raises(T.TbslaError) as e:
+        batch.cg(rhs, max_iterations=2000, rel_tol=TOL, precond=1)
+    assert e.value.status == T._lib.ERR_TIMEOUT
+    batch.set_wait_limit(2_000_000_000)
+    x, its, rr, ok = batch.cg(rhs, max_iterations=2000, rel_tol=TOL, precond=1)
+    assert ok and (rr <= TOL).all()
+    assert batch.engine()["persistent"]
