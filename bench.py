@@ -930,24 +930,20 @@ def run_cg(a):
     print(json.dumps(line), flush=True)
 
 
-def run_learned(a):
+def learned_vs_jacobi(a, T, local: int) -> dict:
     """The learned-preconditioner workload: the network is trained on the
     GPU (one Adam step per system, lr 1e-3, 8 Gaussian probes) on diffusion
-    systems with n in [32, 64] (seeds 1000..), then 32 held-out 128^3 systems
-    (seeds 9000..9031, RHS U[-1,1)) are solved in one batch by Jacobi-PCG and
-    by PCG with M^-1 = L L^T from the network, both with FP32 values, FP64
-    refresh every 50 iterations, to a 1e-8 FP64-verified relative residual.
-    value: learned-PCG wall time / Jacobi-PCG wall time (lower is better)."""
+    systems with n in [32, 64] (seeds 1000..), then held-out 128^3 systems
+    (seeds 9000.., RHS U[-1,1)) are solved in one batch by Jacobi-PCG and by
+    PCG with M^-1 = L L^T from the network; FP32 values, FP64 refinement
+    every 50 iterations, to a 1e-8 FP64-verified relative residual.  Both
+    solvers run on the same batch in the persistent engine.  The learned
+    solver's timed region holds the network inference on the GPU (L written
+    into the batch's factor storage) AND the solve; Jacobi's holds the
+    building of D^-1 and its solve.  Wall clock of the host calls."""
     from concurrent.futures import ThreadPoolExecutor
 
     import numpy as np
-    import torch
-
-    import tbsla_gb300 as T
-
-    ws, rank, local = dist()
-    torch.cuda.set_device(local)
-    T.device_init(local)
 
     def system(n, seed):
         m = T.MatrixCSR()
@@ -973,45 +969,83 @@ def run_learned(a):
             losses.append(net.train_step(A, probes=8, seed=k, lr=1e-3))
             futs[k] = None
     t_train = time.time() - t0
-    held = [system(a.eval_n, 9000 + k) for k in range(a.eval_systems)]
+    t0 = time.time()
+    with ThreadPoolExecutor(8) as pool:
+        held = list(pool.map(lambda k: system(a.eval_n, 9000 + k), range(a.eval_systems)))
     N = a.eval_n ** 3
     rhs = np.concatenate([T.fill_uniform(N, -1.0, 1.0, 9100 + k) for k in range(a.eval_systems)])
-    t0 = time.time()
-    factors = [net.factor(A) for A in held]
-    t_factor = time.time() - t0
+    bt = T.Batch(held, T.F32)
+    t_setup = time.time() - t0
+    fprec = T.BF16 if a.factor_prec == "bf16" else T.F32
+    reps = max(1, min(a.steps, 3))
+
+    def jacobi():
+        return bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=1, refresh=50)
+
+    def learned():
+        t1 = time.perf_counter()
+        bt.factor_mpnn(net, fprec)
+        tf = time.perf_counter() - t1
+        return bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=2, refresh=50), tf
+
+    # warm-up: one full solve of each (the persistent graphs are captured on
+    # the first call, the network's scratch is allocated)
+    jacobi()
+    learned()
     res = {}
     clk = Clocks(local)
-    for name, pre in (("jacobi_pcg", 1), ("learned_pcg", 2)):
-        bt = T.Batch(held, T.F32)
-        if pre == 2:
-            bt.set_factors(factors, T.BF16 if a.factor_prec == "bf16" else T.F32)
-        bt.cg(rhs, max_iterations=20, rel_tol=1e-8, precond=pre, refresh=50, graph_iters=10)  # warm-up
-        if pre == 2:
-            clk.start()
-        times = []
-        for _ in range(a.steps):
-            t1 = time.perf_counter()
-            x, its, rr, ok = bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=pre, refresh=50,
-                                   graph_iters=10)
-            times.append(time.perf_counter() - t1)
-        res[name] = {"ms": statistics.mean(times) * 1e3, "iterations_mean": float(its.mean()),
-                     "iterations_max": int(its.max()), "all_converged": bool(ok),
-                     "max_rel_residual_fp64": float(rr.max())}
-        del bt
+    clk.start()
+    tj, tl, tfac = [], [], []
+    for _ in range(reps):
+        t1 = time.perf_counter()
+        xj, itj, rrj, okj = jacobi()
+        tj.append(time.perf_counter() - t1)
+        t1 = time.perf_counter()
+        (xl, itl, rrl, okl), tf = learned()
+        tl.append(time.perf_counter() - t1)
+        tfac.append(tf)
     clocks = clk.stop()
+    eng = bt.engine()
+    fb, used = bt.fallbacks()
+    res["jacobi_pcg"] = {"ms": statistics.median(tj) * 1e3, "iterations_mean": float(itj.mean()),
+                         "iterations_max": int(itj.max()), "all_converged": bool(okj),
+                         "max_rel_residual_fp64": float(rrj.max())}
+    res["learned_pcg"] = {"ms": statistics.median(tl) * 1e3, "factor_ms": statistics.median(tfac) * 1e3,
+                          "solve_ms": (statistics.median(tl) - statistics.median(tfac)) * 1e3,
+                          "iterations_mean": float(itl.mean()), "iterations_max": int(itl.max()),
+                          "all_converged": bool(okl), "max_rel_residual_fp64": float(rrl.max()),
+                          "fallbacks": int((fb != 0).sum())}
     ratio = res["learned_pcg"]["ms"] / res["jacobi_pcg"]["ms"]
+    return {"ratio": ratio, "solvers": res, "reps": reps, "engine": eng, "clocks": clocks,
+            "timed": "learned: network inference on the GPU + solve; jacobi: D^-1 + solve (same batch)",
+            "systems": a.eval_systems, "n": a.eval_n, "unknowns": a.eval_systems * N, "factor_storage": a.factor_prec,
+            "train": {"systems": a.train_systems, "epochs": a.epochs, "adam_steps": total,
+                      "seconds": round(t_train, 1), "loss_first_50": float(np.mean(losses[:50])),
+                      "loss_last_50": float(np.mean(losses[-50:]))},
+            "setup_s": round(t_setup, 1)}
+
+
+def run_learned(a):
+    """--workload learned: the learned-vs-Jacobi measurement on its own line.
+    value: (network inference + learned-PCG solve) / (Jacobi-PCG solve)."""
+    import torch
+
+    import tbsla_gb300 as T
+
+    ws, rank, local = dist()
+    torch.cuda.set_device(local)
+    T.device_init(local)
+    r = learned_vs_jacobi(a, T, local)
     line = {
-        "metric": METRIC, "value": ratio, "unit": "learned-PCG time / Jacobi-PCG time", "n_gpus": ws,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": res["learned_pcg"]["ms"], "higher_is_better": False,
-        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 weights / f32 network; f32 values, f64 vectors",
+        "metric": METRIC, "value": r["ratio"], "unit": "learned-PCG time / Jacobi-PCG time", "n_gpus": ws,
+        "steps": r["reps"], "warmup": 1, "ms_per_step": r["solvers"]["learned_pcg"]["ms"],
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 weights / f32 network; f32 values and iteration, f64 refinement",
         "data": "synthetic: seeded diffusion systems (train seeds 1000.., held-out 9000..)",
         "config": {"workload": f"learned_pcg_mpnn3x32_train{a.train_systems}_n32to64_eval{a.eval_systems}x{a.eval_n}^3",
-                   "unknowns_per_system": N, "rel_tol": 1e-8, "factor_storage": a.factor_prec,
-                   "step": "one batched PCG solve of the held-out systems (host call, wall clock)",
-                   "parallelism": "1 GPU"},
-        "train": {"systems": a.train_systems, "epochs": a.epochs, "adam_steps": total, "seconds": round(t_train, 1),
-                  "loss_first_50": float(np.mean(losses[:50])), "loss_last_50": float(np.mean(losses[-50:]))},
-        "factor_seconds": round(t_factor, 2), "solvers": res, "clocks": clocks,
+                   "unknowns_per_system": a.eval_n ** 3, "rel_tol": 1e-8, "factor_storage": a.factor_prec,
+                   "step": r["timed"], "parallelism": "1 GPU, one persistent launch per solve"},
+        "train": r["train"], "solvers": r["solvers"], "engine": r["engine"], "clocks": r["clocks"],
     }
     print(json.dumps(line), flush=True)
 

@@ -385,6 +385,11 @@ int tbsla_batch_fallbacks(const tbsla_batch* b, int* fallback, int* precond_used
  * (default 2e9).  A wait that runs out ends that solve on the GPU with
  * TBSLA_ERR_TIMEOUT; the batch stays usable. */
 int tbsla_batch_set_wait_limit(tbsla_batch* b, long long ns);
+/* Persistent engine tuning: rows per thread in the hot phases, 4 (the
+ * default where every system's first row and size are multiples of 4 and the
+ * iteration runs in FP32: 16-byte loads) or 1 (one row per thread, as for
+ * every other batch).  The arithmetic of each row is the same either way. */
+int tbsla_batch_set_rows_per_thread(tbsla_batch* b, int rows);
 /* The engine of the last tbsla_batch_cg: persistent = 1 when the whole solve
  * was one cooperative launch (every system's entries on at most 8 diagonals,
  * at most 256 systems, a factor, if used, on at most 8 diagonals), 0 for the
@@ -423,6 +428,20 @@ int tbsla_mpnn_train_step(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, u
 /* Writes L (CSR: per row its strictly lower entries, then the diagonal)
  * into the CSR handle L. */
 int tbsla_mpnn_factor(tbsla_mpnn* net, const tbsla_matrix* A, tbsla_matrix* L);
+/* The network's factor for every system of a batch, computed on the GPU from
+ * the batch's device copy of A and written straight into the batch's factor
+ * storage (precision TBSLA_F32 or TBSLA_BF16; TBSLA_F64 is kept as F32, the
+ * precision the factor is applied in): no host copy of A, L or L^T.  The
+ * same L as tbsla_mpnn_factor on each system (entries of A stored as exact
+ * zeros count as absent).  Requires a batch on the persistent engine
+ * (TBSLA_ERR_UNSUPPORTED otherwise); then tbsla_batch_cg with precond = 2. */
+int tbsla_batch_factor_mpnn(tbsla_batch* b, tbsla_mpnn* net, int precision);
+/* The batch's factor in its diagonal-slot form, for inspection: *slots = the
+ * slots per row (KL); deltas[s * 8 + q] = column - row of slot q of system s
+ * (slot 0 the diagonal); values[q * n + i] = the stored value of row i on
+ * slot q, widened to double (n = the batch's rows).  Any pointer may be NULL.
+ * TBSLA_ERR_UNSUPPORTED when the batch holds no factor in that form. */
+int tbsla_batch_factor_dia(const tbsla_batch* b, int* slots, int* deltas, double* values);
 
 #ifdef __cplusplus
 }

@@ -114,7 +114,10 @@ _SIGS = {
     "tbsla_batch_set_factors": (I, [P, C.POINTER(P), I, I]),
     "tbsla_batch_fallbacks": (I, [P, IP, IP]),
     "tbsla_batch_set_wait_limit": (I, [P, C.c_longlong]),
+    "tbsla_batch_set_rows_per_thread": (I, [P, I]),
     "tbsla_batch_engine": (I, [P, IP, IP]),
+    "tbsla_batch_factor_mpnn": (I, [P, P, I]),
+    "tbsla_batch_factor_dia": (I, [P, IP, IP, DP]),
     "tbsla_mpnn_create": (I, [C.POINTER(P), ULL]),
     "tbsla_mpnn_destroy": (I, [P]),
     "tbsla_mpnn_params": (I, [P, P, IP]),

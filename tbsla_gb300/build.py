@@ -58,7 +58,7 @@ def _compile(src: str, hdr: list[str], verbose: bool) -> str:
     if src.endswith(".cu"):
         cmd = [_nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--extended-lambda",
                "--expt-relaxed-constexpr",
-               "-Xcompiler", "-fPIC", *inc, "-c", src, "-o", obj]
+               "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", *inc, "-c", src, "-o", obj]
         if os.environ.get("TBSLA_PTXAS_VERBOSE"):
             cmd.insert(1, "-Xptxas=-v")
     else:

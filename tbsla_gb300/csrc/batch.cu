@@ -90,11 +90,15 @@ struct tbsla_batch {
 
   // persistent engine (DIA layout)
   bool dia = false;
+  bool vec4 = false;              // FP32 iteration, every system's first row and size a multiple of 4
+  bool vec4_off = false;          // tuning: one row per thread even where 4 would do
   int K = 0;                      // diagonal slots of A
   std::vector<int> adelta_h;      // [nsys * kDiaMaxDiag]
   int* adelta = nullptr;
   long* sys_off = nullptr;
   int* row_sys = nullptr;
+  int *dchunks = nullptr, *dchunk_sys = nullptr;  // the persistent engine's work chunks
+  int ndchunks = 0;
   void* avals_dia = nullptr;      // [K][n] storage precision
   double* a64_dia = nullptr;      // [K][n]
   float* dinv_f = nullptr;
@@ -103,6 +107,7 @@ struct tbsla_batch {
   std::vector<int> fdelta_h;      // [nsys * kDiaMaxDiag] deltas of the factor's slots
   int* fdelta = nullptr;
   void* lvals_dia = nullptr;      // [KL][n] in lprec_dia
+  size_t lvals_cap = 0;           // bytes allocated at lvals_dia
   int lprec_dia = TBSLA_F32;
   void *dv = nullptr, *r0 = nullptr, *r1 = nullptr, *p0 = nullptr, *p1 = nullptr, *q2 = nullptr,
        *z2 = nullptr, *t2 = nullptr;
@@ -113,6 +118,7 @@ struct tbsla_batch {
   int pgrid = 0;
   cudaGraphExec_t pgraph = nullptr;
   DiaCg pkey{};                   // the arguments the graph was captured with
+  int pkey_pre = -1;
   bool pgraph_ok = false;
   // last solve
   std::vector<int> fallback_h, mode_h;
@@ -127,7 +133,7 @@ struct tbsla_batch {
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
                   scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf,
                   ldelta, tdelta, zf, adelta, sys_off, row_sys, a64_dia, dinv_f, fdelta, lvals_dia,
-                  dv, r0, r1, p0, p1, q2, z2, t2, mode_d, fallback_d, relres_d, acc, bar};
+                  dv, r0, r1, p0, p1, q2, z2, t2, mode_d, fallback_d, relres_d, acc, bar, dchunks, dchunk_sys};
     for (void* v : ps)
       if (v) cudaFree(v);
     if (avals_dia && avals_dia != (void*)a64_dia) cudaFree(avals_dia);
@@ -277,11 +283,35 @@ int build_dia(tbsla_batch* B, const std::vector<int>& delta, int K) {
   const size_t es = B->prec == TBSLA_F64 ? 8 : 4;
   for (void** v : {&B->dv, &B->r0, &B->r1, &B->p0, &B->p1, &B->q2, &B->z2, &B->t2})
     CK(cudaMalloc(v, std::max<size_t>((size_t)n, 1) * es));
+  // work chunks of the persistent engine: never across a system, sized so
+  // that the batch gives every co-resident CTA about 8 of them (1024 to 4096
+  // rows, i.e. 1 to 4 rows of 4 per thread; 2 CTAs of 256 threads per SM)
+  {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long rows = n / ((long)sms * 2 * 8);
+    rows = std::min<long>(4096, std::max<long>(1024, (rows + 255) / 256 * 256));
+    std::vector<int> ch{0}, chs;
+    for (int s = 0; s < nsys; s++)
+      for (long r0 = B->off[s]; r0 < B->off[s + 1]; r0 += rows) {
+        ch.push_back((int)std::min<long>(B->off[s + 1], r0 + rows));
+        chs.push_back(s);
+      }
+    B->ndchunks = (int)chs.size();
+    CK(alloc(&B->dchunks, ch.size()));
+    CK(alloc(&B->dchunk_sys, std::max<size_t>(chs.size(), 1)));
+    CK(cudaMemcpyAsync(B->dchunks, ch.data(), ch.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B->dchunk_sys, chs.data(), chs.size() * 4, cudaMemcpyHostToDevice, st));
+    CK(cudaStreamSynchronize(st));
+  }
   CK(alloc(&B->mode_d, nsys));
   CK(alloc(&B->fallback_d, nsys));
   CK(alloc(&B->relres_d, nsys));
   CK(alloc(&B->acc, (size_t)12 * nsys));
   CK(alloc(&B->bar, 4));
+  B->vec4 = B->prec != TBSLA_F64;
+  for (int s = 0; s <= nsys; s++) B->vec4 = B->vec4 && B->off[s] % 4 == 0;
   B->adelta_h = delta;
   B->K = K;
   B->dia = true;
@@ -406,6 +436,19 @@ int capture(tbsla_batch* B, const CgBatch& c, int K) {
 
 
 
+// The DIA factor's value array, grown on demand and kept (repeated factor
+// builds of the same batch allocate nothing).
+cudaError_t lvals_reserve(tbsla_batch* B, size_t bytes) {
+  bytes = std::max<size_t>(bytes, 16);
+  if (B->lvals_dia && B->lvals_cap >= bytes) return cudaSuccess;
+  if (B->lvals_dia) cudaFree(B->lvals_dia);
+  B->lvals_dia = nullptr;
+  B->lvals_cap = 0;
+  cudaError_t e = cudaMalloc(&B->lvals_dia, bytes);
+  if (e == cudaSuccess) B->lvals_cap = bytes;
+  return e;
+}
+
 // A factor on at most kDiaMaxDiag diagonals per system, kept in DIA form for
 // the persistent engine (slot 0 the diagonal, then the other deltas in
 // descending order); TBSLA_ERR_UNSUPPORTED for any other factor.
@@ -452,11 +495,9 @@ int set_dia_factor(tbsla_batch* B, const std::vector<int>& rp, const std::vector
   if ((e = alloc(&rp_d, rp.size())) || (e = alloc(&ci_d, std::max<size_t>(ci.size(), 1))) ||
       (e = alloc(&va_d, std::max<size_t>(va.size(), 1))) || (e = alloc(&l64, (size_t)KL * n)))
     return fail(e);
-  if (B->lvals_dia) cudaFree(B->lvals_dia);
-  B->lvals_dia = nullptr;
   if (!B->fdelta && (e = alloc(&B->fdelta, delta.size()))) return fail(e);
   const int lprec = precision == TBSLA_BF16 ? TBSLA_BF16 : TBSLA_F32;
-  if ((e = cudaMalloc(&B->lvals_dia, std::max<size_t>((size_t)KL * n, 1) * (lprec == TBSLA_BF16 ? 2 : 4))) ||
+  if ((e = lvals_reserve(B, (size_t)KL * n * (lprec == TBSLA_BF16 ? 2 : 4))) ||
       (e = cudaMemcpyAsync(rp_d, rp.data(), rp.size() * 4, cudaMemcpyHostToDevice, st)) ||
       (!ci.empty() && (e = cudaMemcpyAsync(ci_d, ci.data(), ci.size() * 4, cudaMemcpyHostToDevice, st))) ||
       (!va.empty() && (e = cudaMemcpyAsync(va_d, va.data(), va.size() * 8, cudaMemcpyHostToDevice, st))) ||
@@ -493,9 +534,9 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   c.K = B->K;
   c.KL = precond == 2 ? B->KL : 0;
   c.sys_off = B->sys_off;
-  c.chunks = B->chunks;
-  c.chunk_sys = B->chunk_sys;
-  c.nchunks = B->nchunks;
+  c.chunks = B->dchunks;
+  c.chunk_sys = B->dchunk_sys;
+  c.nchunks = B->ndchunks;
   c.adelta = B->adelta;
   c.avals = B->avals_dia;
   c.prec = B->prec;
@@ -525,19 +566,24 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   c.max_it = max_iterations;
   c.refresh = B->prec != TBSLA_F64 ? refresh : 0;
   c.wait_ns = B->wait_ns;
+  c.vec4 = B->vec4 && !B->vec4_off ? 1 : 0;
   std::vector<int> mode(ns, precond);
   CK(cudaMemcpyAsync(B->b, rhs, n * 8, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->x, x, n * 8, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->mode_d, mode.data(), ns * sizeof(int), cudaMemcpyHostToDevice, s));
   const size_t es = B->prec == TBSLA_F64 ? 8 : 4;
   auto enqueue = [&](cudaStream_t st) -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(B->dv, 0, (size_t)n * es, st);
+    cudaError_t e = cudaSuccess;
+    // Jacobi builds its preconditioner (D^-1 from A's diagonal) inside every
+    // solve, as the factored form builds L before its solve
+    if (precond == 1) e = dia_dinv(B->a64_dia, B->row_sys, B->adelta, B->K, n, B->dinv_f, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B->dv, 0, (size_t)n * es, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B->acc, 0, (size_t)12 * ns * 8, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B->bar, 0, 4 * sizeof(unsigned), st);
     if (e == cudaSuccess) e = cg_dia_solve(c, grid, st);
     return e;
   };
-  if (!B->pgraph || std::memcmp(&B->pkey, &c, sizeof c) != 0) {
+  if (!B->pgraph || std::memcmp(&B->pkey, &c, sizeof c) != 0 || B->pkey_pre != precond) {
     if (B->pgraph) cudaGraphExecDestroy(B->pgraph);
     B->pgraph = nullptr;
     cudaGraph_t g = nullptr;
@@ -555,6 +601,7 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
       B->pgraph = nullptr;
     }
     B->pkey = c;
+    B->pkey_pre = precond;
   }
   if (B->pgraph) CK(cudaGraphLaunch(B->pgraph, s));
   else CK(enqueue(s));
@@ -874,12 +921,80 @@ int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterati
   return all ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
 }
 
+int tbsla_batch_factor_mpnn(tbsla_batch* B, tbsla_mpnn* net, int precision) {
+  if (!B || !net || precision < TBSLA_F64 || precision > TBSLA_BF16) return TBSLA_ERR_INVALID_ARG;
+  if (!B->dia) return TBSLA_ERR_UNSUPPORTED;
+  const int nsys = B->nsys;
+  // L's slots: the diagonal, then A's negative deltas in descending order
+  // (the pattern of tril(A))
+  std::vector<int> ld((size_t)nsys * kDiaMaxDiag, 0);
+  int KL = 1;
+  for (int s = 0; s < nsys; s++) {
+    int* q = ld.data() + (size_t)s * kDiaMaxDiag;
+    int c = 1;
+    for (int k = 0; k < B->K; k++) {
+      const int d = B->adelta_h[(size_t)s * kDiaMaxDiag + k];
+      if (d < 0) q[c++] = d;
+    }
+    std::sort(q + 1, q + c, [](int a, int b) { return a > b; });
+    KL = std::max(KL, c);
+  }
+  cudaSetDevice(B->device);
+  cudaStream_t st = B->stream;
+  const int lprec = precision == TBSLA_BF16 ? TBSLA_BF16 : TBSLA_F32;
+  B->dia_factor = false;
+  if (!B->fdelta) CK(alloc(&B->fdelta, ld.size()));
+  CK(lvals_reserve(B, (size_t)KL * B->n * (lprec == TBSLA_BF16 ? 2 : 4)));
+  CK(cudaMemcpyAsync(B->fdelta, ld.data(), ld.size() * 4, cudaMemcpyHostToDevice, st));
+  const int r = tbsla_impl::mpnn_factor_dia(net, B->n, B->K, B->a64_dia, B->adelta, B->row_sys, KL, B->fdelta,
+                                            B->lvals_dia, lprec, st);
+  if (r) return r;
+  B->fdelta_h = ld;
+  B->KL = KL;
+  B->lprec_dia = lprec;
+  B->dia_factor = true;
+  B->factor_fb.assign(nsys, 0);
+  return TBSLA_OK;
+}
+
+int tbsla_batch_factor_dia(const tbsla_batch* B, int* slots, int* deltas, double* values) {
+  if (!B) return TBSLA_ERR_INVALID_ARG;
+  if (!B->dia_factor) return TBSLA_ERR_UNSUPPORTED;
+  if (slots) *slots = B->KL;
+  if (deltas) std::copy(B->fdelta_h.begin(), B->fdelta_h.end(), deltas);
+  if (values) {
+    const size_t len = (size_t)B->KL * B->n;
+    cudaSetDevice(B->device);
+    if (B->lprec_dia == TBSLA_BF16) {
+      std::vector<unsigned short> h(len);
+      CK(cudaMemcpy(h.data(), B->lvals_dia, len * 2, cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < len; k++) {
+        const unsigned u = (unsigned)h[k] << 16;
+        float f;
+        std::memcpy(&f, &u, 4);
+        values[k] = f;
+      }
+    } else {
+      std::vector<float> h(len);
+      CK(cudaMemcpy(h.data(), B->lvals_dia, len * 4, cudaMemcpyDeviceToHost));
+      for (size_t k = 0; k < len; k++) values[k] = h[k];
+    }
+  }
+  return TBSLA_OK;
+}
+
 int tbsla_batch_fallbacks(const tbsla_batch* B, int* fallback, int* precond_used) {
   if (!B) return TBSLA_ERR_INVALID_ARG;
   for (int k = 0; k < B->nsys; k++) {
     if (fallback) fallback[k] = k < (int)B->fallback_h.size() ? B->fallback_h[k] : 0;
     if (precond_used) precond_used[k] = k < (int)B->mode_h.size() ? B->mode_h[k] : 0;
   }
+  return TBSLA_OK;
+}
+
+int tbsla_batch_set_rows_per_thread(tbsla_batch* B, int rows) {
+  if (!B || (rows != 1 && rows != 4)) return TBSLA_ERR_INVALID_ARG;
+  B->vec4_off = rows == 1;
   return TBSLA_OK;
 }
 

@@ -6,6 +6,8 @@
 
 #include "host/matrix.hpp"
 
+struct tbsla_mpnn;
+
 namespace tbsla_impl {
 
 int dev_select(int device);
@@ -58,5 +60,14 @@ int dev_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* tr
 long dev_noalloc_max_items();
 int dev_csr_ax_noalloc(int n_row, long nnz, int f_col, const int* rowptr, const int* colidx,
                        const double* values, const double* v, double* r, void* stream);
+
+// The learned factor of every system of a batch, computed on the device from
+// the batch's diagonal-slot copy of A (FP64 values a64[k * n + i], slot deltas
+// adelta[sys * 8 + k], row_sys[i] the system of row i) and written straight
+// into the batch's diagonal-slot factor lvals[q * n + i] in lprec (F32 /
+// BF16; slot deltas ldelta: slot 0 the diagonal, then A's negative deltas).
+// TBSLA_ERR_BAD_MATRIX when a diagonal entry of A is <= 0.
+int mpnn_factor_dia(tbsla_mpnn* net, long n, int K, const double* a64, const int* adelta, const int* row_sys,
+                    int KL, const int* ldelta, void* lvals, int lprec, void* stream);
 
 }  // namespace tbsla_impl

@@ -128,36 +128,116 @@ __device__ bool grid_sync(unsigned* bar, unsigned& gen, long long wait_ns, int* 
   return !*s_stop;
 }
 
-// Sum of up to 3 per-thread partials over the CTA, added to acc[what * ns +
-// sys] (FP64 atomics).  Warps sum in T, the CTA in FP64.
+// ---- 4-row vectors (FP32 iteration) --------------------------------------------
+// With every system's first row and size a multiple of 4, a thread takes 4
+// consecutive rows: own-row streams are 16-byte loads, and the rows of a
+// neighbour diagonal, [i0 + s, i0 + s + 4), are put together from the two
+// aligned vectors that cover them.  An aligned vector lies wholly inside or
+// wholly outside its system, so rows outside read as 0 (their slot value is
+// 0 too).  Every row's arithmetic is that of the scalar loops.
+__device__ __forceinline__ float4 f4zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float4 ld4(const __nv_bfloat16* p) {
+  const uint2 u = *reinterpret_cast<const uint2*>(p);
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
+                     __uint_as_float(u.y & 0xffff0000u));
+}
+__device__ __forceinline__ float4 ld4_stream(const float* p, uint64_t pol) {
+  float4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "l"(p), "l"(pol));
+  return v;
+}
+__device__ __forceinline__ float4 ld4_stream(const __nv_bfloat16* p, uint64_t pol) {
+  unsigned a, b;
+  asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+               : "=r"(a), "=r"(b) : "l"(p), "l"(pol));
+  return make_float4(__uint_as_float(a << 16), __uint_as_float(a & 0xffff0000u), __uint_as_float(b << 16),
+                     __uint_as_float(b & 0xffff0000u));
+}
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+template <class E>
+__device__ __forceinline__ float4 rows4(const E* v, long i0, long s, long lo, long hi) {
+  const int r = (int)(s & 3);
+  const long b = i0 + s - r;
+  const float4 v0 = b >= lo && b < hi ? ld4(v + b) : f4zero();
+  if (r == 0) return v0;
+  const float4 v1 = b + 4 >= lo && b + 4 < hi ? ld4(v + b + 4) : f4zero();
+  if (r == 1) return make_float4(v0.y, v0.z, v0.w, v1.x);
+  if (r == 2) return make_float4(v0.z, v0.w, v1.x, v1.y);
+  return make_float4(v0.w, v1.x, v1.y, v1.z);
+}
+__device__ __forceinline__ float4 fma4(float4 a, float4 b, float4 c) {
+  return make_float4(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z), fmaf(a.w, b.w, c.w));
+}
+__device__ __forceinline__ float4 fma4s(float a, float4 b, float4 c) {
+  return make_float4(fmaf(a, b.x, c.x), fmaf(a, b.y, c.y), fmaf(a, b.z, c.z), fmaf(a, b.w, c.w));
+}
+__device__ __forceinline__ float dot4(float4 a, float4 b, float acc) {
+  return fmaf(a.w, b.w, fmaf(a.z, b.z, fmaf(a.y, b.y, fmaf(a.x, b.x, acc))));
+}
+
+// Per-warp running sums of up to 3 values for one system at a time: lanes
+// add their rows' terms; when the warp moves to another system (or the phase
+// ends) the warp reduces them and lane 0 adds them to acc[what * ns + sys] in
+// FP64.  No CTA-wide barrier.  Every lane of the warp calls to() / flush()
+// at the same points (the chunk loops are uniform over the CTA).
 template <class T, int NV>
-__device__ __forceinline__ void cta_add(T (&v)[NV], double* s_red, double* acc, int ns, int sys) {
+struct WarpSums {
+  int sys = -1;
+  T v[NV];
+  __device__ __forceinline__ WarpSums() {
 #pragma unroll
-  for (int k = 0; k < NV; k++) {
+    for (int k = 0; k < NV; k++) v[k] = (T)0;
+  }
+  __device__ __forceinline__ void flush(double* acc, int ns) {
+    if (sys >= 0) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-  }
-  const int w = threadIdx.x / 32, l = threadIdx.x % 32;
-  if (l == 0) {
+      for (int k = 0; k < NV; k++) {
 #pragma unroll
-    for (int k = 0; k < NV; k++) s_red[k * (PNT / 32) + w] = (double)v[k];
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+      }
+      if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) atomicAdd(acc + (size_t)k * ns + sys, (double)v[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < NV; k++) v[k] = (T)0;
+    }
+    sys = -1;
   }
-  __syncthreads();
-  if (threadIdx.x < NV) {
-    double s = 0;
-    for (int i = 0; i < PNT / 32; i++) s += s_red[threadIdx.x * (PNT / 32) + i];
-    atomicAdd(acc + threadIdx.x * ns + sys, s);
+  __device__ __forceinline__ void to(int s, double* acc, int ns) {
+    if (s != sys) {
+      flush(acc, ns);
+      sys = s;
+    }
   }
-  __syncthreads();
+};
+
+// Chunks are dealt to CTAs in runs of `run` consecutive chunks (so a CTA
+// rarely changes system within a phase; up to 4, fewer when the batch has
+// too few chunks to give every CTA a run), runs round-robin over the grid.
+constexpr int kRunMax = 4;
+#define FOR_CHUNKS(ch)                                                                         \
+  for (int run_ = blockIdx.x * run; run_ < c.nchunks; run_ += gridDim.x * run)               \
+    for (int ch = run_, end_ = min(run_ + run, c.nchunks); ch < end_; ch++)
+
+// L2 prefetch of rows [r0, r1) of an array by the TMA unit: one bulk
+// prefetch instruction (16-byte aligned start, whole 16-byte units inside
+// the range), issued by one thread; a hint with no completion to wait for.
+template <class E>
+__device__ __forceinline__ void prefetch_rows(const E* a, long r0, long r1) {
+  const uintptr_t lo = (reinterpret_cast<uintptr_t>(a + r0) + 15) & ~(uintptr_t)15;
+  const uintptr_t hi = reinterpret_cast<uintptr_t>(a + r1) & ~(uintptr_t)15;
+  if (hi > lo)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
 }
 
 template <class T, class V, class LV>
 __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
   __shared__ double s_rz[kDiaMaxSys], s_alpha[kDiaMaxSys], s_beta[kDiaMaxSys], s_bb[kDiaMaxSys],
       s_prev[kDiaMaxSys], s_rzj[kDiaMaxSys];
-  __shared__ int s_st[kDiaMaxSys], s_why[kDiaMaxSys], s_mode[kDiaMaxSys], s_it[kDiaMaxSys],
-      s_since[kDiaMaxSys], s_fb[kDiaMaxSys];
-  __shared__ double s_red[3 * (PNT / 32)];
+  __shared__ int s_st[kDiaMaxSys], s_mode[kDiaMaxSys], s_it[kDiaMaxSys], s_since[kDiaMaxSys], s_fb[kDiaMaxSys];
   __shared__ int s_stop;
   const int ns = c.nsys;
   const int tid = threadIdx.x;
@@ -175,11 +255,12 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
   T* __restrict__ Q = static_cast<T*>(c.q);
   T* __restrict__ Z = static_cast<T*>(c.z);
   T* __restrict__ Tt = static_cast<T*>(c.t);
+  const float* __restrict__ dinv = c.dinv;
   const uint64_t pol = policy_evict_first();
+  const int run = max(1, min(kRunMax, c.nchunks / (4 * (int)gridDim.x)));
 
   for (int s = tid; s < ns; s += PNT) {
     s_st[s] = S_CHECK;
-    s_why[s] = 0;
     s_mode[s] = c.mode[s];
     s_it[s] = 0;
     s_since[s] = 0;
@@ -190,11 +271,12 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
   __syncthreads();
 
   unsigned gen = 0;
-  int ph = 0;       // phases done: accumulator slot of the current phase = ph % 3
-  int g = 0;        // iteration parity of the R / P buffers
+  int ph = 0;  // phases done: accumulator slot of the current phase = ph % 3
+  int g = 0;   // iteration parity of the R / P buffers
   bool init = true;
   auto slot = [&](int p) { return c.acc + (size_t)(p % 3) * 4 * ns; };
-  // clear the slot two phases ahead (CTA 0), then run `body`, then the barrier
+  // CTA 0 clears the slot two phases ahead (read at the start of the
+  // previous phase by every CTA, written next in the following phase)
   auto clear_ahead = [&]() {
     if (blockIdx.x == 0) {
       double* a = slot(ph + 1);
@@ -206,6 +288,10 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
     for (int s = tid; s < ns; s += PNT) f |= s_st[s] == st && (mode < 0 || s_mode[s] == mode);
     return __syncthreads_or(f) != 0;
   };
+  auto load_deltas = [&](const int* tab, int s, int kk, int (&dd)[KMAX]) {
+#pragma unroll
+    for (int k = 0; k < KMAX; k++) dd[k] = k < kk ? tab[s * KMAX + k] : 0;
+  };
 
   for (;;) {
     // ================= refinement: systems in S_CHECK ======================
@@ -214,12 +300,13 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
       clear_ahead();
       {
         double* acc = slot(ph);
-        for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+        WarpSums<float, 1> bad;
+        FOR_CHUNKS(ch) {
           const int s = c.chunk_sys[ch];
           if (s_st[s] != S_CHECK) continue;
           const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
           const bool chk = init && s_mode[s] == 2;
-          float bad[1] = {0.f};
+          if (chk) bad.to(s, acc, ns);
           for (int i = r0 + tid; i < r1; i += PNT) {
             const double xi = c.x[i] + (double)D[i];
             if (isfinite(xi)) c.x[i] = xi;  // a non-finite correction is dropped
@@ -227,13 +314,13 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
             if (chk) {
               for (int k = 0; k < c.KL; k++) {
                 const LV lv = Lv[(size_t)k * n + i];
-                if (!finite_v(lv)) bad[0] = 1.f;
-                if (k == 0 && !(to_f(lv) > 0.f)) bad[0] = 1.f;  // slot 0 is the diagonal
+                if (!finite_v(lv)) bad.v[0] = 1.f;
+                if (k == 0 && !(to_f(lv) > 0.f)) bad.v[0] = 1.f;  // slot 0 is the diagonal
               }
             }
           }
-          if (chk) cta_add<float, 1>(bad, s_red, acc, ns, s);
         }
+        bad.flush(acc, ns);
       }
       if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
       {
@@ -251,18 +338,18 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
       clear_ahead();
       {
         double* acc = slot(ph);
-        T* Rn = R(g);
-        T* Po = P(g);
-        for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+        T* __restrict__ Rn = R(g);
+        T* __restrict__ Po = P(g);
+        WarpSums<double, 3> part;
+        FOR_CHUNKS(ch) {
           const int s = c.chunk_sys[ch];
           if (s_st[s] != S_CHECK) continue;
+          part.to(s, acc, ns);
           const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
           const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
           int dd[KMAX];
-#pragma unroll
-          for (int k = 0; k < KMAX; k++) dd[k] = k < c.K ? c.adelta[s * KMAX + k] : 0;
+          load_deltas(c.adelta, s, c.K, dd);
           const bool ident = s_mode[s] == 0;
-          double part[3] = {0, 0, 0};
           for (int i = r0 + tid; i < r1; i += PNT) {
             double ax = 0;
 #pragma unroll
@@ -275,17 +362,17 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
             }
             const double bi = c.b[i];
             const double ri = bi - ax;
-            part[0] = fma_rn(ri, ri, part[0]);
-            part[1] = fma_rn(bi, bi, part[1]);
+            part.v[0] = fma_rn(ri, ri, part.v[0]);
+            part.v[1] = fma_rn(bi, bi, part.v[1]);
             const T rt = (T)ri;
             Rn[i] = rt;
-            const T zi = ident ? rt : (T)c.dinv[i] * rt;
+            const T zi = ident ? rt : (T)dinv[i] * rt;
             Z[i] = zi;
-            part[2] += (double)(rt * zi);
+            part.v[2] += (double)(rt * zi);
             Po[i] = (T)0;
           }
-          cta_add<double, 3>(part, s_red, acc, ns, s);
         }
+        part.flush(acc, ns);
       }
       if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
       {
@@ -322,20 +409,20 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
       }
       __syncthreads();
       if (any_state(S_RESTART_F, -1)) {
-        // R3: t = L^T r (FP32 / T arithmetic), r.z = t.t
+        // R3: t = L^T r (T arithmetic), r.z = t.t
         clear_ahead();
         {
           double* acc = slot(ph);
-          const T* Rc = R(g);
-          for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+          const T* __restrict__ Rc = R(g);
+          WarpSums<T, 1> part;
+          FOR_CHUNKS(ch) {
             const int s = c.chunk_sys[ch];
             if (s_st[s] != S_RESTART_F) continue;
+            part.to(s, acc, ns);
             const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
             const long hi = c.sys_off[s + 1];
             int ld[KMAX];
-#pragma unroll
-            for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
-            T part[1] = {(T)0};
+            load_deltas(c.ldelta, s, c.KL, ld);
             for (int i = r0 + tid; i < r1; i += PNT) {
               T t = (T)0;
 #pragma unroll
@@ -346,10 +433,10 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
                 }
               }
               Tt[i] = t;
-              part[0] += t * t;
+              part.v[0] += t * t;
             }
-            cta_add<T, 1>(part, s_red, acc, ns, s);
           }
+          part.flush(acc, ns);
         }
         if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
         {
@@ -372,15 +459,14 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
         // R4: p = L t
         clear_ahead();
         {
-          T* Po = P(g);
-          for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+          T* __restrict__ Po = P(g);
+          FOR_CHUNKS(ch) {
             const int s = c.chunk_sys[ch];
             if (s_st[s] != S_RESTART_F) continue;
             const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
             const long lo = c.sys_off[s];
             int ld[KMAX];
-#pragma unroll
-            for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
+            load_deltas(c.ldelta, s, c.KL, ld);
             for (int i = r0 + tid; i < r1; i += PNT) {
               T z = (T)0;
 #pragma unroll
@@ -405,23 +491,60 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
     if (!any_state(S_ACTIVE, -1)) break;
 
     // ================= one iteration =======================================
-    T* Pold = P(g);
-    T* Pnew = P(g + 1);
+    const T* __restrict__ Pold = P(g);
+    T* __restrict__ Pnew = P(g + 1);
     // A: q = A p, p.q
     clear_ahead();
     {
       double* acc = slot(ph);
-      for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+      WarpSums<T, 1> part;
+      FOR_CHUNKS(ch) {
         const int s = c.chunk_sys[ch];
         if (s_st[s] != S_ACTIVE) continue;
+        part.to(s, acc, ns);
         const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
         const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
-        int dd[KMAX];
-#pragma unroll
-        for (int k = 0; k < KMAX; k++) dd[k] = k < c.K ? c.adelta[s * KMAX + k] : 0;
         const bool fact = s_mode[s] == 2;
+        if (tid == 0 && ch == run_) {  // the next run's streams into L2 while this one runs
+          const int nx = run_ + gridDim.x * run;
+          if (nx < c.nchunks) {
+            const int q0 = c.chunks[nx], q1 = c.chunks[min(nx + run, c.nchunks)];
+            for (int k = 0; k < c.K; k++) prefetch_rows(A + (size_t)k * n, q0, q1);
+            prefetch_rows(Pold, q0, q1);
+            prefetch_rows(Z, q0, q1);
+          }
+        }
+        int dd[KMAX];
+        load_deltas(c.adelta, s, c.K, dd);
         const T beta = (T)s_beta[s];
-        T part[1] = {(T)0};
+        if constexpr (sizeof(T) == 4) {
+          if (c.vec4) {
+            const float* Zf = reinterpret_cast<const float*>(Z);
+            const float* Pf = reinterpret_cast<const float*>(Pold);
+            for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+              float4 a[KMAX];
+#pragma unroll
+              for (int k = 0; k < KMAX; k++) a[k] = k < c.K ? ld4_stream(A + (size_t)k * n + i0, pol) : f4zero();
+              float4 q = f4zero(), pi;
+              if (fact) {
+#pragma unroll
+                for (int k = 0; k < KMAX; k++)
+                  if (k < c.K) q = fma4(a[k], rows4(Pf, i0, dd[k], lo, hi), q);
+                pi = ld4(Pf + i0);
+              } else {
+#pragma unroll
+                for (int k = 0; k < KMAX; k++)
+                  if (k < c.K)
+                    q = fma4(a[k], fma4s(beta, rows4(Pf, i0, dd[k], lo, hi), rows4(Zf, i0, dd[k], lo, hi)), q);
+                pi = fma4s(beta, ld4(Pf + i0), ld4(Zf + i0));
+                st4(reinterpret_cast<float*>(Pnew) + i0, pi);
+              }
+              st4(reinterpret_cast<float*>(Q) + i0, q);
+              part.v[0] = dot4(pi, q, part.v[0]);
+            }
+            continue;
+          }
+        }
         for (int i = r0 + tid; i < r1; i += PNT) {
           T a[KMAX];
 #pragma unroll
@@ -450,10 +573,10 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
             Pnew[i] = pi;
           }
           Q[i] = q;
-          part[0] += pi * q;
+          part.v[0] += pi * q;
         }
-        cta_add<T, 1>(part, s_red, acc, ns, s);
       }
+      part.flush(acc, ns);
     }
     if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
     {
@@ -470,25 +593,86 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
     clear_ahead();
     {
       double* acc = slot(ph);
-      const T* Ro = R(g);
-      T* Rn = R(g + 1);
-      for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+      const T* __restrict__ Ro = R(g);
+      T* __restrict__ Rn = R(g + 1);
+      WarpSums<T, 2> part;
+      FOR_CHUNKS(ch) {
         const int s = c.chunk_sys[ch];
         if (s_st[s] != S_ACTIVE) continue;
+        part.to(s, acc, ns);
         const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
         const T alpha = (T)s_alpha[s];
         const int mode = s_mode[s];
-        T part[2] = {(T)0, (T)0};
+        if (tid == 0 && ch == run_) {
+          const int nx = run_ + gridDim.x * run;
+          if (nx < c.nchunks) {
+            const int q0 = c.chunks[nx], q1 = c.chunks[min(nx + run, c.nchunks)];
+            prefetch_rows(Ro, q0, q1);
+            prefetch_rows(Q, q0, q1);
+            prefetch_rows(D, q0, q1);
+            if (s_mode[c.chunk_sys[nx]] == 2) {
+              prefetch_rows(Pold, q0, q1);
+              for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
+            } else {
+              prefetch_rows(Pnew, q0, q1);
+              prefetch_rows(dinv, q0, q1);
+            }
+          }
+        }
+        if constexpr (sizeof(T) == 4) {
+          if (c.vec4) {
+            const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
+            float* Df = reinterpret_cast<float*>(D);
+            const float* Rof = reinterpret_cast<const float*>(Ro);
+            const float* Qf = reinterpret_cast<const float*>(Q);
+            float* Rnf = reinterpret_cast<float*>(Rn);
+            if (mode == 2) {
+              int ld[KMAX];
+              load_deltas(c.ldelta, s, c.KL, ld);
+              for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+                st4(Df + i0, fma4s(alpha, ld4(reinterpret_cast<const float*>(Pold) + i0), ld4(Df + i0)));
+                const float4 ri = fma4s(-alpha, ld4(Qf + i0), ld4(Rof + i0));
+                st4(Rnf + i0, ri);
+                part.v[1] = dot4(ri, ri, part.v[1]);
+                float4 t = f4zero();
+#pragma unroll
+                for (int k = 0; k < KMAX; k++) {
+                  if (k < c.KL) {
+                    const long sh = -(long)ld[k];  // L_{j,i} sits on row j = i - delta
+                    const float4 rf = fma4s(-alpha, rows4(Qf, i0, sh, lo, hi), rows4(Rof, i0, sh, lo, hi));
+                    t = fma4(rows4(Lv + (size_t)k * n, i0, sh, lo, hi), rf, t);
+                  }
+                }
+                st4(reinterpret_cast<float*>(Tt) + i0, t);
+                part.v[0] = dot4(t, t, part.v[0]);
+              }
+            } else {
+              for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+                st4(Df + i0, fma4s(alpha, ld4(reinterpret_cast<const float*>(Pnew) + i0), ld4(Df + i0)));
+                const float4 ri = fma4s(-alpha, ld4(Qf + i0), ld4(Rof + i0));
+                st4(Rnf + i0, ri);
+                float4 zi = ri;
+                if (mode == 1) {
+                  const float4 dv = ld4(dinv + i0);
+                  zi = make_float4(dv.x * ri.x, dv.y * ri.y, dv.z * ri.z, dv.w * ri.w);
+                }
+                st4(reinterpret_cast<float*>(Z) + i0, zi);
+                part.v[0] = dot4(ri, zi, part.v[0]);
+                part.v[1] = dot4(ri, ri, part.v[1]);
+              }
+            }
+            continue;
+          }
+        }
         if (mode == 2) {
           const long hi = c.sys_off[s + 1];
           int ld[KMAX];
-#pragma unroll
-          for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
+          load_deltas(c.ldelta, s, c.KL, ld);
           for (int i = r0 + tid; i < r1; i += PNT) {
             D[i] += alpha * Pold[i];
             const T ri = Ro[i] - alpha * Q[i];
             Rn[i] = ri;
-            part[1] += ri * ri;
+            part.v[1] += ri * ri;
             T t = (T)0;
 #pragma unroll
             for (int k = 0; k < KMAX; k++) {
@@ -498,21 +682,21 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
               }
             }
             Tt[i] = t;
-            part[0] += t * t;
+            part.v[0] += t * t;
           }
         } else {
           for (int i = r0 + tid; i < r1; i += PNT) {
             D[i] += alpha * Pnew[i];
             const T ri = Ro[i] - alpha * Q[i];
             Rn[i] = ri;
-            const T zi = mode == 1 ? (T)c.dinv[i] * ri : ri;
+            const T zi = mode == 1 ? (T)dinv[i] * ri : ri;
             Z[i] = zi;
-            part[0] += ri * zi;
-            part[1] += ri * ri;
+            part.v[0] += ri * zi;
+            part.v[1] += ri * ri;
           }
         }
-        cta_add<T, 2>(part, s_red, acc, ns, s);
       }
+      part.flush(acc, ns);
     }
     if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
     {
@@ -524,19 +708,14 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
         const double rzn = acc[s], rr = acc[ns + s];
         s_beta[s] = s_rz[s] != 0 ? rzn / s_rz[s] : 0.0;
         s_rz[s] = rzn;
-        if (rr <= c.tol2 * s_bb[s]) {
-          s_st[s] = S_CHECK;
-          s_why[s] = 1;
-        } else if (s_it[s] >= c.max_it) {
-          s_st[s] = S_CHECK;
-          s_why[s] = 3;
-        } else if (c.refresh > 0 && s_since[s] >= c.refresh) {
-          s_st[s] = S_CHECK;
-          s_why[s] = 2;
-        } else if (!(rzn > 0) || !isfinite(rzn) || !isfinite(rr)) {
+        if (rr <= c.tol2 * s_bb[s])
+          s_st[s] = S_CHECK;  // apparently converged: verify on the FP64 residual
+        else if (s_it[s] >= c.max_it)
+          s_st[s] = S_CHECK;  // iteration limit: final refinement
+        else if (c.refresh > 0 && s_since[s] >= c.refresh)
+          s_st[s] = S_CHECK;  // periodic refinement
+        else if (!(rzn > 0) || !isfinite(rzn) || !isfinite(rr))
           s_st[s] = S_CHECK;  // breakdown: refine (and fall back if it does not help)
-          s_why[s] = 4;
-        }
       }
       ph++;
     }
@@ -544,15 +723,37 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
     if (any_state(S_ACTIVE, 2)) {
       // D: z = L t, p = z + beta p
       clear_ahead();
-      for (int ch = blockIdx.x; ch < c.nchunks; ch += gridDim.x) {
+      FOR_CHUNKS(ch) {
         const int s = c.chunk_sys[ch];
         if (s_st[s] != S_ACTIVE || s_mode[s] != 2) continue;
         const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
         const long lo = c.sys_off[s];
         const T beta = (T)s_beta[s];
+        if (tid == 0 && ch == run_) {
+          const int nx = run_ + gridDim.x * run;
+          if (nx < c.nchunks) {
+            const int q0 = c.chunks[nx], q1 = c.chunks[min(nx + run, c.nchunks)];
+            prefetch_rows(Tt, q0, q1);
+            prefetch_rows(Pold, q0, q1);
+            for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
+          }
+        }
         int ld[KMAX];
+        load_deltas(c.ldelta, s, c.KL, ld);
+        if constexpr (sizeof(T) == 4) {
+          if (c.vec4) {
+            const long hi = c.sys_off[s + 1];
+            const float* Tf = reinterpret_cast<const float*>(Tt);
+            for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+              float4 z = f4zero();
 #pragma unroll
-        for (int k = 0; k < KMAX; k++) ld[k] = k < c.KL ? c.ldelta[s * KMAX + k] : 0;
+              for (int k = 0; k < KMAX; k++)
+                if (k < c.KL) z = fma4(ld4(Lv + (size_t)k * n + i0), rows4(Tf, i0, ld[k], lo, hi), z);
+              st4(reinterpret_cast<float*>(Pnew) + i0, fma4s(beta, ld4(reinterpret_cast<const float*>(Pold) + i0), z));
+            }
+            continue;
+          }
+        }
         for (int i = r0 + tid; i < r1; i += PNT) {
           T z = (T)0;
 #pragma unroll
@@ -582,6 +783,7 @@ __global__ void __launch_bounds__(PNT, 2) k_cg_persistent(DiaCg c) {
     }
   }
 }
+#undef FOR_CHUNKS
 
 // ---- layout builders ----------------------------------------------------------
 

@@ -260,6 +260,8 @@ struct DiaCg {
   double tol2;
   int max_it;
   int refresh;            // iterations per refinement cycle (narrow storage), 0 = never
+  int vec4;               // every system's first row and size a multiple of 4, FP32 iteration:
+                          // the hot phases take 4 rows per thread with 16-byte loads
   long long wait_ns;      // bound on one grid-wide wait
 };
 // Co-resident CTAs of the persistent kernel for (prec, lprec) on this device.

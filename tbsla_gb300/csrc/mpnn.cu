@@ -5,7 +5,8 @@
 // CG); this is the project's own model, with Jacobi (L = D^-1/2, the
 // network's starting point) as its fallback.
 //
-//   s_i = a_ii^-1/2, e_ij = a_ij s_i s_j on the stored entries (symmetric A)
+//   s_i = a_ii^-1/2, e_ij = a_ij s_i s_j on the stored entries (symmetric A),
+//   computed in FP32
 //   x_i = [1, sum_{j!=i} e_ij, sum_{j!=i} e_ij^2, deg_i / 8]
 //   h0  = relu(W0 x + b0)                                  (width H = 32)
 //   3 layers: m_i = sum_{j!=i} e_ij h_j;  z = W_l [h; m] + b_l;  h += relu(z)
@@ -82,31 +83,33 @@ int build_graph(const tbsla_matrix* m, HostGraph* g) {
       g->aval[k] = (float)m->values[base + k];
       if (g->colidx[k] == i) d[i] += m->values[base + k];
     }
+  // s, e and the node inputs in FP32, in the operations the device-side
+  // feature kernel uses (k_dia_features), so that both give the same bits
   g->s.resize(n);
   for (int i = 0; i < n; i++) {
     if (!(d[i] > 0)) return TBSLA_ERR_BAD_MATRIX;
-    g->s[i] = (float)(1.0 / std::sqrt(d[i]));
+    g->s[i] = 1.0f / std::sqrt((float)d[i]);
   }
   g->e.resize(nnz);
   g->x.assign((size_t)n * F0, 0.f);
   g->lrowptr.assign(n + 1, 0);
   for (int i = 0; i < n; i++) {
-    double se = 0, se2 = 0;
+    float se = 0.f, se2 = 0.f;
     int deg = 0, nl = 0;
     for (long k = g->rowptr[i]; k < g->rowptr[i + 1]; k++) {
       const int j = g->colidx[k];
-      const double e = m->values[base + k] / std::sqrt(d[i]) / std::sqrt(d[j]);
-      g->e[k] = (float)e;
+      const float e = (float)m->values[base + k] * g->s[i] * g->s[j];
+      g->e[k] = e;
       if (j != i) {
-        se += e;
-        se2 += e * e;
+        se = se + e;
+        se2 = std::fma(e, e, se2);
         deg++;
       }
       if (j < i) nl++;
     }
     g->x[(size_t)i * F0 + 0] = 1.f;
-    g->x[(size_t)i * F0 + 1] = (float)se;
-    g->x[(size_t)i * F0 + 2] = (float)se2;
+    g->x[(size_t)i * F0 + 1] = se;
+    g->x[(size_t)i * F0 + 2] = se2;
     g->x[(size_t)i * F0 + 3] = deg / 8.f;
     g->lrowptr[i + 1] = g->lrowptr[i] + nl + 1;
   }
@@ -149,7 +152,8 @@ __device__ __forceinline__ float sigmoid(float v) { return 1.f / (1.f + expf(-v)
 __device__ __forceinline__ long warp_id() { return ((long)blockIdx.x * NT + threadIdx.x) / kWarp; }
 __device__ __forceinline__ long warp_count() { return (long)gridDim.x * NT / kWarp; }
 
-// h0 = relu(W0 x + b0); lane o is feature o.
+// h0 = relu(W0 x + b0); lane o is feature o.  z0 (the pre-activation, kept
+// for the backward pass) may be null for inference.
 __global__ void __launch_bounds__(NT) k_layer0(int n, const float* __restrict__ x, const float* __restrict__ w,
                                               float* __restrict__ z0, float* __restrict__ h0) {
   const int o = threadIdx.x & 31;
@@ -161,7 +165,7 @@ __global__ void __launch_bounds__(NT) k_layer0(int n, const float* __restrict__ 
     float z = b;
 #pragma unroll
     for (int k = 0; k < F0; k++) z += wr[k] * x[i * F0 + k];
-    z0[i * H + o] = z;
+    if (z0) z0[i * H + o] = z;
     h0[i * H + o] = relu(z);
   }
 }
@@ -465,6 +469,191 @@ __global__ void k_adam(int np, float* __restrict__ theta, const float* __restric
   }
 }
 
+
+// ---- device kernels: inference on a batch's DIA copy ----------------------------------
+// The batch keeps A slot-major per diagonal: a64[k * n + i] is the entry of row i
+// on diagonal k of its system (delta adelta[sys * 8 + k], ascending, so slot
+// order is the CSR order of a sorted row); 0 where the row has none.  Entries
+// stored as exact zeros are therefore absent here.  Activations are kept
+// feature-major, hT[f * n + i], so that a thread per node reads and writes
+// them coalesced across its warp (32 consecutive nodes, 128 bytes per
+// feature).  Every kernel does the FP32 operations of the training path's
+// kernels (k_layer0, k_aggregate + k_layer, k_head) in the same order, so the
+// factor is bit-identical to tbsla_mpnn_factor's.
+
+constexpr int DMAX = 8;  // diagonal slots per system
+
+// The weights of one kernel, passed by value: every multiply-add takes its
+// weight from the constant bank (a compile-time offset), no load at all.
+struct InputW {
+  float w0[H * F0];
+  float b0[H];
+};
+struct LayerW {
+  float w[2 * H * H];  // W (H x 2H) row-major
+  float b[H];
+};
+struct HeadW {
+  float we[H], wd[H];
+  float ce, be, bd;
+};
+
+// s_i = a_ii^-1/2, e_ij = a_ij s_i s_j and the node inputs x_i (FP32, as
+// build_graph), then h0 = relu(W0 x + b0) written feature-major; *bad set
+// when a diagonal entry is <= 0.
+__global__ void __launch_bounds__(NT) k_dia_features(long n, int K, const double* __restrict__ a64,
+                                                     const int* __restrict__ adelta, const int* __restrict__ row_sys,
+                                                     const __grid_constant__ InputW P, float* __restrict__ e,
+                                                     float* __restrict__ s, float* __restrict__ h0,
+                                                     int* __restrict__ bad) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const int sys = row_sys[i];
+    int kd = -1;
+    for (int k = 0; k < K && kd < 0; k++)
+      if (adelta[sys * DMAX + k] == 0) kd = k;
+    const double di = kd >= 0 ? a64[(size_t)kd * n + i] : 0.0;
+    if (!(di > 0)) {
+      atomicExch(bad, 1);
+      for (int k = 0; k < K; k++) e[(size_t)k * n + i] = 0.f;
+      s[i] = 0.f;
+      for (int o = 0; o < H; o++) h0[(size_t)o * n + i] = 0.f;
+      continue;
+    }
+    const float si = 1.0f / sqrtf((float)di);
+    s[i] = si;
+    float se = 0.f, se2 = 0.f;
+    int deg = 0;
+    for (int k = 0; k < K; k++) {
+      const double a = a64[(size_t)k * n + i];
+      const int dl = adelta[sys * DMAX + k];
+      if (a == 0.0) {
+        e[(size_t)k * n + i] = 0.f;
+        continue;
+      }
+      const double dj = a64[(size_t)kd * n + i + dl];
+      const float sj = dl == 0 ? si : 1.0f / sqrtf((float)dj);
+      const float ev = __fmul_rn(__fmul_rn((float)a, si), sj);
+      e[(size_t)k * n + i] = ev;
+      if (dl != 0) {
+        se = __fadd_rn(se, ev);
+        se2 = fmaf(ev, ev, se2);
+        deg++;
+      }
+    }
+    const float x1 = se, x2 = se2, x3 = deg / 8.f;
+#pragma unroll
+    for (int o = 0; o < H; o++) {
+      float z = P.b0[o];
+      z = fmaf(P.w0[o * F0 + 0], 1.f, z);
+      z = fmaf(P.w0[o * F0 + 1], x1, z);
+      z = fmaf(P.w0[o * F0 + 2], x2, z);
+      z = fmaf(P.w0[o * F0 + 3], x3, z);
+      h0[(size_t)o * n + i] = relu(z);
+    }
+  }
+}
+
+// One message layer for inference, a thread per node: m_i = sum_{j != i}
+// e_ij h_j over the DIA slots, z = b + W [h; m] (per k the h term, then the
+// m term, as k_layer), h_out = h + relu(z).  Four outputs at a time give the
+// FMA pipe independent chains.
+__global__ void __launch_bounds__(NT, 2) k_layer_fm(long n, int K, const int* __restrict__ adelta,
+                                                    const int* __restrict__ row_sys, const float* __restrict__ e,
+                                                    const __grid_constant__ LayerW P, const float* __restrict__ hT,
+                                                    float* __restrict__ outT) {
+  for (long i = blockIdx.x * (long)NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
+    const int sys = row_sys[i];
+    float h[H], m[H];
+#pragma unroll
+    for (int f = 0; f < H; f++) {
+      h[f] = hT[(size_t)f * n + i];
+      m[f] = 0.f;
+    }
+    for (int k = 0; k < K; k++) {
+      const int dl = adelta[sys * DMAX + k];
+      const float ev = e[(size_t)k * n + i];
+      if (dl == 0 || ev == 0.f) continue;
+      const float* hj = hT + i + dl;
+#pragma unroll
+      for (int f = 0; f < H; f++) m[f] = fmaf(ev, hj[(size_t)f * n], m[f]);
+    }
+#pragma unroll
+    for (int o = 0; o < H; o += 4) {
+      float a0 = P.b[o], a1 = P.b[o + 1], a2 = P.b[o + 2], a3 = P.b[o + 3];
+#pragma unroll
+      for (int k = 0; k < H; k++) {
+        a0 = fmaf(P.w[(o + 0) * 2 * H + k], h[k], a0);
+        a1 = fmaf(P.w[(o + 1) * 2 * H + k], h[k], a1);
+        a2 = fmaf(P.w[(o + 2) * 2 * H + k], h[k], a2);
+        a3 = fmaf(P.w[(o + 3) * 2 * H + k], h[k], a3);
+        a0 = fmaf(P.w[(o + 0) * 2 * H + H + k], m[k], a0);
+        a1 = fmaf(P.w[(o + 1) * 2 * H + H + k], m[k], a1);
+        a2 = fmaf(P.w[(o + 2) * 2 * H + H + k], m[k], a2);
+        a3 = fmaf(P.w[(o + 3) * 2 * H + H + k], m[k], a3);
+      }
+      outT[(size_t)(o + 0) * n + i] = h[o + 0] + relu(a0);
+      outT[(size_t)(o + 1) * n + i] = h[o + 1] + relu(a1);
+      outT[(size_t)(o + 2) * n + i] = h[o + 2] + relu(a2);
+      outT[(size_t)(o + 3) * n + i] = h[o + 3] + relu(a3);
+    }
+  }
+}
+
+__device__ __forceinline__ void store_l(float* p, float v) { *p = v; }
+__device__ __forceinline__ void store_l(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
+
+// The warp butterfly of wsum() restated over 32 values held by one thread:
+// the same pairs in the same order, so the same sum.
+__device__ __forceinline__ float tree_sum(float (&p)[H]) {
+#pragma unroll
+  for (int f = 0; f < 16; f++) p[f] = p[f] + p[f + 16];
+#pragma unroll
+  for (int f = 0; f < 8; f++) p[f] = p[f] + p[f + 8];
+#pragma unroll
+  for (int f = 0; f < 4; f++) p[f] = p[f] + p[f + 4];
+#pragma unroll
+  for (int f = 0; f < 2; f++) p[f] = p[f] + p[f + 2];
+  return p[0] + p[1];
+}
+
+// L into the batch's DIA factor, a thread per node: slot 0 the diagonal s_i
+// softplus(w_d . h_i + b_d); slot q > 0 (delta ldelta[q] < 0, 0 = padding)
+// s_i (w_e . (h_i * h_j) + c_e e_ij + b_e) where A has the entry, else 0.
+template <class LV>
+__global__ void __launch_bounds__(NT, 2) k_head_fm(long n, int K, const int* __restrict__ adelta, int KL,
+                                                   const int* __restrict__ ldelta, const int* __restrict__ row_sys,
+                                                   const float* __restrict__ e, const float* __restrict__ s,
+                                                   const __grid_constant__ HeadW P, const float* __restrict__ hT,
+                                                   LV* __restrict__ lv) {
+  for (long i = blockIdx.x * (long)NT + threadIdx.x; i < n; i += (long)gridDim.x * NT) {
+    const int sys = row_sys[i];
+    const float si = s[i];
+    float h[H], p[H];
+#pragma unroll
+    for (int f = 0; f < H; f++) h[f] = hT[(size_t)f * n + i];
+    for (int q = 1; q < KL; q++) {
+      const int dl = ldelta[sys * DMAX + q];
+      float ev = 0.f;
+      if (dl != 0)
+        for (int k = 0; k < K; k++)
+          if (adelta[sys * DMAX + k] == dl) ev = e[(size_t)k * n + i];
+      float out = 0.f;
+      if (ev != 0.f) {
+        const float* hj = hT + i + dl;
+#pragma unroll
+        for (int f = 0; f < H; f++) p[f] = P.we[f] * h[f] * hj[(size_t)f * n];
+        const float o = tree_sum(p) + P.ce * ev + P.be;
+        out = si * o;
+      }
+      store_l(lv + (size_t)q * n + i, out);
+    }
+#pragma unroll
+    for (int f = 0; f < H; f++) p[f] = P.wd[f] * h[f];
+    const float xd = tree_sum(p) + P.bd;
+    store_l(lv + i, si * softplus(xd));
+  }
+}
+
 // ---- host orchestration --------------------------------------------------------------
 
 #define MCK(call)                                               \
@@ -625,6 +814,64 @@ struct tbsla_mpnn {
     return TBSLA_OK;
   }
 };
+
+
+namespace tbsla_impl {
+
+int mpnn_factor_dia(tbsla_mpnn* net, long n, int K, const double* a64, const int* adelta, const int* row_sys,
+                    int KL, const int* ldelta, void* lvals, int lprec, void* stream) {
+  if (!net || n <= 0 || K <= 0 || K > DMAX || KL <= 0 || KL > DMAX || !a64 || !adelta || !row_sys || !ldelta ||
+      !lvals || (lprec != TBSLA_F32 && lprec != TBSLA_BF16))
+    return TBSLA_ERR_INVALID_ARG;
+  cudaSetDevice(net->device);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  Work& w = net->work;
+  int st;
+  // scratch kept with the network and grown on demand: e [K][n], s, two
+  // feature-major activation buffers and the error flag
+  if ((st = w.e.need((size_t)K * n)) || (st = w.s.need(n)) || (st = w.h[0].need((size_t)n * H)) ||
+      (st = w.h[1].need((size_t)n * H)) || (st = w.xi.need(1)))
+    return st;
+  int* bad = reinterpret_cast<int*>(w.xi.p);
+  MCK(cudaMemsetAsync(bad, 0, sizeof(int), s));
+  // the bfloat16-rounded forward weights, by value into each kernel
+  std::vector<float> wh(NPARAMS);
+  MCK(cudaMemcpyAsync(wh.data(), net->wq, NPARAMS * 4, cudaMemcpyDeviceToHost, s));
+  MCK(cudaStreamSynchronize(s));
+  InputW pin;
+  std::memcpy(pin.w0, wh.data() + OFF_W0, sizeof pin.w0);
+  std::memcpy(pin.b0, wh.data() + OFF_B0, sizeof pin.b0);
+  HeadW phd;
+  std::memcpy(phd.we, wh.data() + OFF_WE, sizeof phd.we);
+  std::memcpy(phd.wd, wh.data() + OFF_WD, sizeof phd.wd);
+  phd.ce = wh[OFF_CE];
+  phd.be = wh[OFF_BE];
+  phd.bd = wh[OFF_BD];
+  const int grow = row_grid(n);
+  float* cur = w.h[0].p;  // feature-major activations [H][n]
+  float* nxt = w.h[1].p;
+  k_dia_features<<<grow, NT, 0, s>>>(n, K, a64, adelta, row_sys, pin, w.e.p, w.s.p, cur, bad);
+  for (int l = 1; l <= NL; l++) {
+    LayerW pl;
+    std::memcpy(pl.w, wh.data() + off_layer(l), sizeof pl.w);
+    std::memcpy(pl.b, wh.data() + off_layer(l) + 2 * H * H, sizeof pl.b);
+    k_layer_fm<<<grow, NT, 0, s>>>(n, K, adelta, row_sys, w.e.p, pl, cur, nxt);
+    std::swap(cur, nxt);
+  }
+  if (lprec == TBSLA_BF16)
+    k_head_fm<__nv_bfloat16><<<grow, NT, 0, s>>>(n, K, adelta, KL, ldelta, row_sys, w.e.p, w.s.p, phd, cur,
+                                                 static_cast<__nv_bfloat16*>(lvals));
+  else
+    k_head_fm<float><<<grow, NT, 0, s>>>(n, K, adelta, KL, ldelta, row_sys, w.e.p, w.s.p, phd, cur,
+                                         static_cast<float*>(lvals));
+  MCK(cudaGetLastError());
+  int hbad = 0;
+  MCK(cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s));
+  MCK(cudaStreamSynchronize(s));
+  return hbad ? TBSLA_ERR_BAD_MATRIX : TBSLA_OK;
+}
+
+}  // namespace tbsla_impl
 
 // ---- C ABI ---------------------------------------------------------------------------
 

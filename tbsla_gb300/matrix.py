@@ -439,6 +439,25 @@ class Batch:
         arr = (C.c_void_p * len(factors))(*[f._h.value for f in factors])
         check(lib.tbsla_batch_set_factors(self._h, arr, len(factors), precision), "batch_set_factors")
 
+    def factor_mpnn(self, net, precision=L.BF16):
+        """The network's factor of every system, computed on the GPU from the
+        batch's device copy of A straight into the batch's factor storage
+        (no host round trip); then cg(precond=2)."""
+        check(lib.tbsla_batch_factor_mpnn(self._h, net._h, precision), "batch_factor_mpnn")
+
+    def factor_dia(self):
+        """The factor in its diagonal-slot form: (deltas [nsys, 8], values
+        [slots, n]) with slot 0 the diagonal."""
+        k = C.c_int()
+        check(lib.tbsla_batch_factor_dia(self._h, C.byref(k), None, None), "batch_factor_dia")
+        ns = len(self.offsets) - 1
+        n = int(self.offsets[-1])
+        deltas = np.zeros(ns * 8, np.int32)
+        vals = np.zeros(k.value * n)
+        check(lib.tbsla_batch_factor_dia(self._h, None, deltas.ctypes.data_as(C.POINTER(C.c_int)),
+                                         vals.ctypes.data_as(C.POINTER(C.c_double))), "batch_factor_dia")
+        return deltas.reshape(ns, 8), vals.reshape(k.value, n)
+
     def fallbacks(self):
         """Per system after the last cg(): (fallback code, preconditioner
         used at exit).  Codes: 0 none, 1 the factor failed its check and
@@ -450,6 +469,11 @@ class Batch:
         check(lib.tbsla_batch_fallbacks(self._h, fb.ctypes.data_as(C.POINTER(C.c_int)),
                                         used.ctypes.data_as(C.POINTER(C.c_int))), "batch_fallbacks")
         return fb, used
+
+    def set_rows_per_thread(self, rows: int):
+        """Persistent engine: 4 rows per thread (16-byte loads, the default
+        where the layout allows) or 1."""
+        check(lib.tbsla_batch_set_rows_per_thread(self._h, int(rows)), "batch_set_rows_per_thread")
 
     def set_wait_limit(self, ns: int):
         """Bound on one grid-wide wait of the persistent solver (ns)."""

@@ -167,3 +167,27 @@ def test_bounded_wait_returns_timeout_status(gpu):
     x, its, rr, ok = batch.cg(rhs, max_iterations=2000, rel_tol=TOL, precond=1)
     assert ok and (rr <= TOL).all()
     assert batch.engine()["persistent"]
+
+
+def test_vector_rows_match_scalar_rows(gpu):
+    """With every system size a multiple of 4 the FP32 iteration takes 4 rows
+    per thread (16-byte loads); each row's arithmetic is that of the
+    one-row-per-thread loops, so both forms give the same iterate up to the
+    order of the FP64 atomic dot products: iteration counts within one,
+    solutions within the tolerance, every system FP64-verified."""
+    T = gpu
+    sizes = [8, 12, 16, 10]
+    systems = [diffusion(T, s, 700 + i) for i, s in enumerate(sizes)]
+    rhs = np.concatenate([T.fill_uniform(s ** 3, -1.0, 1.0, 710 + i) for i, s in enumerate(sizes)])
+    batch = T.Batch(systems, T.F32)
+    off = batch.offsets
+    for precond in (0, 1):
+        out = []
+        for rows in (4, 1):
+            batch.set_rows_per_thread(rows)
+            x, its, rr, ok = batch.cg(rhs, max_iterations=4000, rel_tol=TOL, precond=precond, refresh=50)
+            assert ok and (rr <= TOL).all()
+            for k, m in enumerate(systems):
+                assert true_rel_residual(m, x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]) <= TOL
+            out.append(its)
+        assert np.abs(out[0] - out[1]).max() <= 1, out

@@ -117,7 +117,8 @@ def test_factor_layouts_agree(gpu):
     engine (ELL or CSR copies).  The same factor padded with explicit zeros
     at the columns i - z, 0 < z <= pad, stays a DIA factor for pad 2 (five
     diagonals: the extra zero slot leaves every FP32 sum unchanged, so the
-    iteration counts are identical) and becomes a CSR factor of the
+    iteration counts agree up to the one that the order of the FP64 atomic
+    dot products can move) and becomes a CSR factor of the
     multi-launch engine for pad 7 (eleven diagonals).  Every solve reaches
     the FP64-verified 1e-8 residual; the two engines' counts stay close."""
     T = gpu
@@ -144,7 +145,8 @@ def test_factor_layouts_agree(gpu):
     for f in layouts.values():
         bt_its = _solve(T, systems, f, 2, T.F32)
         its.append(np.asarray(bt_its))
-    assert np.array_equal(its[0], its[1]), its
+    # identical FP32 sums; the FP64 atomic dot products may move one count
+    assert np.abs(its[0] - its[1]).max() <= 1, its
     assert np.abs(its[2] - its[0]).max() <= max(3, int(0.1 * its[0].max())), its
 
 
@@ -206,3 +208,40 @@ def test_jacobi_fallback_on_bad_factors(gpu):
             res = rhs[o:o + k] - oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x[o:o + k])
             assert np.linalg.norm(res) <= 1.0001e-8 * np.linalg.norm(rhs[o:o + k])
             o += k
+
+
+def test_device_factor_pipeline_matches_host_factor(gpu):
+    """tbsla_batch_factor_mpnn runs the network on the batch's device copy of
+    A and writes L into the batch's factor storage with no host round trip.
+    It must produce the factor of tbsla_mpnn_factor (the network on the
+    host-built graph) loaded through tbsla_batch_set_factors: the same FP32
+    operations in the same order, so equal to a few units in the last place
+    of FP32 (1e-6 of max |L|; the oracle bar for the factor is 1e-5).  Both
+    solves then reach the FP64-verified 1e-8 in the same iterations, up to
+    the one that the order of the FP64 atomic dot products can move."""
+    T = gpu
+    net = T.MPNN(11)
+    train = [diffusion(T, 9 + (i % 5), 2000 + i) for i in range(10)]
+    for step in range(60):
+        net.train_step(train[step % len(train)], probes=8, seed=step, lr=3e-3)
+    systems = [diffusion(T, 8 + 3 * i, 3000 + i) for i in range(4)]
+    rhs = np.concatenate([T.fill_uniform(len(s.arrays()["rowptr"]) - 1, -1.0, 1.0, 70 + i)
+                          for i, s in enumerate(systems)])
+    for prec in (T.F32, T.BF16):
+        host = T.Batch(systems, T.F32)
+        host.set_factors([net.factor(A) for A in systems], prec)
+        dev = T.Batch(systems, T.F32)
+        dev.factor_mpnn(net, prec)
+        dh, vh = host.factor_dia()
+        dd, vd = dev.factor_dia()
+        assert np.array_equal(dh, dd)
+        assert np.abs(vh - vd).max() <= 1e-6 * np.abs(vh).max(), np.abs(vh - vd).max()
+        its = []
+        for bt in (host, dev):
+            x, it, rr, ok = bt.cg(rhs, max_iterations=5000, rel_tol=1e-8, precond=2, refresh=50)
+            assert ok and (rr <= 1e-8).all()
+            assert bt.engine()["persistent"]
+            fb, used = bt.fallbacks()
+            assert (fb == 0).all() and (used == 2).all()
+            its.append(it)
+        assert np.abs(its[0] - its[1]).max() <= 1, its
