@@ -69,6 +69,8 @@ def parse_args():
     p.add_argument("--items", type=int, default=0,
                    help="merge: items per thread (0 = 8); sell: steps per lane in flight (0 = automatic)")
     p.add_argument("--no-forms", action="store_true", help="skip the FP32 / BF16 side measurements")
+    p.add_argument("--no-learned", action="store_true",
+                   help="spmv: skip the learned-vs-Jacobi and batched-CG measurements of the default run")
     p.add_argument("--autotune", action="store_true",
                    help="time the CSR kernel configurations on the matrix first and keep the fastest")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
@@ -377,6 +379,25 @@ def run_ours(a):
                                        "GB/s": algorithmic_bytes(n, nnz, sv) / (ms * 1e-3) / 1e9,
                                        "frac_of_peak": algorithmic_bytes(n, nnz, sv) / (ms * 1e-3) / 1e9 / peak}
         m.set_precision(prec)
+
+    if ws == 1 and not a.no_learned:
+        # the metric's second half, in the same default run: learned-PCG
+        # (network inference on the GPU + solve) against Jacobi-PCG on the
+        # 32 held-out 128^3 diffusion systems, and the 64-system batched
+        # Jacobi-PCG workload
+        r = learned_vs_jacobi(a, T, local)
+        extra["learned_vs_jacobi"] = {
+            "ratio": r["ratio"], "target": 0.5, "timed": r["timed"],
+            "learned_ms": r["solvers"]["learned_pcg"]["ms"], "factor_ms": r["solvers"]["learned_pcg"]["factor_ms"],
+            "jacobi_ms": r["solvers"]["jacobi_pcg"]["ms"],
+            "iterations_mean": {"learned": r["solvers"]["learned_pcg"]["iterations_mean"],
+                                "jacobi": r["solvers"]["jacobi_pcg"]["iterations_mean"]},
+            "max_rel_residual_fp64": max(r["solvers"]["learned_pcg"]["max_rel_residual_fp64"],
+                                         r["solvers"]["jacobi_pcg"]["max_rel_residual_fp64"]),
+            "all_converged": r["solvers"]["learned_pcg"]["all_converged"] and r["solvers"]["jacobi_pcg"]["all_converged"],
+            "fallbacks": r["solvers"]["learned_pcg"]["fallbacks"], "engine": r["engine"],
+            "systems": r["systems"], "n": r["n"], "reps": r["reps"], "train": r["train"], "clocks": r["clocks"]}
+        extra["batched_cg_jacobi"] = batched_cg_jacobi(T, reps=3)
 
     cpu = None
     if rank == 0 and ws == 1:
@@ -849,6 +870,45 @@ def run_pagerank(a):
     print(json.dumps(line), flush=True)
 
 
+def cg_systems(T):
+    """The batched-CG workload: 64 SPD 7-point diffusion systems, n^3 grids
+    with n cycling through 16, 24, ..., 96, coefficients exp(g) of a Gaussian
+    field (sigma 1, correlation 8 cells), Dirichlet boundaries, RHS U[-1,1),
+    seed 3."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import numpy as np
+
+    sizes = [16 + 8 * (i % 11) for i in range(64)]
+
+    def make(i):
+        m = T.MatrixCSR()
+        m.fill_diffusion7(sizes[i], 1.0, 8.0, 3000 + i)
+        return m
+
+    with ThreadPoolExecutor(8) as pool:
+        systems = list(pool.map(make, range(len(sizes))))
+    rhs = np.concatenate([T.fill_uniform(sz ** 3, -1.0, 1.0, 4000 + i) for i, sz in enumerate(sizes)])
+    return sizes, systems, rhs
+
+
+def batched_cg_jacobi(T, reps: int = 3) -> dict:
+    """One batched Jacobi-PCG solve of the 64-system workload (FP32 values,
+    FP64 refinement every 50 iterations, 1e-8), median of `reps` host calls."""
+    sizes, systems, rhs = cg_systems(T)
+    bt = T.Batch(systems, T.F32)
+    bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=1, refresh=50)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        x, its, rr, ok = bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=1, refresh=50)
+        times.append(time.perf_counter() - t0)
+    ms = statistics.median(times) * 1e3
+    return {"ms": ms, "solves_per_s": len(sizes) / (ms * 1e-3), "iterations_max": int(its.max()),
+            "all_converged": bool(ok), "max_rel_residual_fp64": float(rr.max()), "engine": bt.engine(),
+            "workload": "batched_cg_diffusion7_64_systems_n16to96_grf_sigma1_corr8_f32_refresh50"}
+
+
 def run_cg(a):
     """The batched-CG workload: 64 SPD 7-point diffusion systems, n^3 grids
     with n cycling through 16, 24, ..., 96, coefficients exp(g) of a Gaussian
@@ -865,13 +925,7 @@ def run_cg(a):
     ws, rank, local = dist()
     torch.cuda.set_device(local)
     T.device_init(local)
-    sizes = [16 + 8 * (i % 11) for i in range(64)]
-    systems = []
-    for i, sz in enumerate(sizes):
-        m = T.MatrixCSR()
-        m.fill_diffusion7(sz, 1.0, 8.0, 3000 + i)
-        systems.append(m)
-    rhs = np.concatenate([T.fill_uniform(sz ** 3, -1.0, 1.0, 4000 + i) for i, sz in enumerate(sizes)])
+    sizes, systems, rhs = cg_systems(T)
     N = np.array([sz ** 3 for sz in sizes])
     nnz = np.array([m.get_nnz() for m in systems])
     res = {}
@@ -888,13 +942,15 @@ def run_cg(a):
             x, its, rr, ok = bt.cg(rhs, max_iterations=20000, rel_tol=1e-8, precond=pre, refresh=50,
                                    graph_iters=10)
             times.append(time.perf_counter() - t0)
-        # algorithmic bytes per iteration of a system: SpMV (FP32 values,
-        # int32 indices, p gathered once, q), update (p, q, x, r read; x, r
-        # written), direction (r or z, p read; p written); Jacobi adds
-        # diag^-1 read and z written
-        per_it = nnz * 8 + 4 * (N + 1) + 16 * N + 72 * N + (16 * N if pre else 0)
+        # algorithmic bytes per iteration and row, persistent engine (FP32
+        # iteration, A in 7 diagonal slots of FP32): q = A p reads the 7
+        # slots (28 B), z and p_old once (8 B), writes p and q (8 B); the
+        # update reads p, q, r and the correction d, writes r, d and z
+        # (28 B), Jacobi adds D^-1 (4 B)
+        per_it = N * (28 + 16 + 28 + (4 if pre else 0))
+        eng = bt.engine()
         sec = statistics.mean(times)
-        res[name] = {"ms": sec * 1e3, "solves_per_s": len(sizes) / sec, "iterations_max": int(its.max()),
+        res[name] = {"ms": sec * 1e3, "solves_per_s": len(sizes) / sec, "iterations_max": int(its.max()), "engine": eng,
                      "iterations_mean": float(its.mean()), "all_converged": bool(ok),
                      "max_rel_residual_fp64": float(rr.max()),
                      "GB/s": float((per_it * its).sum()) / sec / 1e9}
@@ -914,11 +970,11 @@ def run_cg(a):
     line = {
         "metric": METRIC, "value": j["ms"], "unit": "ms", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": j["ms"], "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 values, f64 vectors, f64 residual refresh", "data": "synthetic: seeded diffusion systems (seed 3)",
+        "dtype": "f32 values and iteration, f64 refinement", "data": "synthetic: seeded diffusion systems (seed 3)",
         "config": {"workload": "batched_cg_diffusion7_64_systems_n16to96_grf_sigma1_corr8_f32_refresh50",
                    "systems": len(sizes), "unknowns": int(N.sum()), "nnz": int(nnz.sum()), "rel_tol": 1e-8,
                    "step": "one batched Jacobi-PCG solve of all 64 systems (host call, wall clock)",
-                   "parallelism": "1 GPU, one block-diagonal matrix, CUDA graph of 10 iterations"},
+                   "parallelism": "1 GPU, one block-diagonal matrix, one persistent cooperative launch per solve"},
         "solvers": res,
         "roofline": {"bound": "hbm", "achieved": j["GB/s"], "peak": peak, "unit": "GB/s",
                      "frac": j["GB/s"] / peak, "peak_source": peak_kind, "traffic": None},

@@ -472,8 +472,9 @@ int build(const tbsla_matrix* m, DeviceMatrix* d) {
       const size_t n = (size_t)I.ln_row * I.ln_col;
       int st = upload_values(d, m->values.data(), n);
       if (!st) st = status_of(cudaStreamSynchronize(d->stream));
-      if (st || d->prec == TBSLA_F64) return st;
-      // narrow values: the double-float GEMV when every value is in its range
+      if (st) return st;
+      // the double-float GEMV when every value is in its range (FP64 values
+      // split on load into two floats; FP32 / BF16 values exact in one)
       if ((st = dalloc(&d->df_flag, 1))) return st;
       bool ok = false;
       TRY(dense_values_df_range(d->vals, d->prec, n, d->df_flag, &ok, d->stream));

@@ -7,8 +7,10 @@
 // doubles) where the row start is 16-byte aligned, x through L1 (every row
 // reuses it), one FP64 multiply-add per entry (GB300's FP64 pipe, not HBM,
 // bounds an FP64 GEMV), partial sums combined in a fixed order and added to
-// r_i.  FP32 / BF16 values: double-float arithmetic on the FP32 pipes
-// (dense_gemv_df, below).
+// r_i.  Values of every precision whose magnitudes lie in [2^-40, 2^40]
+// (checked once at upload): double-float arithmetic on the FP32 pipes
+// (dense_gemv_df, below); an FP64 value is split on load, on the integer
+// pipe, into two floats that hold it to 2^-48.
 #include <algorithm>
 
 #include "common.cuh"
@@ -162,6 +164,44 @@ __global__ void k_df_range_vals(const V* __restrict__ a, size_t n, int* __restri
   if (__any_sync(0xffffffffu, any) && threadIdx.x % kWarp == 0) atomicOr(bad, 1);
 }
 
+// An FP64 value a = h + l split into two floats on the integer pipe: h is a
+// truncated to its 24 leading significand bits (exact), l the float nearest
+// to the rest a - h (29 bits, exact in FP64, rounded to 24: a is held to
+// about 2^-48 relative).  For a == 0 or |a| in [2^-74, 2^128); the values
+// reaching it passed the [2^-40, 2^40] check.  No FP64 instruction.
+__device__ __forceinline__ void split_f64(double a, float& h, float& l) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(a);
+  const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+  const unsigned sign = hi & 0x80000000u;
+  const int e = (int)((hi >> 20) & 0x7ffu);
+  if (e == 0) {
+    h = l = 0.f;
+    return;
+  }
+  h = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+  const float scale = __uint_as_float((unsigned)(e - 948) << 23);  // 2^(e - 1075)
+  const float r = __fmul_rn(__uint2float_rn(lo & 0x1fffffffu), scale);
+  l = sign ? -r : r;
+}
+
+// Values of one lane: out[k] (+ outl[k], the low parts of FP64 values).
+template <class V, int VEC>
+__device__ __forceinline__ void ld_vals_dd(float (&out)[VEC], float (&outl)[VEC], const V* p, uint64_t pol) {
+  static_assert(sizeof(V) == 8, "FP64 values");
+  if constexpr (VEC == 1) {
+    split_f64(ld_stream(reinterpret_cast<const double*>(p), pol), out[0], outl[0]);
+  } else {
+    static_assert(VEC == 4, "four values per lane");
+    double v[4];
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+                 : "=d"(v[0]), "=d"(v[1]) : "l"(p), "l"(pol));
+    asm volatile("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.f64 {%0, %1}, [%2], %3;"
+                 : "=d"(v[2]), "=d"(v[3]) : "l"(reinterpret_cast<const double*>(p) + 2), "l"(pol));
+#pragma unroll
+    for (int k = 0; k < 4; k++) split_f64(v[k], out[k], outl[k]);
+  }
+}
+
 template <class V, int VEC>
 __device__ __forceinline__ void ld_vals(float (&out)[VEC], const V* p, uint64_t pol) {
   if constexpr (VEC == 1) {
@@ -232,9 +272,21 @@ __global__ void __launch_bounds__(NT) k_dense_rows_df(const V* __restrict__ A, i
         for (int r = 0; r < R; r++) {
           if (r < nr) {
             float av[VEC];
-            ld_vals<V, VEC>(av, A + (size_t)(row0 + r) * ln_col + (size_t)g * VEC, pol);
+            if constexpr (sizeof(V) == 8) {
+              // a = ah + al: Dot2 on ah (x as xh + xl), then al * xh into the
+              // error term (al * xl is below 2^-48 of the product)
+              float al[VEC];
+              ld_vals_dd<V, VEC>(av, al, A + (size_t)(row0 + r) * ln_col + (size_t)g * VEC, pol);
 #pragma unroll
-            for (int k = 0; k < VEC; k++) dot2_step(sh[r], sc[r], av[k], DF{xh[k], xl[k]});
+              for (int k = 0; k < VEC; k++) {
+                dot2_step(sh[r], sc[r], av[k], DF{xh[k], xl[k]});
+                sc[r] = __fmaf_rn(al[k], xh[k], sc[r]);
+              }
+            } else {
+              ld_vals<V, VEC>(av, A + (size_t)(row0 + r) * ln_col + (size_t)g * VEC, pol);
+#pragma unroll
+              for (int k = 0; k < VEC; k++) dot2_step(sh[r], sc[r], av[k], DF{xh[k], xl[k]});
+            }
           }
         }
       }
@@ -407,11 +459,12 @@ cudaError_t dense_gemv(const void* vals, int prec, int ln_row, int ln_col, const
 
 cudaError_t dense_values_df_range(const void* vals, int prec, size_t n, int* flag, bool* ok, cudaStream_t s) {
   *ok = false;
-  if (prec == kF64 || n == 0) return cudaSuccess;
+  if (n == 0) return cudaSuccess;
   cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), s);
   if (e) return e;
   const int grid = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 16));
-  if (prec == kF32) k_df_range_vals<float><<<grid, 256, 0, s>>>(static_cast<const float*>(vals), n, flag);
+  if (prec == kF64) k_df_range_vals<double><<<grid, 256, 0, s>>>(static_cast<const double*>(vals), n, flag);
+  else if (prec == kF32) k_df_range_vals<float><<<grid, 256, 0, s>>>(static_cast<const float*>(vals), n, flag);
   else k_df_range_vals<__nv_bfloat16><<<grid, 256, 0, s>>>(static_cast<const __nv_bfloat16*>(vals), n, flag);
   int h = 1;
   if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, s)) ||
@@ -424,7 +477,6 @@ cudaError_t dense_values_df_range(const void* vals, int prec, size_t n, int* fla
 cudaError_t dense_gemv_df(const void* vals, int prec, int ln_row, int ln_col, const double* x, float* xs,
                           int* bad, double* y, cudaStream_t s) {
   if (ln_row == 0 || ln_col == 0) return cudaSuccess;
-  if (prec == kF64) return cudaErrorInvalidValue;
   cudaError_t e = cudaMemsetAsync(bad, 0, sizeof(int), s);
   if (e) return e;
   k_df_split_x<<<std::min((ln_col + 255) / 256, 152 * 4), 256, 0, s>>>(x, ln_col, xs, bad);
@@ -432,7 +484,11 @@ cudaError_t dense_gemv_df(const void* vals, int prec, int ln_row, int ln_col, co
   const bool vec = (uintptr_t)vals % 16 == 0 && (uintptr_t)xs % 16 == 0 && ln_col % 4 == 0;
   constexpr int R = kDenseDfRows;
   const int grid = (ln_row + R - 1) / R;
-  if (prec == kF32) {
+  if (prec == kF64) {
+    const double* a = static_cast<const double*>(vals);
+    if (vec) k_dense_rows_df<double, 4, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);
+    else k_dense_rows_df<double, 1, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);
+  } else if (prec == kF32) {
     const float* a = static_cast<const float*>(vals);
     if (vec) k_dense_rows_df<float, 4, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);
     else k_dense_rows_df<float, 1, R><<<grid, NT, 0, s>>>(a, ln_row, ln_col, xs, x, bad, y);

@@ -261,19 +261,22 @@ def test_precision_forms(gpu, prec):
         assert err <= bound * 1.01, (fmt, err)
 
 
-@pytest.mark.parametrize("prec", ["f32", "bf16"])
+@pytest.mark.parametrize("prec", ["f64", "f32", "bf16"])
 def test_dense_narrow_values_double_float(gpu, prec):
-    """DENSE with FP32 / BF16 values computes in double-float arithmetic on
-    the FP32 pipes: within the FP64 tolerance of the oracle on the same
-    rounded values, for rows that take 16-byte value loads and rows that do
-    not.  x with an entry outside [2^-40, 2^40] makes the same launch compute
-    in FP64; values outside that range are found at upload and keep the
-    FP64 kernel (one launch instead of two)."""
+    """DENSE computes in double-float arithmetic on the FP32 pipes (FP64
+    values split on load into two floats, FP32 / BF16 values exact in one):
+    within the FP64 tolerance of the oracle on the same rounded values, for
+    rows that take 16-byte value loads and rows that do not.  x with an
+    entry outside [2^-40, 2^40] makes the same launch compute in FP64;
+    values outside that range are found at upload and keep the FP64 kernel
+    (one launch instead of two)."""
     T = gpu
     rng = np.random.default_rng(31)
-    P = T.F32 if prec == "f32" else T.BF16
+    P = {"f64": T.F64, "f32": T.F32, "bf16": T.BF16}[prec]
 
     def rounded(v):
+        if prec == "f64":
+            return v
         return v.astype(np.float32).astype(np.float64) if prec == "f32" else oracle.bf16_round(v)
 
     for nr, nc in ((300, 4096), (257, 2001), (5, 8), (3, 1)):
