@@ -37,7 +37,7 @@ def lib() -> C.CDLL:
         _o.orc_cg.restype = I
         _o.orc_ell_max_col.restype = I
         _o.orc_gen_powerlaw_rows.restype = L
-        _o.orc_gen_powerlaw_rows.argtypes = [I, D, D, I, C.c_ulonglong, P]
+        _o.orc_gen_powerlaw_rows.argtypes = [I, D, D, I, D, I, C.c_ulonglong, P]
         _o.orc_gen_powerlaw_entries.argtypes = [I, D, I, C.c_ulonglong, P, P, P]
         _o.orc_gen_uniform.argtypes = [P, L, D, D, C.c_ulonglong]
     return _o
@@ -91,7 +91,8 @@ def gen_powerlaw(n, mean_len=16.0, zipf_s=2.0, max_len=4096, local_frac=0.3, ban
     restated from this library's generator so that the CPU baseline does not
     load the library it is compared with."""
     rowptr = np.zeros(n + 1, np.int32)
-    nnz = lib().orc_gen_powerlaw_rows(I(n), D(mean_len), D(zipf_s), I(max_len), C.c_ulonglong(seed), _p(rowptr))
+    nnz = lib().orc_gen_powerlaw_rows(I(n), D(mean_len), D(zipf_s), I(max_len), D(local_frac), I(band),
+                                      C.c_ulonglong(seed), _p(rowptr))
     if nnz < 0:
         raise ValueError("bad power-law parameters")
     colidx = np.empty(nnz, np.int32)

@@ -526,7 +526,7 @@ static int cmp_int(const void* a, const void* b) {
   return (x > y) - (x < y);
 }
 
-long orc_gen_powerlaw_rows(int n, double mean_len, double zipf_s, int max_len,
+long orc_gen_powerlaw_rows(int n, double mean_len, double zipf_s, int max_len, double local_frac, int band,
                            unsigned long long seed, int* rowptr) {
   if (n <= 0 || max_len <= 0 || max_len > n) return -1;
   gen_zipf z;
@@ -536,7 +536,12 @@ long orc_gen_powerlaw_rows(int n, double mean_len, double zipf_s, int max_len,
   long acc = 0;
   for (long i = 0; i < n; i++) {
     int k = zipf_draw(&z, gen_u01(gen_hash3(seed, 1, (uint64_t)i)));
-    acc += zipf_rescale(k, scale, gen_u01(gen_hash3(seed, 12, (uint64_t)i)), 1, max_len);
+    long len = zipf_rescale(k, scale, gen_u01(gen_hash3(seed, 12, (uint64_t)i)), 1, max_len);
+    if (local_frac >= 1.0) { /* all columns near the diagonal: at most the band's columns */
+      long lo = i - band < 0 ? 0 : i - band, hi = i + band > (long)n - 1 ? (long)n - 1 : i + band;
+      if (len > hi - lo + 1) len = hi - lo + 1;
+    }
+    acc += len;
     if (acc > 0x7fffffffL) {
       free(z.cdf);
       return -1;

@@ -69,7 +69,7 @@ int orc_cg(int n, const int* rowptr, const int* colidx, const double* values,
            double rel_tol, double* rel_residual);
 
 /* ---- the power-law workload matrix (this library's generator, restated) */
-long orc_gen_powerlaw_rows(int n, double mean_len, double zipf_s, int max_len,
+long orc_gen_powerlaw_rows(int n, double mean_len, double zipf_s, int max_len, double local_frac, int band,
                            unsigned long long seed, int* rowptr);
 void orc_gen_powerlaw_entries(int n, double local_frac, int band, unsigned long long seed,
                               const int* rowptr, int* colidx, double* values);

@@ -638,10 +638,18 @@ int fill_powerlaw(tbsla_matrix* m, int n, double mean_len, double zipf_s, int ma
   const double scale = z.scale_for(mean_len, 1, max_len);
   m->idx0.resize(n + 1);
   std::vector<int> len(n);
+  // with every column drawn near the diagonal (local_frac >= 1) a row holds
+  // at most the columns of its band; capped there, the distinct-column draw
+  // below always ends
+  const bool all_local = local_frac >= 1.0;
   parallel_for(n, [&](long b, long e) {
     for (long i = b; i < e; i++) {
       int k = z.draw(u01(hash3(seed, 1, (uint64_t)i)));
       len[i] = (int)Zipf::rescale(k, scale, u01(hash3(seed, 12, (uint64_t)i)), 1, max_len);
+      if (all_local) {
+        const long cap = std::min<long>((long)n - 1, i + band) - std::max<long>(0, i - band) + 1;
+        len[i] = (int)std::min<long>(len[i], cap);
+      }
     }
   });
   long acc = 0;

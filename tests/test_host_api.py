@@ -250,7 +250,8 @@ def test_project_generators_are_deterministic():
     assert np.linalg.eigvalsh(dense).min() > 0
 
 
-@pytest.mark.parametrize("n,max_len,local,band,seed", [(1 << 18, 4096, 0.3, 1024, 1), (5000, 300, 0.6, 16, 7)])
+@pytest.mark.parametrize("n,max_len,local,band,seed", [(1 << 18, 4096, 0.3, 1024, 1), (5000, 300, 0.6, 16, 7),
+                                                       (20000, 4096, 1.0, 64, 3)])
 def test_oracle_powerlaw_generator_matches_library(n, max_len, local, band, seed):
     """The CPU baseline builds the large-SpMV matrix with the oracle's
     restatement of the library's power-law generator (so that it loads no
