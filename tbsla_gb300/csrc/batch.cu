@@ -285,12 +285,12 @@ int build_dia(tbsla_batch* B, const std::vector<int>& delta, int K) {
     CK(cudaMalloc(v, std::max<size_t>((size_t)n, 1) * es));
   // work chunks of the persistent engine: never across a system, sized so
   // that the batch gives every co-resident CTA about 8 of them (1024 to 4096
-  // rows, i.e. 1 to 4 rows of 4 per thread; 2 CTAs of 256 threads per SM)
+  // rows, i.e. 1 to 4 rows of 4 per thread; 3 CTAs of 256 threads per SM)
   {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long rows = n / ((long)sms * 2 * 8);
+    long rows = n / ((long)sms * 3 * 8);
     rows = std::min<long>(4096, std::max<long>(1024, (rows + 255) / 256 * 256));
     std::vector<int> ch{0}, chs;
     for (int s = 0; s < nsys; s++)
