@@ -72,7 +72,9 @@ def parse_args():
     p.add_argument("--no-learned", action="store_true",
                    help="spmv: skip the learned-vs-Jacobi and batched-CG measurements of the default run")
     p.add_argument("--autotune", action="store_true",
-                   help="time the CSR kernel configurations on the matrix first and keep the fastest")
+                   help="spmv: time the CSR kernel configurations on the matrix first and keep the fastest; "
+                        "cg / pagerank: tune the batched forms' settings (cached in a JSON file, "
+                        "TBSLA_TUNE_CACHE)")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     a = p.parse_args()
     a.warmup = max(a.warmup, 3)
@@ -834,6 +836,12 @@ def run_pagerank(a):
     tele = np.zeros((n, 32))
     for k in range(32):
         tele[rng.choice(n, 100, replace=False), k] = 1.0 / 100
+    tuned = None
+    if a.autotune:
+        from tbsla_gb300 import autotune as AT
+
+        r = AT.tune_pagerank_batched(g, tele, T.F32)
+        tuned = {"settings": r["settings"], "cached": r["cached"], "key": r["key"], "trials": r.get("trials")}
     g.page_rank_batched(tele, 0.85, 1e-10, 3)
     t0 = time.perf_counter()
     X, itb, okb = g.page_rank_batched(tele, 0.85, 1e-10, 1000)
@@ -862,7 +870,7 @@ def run_pagerank(a):
         "l1_vs_oracle_equal_iterations": float(np.abs(x - xo).sum()),
         "cpu_baseline": {"value": b_it * ito / to / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
                          "sample": f"oracle PageRank, {ito} iterations on the same FP32-rounded graph"},
-        "batched": {"nvec": 32, "iterations": itb, "converged": bool(okb), "ms": tb * 1e3,
+        "batched": {"nvec": 32, "iterations": itb, "converged": bool(okb), "ms": tb * 1e3, "autotune": tuned,
                     "arithmetic": "double-float (float pairs) products and sums (compensated, Dot2), FP64 reductions",
                     "GB/s": b_itb * itb / tb / 1e9, "bytes_per_iteration": b_itb},
         "clocks": clocks, "gpu_launches": it,
@@ -930,8 +938,14 @@ def run_cg(a):
     nnz = np.array([m.get_nnz() for m in systems])
     res = {}
     clk = Clocks(local)
+    tuned = {}
     for pre, name in ((0, "cg"), (1, "jacobi_pcg")):
         bt = T.Batch(systems, T.F32)
+        if a.autotune:
+            from tbsla_gb300 import autotune as AT
+
+            r = AT.tune_batch_cg(bt, rhs, T.F32, precond=pre)
+            tuned[name] = {"settings": r["settings"], "cached": r["cached"], "key": r["key"]}
         for _ in range(a.warmup):
             bt.cg(rhs, max_iterations=20, rel_tol=1e-8, precond=pre, refresh=50, graph_iters=10)
         if pre == 1:
@@ -975,7 +989,7 @@ def run_cg(a):
                    "systems": len(sizes), "unknowns": int(N.sum()), "nnz": int(nnz.sum()), "rel_tol": 1e-8,
                    "step": "one batched Jacobi-PCG solve of all 64 systems (host call, wall clock)",
                    "parallelism": "1 GPU, one block-diagonal matrix, one persistent cooperative launch per solve"},
-        "solvers": res,
+        "solvers": res, "autotune": tuned or None,
         "roofline": {"bound": "hbm", "achieved": j["GB/s"], "peak": peak, "unit": "GB/s",
                      "frac": j["GB/s"] / peak, "peak_source": peak_kind, "traffic": None},
         "cpu_baseline": {"value": to * 1e3, "unit": "ms", "cores": 1, "kind": "port",

@@ -156,10 +156,12 @@ int tbsla_fill_uniform(double* out, long n, double lo, double hi, unsigned long 
  *      (MatrixCSR.cpp:49-96, MatrixELL.cpp:25-79, MatrixSCOO.cpp:75-101,
  *      MatrixDENSE.cpp:15-37) --------------------------------------------- */
 int tbsla_matrix_convert(tbsla_matrix** out, const tbsla_matrix* coo, int format);
-/* The same conversion with the (row, column) ordering of CSR / ELL done by a
- * stable radix sort on the GPU (MatrixCSR.cpp:49-96 sorts on the host):
- * identical arrays, TBSLA_ERR_NO_DEVICE without a GPU.  SCOO and DENSE are
- * the host copy / scatter either way. */
+/* The same conversion on the GPU: the (row, column) ordering of CSR / ELL by
+ * a stable radix sort (MatrixCSR.cpp:49-96 sorts on the host), the DENSE
+ * scatter-add (MatrixDENSE.cpp:15-37) by a kernel over that order, which
+ * sums duplicate positions in storage order from 0 as the reference does:
+ * identical arrays, TBSLA_ERR_NO_DEVICE without a GPU.  SCOO, a plain copy
+ * of the arrays (MatrixSCOO.cpp:75-101), stays on the host. */
 int tbsla_matrix_convert_device(tbsla_matrix** out, const tbsla_matrix* coo, int format);
 
 /* ---- binary I/O: write/read (e.g. MatrixCSR.cpp:236-295), the reference's
@@ -214,6 +216,9 @@ int tbsla_matrix_set_csr_algorithm(tbsla_matrix* m, int algorithm, int items);
  * per-block row lengths are about halved, else 64).  Changing them rebuilds the
  * device copy. */
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block);
+/* Batched personalised PageRank with FP32 / BF16 values: gathers of X rows
+ * in flight per warp, 8 (default) or 16; a tuning choice, same results. */
+int tbsla_matrix_set_pagerank_gather(tbsla_matrix* m, int gather);
 
 /* One CSR kernel configuration and its measured time. */
 typedef struct {
@@ -390,6 +395,12 @@ int tbsla_batch_set_wait_limit(tbsla_batch* b, long long ns);
  * iteration runs in FP32: 16-byte loads) or 1 (one row per thread, as for
  * every other batch).  The arithmetic of each row is the same either way. */
 int tbsla_batch_set_rows_per_thread(tbsla_batch* b, int rows);
+/* Persistent engine tuning: rows per work chunk (a multiple of 256; 0 =
+ * automatic, about 8 chunks per co-resident CTA within [1024, 4096]).
+ * TBSLA_ERR_UNSUPPORTED for a batch on the multi-launch engine. */
+int tbsla_batch_set_chunk_rows(tbsla_batch* b, long rows);
+/* The persistent engine's current chunk rows and rows per thread. */
+int tbsla_batch_tuning(const tbsla_batch* b, long* chunk_rows, int* rows_per_thread);
 /* The engine of the last tbsla_batch_cg: persistent = 1 when the whole solve
  * was one cooperative launch (every system's entries on at most 8 diagonals,
  * at most 256 systems, a factor, if used, on at most 8 diagonals), 0 for the

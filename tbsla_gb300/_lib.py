@@ -106,6 +106,7 @@ _SIGS = {
     "tbsla_matrix_set_csr_tile": (I, [P, I]),
     "tbsla_matrix_set_csr_algorithm": (I, [P, I, I]),
     "tbsla_matrix_set_sell_params": (I, [P, I, I, I, I]),
+    "tbsla_matrix_set_pagerank_gather": (I, [P, I]),
     "tbsla_matrix_autotune": (I, [P, I, C.POINTER(Tuning), C.POINTER(Tuning), I, IP]),
     "tbsla_batch_create": (I, [C.POINTER(P), C.POINTER(P), I, I]),
     "tbsla_batch_destroy": (I, [P]),
@@ -115,6 +116,8 @@ _SIGS = {
     "tbsla_batch_fallbacks": (I, [P, IP, IP]),
     "tbsla_batch_set_wait_limit": (I, [P, C.c_longlong]),
     "tbsla_batch_set_rows_per_thread": (I, [P, I]),
+    "tbsla_batch_set_chunk_rows": (I, [P, L]),
+    "tbsla_batch_tuning": (I, [P, C.POINTER(L), IP]),
     "tbsla_batch_engine": (I, [P, IP, IP]),
     "tbsla_batch_factor_mpnn": (I, [P, P, I]),
     "tbsla_batch_factor_dia": (I, [P, IP, IP, DP]),

@@ -99,6 +99,7 @@ struct tbsla_batch {
   int* row_sys = nullptr;
   int *dchunks = nullptr, *dchunk_sys = nullptr;  // the persistent engine's work chunks
   int ndchunks = 0;
+  long chunk_rows = 0;            // rows per work chunk
   void* avals_dia = nullptr;      // [K][n] storage precision
   double* a64_dia = nullptr;      // [K][n]
   float* dinv_f = nullptr;
@@ -253,6 +254,39 @@ bool dia_deltas(const tbsla_batch* B, const std::vector<int>& rp, const std::vec
   return *K > 0;
 }
 
+// Work chunks of the persistent engine: never across a system; `rows` per
+// chunk (a multiple of 256), or 0: sized so that the batch gives every
+// co-resident CTA about 8 of them (1024 to 4096 rows, i.e. 1 to 4 rows of 4
+// per thread; 3 CTAs of 256 threads per SM).
+cudaError_t dia_chunks(tbsla_batch* B, long rows) {
+  cudaStream_t st = B->stream;
+  const long n = B->n;
+  if (rows <= 0) {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    rows = n / ((long)sms * 3 * 8);
+    rows = std::min<long>(4096, std::max<long>(1024, (rows + 255) / 256 * 256));
+  }
+  std::vector<int> ch{0}, chs;
+  for (int s = 0; s < B->nsys; s++)
+    for (long r0 = B->off[s]; r0 < B->off[s + 1]; r0 += rows) {
+      ch.push_back((int)std::min<long>(B->off[s + 1], r0 + rows));
+      chs.push_back(s);
+    }
+  if (B->dchunks) cudaFree(B->dchunks);
+  if (B->dchunk_sys) cudaFree(B->dchunk_sys);
+  B->dchunks = B->dchunk_sys = nullptr;
+  B->ndchunks = (int)chs.size();
+  B->chunk_rows = rows;
+  cudaError_t e;
+  if ((e = alloc(&B->dchunks, ch.size())) || (e = alloc(&B->dchunk_sys, std::max<size_t>(chs.size(), 1))) ||
+      (e = cudaMemcpyAsync(B->dchunks, ch.data(), ch.size() * 4, cudaMemcpyHostToDevice, st)) ||
+      (e = cudaMemcpyAsync(B->dchunk_sys, chs.data(), chs.size() * 4, cudaMemcpyHostToDevice, st)))
+    return e;
+  return cudaStreamSynchronize(st);
+}
+
 // The DIA copy of the batch and the persistent engine's vectors.
 int build_dia(tbsla_batch* B, const std::vector<int>& delta, int K) {
   cudaStream_t st = B->stream;
@@ -283,28 +317,7 @@ int build_dia(tbsla_batch* B, const std::vector<int>& delta, int K) {
   const size_t es = B->prec == TBSLA_F64 ? 8 : 4;
   for (void** v : {&B->dv, &B->r0, &B->r1, &B->p0, &B->p1, &B->q2, &B->z2, &B->t2})
     CK(cudaMalloc(v, std::max<size_t>((size_t)n, 1) * es));
-  // work chunks of the persistent engine: never across a system, sized so
-  // that the batch gives every co-resident CTA about 8 of them (1024 to 4096
-  // rows, i.e. 1 to 4 rows of 4 per thread; 3 CTAs of 256 threads per SM)
-  {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long rows = n / ((long)sms * 3 * 8);
-    rows = std::min<long>(4096, std::max<long>(1024, (rows + 255) / 256 * 256));
-    std::vector<int> ch{0}, chs;
-    for (int s = 0; s < nsys; s++)
-      for (long r0 = B->off[s]; r0 < B->off[s + 1]; r0 += rows) {
-        ch.push_back((int)std::min<long>(B->off[s + 1], r0 + rows));
-        chs.push_back(s);
-      }
-    B->ndchunks = (int)chs.size();
-    CK(alloc(&B->dchunks, ch.size()));
-    CK(alloc(&B->dchunk_sys, std::max<size_t>(chs.size(), 1)));
-    CK(cudaMemcpyAsync(B->dchunks, ch.data(), ch.size() * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(B->dchunk_sys, chs.data(), chs.size() * 4, cudaMemcpyHostToDevice, st));
-    CK(cudaStreamSynchronize(st));
-  }
+  CK(dia_chunks(B, 0));
   CK(alloc(&B->mode_d, nsys));
   CK(alloc(&B->fallback_d, nsys));
   CK(alloc(&B->relres_d, nsys));
@@ -989,6 +1002,20 @@ int tbsla_batch_fallbacks(const tbsla_batch* B, int* fallback, int* precond_used
     if (fallback) fallback[k] = k < (int)B->fallback_h.size() ? B->fallback_h[k] : 0;
     if (precond_used) precond_used[k] = k < (int)B->mode_h.size() ? B->mode_h[k] : 0;
   }
+  return TBSLA_OK;
+}
+
+int tbsla_batch_set_chunk_rows(tbsla_batch* B, long rows) {
+  if (!B || rows < 0 || rows % 256 != 0 || rows > (1L << 20)) return TBSLA_ERR_INVALID_ARG;
+  if (!B->dia) return TBSLA_ERR_UNSUPPORTED;
+  cudaSetDevice(B->device);
+  return st_of(dia_chunks(B, rows));
+}
+
+int tbsla_batch_tuning(const tbsla_batch* B, long* chunk_rows, int* rows_per_thread) {
+  if (!B) return TBSLA_ERR_INVALID_ARG;
+  if (chunk_rows) *chunk_rows = B->chunk_rows;
+  if (rows_per_thread) *rows_per_thread = B->vec4 && !B->vec4_off ? 4 : 1;
   return TBSLA_OK;
 }
 

@@ -276,6 +276,12 @@ int tbsla_matrix_set_csr_tile(tbsla_matrix* m, int nnz_per_block) {
   return TBSLA_OK;
 }
 
+int tbsla_matrix_set_pagerank_gather(tbsla_matrix* m, int gather) {
+  if (!m || (gather != 8 && gather != 16)) return TBSLA_ERR_INVALID_ARG;
+  m->pr_gather = gather;  // a launch parameter: the device copy stays
+  return TBSLA_OK;
+}
+
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block) {
   if (!m || short_thr < 0 || short_thr > 255 || long_thr < 0 || sigma < 32 || sigma > (1 << 23) ||
       col_block < 0)

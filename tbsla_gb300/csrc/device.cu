@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "device.hpp"
@@ -219,6 +220,68 @@ void sort_by_row(const tbsla_matrix* m, long nnz, int rmin, int rmax, std::vecto
   }
 }
 
+// Host -> device copy of a large array through pinned staging buffers.  A
+// copy from pageable memory is staged by the driver one small buffer at a
+// time; here the host array is copied (by several threads) into one of two
+// pinned 64 MiB buffers while the other one's DMA runs, so the host copy and
+// the link overlap.  The buffers are allocated once per device and shared
+// under a mutex; arrays below 16 MiB take the plain copy.
+constexpr size_t kStageBytes = 64u << 20;
+struct Staging {
+  std::mutex mu;
+  void* buf[2] = {nullptr, nullptr};
+  cudaEvent_t done[2] = {nullptr, nullptr};
+  bool tried = false;
+};
+Staging g_stage[64];
+
+int h2d_staged(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (bytes < (16u << 20) || dev < 0 || dev >= 64)
+    return status_of(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  Staging& g = g_stage[dev];
+  std::lock_guard<std::mutex> lock(g.mu);
+  if (!g.tried) {
+    g.tried = true;
+    for (int b = 0; b < 2; b++)
+      if (cudaHostAlloc(&g.buf[b], kStageBytes, cudaHostAllocDefault) != cudaSuccess ||
+          cudaEventCreateWithFlags(&g.done[b], cudaEventDisableTiming) != cudaSuccess) {
+        cudaGetLastError();
+        for (int c = 0; c < 2; c++) {
+          if (g.buf[c]) cudaFreeHost(g.buf[c]);
+          if (g.done[c]) cudaEventDestroy(g.done[c]);
+          g.buf[c] = nullptr;
+          g.done[c] = nullptr;
+        }
+        break;
+      }
+  }
+  if (!g.buf[0]) return status_of(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  const char* from = static_cast<const char*>(src);
+  char* to = static_cast<char*>(dst);
+  bool used[2] = {false, false};
+  for (size_t off = 0, k = 0; off < bytes; off += kStageBytes, k++) {
+    const int b = (int)(k & 1);
+    const size_t len = std::min(kStageBytes, bytes - off);
+    if (used[b]) TRY(cudaEventSynchronize(g.done[b]));  // the buffer's previous DMA is over
+    char* stage = static_cast<char*>(g.buf[b]);
+    tbsla_impl::parallel_for_items(8, [&](long p0, long p1) {
+      for (long part = p0; part < p1; part++) {
+        const size_t a = len * part / 8, z = len * (part + 1) / 8;
+        std::memcpy(stage + a, from + off + a, z - a);
+      }
+    });
+    TRY(cudaMemcpyAsync(to + off, stage, len, cudaMemcpyHostToDevice, s));
+    TRY(cudaEventRecord(g.done[b], s));
+    used[b] = true;
+  }
+  // both buffers free again before the lock is released
+  for (int b = 0; b < 2; b++)
+    if (used[b]) TRY(cudaEventSynchronize(g.done[b]));
+  return TBSLA_OK;
+}
+
 // FP64 host values -> device storage precision.
 int upload_values(DeviceMatrix* d, const double* host, size_t n) {
   if (n == 0) return TBSLA_OK;
@@ -230,11 +293,11 @@ int upload_values(DeviceMatrix* d, const double* host, size_t n) {
   }
   d->vals = dst;
   d->bytes += n * prec_size(d->prec);
-  if (d->prec == TBSLA_F64) return status_of(cudaMemcpyAsync(dst, host, n * 8, cudaMemcpyHostToDevice, d->stream));
+  if (d->prec == TBSLA_F64) return h2d_staged(dst, host, n * 8, d->stream);
   double* tmp = nullptr;
   int st = dalloc(&tmp, n);
   if (st) return st;
-  TRY(cudaMemcpyAsync(tmp, host, n * 8, cudaMemcpyHostToDevice, d->stream));
+  if ((st = h2d_staged(tmp, host, n * 8, d->stream))) return st;
   TRY(convert_values(tmp, dst, d->prec, (long)n, d->stream));
   TRY(cudaStreamSynchronize(d->stream));
   cudaFree(tmp);
@@ -246,7 +309,7 @@ int upload_ints(DeviceMatrix* d, int** dst, const int* host, size_t n) {
   if (st) return st;
   d->bytes += n * 4;
   if (n == 0) return TBSLA_OK;
-  return status_of(cudaMemcpyAsync(*dst, host, n * 4, cudaMemcpyHostToDevice, d->stream));
+  return h2d_staged(*dst, host, n * 4, d->stream);
 }
 
 template <class T>
@@ -1092,7 +1155,8 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   const bool df = d->prec != TBSLA_F64;
   double *X0 = nullptr, *X1 = nullptr, *T = nullptr, *coef = nullptr, *W = nullptr;
   int* flags = nullptr;
-  int grid = csr_pagerank_batched_grid(d->prec);
+  const int gather = m->pr_gather == 16 ? 16 : 8;
+  int grid = csr_pagerank_batched_grid(d->prec, gather);
   auto cleanup = [&]() {
     for (void* p : {(void*)X0, (void*)X1, (void*)T, (void*)coef, (void*)flags, (void*)W})
       if (p) cudaFree(p);
@@ -1130,7 +1194,8 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
       const bool even = (launched % 2) == 0;
       p.coef_in = coef + (even ? 0 : 64);
       p.coef_out = coef + (even ? 64 : 0);
-      cudaError_t e = df ? csr_pagerank_batched_df_step(a, nvec, even ? X0 : X1, even ? X1 : X0, T, W, p, ctl, grid, s)
+      cudaError_t e = df ? csr_pagerank_batched_df_step(a, nvec, even ? X0 : X1, even ? X1 : X0, T, W, p, ctl, grid,
+                                                        gather, s)
                          : csr_pagerank_batched_step(a, n, nvec, even ? X0 : X1, even ? X1 : X0, T, p, ctl, grid, s);
       if (e != cudaSuccess) {
         cleanup();
@@ -1287,6 +1352,45 @@ int dev_coo_order(const int* row, const int* col, long n, int n_row, int n_col, 
   for (size_t i = 0; i < hs.size(); i++) start[i] = hs[i];
   for (long k = 0; k < n; k++) perm[k] = hp[k];
   return TBSLA_OK;
+}
+
+int dev_coo_to_dense(const int* row, const int* col, const double* val, long n, int ln_row, int ln_col,
+                     double* dense_host) {
+  int st = check_device();
+  if (st) return st;
+  if (n >= (1L << 31) - 1) return TBSLA_ERR_INVALID_ARG;
+  cudaSetDevice(g_device);
+  const size_t cells = (size_t)ln_row * ln_col;
+  cudaStream_t s = nullptr;
+  int *drow = nullptr, *dcol = nullptr, *p0 = nullptr, *p1 = nullptr;
+  double *dval = nullptr, *dense = nullptr;
+  uint64_t *k0 = nullptr, *k1 = nullptr;
+  unsigned *cnt = nullptr, *scr = nullptr;
+  const size_t ns = std::max<size_t>(1, std::max(radix_scratch(n), scan_scratch((long)ln_row + 1)));
+  auto cleanup = [&]() {
+    for (void* q : {(void*)drow, (void*)dcol, (void*)p0, (void*)p1, (void*)dval, (void*)dense, (void*)k0, (void*)k1,
+                    (void*)cnt, (void*)scr})
+      if (q) cudaFree(q);
+    if (s) cudaStreamDestroy(s);
+  };
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess || (st = dalloc(&drow, n)) ||
+      (st = dalloc(&dcol, n)) || (st = dalloc(&dval, n)) || (st = dalloc(&p0, n)) || (st = dalloc(&p1, n)) ||
+      (st = dalloc(&k0, n)) || (st = dalloc(&k1, n)) || (st = dalloc(&cnt, (size_t)ln_row + 1)) ||
+      (st = dalloc(&scr, ns)) || (st = dalloc(&dense, cells))) {
+    cleanup();
+    return st ? st : TBSLA_ERR_CUDA;
+  }
+  int alt = 0;
+  if (cells) st = status_of(cudaMemsetAsync(dense, 0, cells * 8, s));
+  if (!st && n) st = h2d_staged(drow, row, n * 4, s);
+  if (!st && n) st = h2d_staged(dcol, col, n * 4, s);
+  if (!st && n) st = h2d_staged(dval, val, n * 8, s);
+  if (!st) st = status_of(coo_order(drow, dcol, n, ln_row, ln_col, k0, k1, p0, p1, cnt, scr, &alt, s));
+  if (!st) st = status_of(coo_dense_scatter(alt ? p1 : p0, drow, dcol, dval, n, ln_col, dense, s));
+  if (!st && cells) st = status_of(cudaMemcpyAsync(dense_host, dense, cells * 8, cudaMemcpyDeviceToHost, s));
+  if (!st) st = status_of(cudaStreamSynchronize(s));
+  cleanup();
+  return st;
 }
 
 int dev_ready(int* device) {

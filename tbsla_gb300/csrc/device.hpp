@@ -50,6 +50,11 @@ int dev_cg(tbsla_matrix* m, const double* b, double* x, int max_it, double rel_t
 // COO -> CSR ordering on the GPU: start[n_row + 1] row starts and perm[n]
 // the storage indices in (row, col) order, ties in storage order.
 int dev_coo_order(const int* row, const int* col, long n, int n_row, int n_col, long* start, long* perm);
+// COO -> DENSE on the GPU (MatrixDENSE.cpp:15-37): entries ordered by the
+// radix sort, duplicates summed in storage order from 0, the ln_row x
+// ln_col row-major result copied to dense_host.
+int dev_coo_to_dense(const int* row, const int* col, const double* val, long n, int ln_row, int ln_col,
+                     double* dense_host);
 
 // Autotuner: times the CSR kernel configurations, keeps the fastest.
 int dev_autotune(tbsla_matrix* m, int reps, tbsla_tuning* best, tbsla_tuning* trials, int max_trials,

@@ -128,6 +128,10 @@ int convert_from_coo(tbsla_matrix* out, const tbsla_matrix* coo, int format, boo
     return TBSLA_OK;
   }
   if (format == TBSLA_DENSE) {  // MatrixDENSE.cpp:15-37: scatter-add in storage order
+    if (device) {  // the same sums on the GPU, duplicates added in storage order
+      out->values.resize((size_t)I.ln_row * I.ln_col);
+      return dev_coo_to_dense(row, col, val, nnz, I.ln_row, I.ln_col, out->values.data());
+    }
     out->values.zeros((size_t)I.ln_row * I.ln_col);
     for (long k = 0; k < nnz; k++) out->values[(size_t)row[k] * I.ln_col + col[k]] += val[k];
     return TBSLA_OK;

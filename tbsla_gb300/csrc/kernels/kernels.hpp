@@ -165,7 +165,7 @@ cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
 // BF16 values: X, Y, T (n x nvec) and W (the column sums, n) are float2
 // arrays of the same byte size as FP64 ones; reductions are FP64.
 cudaError_t csr_pagerank_batched_df_step(const CsrArgs& a, int nvec, const void* X, void* Y, const void* T,
-                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s);
+                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, int gather, cudaStream_t s);
 // FP64 <-> double-float (float2) conversions, element by element (the
 // destination may be the source's own storage).
 cudaError_t f64_to_df(const double* src, void* dst, long n, cudaStream_t s);
@@ -182,7 +182,7 @@ cudaError_t pagerank_epilogue(const double* t, const double* x, double* y, long 
 
 // CTAs of the persistent PageRank kernels (resident capacity of the GPU).
 int csr_pagerank_grid(int items, int prec);
-int csr_pagerank_batched_grid(int prec);
+int csr_pagerank_batched_grid(int prec, int gather);
 
 // ---- batched CG over a block-diagonal concatenation of systems -------------------
 // Per-system status: ACTIVE iterates; VERIFY has a recursive residual below
@@ -346,6 +346,10 @@ cudaError_t exclusive_scan(unsigned* a, long n, unsigned* scratch, cudaStream_t 
 cudaError_t coo_order(const int* row, const int* col, long n, int n_row, int n_col, uint64_t* keys,
                       uint64_t* keys_alt, int* perm, int* perm_alt, unsigned* rowcount, unsigned* scratch,
                       int* perm_in_alt, cudaStream_t s);
+// dense[row * ln_col + col] = the sum, in storage order from 0, of the values
+// at each (row, col), given perm from coo_order (dense zeroed by the caller).
+cudaError_t coo_dense_scatter(const int* perm, const int* row, const int* col, const double* val, long n,
+                              long ln_col, double* dense, cudaStream_t s);
 
 // C = A B (MatrixCSR::dense_multiply): B (rows indexed by the stored
 // column) and C row-major with k columns; C rows [0, n_row) written.

@@ -192,6 +192,37 @@ cudaError_t radix_sort_pairs(uint64_t* keys, uint64_t* keys_alt, int* vals, int*
   return cudaSuccess;
 }
 
+// COO -> DENSE (MatrixDENSE.cpp:15-37): the entries in (row, column) order,
+// ties in storage order, so each run of one position sums its values in the
+// reference's order (starting from 0), written once; a thread per sorted
+// entry, the first of a run does the run.
+__global__ void k_dense_scatter(const int* __restrict__ perm, const int* __restrict__ row,
+                                const int* __restrict__ col, const double* __restrict__ val, long n, long ln_col,
+                                double* __restrict__ dense) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    const int p = perm[k];
+    const int r = row[p], c = col[p];
+    if (k > 0) {
+      const int q = perm[k - 1];
+      if (row[q] == r && col[q] == c) continue;  // inside a run
+    }
+    double sum = 0.0;
+    for (long t = k; t < n; t++) {
+      const int u = perm[t];
+      if (row[u] != r || col[u] != c) break;
+      sum = __dadd_rn(sum, val[u]);
+    }
+    dense[(size_t)r * ln_col + c] = sum;
+  }
+}
+
+cudaError_t coo_dense_scatter(const int* perm, const int* row, const int* col, const double* val, long n,
+                              long ln_col, double* dense, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_dense_scatter<<<grid_for(n), RT, 0, s>>>(perm, row, col, val, n, ln_col, dense);
+  return cudaGetLastError();
+}
+
 cudaError_t coo_order(const int* row, const int* col, long n, int n_row, int n_col, uint64_t* keys,
                       uint64_t* keys_alt, int* perm, int* perm_alt, unsigned* rowcount, unsigned* scratch,
                       int* perm_in_alt, cudaStream_t s) {

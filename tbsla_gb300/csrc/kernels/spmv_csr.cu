@@ -199,7 +199,7 @@ __device__ __forceinline__ float as_f32(__nv_bfloat16 v) { return __bfloat162flo
 // dot product (Dot2: about twice FP32 precision), and the epilogue forms the single-vector epilogue's quantities (y = beta s acc +
 // t T, |y - x s|, y, w y) in the same arithmetic.  The CTA and grid
 // reductions run in FP64 (batched_finish).
-template <class V>
+template <class V, int GB>
 __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int nvec, const float2* __restrict__ X,
                                                                float2* __restrict__ Y, const float2* __restrict__ T,
                                                                const float2* __restrict__ W, PageRankArgs p,
@@ -228,15 +228,16 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int n
           v = as_f32(ld_stream(vals + j, pol));
         }
         const int m = min(kWarp, e - base);
-        // 8 entries' gathers of X in flight, then their products added in
-        // entry order; a short tail runs as a masked batch (a dead slot adds
-        // 0 * 0, which leaves s and c as they are), so a row of a few
-        // entries waits for one gather latency, not one per entry
-        for (int t = 0; t < m; t += 8) {
-          DF xv[8];
-          float vv[8];
+        // GB entries' gathers of X in flight (8 or 16, a tuning choice),
+        // then their products added in entry order; a short tail runs as a
+        // masked batch (a dead slot adds 0 * 0, which leaves s and c as they
+        // are), so a row of a few entries waits for one gather latency, not
+        // one per entry
+        for (int t = 0; t < m; t += GB) {
+          DF xv[GB];
+          float vv[GB];
 #pragma unroll
-          for (int u = 0; u < 8; u++) {
+          for (int u = 0; u < GB; u++) {
             const bool live = t + u < m;
             const int ct = __shfl_sync(0xffffffffu, c, (t + u) & (kWarp - 1));
             const float vu = __shfl_sync(0xffffffffu, v, (t + u) & (kWarp - 1));
@@ -244,7 +245,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int n
             xv[u] = (active && live) ? df_ld(X + (size_t)(ct - a.f_col) * nvec + lane) : DF{0.f, 0.f};
           }
 #pragma unroll
-          for (int u = 0; u < 8; u++) dot2_step(as, ac, vv[u], xv[u]);
+          for (int u = 0; u < GB; u++) dot2_step(as, ac, vv[u], xv[u]);
         }
       }
       if (active) {
@@ -437,24 +438,37 @@ int csr_pagerank_grid(int items, int prec) {
   return 152;
 }
 
-int csr_pagerank_batched_grid(int prec) {
+int csr_pagerank_batched_grid(int prec, int gather) {
+  const bool wide = gather == 16;
   switch (prec) {
     case kF64: return resident_grid<k_csr_pagerank_batched<double>>();
-    case kF32: return resident_grid<k_csr_pagerank_batched_df<float>>();
-    case kBF16: return resident_grid<k_csr_pagerank_batched_df<__nv_bfloat16>>();
+    case kF32:
+      return wide ? resident_grid<k_csr_pagerank_batched_df<float, 16>>()
+                  : resident_grid<k_csr_pagerank_batched_df<float, 8>>();
+    case kBF16:
+      return wide ? resident_grid<k_csr_pagerank_batched_df<__nv_bfloat16, 16>>()
+                  : resident_grid<k_csr_pagerank_batched_df<__nv_bfloat16, 8>>();
   }
   return 152;
 }
 
 cudaError_t csr_pagerank_batched_df_step(const CsrArgs& a, int nvec, const void* X, void* Y, const void* T,
-                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s) {
+                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, int gather,
+                                         cudaStream_t s) {
   if (nvec < 1 || nvec > kWarp) return cudaErrorInvalidValue;
   const float2 *x = static_cast<const float2*>(X), *t = static_cast<const float2*>(T),
                *w = static_cast<const float2*>(W);
   float2* y = static_cast<float2*>(Y);
+  const bool wide = gather == 16;
   switch (a.prec) {
-    case kF32: k_csr_pagerank_batched_df<float><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
-    case kBF16: k_csr_pagerank_batched_df<__nv_bfloat16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
+    case kF32:
+      if (wide) k_csr_pagerank_batched_df<float, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+      else k_csr_pagerank_batched_df<float, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+      break;
+    case kBF16:
+      if (wide) k_csr_pagerank_batched_df<__nv_bfloat16, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+      else k_csr_pagerank_batched_df<__nv_bfloat16, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+      break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -39,7 +39,8 @@ class Matrix:
 
     def __init__(self, coo: "MatrixCOO | None" = None, _handle=None, device: bool = False):
         """coo: converting constructor (MatrixCSR(const MatrixCOO&) ...);
-        device=True orders the entries with the GPU radix sort."""
+        device=True does the conversion on the GPU: the (row, column) order
+        of CSR / ELL by the radix sort, the DENSE scatter by a kernel."""
         h = C.c_void_p()
         if _handle is not None:
             h = _handle
@@ -274,6 +275,11 @@ class MatrixCSR(Matrix):
         check(lib.tbsla_matrix_autotune(self._h, reps, C.byref(best), trials, max_trials, C.byref(nt)), "autotune")
         return best.as_dict(), [trials[i].as_dict() for i in range(nt.value)]
 
+    def set_pagerank_gather(self, gather: int):
+        """Batched PageRank (FP32 / BF16 values): X-row gathers in flight per
+        warp, 8 or 16."""
+        check(lib.tbsla_matrix_set_pagerank_gather(self._h, int(gather)), "set_pagerank_gather")
+
     def set_sell_params(self, short_thr: int = 0, long_thr: int = 0, sigma: int = 16384, col_block: int = 0):
         """Sliced-ELL layout thresholds (0: automatic), window and column
         block (0: 8,388,608 columns)."""
@@ -474,6 +480,17 @@ class Batch:
         """Persistent engine: 4 rows per thread (16-byte loads, the default
         where the layout allows) or 1."""
         check(lib.tbsla_batch_set_rows_per_thread(self._h, int(rows)), "batch_set_rows_per_thread")
+
+    def set_chunk_rows(self, rows: int):
+        """Persistent engine: rows per work chunk (multiple of 256; 0 =
+        automatic)."""
+        check(lib.tbsla_batch_set_chunk_rows(self._h, int(rows)), "batch_set_chunk_rows")
+
+    def tuning(self) -> dict:
+        """Current persistent-engine settings."""
+        cr, rpt = C.c_long(), C.c_int()
+        check(lib.tbsla_batch_tuning(self._h, C.byref(cr), C.byref(rpt)), "batch_tuning")
+        return {"chunk_rows": cr.value, "rows_per_thread": rpt.value}
 
     def set_wait_limit(self, ns: int):
         """Bound on one grid-wide wait of the persistent solver (ns)."""

@@ -191,3 +191,28 @@ def test_vector_rows_match_scalar_rows(gpu):
                 assert true_rel_residual(m, x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]) <= TOL
             out.append(its)
         assert np.abs(out[0] - out[1]).max() <= 1, out
+
+
+def test_autotune_batch_cg_and_cache(gpu, tmp_path):
+    """The autotuner times the persistent engine's settings on the batch's
+    own solve, keeps the fastest, caches it, and a second call applies the
+    cached settings without timing; the tuned batch still solves to the
+    FP64-verified tolerance."""
+    from tbsla_gb300 import autotune as A
+
+    T = gpu
+    sizes = [12, 16, 8]
+    systems = [diffusion(T, s, 900 + i) for i, s in enumerate(sizes)]
+    rhs = np.concatenate([T.fill_uniform(s ** 3, -1.0, 1.0, 910 + i) for i, s in enumerate(sizes)])
+    batch = T.Batch(systems, T.F32)
+    path = str(tmp_path / "tune.json")
+    r = A.tune_batch_cg(batch, rhs, T.F32, precond=1, iters=10, reps=1, path=path)
+    assert not r["cached"] and len(r["trials"]) == 6
+    assert batch.tuning() == r["settings"]
+    r2 = A.tune_batch_cg(T.Batch(systems, T.F32), rhs, T.F32, precond=1, path=path)
+    assert r2["cached"] and r2["settings"] == r["settings"]
+    x, its, rr, ok = batch.cg(rhs, max_iterations=4000, rel_tol=TOL, precond=1)
+    assert ok and (rr <= TOL).all()
+    off = batch.offsets
+    for k, m in enumerate(systems):
+        assert true_rel_residual(m, x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]) <= TOL

@@ -1,8 +1,9 @@
-"""COO -> CSR / ELL with the (row, column) ordering sorted on the GPU
-(tbsla_matrix_convert_device, kernels/sort.cu): the arrays equal the host
-conversion's exactly -- the host conversion itself is pinned to the
-reference's MatrixCSR(const MatrixCOO&) by the golden tests -- including
-duplicate (row, column) pairs, which keep their storage order."""
+"""COO -> CSR / ELL with the (row, column) ordering sorted on the GPU, and
+COO -> DENSE scattered on the GPU (tbsla_matrix_convert_device,
+kernels/sort.cu): the arrays equal the host conversion's exactly -- the host
+conversion itself is pinned to the reference's converting constructors by
+the golden tests -- including duplicate (row, column) pairs, which keep
+their storage order (DENSE: summed in that order)."""
 import numpy as np
 import pytest
 
@@ -41,6 +42,8 @@ def test_device_order_equals_host(gpu, shape):
     coo = coo_of(T, n_row, n_col, row, col, val)
     for cls in (T.MatrixCSR, T.MatrixELL):
         same(cls(coo), cls(coo, device=True))
+    if n_row * n_col <= (1 << 27):
+        same(T.MatrixDENSE(coo), T.MatrixDENSE(coo, device=True))
 
 
 def test_device_order_power_law_and_empty(gpu):
@@ -58,3 +61,18 @@ def test_device_order_power_law_and_empty(gpu):
     same(m, d)
     empty = coo_of(T, 5, 5, [], [], [])
     same(T.MatrixCSR(empty), T.MatrixCSR(empty, device=True))
+
+
+def test_device_dense_scatter_duplicates_and_cdiag(gpu):
+    """Many duplicates of a few positions, summed in storage order exactly as
+    MatrixDENSE(const MatrixCOO&) does; and the reference's cdiag matrix."""
+    T = gpu
+    rng = np.random.default_rng(9)
+    row = rng.integers(0, 7, 5000)
+    col = rng.integers(0, 5, 5000)
+    val = rng.uniform(-1, 1, 5000) * 10.0 ** rng.integers(-8, 8, 5000)
+    coo = coo_of(T, 7, 5, row, col, val)
+    same(T.MatrixDENSE(coo), T.MatrixDENSE(coo, device=True))
+    c = T.MatrixCOO()
+    c.fill_cdiag(300, 200, 3)
+    same(T.MatrixDENSE(c), T.MatrixDENSE(c, device=True))

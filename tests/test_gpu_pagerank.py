@@ -94,3 +94,34 @@ def test_batched_personalised_pagerank(gpu):
         xr, _, _ = oracle.pagerank(a["rowptr"], a["colidx"], a["values"], 0.85, 1e-10, it, stop_early=False,
                                    teleport=np.ascontiguousarray(tele[:, k]))
         assert np.abs(X[:, k] - xr).sum() <= 1e-10, k
+
+
+def test_batched_pagerank_gather_width(gpu, tmp_path):
+    """FP32-valued batched PageRank with 8 or 16 X-row gathers in flight per
+    warp: each row's products are added in the same entry order; only the
+    grid (the resident CTAs of each form) and so the order of the FP64
+    per-CTA partial sums of the norms differ.  Same iterations, vectors
+    within 1e-13 in L1; the autotuner picks one of the two and caches it."""
+    from tbsla_gb300 import autotune as A
+
+    T = gpu
+    n = 1 << 14
+    g = graph(T, n, seed=6)
+    g.make_stochastic(np.zeros(n))
+    g.set_precision(T.F32)
+    rng = np.random.default_rng(3)
+    nvec = 16
+    tele = np.zeros((n, nvec))
+    for k in range(nvec):
+        tele[rng.choice(n, 50, replace=False), k] = 1.0 / 50
+    out = []
+    for w in (8, 16):
+        g.set_pagerank_gather(w)
+        X, it, ok = g.page_rank_batched(tele, 0.85, 1e-10, 500)
+        assert ok
+        out.append((X, it))
+    assert out[0][1] == out[1][1]
+    assert np.abs(out[0][0] - out[1][0]).sum(axis=0).max() <= 1e-13
+    r = A.tune_pagerank_batched(g, tele, T.F32, iters=3, reps=1, path=str(tmp_path / "t.json"))
+    assert r["settings"]["gather"] in (8, 16) and not r["cached"]
+    assert A.tune_pagerank_batched(g, tele, T.F32, path=str(tmp_path / "t.json"))["cached"]
