@@ -219,6 +219,12 @@ int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, i
 /* Batched personalised PageRank with FP32 / BF16 values: gathers of X rows
  * in flight per warp, 8 (default) or 16; a tuning choice, same results. */
 int tbsla_matrix_set_pagerank_gather(tbsla_matrix* m, int gather);
+/* PageRank with the sliced-ELL kernel and one column block: 1 (default)
+ * runs each step's epilogue -- the new iterate and its three FP64 sums --
+ * inside the SpMV launch; 0 writes A x and runs the epilogue as a pass of
+ * its own (the form used with several column blocks).  Both sum in a fixed
+ * order; their vectors agree to rounding.  No reference counterpart. */
+int tbsla_matrix_set_pagerank_fused(tbsla_matrix* m, int fused);
 
 /* One CSR kernel configuration and its measured time. */
 typedef struct {

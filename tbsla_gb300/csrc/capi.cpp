@@ -282,6 +282,12 @@ int tbsla_matrix_set_pagerank_gather(tbsla_matrix* m, int gather) {
   return TBSLA_OK;
 }
 
+int tbsla_matrix_set_pagerank_fused(tbsla_matrix* m, int fused) {
+  if (!m || (fused != 0 && fused != 1)) return TBSLA_ERR_INVALID_ARG;
+  m->pr_fused = fused;  // a launch choice: the device copy stays
+  return TBSLA_OK;
+}
+
 int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, int sigma, int col_block) {
   if (!m || short_thr < 0 || short_thr > 255 || long_thr < 0 || sigma < 32 || sigma > (1 << 23) ||
       col_block < 0)

@@ -110,6 +110,7 @@ struct DeviceMatrix {
   double colw_s0 = 0, colw_m0 = 0;  // S and M of the start vector 1/n
   long nnz = 0;  // entries on the device
   int min_row = 0, max_row = -1;
+  double* coo_carry = nullptr;  // COO / SCOO: head, tail carries (double) and flags (int) per chunk
   double* x = nullptr;
   size_t x_len = 0;
   double* y = nullptr;
@@ -133,7 +134,7 @@ struct DeviceMatrix {
     for (void* p : {vals, (void*)idx0, (void*)idx1, (void*)blocks, (void*)x, (void*)y, (void*)t, (void*)pr_ctl,
                     (void*)counter, (void*)partials, (void*)result, (void*)coord, (void*)carry_row,
                     (void*)carry_val, svals, (void*)scols, (void*)sell_counter, (void*)colw, (void*)xdf,
-                    (void*)df_flag})
+                    (void*)df_flag, (void*)coo_carry})
       if (p) cudaFree(p);
     for (SellPlan& p : sell)
       for (void* q : {(void*)p.slice, (void*)p.lane, (void*)p.lane_len})
@@ -527,6 +528,9 @@ int build(const tbsla_matrix* m, DeviceMatrix* d) {
       int st = upload_ints(d, &d->idx0, rows.data(), nnz);
       if (!st) st = upload_ints(d, &d->idx1, cols.data(), nnz);
       if (!st) st = upload_values(d, vals.data(), nnz);
+      const long nch = coo_chunks(nnz);
+      if (!st) st = dalloc(&d->coo_carry, (size_t)(2 * nch + (nch + 1) / 2));
+      if (!st) d->bytes += (size_t)nch * 20;
       if (!st) st = status_of(cudaStreamSynchronize(d->stream));
       return st;
     }
@@ -636,8 +640,10 @@ int ax_device(const tbsla_matrix* m, DeviceMatrix* d, double* r, const double* v
       long off = (long)vect_incr - (scoo ? I.f_row : 0);
       long len = scoo ? I.ln_row : I.n_row;
       if (d->min_row + off < 0 || d->max_row + off >= len) return TBSLA_ERR_INVALID_ARG;
+      const long nch = coo_chunks(d->nnz);
+      CooCarry cc{d->coo_carry, d->coo_carry + nch, reinterpret_cast<int*>(d->coo_carry + 2 * nch)};
       return status_of(coo_spmv(d->vals, d->prec, d->idx0, d->idx1, d->nnz, (int)off,
-                                scoo ? -I.f_col : 0, v, r, s));
+                                scoo ? -I.f_col : 0, v, r, cc, s));
     }
     case TBSLA_DENSE:
       if (d->dense_df)
@@ -1097,6 +1103,14 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
   cudaMemcpyAsync(coef, c0, 16, cudaMemcpyHostToDevice, s);
   cudaMemsetAsync(flags, 0, 2 * sizeof(int), s);
   CsrArgs a = csr_args(m, d);
+  // one column block: the epilogue runs inside the sliced-ELL kernel
+  // (sell_pagerank); several: a separate pass over t = A x
+  SellArgs sa{};
+  bool fused = false;
+  if (sell && I.nnz > 0) {
+    sa = sell_args(m, d);
+    fused = sa.nblocks == 1 && sa.parts == 1 && m->pr_fused;
+  }
   PageRankArgs p{beta, (double)n, eps, nullptr, d->colw, coef, coef + 2, flags, flags + 1};
   Ctl ctl{d->counter, d->partials, d->result};
   int launched = 0, hflags[2] = {0, 0};
@@ -1108,8 +1122,10 @@ int dev_page_rank(tbsla_matrix* m, double beta, double eps, int max_it, double* 
       p.coef_in = coef + (even ? 0 : 2);
       p.coef_out = coef + (even ? 2 : 0);
       cudaError_t e = cudaErrorInvalidValue;
-      if (I.nnz > 0 && sell) {
-        e = sell_spmv(sell_args(m, d), even ? x0 : x1, d->t, d->sell_counter, s, flags);
+      if (I.nnz > 0 && sell && fused) {
+        e = sell_pagerank(sa, even ? x0 : x1, even ? x1 : x0, p, ctl, s);
+      } else if (I.nnz > 0 && sell) {
+        e = sell_spmv(sa, even ? x0 : x1, d->t, d->sell_counter, s, flags);
         if (e == cudaSuccess) e = pagerank_epilogue(d->t, even ? x0 : x1, even ? x1 : x0, n, p, ctl, grid, s);
       } else if (I.nnz > 0) {
         e = csr_pagerank_step(a, even ? x0 : x1, even ? x1 : x0, p, ctl, grid, s);

@@ -141,5 +141,55 @@ __device__ __forceinline__ void reduce_and_finish(Ctl ctl, double* red, Smem& sm
 }
 
 
+// ---- PageRank step epilogue ----------------------------------------------------
+
+// x is used normalised by its sum S (scale s = 1/S, carried from the
+// previous step): y_i = (beta * (A x)_i) * s + c_i with c_i = t / n or
+// t * tele_i and t = 1 - (beta * M) * s, M = sum_j w_j x_j (w = column sums
+// of A as stored), so that y sums to 1.  Reductions: L1 change, sum y and
+// sum w y (the next step's S and M).
+// Four FP64 operations per row (GB300's FP64 pipe is the epilogue's
+// bound): yn = fma(beta s, sum, c), the change fma(-x, s, yn), S += yn,
+// M = fma(w, yn, M).
+struct EpiPageRank {
+  double* y;
+  const double* x;
+  const double* colw;
+  const double* tele;
+  double bs, s, t, c_uniform;  // bs = beta * s, formed once per thread
+  __device__ __forceinline__ void emit(int row, double sum, double* red) const {
+    const double c = tele ? mul_rn(t, tele[row]) : c_uniform;
+    const double yn = fma_rn(bs, sum, c);
+    red[0] = add_rn(red[0], fabs(fma_rn(-x[row], s, yn)));
+    red[1] = add_rn(red[1], yn);
+    red[2] = fma_rn(colw[row], yn, red[2]);
+    y[row] = yn;
+  }
+};
+
+// t of the next step from its S (r1) and M (r2): 1 - (beta * M) / S.
+__device__ __forceinline__ double teleport_weight(double beta, double s1, double m) {
+  return add_rn(1.0, -mul_rn(mul_rn(beta, m), s1));
+}
+
+// The last CTA's step: the next coefficients from the sums r = {L1 change,
+// S, M}, the iteration count and the done flag.
+struct PageRankFinish {
+  double beta, eps;
+  double* coef_out;
+  int* done;
+  int* iters;
+  static __device__ __forceinline__ PageRankFinish of(const PageRankArgs& p) {
+    return PageRankFinish{p.beta, p.eps, p.coef_out, p.done, p.iters};
+  }
+  __device__ __forceinline__ void operator()(const double* r) const {
+    const double s1 = 1.0 / r[1];
+    coef_out[0] = s1;
+    coef_out[1] = teleport_weight(beta, s1, r[2]);
+    *iters += 1;
+    if (r[0] < eps) *done = 1;
+  }
+};
+
 }  // namespace csr
 }  // namespace tbsla_gpu

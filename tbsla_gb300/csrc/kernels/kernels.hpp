@@ -155,6 +155,12 @@ struct PageRankArgs {
 };
 cudaError_t csr_pagerank_step(const CsrArgs& a, const double* x, double* y,
                               const PageRankArgs& p, Ctl ctl, int grid, cudaStream_t s);
+// One PageRank step on the sliced-ELL layout of a single column block (one
+// plan, no row parts): y = the next iterate, its sums reduced in a fixed
+// order, as csr_pagerank_step; ctl.partials holds 3 doubles for each of up
+// to 8 CTAs per SM.  cudaErrorInvalidValue for a plan of several blocks.
+cudaError_t sell_pagerank(const SellArgs& a, const double* x, double* y, const PageRankArgs& p, Ctl ctl,
+                          cudaStream_t s);
 // Batched personalised PageRank step: X, Y, T are n x nvec row-major
 // (nvec <= 32); column k as above with s_k = coef_in[k], t_k =
 // coef_in[32 + k] and c_i = t_k * T[i, k].  Reductions per column k:
@@ -298,9 +304,20 @@ cudaError_t ell_spmv(const void* vals, int prec, const int* cols, int ln_row, in
                      int f_col, const double* x, double* y, cudaStream_t s);
 
 // ---- COO / SCOO (row-sorted device copy, reduce-by-key) ----------------------
-// y[row + row_off] += sum of vals * x[col + col_off] over entries of that row.
+// Triplets per warp chunk, and the carry scratch of a launch: per chunk the
+// partial sums of its first / last row when that row crosses into a
+// neighbouring chunk, and flags (int).
+constexpr int kCooChunk = 256;
+inline long coo_chunks(long nnz) { return (nnz + kCooChunk - 1) / kCooChunk; }
+struct CooCarry {
+  double* head;  // [chunks]
+  double* tail;  // [chunks]
+  int* flags;    // [chunks]
+};
+// y[row + row_off] += sum of vals * x[col + col_off] over entries of that
+// row: one addition per row, the same from run to run.
 cudaError_t coo_spmv(const void* vals, int prec, const int* rows, const int* cols, long nnz,
-                     int row_off, int col_off, const double* x, double* y, cudaStream_t s);
+                     int row_off, int col_off, const double* x, double* y, const CooCarry& cc, cudaStream_t s);
 
 // ---- DENSE (row-major GEMV, accumulating) -------------------------------------
 cudaError_t dense_gemv(const void* vals, int prec, int ln_row, int ln_col, const double* x,

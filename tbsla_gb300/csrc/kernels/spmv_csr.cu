@@ -51,35 +51,6 @@ __global__ void __launch_bounds__(NT) k_csr_spmv(CsrArgs a, const double* __rest
   csr_block<V, ITEMS>(a, blockIdx.x, x, epi, nullptr, stage, sm, pol);
 }
 
-// x is used normalised by its sum S (scale s = 1/S, carried from the
-// previous step): y_i = (beta * (A x)_i) * s + c_i with c_i = t / n or
-// t * tele_i and t = 1 - (beta * M) * s, M = sum_j w_j x_j (w = column sums
-// of A as stored), so that y sums to 1.  Reductions: L1 change, sum y and
-// sum w y (the next step's S and M).
-// Four FP64 operations per row (GB300's FP64 pipe is the epilogue's
-// bound): yn = fma(beta s, sum, c), the change fma(-x, s, yn), S += yn,
-// M = fma(w, yn, M).
-struct EpiPageRank {
-  double* y;
-  const double* x;
-  const double* colw;
-  const double* tele;
-  double bs, s, t, c_uniform;  // bs = beta * s, formed once per thread
-  __device__ __forceinline__ void emit(int row, double sum, double* red) const {
-    const double c = tele ? mul_rn(t, tele[row]) : c_uniform;
-    const double yn = fma_rn(bs, sum, c);
-    red[0] = add_rn(red[0], fabs(fma_rn(-x[row], s, yn)));
-    red[1] = add_rn(red[1], yn);
-    red[2] = fma_rn(colw[row], yn, red[2]);
-    y[row] = yn;
-  }
-};
-
-// t of the next step from its S (r1) and M (r2): 1 - (beta * M) / S.
-__device__ __forceinline__ double teleport_weight(double beta, double s1, double m) {
-  return add_rn(1.0, -mul_rn(mul_rn(beta, m), s1));
-}
-
 template <class V, int ITEMS>
 __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __restrict__ x,
                                                     double* __restrict__ y, PageRankArgs p,
@@ -93,17 +64,7 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank(CsrArgs a, const double* __
   double red[3] = {0, 0, 0};
   for (int b = next_block(ctl, sm); b < a.nblocks; b = next_block(ctl, sm))
     csr_block<V, ITEMS>(a, b, x, epi, red, stage, sm, pol);
-  const double beta = p.beta, eps = p.eps;
-  double* coef_out = p.coef_out;
-  int* done = p.done;
-  int* iters = p.iters;
-  reduce_and_finish<3>(ctl, red, sm, [=] __device__(double* r) {
-    const double s1 = 1.0 / r[1];
-    coef_out[0] = s1;
-    coef_out[1] = teleport_weight(beta, s1, r[2]);
-    *iters += 1;
-    if (r[0] < eps) *done = 1;
-  });
+  reduce_and_finish<3>(ctl, red, sm, PageRankFinish::of(p));
 }
 
 // PageRank epilogue over a separately computed t = A x: the EpiPageRank
@@ -119,17 +80,7 @@ __global__ void __launch_bounds__(NT) k_pagerank_epilogue(const double* __restri
   double red[3] = {0, 0, 0};
   for (long i = blockIdx.x * (long)NT + threadIdx.x; i < n; i += (long)gridDim.x * NT)
     epi.emit((int)i, t[i], red);
-  const double beta = p.beta, eps = p.eps;
-  double* coef_out = p.coef_out;
-  int* done = p.done;
-  int* iters = p.iters;
-  reduce_and_finish<3>(ctl, red, sm, [=] __device__(double* r) {
-    const double s1 = 1.0 / r[1];
-    coef_out[0] = s1;
-    coef_out[1] = teleport_weight(beta, s1, r[2]);
-    *iters += 1;
-    if (r[0] < eps) *done = 1;
-  });
+  reduce_and_finish<3>(ctl, red, sm, PageRankFinish::of(p));
 }
 
 // The end of a batched PageRank step: per-column CTA sums over warps (in

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "csr_block.cuh"
 #include "host/parallel.hpp"
 #include "kernels.hpp"
 
@@ -174,28 +175,52 @@ struct Claims {
 
 // One column block: y = A_block x (block 0) or y += A_block x (later blocks,
 // whose plans leave out the rows without entries in the block).
-template <class V, int U>
+//
+// PR: a one-block plan runs the PageRank step's epilogue (EpiPageRank) on
+// each row as it is summed, instead of writing A x for a separate pass: the
+// head lane of a row forms the new iterate and adds its terms of the three
+// sums in registers.  For a fixed order of those sums the slices are then
+// dealt to the warps statically (warp w takes w, w + W, ...: the plan's
+// widest-first order interleaves evenly), the CTA partials are summed in
+// CTA order by the last CTA to finish (csr::reduce_and_finish), and the
+// launch grid is fixed by the plan and the occupancy, so every step of a
+// solve adds its terms in the same order.  The FP64 operations of the
+// epilogue then overlap the gathers of x instead of running in a pass of
+// their own that GB300's FP64 pipe bounds.
+template <class V, int U, bool PR>
 __global__ void __launch_bounds__(NT) k_sell(SellPlan p, const V* __restrict__ sv, const int* __restrict__ sc,
                                             int f_col, int accumulate, const double* __restrict__ x,
                                             double* __restrict__ y, unsigned* __restrict__ counter,
-                                            const int* __restrict__ done) {
+                                            const int* __restrict__ done, PageRankArgs pr, Ctl ctl) {
   // a set done flag (an iteration that has converged) makes the launch a
   // no-op; no warp has touched the counters then
   if (done && *(volatile const int*)done) return;
   const int lane = threadIdx.x & 31;
   const int nitems = p.nslices;
   const uint64_t pol = policy_evict_first();
+  double red[3] = {0, 0, 0};
+  csr::EpiPageRank epi{};
+  if constexpr (PR) {
+    const double s = pr.coef_in[0], t = pr.coef_in[1];
+    epi = csr::EpiPageRank{y, x, pr.colw, pr.tele, mul_rn(pr.beta, s), s, t, t / pr.n_nodes};
+  }
   // Two items are claimed ahead, and the descriptor of the next one is
   // loaded while the current one runs, so neither the work counters'
   // atomics nor the descriptor loads sit on the critical path.
-  Claims cl{counter, nitems, (int)((blockIdx.x * (NT / 32) + (threadIdx.x >> 5)) % kQueues), kQueues - 1};
+  const int warp = blockIdx.x * (NT / 32) + (threadIdx.x >> 5), nwarps = gridDim.x * (NT / 32);
+  Claims cl{counter, nitems, warp % kQueues, kQueues - 1};
   int cur = 0, nxt = 0;
-  if (lane == 0) {
-    cur = cl.resolve(cl.ticket());
-    nxt = cl.resolve(cl.ticket());
+  if constexpr (PR) {
+    cur = warp;
+    nxt = warp + nwarps;
+  } else {
+    if (lane == 0) {
+      cur = cl.resolve(cl.ticket());
+      nxt = cl.resolve(cl.ticket());
+    }
+    cur = __shfl_sync(FULL, cur, 0);
+    nxt = __shfl_sync(FULL, nxt, 0);
   }
-  cur = __shfl_sync(FULL, cur, 0);
-  nxt = __shfl_sync(FULL, nxt, 0);
   int4 d = make_int4(0, 0, 0, 0);
   int meta = -1;
   if (cur < nitems) {
@@ -204,7 +229,7 @@ __global__ void __launch_bounds__(NT) k_sell(SellPlan p, const V* __restrict__ s
   }
   while (cur < nitems) {
     int after = 0;
-    if (lane == 0) after = cl.ticket();
+    if (!PR && lane == 0) after = cl.ticket();
     int4 dn = make_int4(0, 0, 0, 0);
     int mn = -1;
     if (nxt < nitems) {
@@ -213,15 +238,26 @@ __global__ void __launch_bounds__(NT) k_sell(SellPlan p, const V* __restrict__ s
     }
     const Lane l = slice_lane(p, d, meta, cur, lane);
     const bool head = l.row >= 0 && (lane & ((1 << d.z) - 1)) == 0;
-    const double y0 = (accumulate && head) ? y[l.row] : 0.0;  // issued before the sum
+    const double y0 = (!PR && accumulate && head) ? y[l.row] : 0.0;  // issued before the sum
     double acc = slice_rows<V, U>(sv, sc, (long)d.x * 32 + lane, l.steps, d.y, x, f_col, pol);
     for (int o = (1 << d.z) >> 1; o > 0; o >>= 1) acc = add_rn(acc, __shfl_xor_sync(FULL, acc, o));
-    if (head) y[l.row] = accumulate ? add_rn(y0, acc) : acc;
-    if (lane == 0) after = cl.resolve(after);
-    cur = nxt;
-    nxt = __shfl_sync(FULL, after, 0);
+    if constexpr (PR) {
+      if (head) epi.emit(l.row, acc, red);
+      cur = nxt;
+      nxt += nwarps;
+    } else {
+      if (head) y[l.row] = accumulate ? add_rn(y0, acc) : acc;
+      if (lane == 0) after = cl.resolve(after);
+      cur = nxt;
+      nxt = __shfl_sync(FULL, after, 0);
+    }
     d = dn;
     meta = mn;
+  }
+  if constexpr (PR) {
+    __shared__ csr::Smem sm;
+    csr::reduce_and_finish<3>(ctl, red, sm, csr::PageRankFinish::of(pr));
+    return;
   }
   // The last warp to finish resets the work counters for the next launch:
   // every warp's claims were answered before it counts itself out here.
@@ -279,7 +315,7 @@ cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* coun
   int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V, U>, NT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V, U, false>, NT, 0);
   const int grid = std::max(1, sms * std::max(1, per));
   const bool fork = a.side && a.parts > 1 && a.nblocks >= a.parts;
   const int first_part = a.nblocks - a.parts;
@@ -296,8 +332,8 @@ cudaError_t launch(const SellArgs& a, const double* x, double* y, unsigned* coun
     if (e == cudaSuccess && k > 0) e = cudaStreamWaitEvent(ls, a.fork, 0);
     if (e == cudaSuccess && a.ready && b > 0) e = cudaStreamWaitEvent(ls, a.ready[b], 0);
     if (e == cudaSuccess && p.nslices > 0) {
-      k_sell<V, U><<<pg, NT, 0, ls>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0, x, y,
-                                      counter + k * kSellCounterRegion, done);
+      k_sell<V, U, false><<<pg, NT, 0, ls>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, b > 0 ? 1 : 0,
+                                             x, y, counter + k * kSellCounterRegion, done, PageRankArgs{}, Ctl{});
       e = cudaGetLastError();
     }
     // recorded for an empty plan too: the event then marks the earlier plans
@@ -325,6 +361,33 @@ cudaError_t launch_fill(const SellArgs& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+// The PageRank step over a one-block plan (k_sell with PR): grid = the
+// resident CTAs (at most 8 per SM), fewer for a small plan.
+template <class V, int U>
+cudaError_t launch_pr(const SellArgs& a, const double* x, double* y, const PageRankArgs& pr, Ctl ctl,
+                      cudaStream_t s) {
+  if (a.nblocks != 1 || a.parts != 1) return cudaErrorInvalidValue;
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sell<V, U, true>, NT, 0);
+  const SellPlan& p = a.blocks[0];
+  const int grid = std::max(1, std::min(sms * std::max(1, std::min(per, 8)), (p.nslices + NT / 32 - 1) / (NT / 32)));
+  k_sell<V, U, true><<<grid, NT, 0, s>>>(p, static_cast<const V*>(a.svals), a.scols, a.f_col, 0, x, y, nullptr,
+                                         pr.done, pr, ctl);
+  return cudaGetLastError();
+}
+
+template <class V>
+cudaError_t launch_pr_u(const SellArgs& a, const double* x, double* y, const PageRankArgs& pr, Ctl ctl,
+                        cudaStream_t s) {
+  switch (a.unroll) {
+    case 4: return launch_pr<V, 4>(a, x, y, pr, ctl, s);
+    case 16: return launch_pr<V, 16>(a, x, y, pr, ctl, s);
+    default: return launch_pr<V, 8>(a, x, y, pr, ctl, s);
+  }
 }
 
 template <class V>
@@ -467,6 +530,16 @@ cudaError_t sell_spmv(const SellArgs& a, const double* x, double* y, unsigned* c
     case kF64: return launch_u<double>(a, x, y, counter, done, s);
     case kF32: return launch_u<float>(a, x, y, counter, done, s);
     case kBF16: return launch_u<__nv_bfloat16>(a, x, y, counter, done, s);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t sell_pagerank(const SellArgs& a, const double* x, double* y, const PageRankArgs& p, Ctl ctl,
+                          cudaStream_t s) {
+  switch (a.prec) {
+    case kF64: return launch_pr_u<double>(a, x, y, p, ctl, s);
+    case kF32: return launch_pr_u<float>(a, x, y, p, ctl, s);
+    case kBF16: return launch_pr_u<__nv_bfloat16>(a, x, y, p, ctl, s);
   }
   return cudaErrorInvalidValue;
 }

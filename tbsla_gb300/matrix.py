@@ -280,6 +280,11 @@ class MatrixCSR(Matrix):
         warp, 8 or 16."""
         check(lib.tbsla_matrix_set_pagerank_gather(self._h, int(gather)), "set_pagerank_gather")
 
+    def set_pagerank_fused(self, fused: bool):
+        """PageRank on the sliced-ELL kernel with one column block: the step's
+        epilogue inside the SpMV launch (True, default) or a pass of its own."""
+        check(lib.tbsla_matrix_set_pagerank_fused(self._h, int(bool(fused))), "set_pagerank_fused")
+
     def set_sell_params(self, short_thr: int = 0, long_thr: int = 0, sigma: int = 16384, col_block: int = 0):
         """Sliced-ELL layout thresholds (0: automatic), window and column
         block (0: 8,388,608 columns)."""

@@ -449,3 +449,33 @@ def test_autotune_keeps_the_fastest_and_stays_exact(gpu):
     ref = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x, threads=True)
     scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x)
     assert oracle.rel_err_normalized(y, ref, scale) <= TOL
+
+
+def test_coo_scoo_run_to_run_identical(gpu):
+    """COO / SCOO add each row's sum to r once per call: rows crossing warp
+    chunks (power-law rows of up to 4096 triplets span up to 17 chunks of
+    256) are finished by the carry pass in chunk order, so repeated calls
+    give the same bits.  Also within the FP64 tolerance of the oracle, with
+    r accumulated onto a non-zero start and a shifted SCOO block."""
+    T = gpu
+    n = 1 << 17
+    csr = powerlaw(T, n, seed=12, max_len=4096)
+    a = csr.arrays()
+    rows = np.repeat(np.arange(n, dtype=np.int32), np.diff(a["rowptr"]))
+    coo = T.MatrixCOO.from_arrays(n, n, rows, a["colidx"], a["values"])
+    x = T.fill_uniform(n, 0.0, 1.0, 6)
+    r0 = T.fill_uniform(n, -1.0, 1.0, 7)
+    outs = []
+    for _ in range(3):
+        r = r0.copy()
+        coo.Ax(r, x)
+        outs.append(r)
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    ref = oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x, threads=True)
+    scale = oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x) + np.abs(r0)
+    assert oracle.rel_err_normalized(outs[0], r0 + ref, scale) <= TOL
+    scoo = T.MatrixSCOO(coo)
+    s1 = scoo.spmv(x)
+    s2 = scoo.spmv(x)
+    assert np.array_equal(s1, s2)
+    assert oracle.rel_err_normalized(s1, ref, oracle.csr_absrow(a["rowptr"], a["colidx"], a["values"], x)) <= TOL
