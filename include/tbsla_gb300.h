@@ -219,6 +219,12 @@ int tbsla_matrix_set_sell_params(tbsla_matrix* m, int short_thr, int long_thr, i
 /* Batched personalised PageRank with FP32 / BF16 values: gathers of X rows
  * in flight per warp, 8 (default) or 16; a tuning choice, same results. */
 int tbsla_matrix_set_pagerank_gather(tbsla_matrix* m, int gather);
+/* Batched PageRank with FP32 / BF16 values: 1 (default) a warp takes a
+ * whole row block and walks its entries as one stream, `gather` X rows in
+ * flight across row boundaries; 0 a warp per row.  The same Y bit for bit
+ * (each row sums in entry order either way); the norms' partial sums are
+ * added in another order.  No reference counterpart. */
+int tbsla_matrix_set_pagerank_stream(tbsla_matrix* m, int stream);
 /* PageRank with the sliced-ELL kernel and one column block: 1 (default)
  * runs each step's epilogue -- the new iterate and its three FP64 sums --
  * inside the SpMV launch; 0 writes A x and runs the epilogue as a pass of

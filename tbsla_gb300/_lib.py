@@ -108,6 +108,7 @@ _SIGS = {
     "tbsla_matrix_set_sell_params": (I, [P, I, I, I, I]),
     "tbsla_matrix_set_pagerank_gather": (I, [P, I]),
     "tbsla_matrix_set_pagerank_fused": (I, [P, I]),
+    "tbsla_matrix_set_pagerank_stream": (I, [P, I]),
     "tbsla_matrix_autotune": (I, [P, I, C.POINTER(Tuning), C.POINTER(Tuning), I, IP]),
     "tbsla_batch_create": (I, [C.POINTER(P), C.POINTER(P), I, I]),
     "tbsla_batch_destroy": (I, [P]),

@@ -9,7 +9,9 @@ wall clock, the fastest kept):
 * batched CG on the persistent engine (``tune_batch_cg``): rows per thread
   (4, with 16-byte loads, or 1) and rows per work chunk;
 * batched personalised PageRank with FP32 / BF16 values
-  (``tune_pagerank_batched``): X-row gathers in flight per warp (8 or 16).
+  (``tune_pagerank_batched``): X-row gathers in flight per warp (8 or 16)
+  and rows per warp (one at a time, or a whole row block walked as one
+  entry stream).
 
 The cache is one JSON file (``TBSLA_TUNE_CACHE``, else
 ``~/.cache/tbsla_gb300/tune.json``) mapping a key -- the workload kind, the
@@ -184,26 +186,32 @@ def pagerank_key(m, precision: int, nvec: int) -> str:
                f"nvec{nvec}")
 
 
+def apply_pagerank_batched(m, cfg: dict) -> None:
+    m.set_pagerank_gather(cfg["gather"])
+    m.set_pagerank_stream(bool(cfg.get("stream", 1)))
+
+
 def tune_pagerank_batched(m, teleport, precision: int, iters: int = 6, reps: int = 3, path: str | None = None,
                           force: bool = False) -> dict:
-    """X-row gathers in flight per warp (8 or 16) of batched PageRank, timed
-    on `iters` power steps of this graph (epsilon 0: exactly that many)."""
+    """X-row gathers in flight per warp (8 or 16) and the rows-per-warp form
+    of batched PageRank, timed on `iters` power steps of this graph (epsilon
+    0: exactly that many)."""
     nvec = teleport.shape[1]
     k = pagerank_key(m, precision, nvec)
     hit = None if force else lookup(k, path)
     if hit is not None:
-        m.set_pagerank_gather(hit["settings"]["gather"])
+        apply_pagerank_batched(m, hit["settings"])
         return dict(hit, cached=True, key=k)
-    candidates = [{"gather": g} for g in (8, 16)]
+    candidates = [{"gather": g, "stream": s} for s in (1, 0) for g in (8, 16)]
 
     def timer(cfg):
-        m.set_pagerank_gather(cfg["gather"])
+        apply_pagerank_batched(m, cfg)
         run = lambda: m.page_rank_batched(teleport, 0.85, 0.0, iters)  # noqa: E731
         run()
         return _median_time(run, reps)
 
     best, trials = pick(candidates, timer)
-    m.set_pagerank_gather(best["gather"])
+    apply_pagerank_batched(m, best)
     entry = {"settings": best, "iterations": iters,
              "trials": [{"settings": c, "ms_per_iteration": t * 1e3 / iters} for c, t in trials]}
     store(k, entry, path)

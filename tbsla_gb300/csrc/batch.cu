@@ -98,6 +98,7 @@ struct tbsla_batch {
   long* sys_off = nullptr;
   int* row_sys = nullptr;
   int *dchunks = nullptr, *dchunk_sys = nullptr;  // the persistent engine's work chunks
+  int* dsys_chunk = nullptr;                       // [nsys + 1] first chunk of each system
   int ndchunks = 0;
   long chunk_rows = 0;            // rows per work chunk
   void* avals_dia = nullptr;      // [K][n] storage precision
@@ -134,7 +135,8 @@ struct tbsla_batch {
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
                   scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf,
                   ldelta, tdelta, zf, adelta, sys_off, row_sys, a64_dia, dinv_f, fdelta, lvals_dia,
-                  dv, r0, r1, p0, p1, q2, z2, t2, mode_d, fallback_d, relres_d, acc, bar, dchunks, dchunk_sys};
+                  dv, r0, r1, p0, p1, q2, z2, t2, mode_d, fallback_d, relres_d, acc, bar, dchunks, dchunk_sys,
+                  dsys_chunk};
     for (void* v : ps)
       if (v) cudaFree(v);
     if (avals_dia && avals_dia != (void*)a64_dia) cudaFree(avals_dia);
@@ -268,21 +270,27 @@ cudaError_t dia_chunks(tbsla_batch* B, long rows) {
     rows = n / ((long)sms * 3 * 8);
     rows = std::min<long>(4096, std::max<long>(1024, (rows + 255) / 256 * 256));
   }
-  std::vector<int> ch{0}, chs;
-  for (int s = 0; s < B->nsys; s++)
+  std::vector<int> ch{0}, chs, sc;
+  for (int s = 0; s < B->nsys; s++) {
+    sc.push_back((int)chs.size());
     for (long r0 = B->off[s]; r0 < B->off[s + 1]; r0 += rows) {
       ch.push_back((int)std::min<long>(B->off[s + 1], r0 + rows));
       chs.push_back(s);
     }
+  }
+  sc.push_back((int)chs.size());
   if (B->dchunks) cudaFree(B->dchunks);
   if (B->dchunk_sys) cudaFree(B->dchunk_sys);
-  B->dchunks = B->dchunk_sys = nullptr;
+  if (B->dsys_chunk) cudaFree(B->dsys_chunk);
+  B->dchunks = B->dchunk_sys = B->dsys_chunk = nullptr;
   B->ndchunks = (int)chs.size();
   B->chunk_rows = rows;
   cudaError_t e;
   if ((e = alloc(&B->dchunks, ch.size())) || (e = alloc(&B->dchunk_sys, std::max<size_t>(chs.size(), 1))) ||
       (e = cudaMemcpyAsync(B->dchunks, ch.data(), ch.size() * 4, cudaMemcpyHostToDevice, st)) ||
-      (e = cudaMemcpyAsync(B->dchunk_sys, chs.data(), chs.size() * 4, cudaMemcpyHostToDevice, st)))
+      (e = cudaMemcpyAsync(B->dchunk_sys, chs.data(), chs.size() * 4, cudaMemcpyHostToDevice, st)) ||
+      (e = alloc(&B->dsys_chunk, sc.size())) ||
+      (e = cudaMemcpyAsync(B->dsys_chunk, sc.data(), sc.size() * 4, cudaMemcpyHostToDevice, st)))
     return e;
   return cudaStreamSynchronize(st);
 }
@@ -549,6 +557,7 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   c.sys_off = B->sys_off;
   c.chunks = B->dchunks;
   c.chunk_sys = B->dchunk_sys;
+  c.sys_chunk = B->dsys_chunk;
   c.nchunks = B->ndchunks;
   c.adelta = B->adelta;
   c.avals = B->avals_dia;

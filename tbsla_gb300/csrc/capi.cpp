@@ -282,6 +282,12 @@ int tbsla_matrix_set_pagerank_gather(tbsla_matrix* m, int gather) {
   return TBSLA_OK;
 }
 
+int tbsla_matrix_set_pagerank_stream(tbsla_matrix* m, int stream) {
+  if (!m || (stream != 0 && stream != 1)) return TBSLA_ERR_INVALID_ARG;
+  m->pr_stream = stream;  // a launch choice: the device copy stays
+  return TBSLA_OK;
+}
+
 int tbsla_matrix_set_pagerank_fused(tbsla_matrix* m, int fused) {
   if (!m || (fused != 0 && fused != 1)) return TBSLA_ERR_INVALID_ARG;
   m->pr_fused = fused;  // a launch choice: the device copy stays

@@ -75,6 +75,7 @@ struct tbsla_matrix {
   int sell_unroll = 0;     // steps per lane in flight (0: 8)
   int sell_colblock = 0;   // columns per block (0: 8,388,608 = 64 MiB of x)
   int pr_gather = 8;       // batched PageRank (FP32 / BF16 values): X-row gathers in flight per warp, 8 or 16
+  int pr_stream = 1;       // batched PageRank (FP32 / BF16 values): 1 a warp walks a row block's entries as one stream, 0 a warp per row
   int pr_fused = 1;        // PageRank on the sliced-ELL kernel: epilogue inside the SpMV (1) or a pass of its own (0)
   int device = 0;
   mutable tbsla_impl::DeviceMatrix* dev = nullptr;

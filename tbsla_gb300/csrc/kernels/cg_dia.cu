@@ -214,13 +214,22 @@ struct WarpSums {
   }
 };
 
-// Chunks are dealt to CTAs in runs of `run` consecutive chunks (so a CTA
-// rarely changes system within a phase; up to 4, fewer when the batch has
-// too few chunks to give every CTA a run), runs round-robin over the grid.
+// A phase works on the chunks of the systems it selects (SELECT: the
+// systems in a given state).  Only those chunks are dealt out, in runs of up
+// to 4 consecutive ones (so a CTA rarely changes system within a phase;
+// fewer when there are too few to give every CTA a run), runs round-robin
+// over the grid: when systems drop out, every CTA still gets an even share
+// of the rest instead of the CTAs that held the finished systems idling.
+// Every CTA computes the same selection from its own copy of the states.
 constexpr int kRunMax = 4;
-#define FOR_CHUNKS(ch)                                                                         \
-  for (int run_ = blockIdx.x * run; run_ < c.nchunks; run_ += gridDim.x * run)               \
-    for (int ch = run_, end_ = min(run_ + run, c.nchunks); ch < end_; ch++)
+#define SELECT(cond)                        \
+  select_sys([&](int s_) { return (cond); }); \
+  const int nsel_ = s_nsel;                 \
+  const int runs_ = max(1, min(kRunMax, nsel_ / (4 * (int)gridDim.x)))
+#define FOR_CHUNKS(ch)                                                          \
+  for (int k0_ = blockIdx.x * runs_; k0_ < nsel_; k0_ += gridDim.x * runs_) \
+    for (int k_ = k0_, ke_ = min(k0_ + runs_, nsel_); k_ < ke_; k_++)        \
+      for (int ch = sel_chunk(k_), once_ = 1; once_; once_ = 0)
 
 // L2 prefetch of rows [r0, r1) of an array by the TMA unit: one bulk
 // prefetch instruction (16-byte aligned start, whole 16-byte units inside
@@ -243,6 +252,9 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       s_prev[kDiaMaxSys], s_rzj[kDiaMaxSys];
   __shared__ int s_st[kDiaMaxSys], s_mode[kDiaMaxSys], s_it[kDiaMaxSys], s_since[kDiaMaxSys], s_fb[kDiaMaxSys];
   __shared__ int s_stop;
+  __shared__ int s_sc[kDiaMaxSys + 1];  // first chunk of each system, then the chunk count
+  __shared__ int s_end[kDiaMaxSys];     // selected chunks of systems 0..s
+  __shared__ int s_nsel;
   const int ns = c.nsys;
   const int tid = threadIdx.x;
   const long n = c.n;
@@ -261,8 +273,8 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
   T* __restrict__ Tt = static_cast<T*>(c.t);
   const float* __restrict__ dinv = c.dinv;
   const uint64_t pol = policy_evict_first();
-  const int run = max(1, min(kRunMax, c.nchunks / (4 * (int)gridDim.x)));
 
+  for (int s = tid; s <= ns; s += PNT) s_sc[s] = c.sys_chunk[s];
   for (int s = tid; s < ns; s += PNT) {
     s_st[s] = S_CHECK;
     s_mode[s] = c.mode[s];
@@ -292,6 +304,51 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     for (int s = tid; s < ns; s += PNT) f |= s_st[s] == st && (mode < 0 || s_mode[s] == mode);
     return __syncthreads_or(f) != 0;
   };
+  // s_end / s_nsel for the systems where pred(s) holds (warp 0: a scan over
+  // the systems, up to 8 per lane)
+  auto select_sys = [&](auto pred) {
+    __syncthreads();
+    if (tid < 32) {
+      const int per = (ns + 31) / 32, a0 = tid * per, a1 = min(a0 + per, ns);
+      int cnt = 0;
+      for (int s = a0; s < a1; s++)
+        if (pred(s)) cnt += s_sc[s + 1] - s_sc[s];
+      int incl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (tid >= o) incl += v;
+      }
+      int e = incl - cnt;
+      for (int s = a0; s < a1; s++) {
+        if (pred(s)) e += s_sc[s + 1] - s_sc[s];
+        s_end[s] = e;
+      }
+      if (tid == 31) s_nsel = incl;
+    }
+    __syncthreads();
+  };
+  // the k-th selected chunk: in the first system whose s_end exceeds k
+  auto sel_chunk = [&](int k) {
+    int lo = 0, hi = ns - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (s_end[mid] > k) hi = mid;
+      else lo = mid + 1;
+    }
+    return s_sc[lo + 1] - (s_end[lo] - k);
+  };
+  // rows [q0, q1) of the run after the one at k0 (in the system of its first
+  // chunk), for the L2 prefetch; false when this CTA has no further run
+  auto next_run = [&](int k0, int runs, int nsel, int& q0, int& q1, int& sn) {
+    const int kn = k0 + (int)gridDim.x * runs;
+    if (kn >= nsel) return false;
+    const int c0 = sel_chunk(kn), c1 = sel_chunk(min(kn + runs, nsel) - 1);
+    sn = c.chunk_sys[c0];
+    q0 = c.chunks[c0];
+    q1 = c.chunk_sys[c1] == sn ? c.chunks[c1 + 1] : (int)c.sys_off[sn + 1];
+    return true;
+  };
   auto load_deltas = [&](const int* tab, int s, int kk, int (&dd)[KMAX]) {
 #pragma unroll
     for (int k = 0; k < KMAX; k++) dd[k] = k < kk ? tab[s * KMAX + k] : 0;
@@ -303,6 +360,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       // R1: x += d (FP64), d = 0; at the start, check the factors
       clear_ahead();
       {
+        SELECT(s_st[s_] == S_CHECK);
         double* acc = slot(ph);
         WarpSums<float, 1> bad;
         FOR_CHUNKS(ch) {
@@ -341,6 +399,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       // Jacobi (or identity) z and r.z for a restart; p_old = 0
       clear_ahead();
       {
+        SELECT(s_st[s_] == S_CHECK);
         double* acc = slot(ph);
         T* __restrict__ Rn = R(g);
         T* __restrict__ Po = P(g);
@@ -416,6 +475,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
         // R3: t = L^T r (T arithmetic), r.z = t.t
         clear_ahead();
         {
+          SELECT(s_st[s_] == S_RESTART_F);
           double* acc = slot(ph);
           const T* __restrict__ Rc = R(g);
           WarpSums<T, 1> part;
@@ -463,6 +523,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
         // R4: p = L t
         clear_ahead();
         {
+          SELECT(s_st[s_] == S_RESTART_F);
           T* __restrict__ Po = P(g);
           FOR_CHUNKS(ch) {
             const int s = c.chunk_sys[ch];
@@ -500,6 +561,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     // A: q = A p, p.q
     clear_ahead();
     {
+      SELECT(s_st[s_] == S_ACTIVE);
       double* acc = slot(ph);
       WarpSums<T, 1> part;
       FOR_CHUNKS(ch) {
@@ -509,14 +571,12 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
         const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
         const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
         const bool fact = s_mode[s] == 2;
-        if (tid == 0 && ch == run_) {  // the next run's streams into L2 while this one runs
-          const int nx = run_ + gridDim.x * run;
-          if (nx < c.nchunks) {
-            const int q0 = c.chunks[nx], q1 = c.chunks[min(nx + run, c.nchunks)];
-            for (int k = 0; k < c.K; k++) prefetch_rows(A + (size_t)k * n, q0, q1);
-            prefetch_rows(Pold, q0, q1);
-            prefetch_rows(Z, q0, q1);
-          }
+        int q0, q1, sn;
+        if (tid == 0 && k_ == k0_ && next_run(k0_, runs_, nsel_, q0, q1, sn)) {
+          // the next run's streams into L2 while this one runs
+          for (int k = 0; k < c.K; k++) prefetch_rows(A + (size_t)k * n, q0, q1);
+          prefetch_rows(Pold, q0, q1);
+          prefetch_rows(Z, q0, q1);
         }
         int dd[KMAX];
         load_deltas(c.adelta, s, c.K, dd);
@@ -597,6 +657,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     clear_ahead();
     {
       double* acc = slot(ph);
+      SELECT(s_st[s_] == S_ACTIVE);
       const T* __restrict__ Ro = R(g);
       T* __restrict__ Rn = R(g + 1);
       WarpSums<T, 2> part;
@@ -607,20 +668,17 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
         const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
         const T alpha = (T)s_alpha[s];
         const int mode = s_mode[s];
-        if (tid == 0 && ch == run_) {
-          const int nx = run_ + gridDim.x * run;
-          if (nx < c.nchunks) {
-            const int q0 = c.chunks[nx], q1 = c.chunks[min(nx + run, c.nchunks)];
-            prefetch_rows(Ro, q0, q1);
-            prefetch_rows(Q, q0, q1);
-            prefetch_rows(D, q0, q1);
-            if (s_mode[c.chunk_sys[nx]] == 2) {
-              prefetch_rows(Pold, q0, q1);
-              for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
-            } else {
-              prefetch_rows(Pnew, q0, q1);
-              prefetch_rows(dinv, q0, q1);
-            }
+        int q0, q1, sn;
+        if (tid == 0 && k_ == k0_ && next_run(k0_, runs_, nsel_, q0, q1, sn)) {
+          prefetch_rows(Ro, q0, q1);
+          prefetch_rows(Q, q0, q1);
+          prefetch_rows(D, q0, q1);
+          if (s_mode[sn] == 2) {
+            prefetch_rows(Pold, q0, q1);
+            for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
+          } else {
+            prefetch_rows(Pnew, q0, q1);
+            prefetch_rows(dinv, q0, q1);
           }
         }
         if constexpr (sizeof(T) == 4) {
@@ -727,20 +785,18 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     if (any_state(S_ACTIVE, 2)) {
       // D: z = L t, p = z + beta p
       clear_ahead();
+      SELECT(s_st[s_] == S_ACTIVE && s_mode[s_] == 2);
       FOR_CHUNKS(ch) {
         const int s = c.chunk_sys[ch];
         if (s_st[s] != S_ACTIVE || s_mode[s] != 2) continue;
         const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
         const long lo = c.sys_off[s];
         const T beta = (T)s_beta[s];
-        if (tid == 0 && ch == run_) {
-          const int nx = run_ + gridDim.x * run;
-          if (nx < c.nchunks) {
-            const int q0 = c.chunks[nx], q1 = c.chunks[min(nx + run, c.nchunks)];
-            prefetch_rows(Tt, q0, q1);
-            prefetch_rows(Pold, q0, q1);
-            for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
-          }
+        int q0, q1, sn;
+        if (tid == 0 && k_ == k0_ && next_run(k0_, runs_, nsel_, q0, q1, sn)) {
+          prefetch_rows(Tt, q0, q1);
+          prefetch_rows(Pold, q0, q1);
+          for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
         }
         int ld[KMAX];
         load_deltas(c.ldelta, s, c.KL, ld);
@@ -788,6 +844,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
   }
 }
 #undef FOR_CHUNKS
+#undef SELECT
 
 // ---- layout builders ----------------------------------------------------------
 

@@ -169,9 +169,13 @@ cudaError_t sell_pagerank(const SellArgs& a, const double* x, double* y, const P
 // every column's change is < eps.
 // The same in double-float (pairs of floats h + l, about 46 bits) for FP32 /
 // BF16 values: X, Y, T (n x nvec) and W (the column sums, n) are float2
-// arrays of the same byte size as FP64 ones; reductions are FP64.
+// arrays of the same byte size as FP64 ones; reductions are FP64.  gather:
+// X-row gathers in flight per warp (8 or 16); stream: 0 a warp per row (the
+// CTA's warps take a block's rows in turn), 1 a warp per row block, its
+// entries walked as one stream across row boundaries.
 cudaError_t csr_pagerank_batched_df_step(const CsrArgs& a, int nvec, const void* X, void* Y, const void* T,
-                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, int gather, cudaStream_t s);
+                                         const void* W, const PageRankArgs& p, Ctl ctl, int grid, int gather,
+                                         int stream, cudaStream_t s);
 // FP64 <-> double-float (float2) conversions, element by element (the
 // destination may be the source's own storage).
 cudaError_t f64_to_df(const double* src, void* dst, long n, cudaStream_t s);
@@ -188,7 +192,7 @@ cudaError_t pagerank_epilogue(const double* t, const double* x, double* y, long 
 
 // CTAs of the persistent PageRank kernels (resident capacity of the GPU).
 int csr_pagerank_grid(int items, int prec);
-int csr_pagerank_batched_grid(int prec, int gather);
+int csr_pagerank_batched_grid(int prec, int gather, int stream);
 
 // ---- batched CG over a block-diagonal concatenation of systems -------------------
 // Per-system status: ACTIVE iterates; VERIFY has a recursive residual below
@@ -244,6 +248,7 @@ struct DiaCg {
   const long* sys_off;    // [nsys + 1] first row of each system
   const int* chunks;      // [nchunks + 1] row bounds of the work chunks (never across systems)
   const int* chunk_sys;   // [nchunks]
+  const int* sys_chunk;   // [nsys + 1] first chunk of each system (chunks are in system order)
   int nchunks;
   const int* adelta;      // [nsys * kDiaMaxDiag] col - row of each slot of A (padding: 0, value 0)
   const void* avals;      // [K][n] in `prec` (the iteration's A)

@@ -173,9 +173,25 @@ __global__ void __launch_bounds__(NT) k_coo_carry(const int* __restrict__ rows, 
   for (long c = blockIdx.x * (long)NT + threadIdx.x; c < nchunks; c += (long)gridDim.x * NT) {
     const int f = cc.flags[c];
     if (!(f & kHeadCont) || ((f & kOneRow) && (f & kTailCont))) continue;
+    // the nearest chunk before c that is not wholly inside the row (chunk 0
+    // never continues a row), 8 flags per round of loads
     long a = c - 1;
-    while ((cc.flags[a] & kOneRow) && (cc.flags[a] & kHeadCont)) a--;
+    for (;;) {
+      int f8[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) f8[k] = a - k >= 0 ? cc.flags[a - k] : 0;
+      int stop = -1;
+#pragma unroll
+      for (int k = 7; k >= 0; k--)
+        if (!((f8[k] & kOneRow) && (f8[k] & kHeadCont))) stop = k;
+      if (stop >= 0) {
+        a -= stop;
+        break;
+      }
+      a -= 8;
+    }
     double v = cc.tail[a];
+#pragma unroll 8
     for (long k = a + 1; k <= c; k++) v = add_rn(v, cc.head[k]);
     double* yr = y + rows[c * chunk_len] + row_off;
     *yr = add_rn(*yr, v);

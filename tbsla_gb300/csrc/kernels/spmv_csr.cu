@@ -215,6 +215,111 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int n
   batched_finish(df_val(err), df_val(sum), df_val(dsum), nvec, s_red, sm, p, ctl);
 }
 
+// The same step in an entry-stream form: each warp claims whole row blocks
+// of the partition and walks the block's entries as one stream, GB X-row
+// gathers in flight whatever the row boundaries, finishing each row (the
+// same epilogue) where its last entry is added.  Each row's products are
+// added in entry order with the same Dot2 steps as above, so Y is the same
+// bit for bit; only the order in which rows enter the norms' partial sums
+// differs.  Rows of a few entries (most rows of a power-law graph) then
+// share one gather latency instead of paying one each, and a row's
+// epilogue operands (T, X, w) are loaded when the previous row finishes.
+template <class V, int GB>
+__global__ void __launch_bounds__(NT) k_csr_pagerank_batched_dfs(CsrArgs a, int nvec, const float2* __restrict__ X,
+                                                                float2* __restrict__ Y, const float2* __restrict__ T,
+                                                                const float2* __restrict__ W, PageRankArgs p,
+                                                                Ctl ctl) {
+  __shared__ Smem sm;
+  __shared__ double s_red[NT / kWarp][3 * kWarp];
+  if (*(volatile int*)p.done) return;
+  constexpr unsigned full = 0xffffffffu;
+  const uint64_t pol = policy_evict_first();
+  const V* vals = static_cast<const V*>(a.vals);
+  const int lane = threadIdx.x % kWarp;
+  const bool active = lane < nvec;
+  const double scd = active ? p.coef_in[lane] : 0.0;
+  const DF sc = df_of(scd), tc = df_of(active ? p.coef_in[kWarp + lane] : 0.0), bsc = df_of(mul_rn(p.beta, scd));
+  DF err{0.f, 0.f}, sum{0.f, 0.f}, dsum{0.f, 0.f};
+  for (;;) {
+    int b = 0;
+    if (lane == 0) b = (int)atomicAdd(ctl.counter, 1u);
+    b = __shfl_sync(full, b, 0);
+    if (b >= a.nblocks) break;
+    const int r0 = a.blocks[b], r1 = a.blocks[b + 1];
+    const int s0 = a.rowptr[r0], e0 = a.rowptr[r1];
+    // ends of rows [rw, rw + 32): lane k holds rowptr[rw + k + 1]
+    int rw = r0;
+    int rpw = rw + 1 + lane <= r1 ? a.rowptr[rw + 1 + lane] : 0;
+    int row = r0;
+    int row_end = __shfl_sync(full, rpw, 0);
+    DF tn{0.f, 0.f}, xn{0.f, 0.f}, wn;
+    auto load_ops = [&](int r) {
+      if (active) {
+        const size_t o = (size_t)r * nvec + lane;
+        tn = df_ld(T + o);
+        xn = df_ld(X + o);
+      }
+      wn = df_ld(W + r);
+    };
+    load_ops(row);
+    float as = 0.f, ac = 0.f;
+    // the epilogue of `row`, then the next row's end and operands
+    auto finish = [&]() {
+      if (active) {
+        const DF acc = fast_two_sum(as, ac);
+        const DF yn = df_add(df_mul(bsc, acc), df_mul(tc, tn));
+        DF dx = df_add(yn, df_neg(df_mul(xn, sc)));
+        if (dx.h < 0) dx = df_neg(dx);
+        err = df_add(err, dx);
+        sum = df_add(sum, yn);
+        dsum = df_add(dsum, df_mul(wn, yn));
+        Y[(size_t)row * nvec + lane] = make_float2(yn.h, yn.l);
+      }
+      as = ac = 0.f;
+      row++;
+      if (row < r1) {
+        if (row - rw >= kWarp) {
+          rw += kWarp;
+          rpw = rw + 1 + lane <= r1 ? a.rowptr[rw + 1 + lane] : 0;
+        }
+        row_end = __shfl_sync(full, rpw, row - rw);
+        load_ops(row);
+      }
+    };
+    for (int base = s0; base < e0; base += kWarp) {
+      const int j = base + lane;
+      int c = 0;
+      float v = 0.f;
+      if (j < e0) {
+        c = ld_stream(a.colidx + j, pol);
+        v = as_f32(ld_stream(vals + j, pol));
+      }
+      const int m = min(kWarp, e0 - base);
+      for (int t = 0; t < m; t += GB) {
+        DF xv[GB];
+        float vv[GB];
+#pragma unroll
+        for (int u = 0; u < GB; u++) {
+          const bool live = t + u < m;
+          const int ct = __shfl_sync(full, c, (t + u) & (kWarp - 1));
+          const float vu = __shfl_sync(full, v, (t + u) & (kWarp - 1));
+          vv[u] = live ? vu : 0.f;
+          xv[u] = (active && live) ? df_ld(X + (size_t)(ct - a.f_col) * nvec + lane) : DF{0.f, 0.f};
+        }
+#pragma unroll
+        for (int u = 0; u < GB; u++) {
+          if (t + u < m) {
+            while (base + t + u >= row_end) finish();  // rows ending before this entry (empty ones too)
+            dot2_step(as, ac, vv[u], xv[u]);
+          }
+        }
+      }
+    }
+    while (row < r1) finish();  // the last row with entries and the empty rows after it
+  }
+  batched_finish(df_val(err), df_val(sum), df_val(dsum), nvec, s_red, sm, p, ctl);
+}
+
 __global__ void k_f64_to_df(const double* src, float2* dst, long n) {  // may run in place
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const DF v = df_of(src[i]);
@@ -389,14 +494,20 @@ int csr_pagerank_grid(int items, int prec) {
   return 152;
 }
 
-int csr_pagerank_batched_grid(int prec, int gather) {
+int csr_pagerank_batched_grid(int prec, int gather, int stream) {
   const bool wide = gather == 16;
   switch (prec) {
     case kF64: return resident_grid<k_csr_pagerank_batched<double>>();
     case kF32:
+      if (stream)
+        return wide ? resident_grid<k_csr_pagerank_batched_dfs<float, 16>>()
+                    : resident_grid<k_csr_pagerank_batched_dfs<float, 8>>();
       return wide ? resident_grid<k_csr_pagerank_batched_df<float, 16>>()
                   : resident_grid<k_csr_pagerank_batched_df<float, 8>>();
     case kBF16:
+      if (stream)
+        return wide ? resident_grid<k_csr_pagerank_batched_dfs<__nv_bfloat16, 16>>()
+                    : resident_grid<k_csr_pagerank_batched_dfs<__nv_bfloat16, 8>>();
       return wide ? resident_grid<k_csr_pagerank_batched_df<__nv_bfloat16, 16>>()
                   : resident_grid<k_csr_pagerank_batched_df<__nv_bfloat16, 8>>();
   }
@@ -405,20 +516,28 @@ int csr_pagerank_batched_grid(int prec, int gather) {
 
 cudaError_t csr_pagerank_batched_df_step(const CsrArgs& a, int nvec, const void* X, void* Y, const void* T,
                                          const void* W, const PageRankArgs& p, Ctl ctl, int grid, int gather,
-                                         cudaStream_t s) {
+                                         int stream, cudaStream_t s) {
   if (nvec < 1 || nvec > kWarp) return cudaErrorInvalidValue;
   const float2 *x = static_cast<const float2*>(X), *t = static_cast<const float2*>(T),
                *w = static_cast<const float2*>(W);
   float2* y = static_cast<float2*>(Y);
   const bool wide = gather == 16;
-  switch (a.prec) {
-    case kF32:
-      if (wide) k_csr_pagerank_batched_df<float, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
-      else k_csr_pagerank_batched_df<float, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+  switch (a.prec * 4 + (wide ? 2 : 0) + (stream ? 1 : 0)) {
+    case kF32 * 4 + 0: k_csr_pagerank_batched_df<float, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
+    case kF32 * 4 + 1: k_csr_pagerank_batched_dfs<float, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
+    case kF32 * 4 + 2: k_csr_pagerank_batched_df<float, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
+    case kF32 * 4 + 3: k_csr_pagerank_batched_dfs<float, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl); break;
+    case kBF16 * 4 + 0:
+      k_csr_pagerank_batched_df<__nv_bfloat16, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
       break;
-    case kBF16:
-      if (wide) k_csr_pagerank_batched_df<__nv_bfloat16, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
-      else k_csr_pagerank_batched_df<__nv_bfloat16, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+    case kBF16 * 4 + 1:
+      k_csr_pagerank_batched_dfs<__nv_bfloat16, 8><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+      break;
+    case kBF16 * 4 + 2:
+      k_csr_pagerank_batched_df<__nv_bfloat16, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
+      break;
+    case kBF16 * 4 + 3:
+      k_csr_pagerank_batched_dfs<__nv_bfloat16, 16><<<grid, NT, 0, s>>>(a, nvec, x, y, t, w, p, ctl);
       break;
     default: return cudaErrorInvalidValue;
   }

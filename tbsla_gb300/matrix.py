@@ -280,6 +280,12 @@ class MatrixCSR(Matrix):
         warp, 8 or 16."""
         check(lib.tbsla_matrix_set_pagerank_gather(self._h, int(gather)), "set_pagerank_gather")
 
+    def set_pagerank_stream(self, stream: bool):
+        """Batched PageRank (FP32 / BF16 values): a warp walks a whole row
+        block's entries as one stream (True, default) or takes one row at a
+        time."""
+        check(lib.tbsla_matrix_set_pagerank_stream(self._h, int(bool(stream))), "set_pagerank_stream")
+
     def set_pagerank_fused(self, fused: bool):
         """PageRank on the sliced-ELL kernel with one column block: the step's
         epilogue inside the SpMV launch (True, default) or a pass of its own."""

@@ -98,10 +98,11 @@ def test_batched_personalised_pagerank(gpu):
 
 def test_batched_pagerank_gather_width(gpu, tmp_path):
     """FP32-valued batched PageRank with 8 or 16 X-row gathers in flight per
-    warp: each row's products are added in the same entry order; only the
-    grid (the resident CTAs of each form) and so the order of the FP64
-    per-CTA partial sums of the norms differ.  Same iterations, vectors
-    within 1e-13 in L1; the autotuner picks one of the two and caches it."""
+    warp, a warp per row or a warp per row block (entry stream): each row's
+    products are added in the same entry order; only the grid and the rows
+    each warp takes, and so the order of the norms' partial sums, differ.
+    Same iterations, vectors within 1e-13 in L1, each form within 1e-10 of
+    the oracle; the autotuner picks one of the forms and caches it."""
     from tbsla_gb300 import autotune as A
 
     T = gpu
@@ -115,15 +116,25 @@ def test_batched_pagerank_gather_width(gpu, tmp_path):
     for k in range(nvec):
         tele[rng.choice(n, 50, replace=False), k] = 1.0 / 50
     out = []
-    for w in (8, 16):
-        g.set_pagerank_gather(w)
-        X, it, ok = g.page_rank_batched(tele, 0.85, 1e-10, 500)
-        assert ok
-        out.append((X, it))
-    assert out[0][1] == out[1][1]
-    assert np.abs(out[0][0] - out[1][0]).sum(axis=0).max() <= 1e-13
+    for stream in (False, True):
+        for w in (8, 16):
+            g.set_pagerank_stream(stream)
+            g.set_pagerank_gather(w)
+            X, it, ok = g.page_rank_batched(tele, 0.85, 1e-10, 500)
+            assert ok
+            out.append((X, it))
+    for X, it in out[1:]:
+        assert it == out[0][1]
+        assert np.abs(X - out[0][0]).sum(axis=0).max() <= 1e-13
+    a = g.arrays()
+    v32 = a["values"].astype(np.float32).astype(np.float64)
+    for k in (0, 7):
+        xr, _, _ = oracle.pagerank(a["rowptr"], a["colidx"], v32, 0.85, 1e-10, out[0][1], stop_early=False,
+                                   teleport=np.ascontiguousarray(tele[:, k]))
+        for X, _ in out:
+            assert np.abs(X[:, k] - xr).sum() <= 1e-10, k
     r = A.tune_pagerank_batched(g, tele, T.F32, iters=3, reps=1, path=str(tmp_path / "t.json"))
-    assert r["settings"]["gather"] in (8, 16) and not r["cached"]
+    assert r["settings"]["gather"] in (8, 16) and r["settings"]["stream"] in (0, 1) and not r["cached"]
     assert A.tune_pagerank_batched(g, tele, T.F32, path=str(tmp_path / "t.json"))["cached"]
 
 
