@@ -411,8 +411,16 @@ int tbsla_batch_set_rows_per_thread(tbsla_batch* b, int rows);
  * automatic, about 8 chunks per co-resident CTA within [1024, 4096]).
  * TBSLA_ERR_UNSUPPORTED for a batch on the multi-launch engine. */
 int tbsla_batch_set_chunk_rows(tbsla_batch* b, long rows);
-/* The persistent engine's current chunk rows and rows per thread. */
-int tbsla_batch_tuning(const tbsla_batch* b, long* chunk_rows, int* rows_per_thread);
+/* The persistent engine's current chunk rows, rows per thread and work
+ * dealing (the set_claim value, -1 for the size-based choice); any pointer
+ * may be NULL. */
+int tbsla_batch_tuning(const tbsla_batch* b, long* chunk_rows, int* rows_per_thread, int* claim);
+/* Work dealing of the persistent engine's phases: 1 every CTA claims its
+ * next run of chunks from a counter as it finishes one (balanced, an atomic
+ * round trip per run), 0 runs dealt round-robin, -1 (default) claimed when
+ * every CTA has at least 16 chunks.  Persistent engine only; results agree
+ * to the FP64 atomics' summation order. */
+int tbsla_batch_set_claim(tbsla_batch* b, int claim);
 /* The engine of the last tbsla_batch_cg: persistent = 1 when the whole solve
  * was one cooperative launch (every system's entries on at most 8 diagonals,
  * at most 256 systems, a factor, if used, on at most 8 diagonals), 0 for the

@@ -7,7 +7,8 @@ wall clock, the fastest kept):
   sliced-ELL thresholds, column blocks, steps in flight; merge path; row
   blocks), whose choice is cached here;
 * batched CG on the persistent engine (``tune_batch_cg``): rows per thread
-  (4, with 16-byte loads, or 1) and rows per work chunk;
+  (4, with 16-byte loads, or 1), rows per work chunk, and whether CTAs claim
+  their runs of chunks from a counter or take them round-robin;
 * batched personalised PageRank with FP32 / BF16 values
   (``tune_pagerank_batched``): X-row gathers in flight per warp (8 or 16)
   and rows per warp (one at a time, or a whole row block walked as one
@@ -146,6 +147,7 @@ def batch_key(batch, precision: int, precond: int) -> str:
 def apply_batch_cg(batch, cfg: dict) -> None:
     batch.set_rows_per_thread(cfg["rows_per_thread"])
     batch.set_chunk_rows(cfg["chunk_rows"])
+    batch.set_claim(cfg.get("claim", -1))
 
 
 def tune_batch_cg(batch, rhs, precision: int, precond: int = 1, iters: int = 30, reps: int = 3,
@@ -160,7 +162,8 @@ def tune_batch_cg(batch, rhs, precision: int, precond: int = 1, iters: int = 30,
         return dict(hit, cached=True, key=k)
     start = batch.tuning()
     rows_opts = (4, 1) if start["rows_per_thread"] == 4 else (1,)
-    candidates = [{"rows_per_thread": r, "chunk_rows": c} for r in rows_opts for c in (1024, 2048, 4096)]
+    candidates = [{"rows_per_thread": r, "chunk_rows": c, "claim": cl}
+                  for r in rows_opts for c in (1024, 2048, 4096) for cl in (0, 1)]
 
     def timer(cfg):
         apply_batch_cg(batch, cfg)
@@ -204,9 +207,11 @@ def tune_pagerank_batched(m, teleport, precision: int, iters: int = 6, reps: int
         return dict(hit, cached=True, key=k)
     candidates = [{"gather": g, "stream": s} for s in (1, 0) for g in (8, 16)]
 
+    out = np.empty(teleport.shape)
+
     def timer(cfg):
         apply_pagerank_batched(m, cfg)
-        run = lambda: m.page_rank_batched(teleport, 0.85, 0.0, iters)  # noqa: E731
+        run = lambda: m.page_rank_batched(teleport, 0.85, 0.0, iters, out=out)  # noqa: E731
         run()
         return _median_time(run, reps)
 

@@ -215,20 +215,23 @@ struct WarpSums {
 };
 
 // A phase works on the chunks of the systems it selects (SELECT: the
-// systems in a given state).  Only those chunks are dealt out, in runs of up
-// to 4 consecutive ones (so a CTA rarely changes system within a phase;
-// fewer when there are too few to give every CTA a run), runs round-robin
-// over the grid: when systems drop out, every CTA still gets an even share
-// of the rest instead of the CTAs that held the finished systems idling.
-// Every CTA computes the same selection from its own copy of the states.
+// systems in a given state); every CTA computes the same selection from its
+// own copy of the states, so none idles on finished systems.  Only those
+// chunks are handed out, in runs of up to 4 consecutive ones (so a CTA
+// rarely changes system within a phase; fewer when there are too few to
+// give every CTA several runs), either dealt round-robin (c.claim = 0) or
+// claimed from the phase's counter by each CTA as it finishes a run
+// (c.claim = 1: the CTAs end a phase together, at the cost of an atomic
+// round trip per run; a CTA holds one claim ahead).  The run after the
+// current one is prefetched into L2 either way.
 constexpr int kRunMax = 4;
 #define SELECT(cond)                        \
   select_sys([&](int s_) { return (cond); }); \
   const int nsel_ = s_nsel;                 \
   const int runs_ = max(1, min(kRunMax, nsel_ / (4 * (int)gridDim.x)))
-#define FOR_CHUNKS(ch)                                                          \
-  for (int k0_ = blockIdx.x * runs_; k0_ < nsel_; k0_ += gridDim.x * runs_) \
-    for (int k_ = k0_, ke_ = min(k0_ + runs_, nsel_); k_ < ke_; k_++)        \
+#define FOR_CHUNKS(ch)                                                                           \
+  for (int k0_ = first_run(runs_); k0_ < nsel_; k0_ = after_run(k0_, runs_))                      \
+    for (int k_ = k0_, ke_ = min(k0_ + runs_, nsel_); k_ < ke_; k_++)                         \
       for (int ch = sel_chunk(k_), once_ = 1; once_; once_ = 0)
 
 // L2 prefetch of rows [r0, r1) of an array by the TMA unit: one bulk
@@ -255,6 +258,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
   __shared__ int s_sc[kDiaMaxSys + 1];  // first chunk of each system, then the chunk count
   __shared__ int s_end[kDiaMaxSys];     // selected chunks of systems 0..s
   __shared__ int s_nsel;
+  __shared__ int s_claim[2];  // this CTA's current and next run of the phase
   const int ns = c.nsys;
   const int tid = threadIdx.x;
   const long n = c.n;
@@ -297,6 +301,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     if (blockIdx.x == 0) {
       double* a = slot(ph + 1);
       for (int t = tid; t < 4 * ns; t += PNT) a[t] = 0.0;
+      if (tid == 0) c.bar[32 * (1 + (ph + 1) % 3)] = 0u;
     }
   };
   auto any_state = [&](int st, int mode) {
@@ -338,10 +343,34 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     }
     return s_sc[lo + 1] - (s_end[lo] - k);
   };
-  // rows [q0, q1) of the run after the one at k0 (in the system of its first
-  // chunk), for the L2 prefetch; false when this CTA has no further run
+  // this CTA's runs of the phase: round-robin, or claimed from the counter
+  // of slot ph % 3 (in a line of its own)
+  const bool claim = c.claim != 0;
+  auto first_run = [&](int runs) {
+    if (!claim) return (int)blockIdx.x * runs;
+    __syncthreads();
+    if (tid == 0) {
+      unsigned* ctr = c.bar + 32 * (1 + ph % 3);
+      s_claim[0] = (int)atomicAdd(ctr, 1u);
+      s_claim[1] = (int)atomicAdd(ctr, 1u);
+    }
+    __syncthreads();
+    return s_claim[0] * runs;
+  };
+  auto after_run = [&](int k0, int runs) {
+    if (!claim) return k0 + (int)gridDim.x * runs;
+    __syncthreads();  // every thread is done with the current run
+    if (tid == 0) {
+      s_claim[0] = s_claim[1];
+      s_claim[1] = (int)atomicAdd(c.bar + 32 * (1 + ph % 3), 1u);
+    }
+    __syncthreads();
+    return s_claim[0] * runs;
+  };
+  // rows [q0, q1) of this CTA's next run after the one at k0 (in the system
+  // of its first chunk), for the L2 prefetch; false when it has none
   auto next_run = [&](int k0, int runs, int nsel, int& q0, int& q1, int& sn) {
-    const int kn = k0 + (int)gridDim.x * runs;
+    const int kn = claim ? s_claim[1] * runs : k0 + (int)gridDim.x * runs;
     if (kn >= nsel) return false;
     const int c0 = sel_chunk(kn), c1 = sel_chunk(min(kn + runs, nsel) - 1);
     sn = c.chunk_sys[c0];

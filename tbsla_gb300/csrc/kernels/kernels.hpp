@@ -267,12 +267,14 @@ struct DiaCg {
   int* fallback;          // [nsys] out: DiaFallback
   double* relres;         // [nsys] out: FP64 true relative residual at exit
   double* acc;            // [3][4][nsys] rotating accumulator slots (zeroed before launch)
-  unsigned* bar;          // [4] grid barrier: count, generation, error (zeroed before launch)
+  unsigned* bar;          // [128] grid barrier count, generation, error at [0, 3); the work-claim counters
+                          // of the three rotating phase slots at [32], [64], [96] (zeroed before launch)
   double tol2;
   int max_it;
   int refresh;            // iterations per refinement cycle (narrow storage), 0 = never
   int vec4;               // every system's first row and size a multiple of 4, FP32 iteration:
                           // the hot phases take 4 rows per thread with 16-byte loads
+  int claim;              // 1: CTAs claim runs of chunks from a counter per phase; 0: runs dealt round-robin
   long long wait_ns;      // bound on one grid-wide wait
 };
 // Co-resident CTAs of the persistent kernel for (prec, lprec) on this device.

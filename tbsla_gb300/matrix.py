@@ -359,10 +359,21 @@ class MatrixCSR(Matrix):
             check(st, "page_rank")
         return x, it.value, err.value, st == L.OK
 
-    def page_rank_batched(self, teleport: np.ndarray, beta=0.85, epsilon=1e-10, max_iterations=1000):
+    def page_rank_batched(self, teleport: np.ndarray, beta=0.85, epsilon=1e-10, max_iterations=1000,
+                          out: np.ndarray | None = None):
+        """Personalised PageRank for the columns of `teleport` (n x nvec,
+        nvec <= 32).  `out` (n x nvec float64, C-contiguous), when given,
+        receives the result: a buffer reused across calls is written at the
+        host link's rate, where a fresh one is first faulted in page by
+        page."""
         n, nvec = teleport.shape
         t = np.ascontiguousarray(teleport, np.float64)
-        x = np.empty((n, nvec))
+        if out is None:
+            x = np.empty((n, nvec))
+        else:
+            if out.shape != (n, nvec) or out.dtype != np.float64 or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float64 array of the teleport's shape")
+            x = out
         it = C.c_int()
         st = lib.tbsla_page_rank_batched(self._h, nvec, _ptr(t), beta, epsilon, max_iterations, _ptr(x),
                                          C.byref(it))
@@ -497,11 +508,16 @@ class Batch:
         automatic)."""
         check(lib.tbsla_batch_set_chunk_rows(self._h, int(rows)), "batch_set_chunk_rows")
 
+    def set_claim(self, claim: int):
+        """Persistent engine: CTAs claim runs of chunks from a counter (1),
+        runs dealt round-robin (0), or chosen by the batch's size (-1)."""
+        check(lib.tbsla_batch_set_claim(self._h, int(claim)), "batch_set_claim")
+
     def tuning(self) -> dict:
         """Current persistent-engine settings."""
-        cr, rpt = C.c_long(), C.c_int()
-        check(lib.tbsla_batch_tuning(self._h, C.byref(cr), C.byref(rpt)), "batch_tuning")
-        return {"chunk_rows": cr.value, "rows_per_thread": rpt.value}
+        cr, rpt, cl = C.c_long(), C.c_int(), C.c_int()
+        check(lib.tbsla_batch_tuning(self._h, C.byref(cr), C.byref(rpt), C.byref(cl)), "batch_tuning")
+        return {"chunk_rows": cr.value, "rows_per_thread": rpt.value, "claim": cl.value}
 
     def set_wait_limit(self, ns: int):
         """Bound on one grid-wide wait of the persistent solver (ns)."""
