@@ -960,7 +960,7 @@ def run_cg(a):
             from tbsla_gb300 import autotune as AT
 
             r = AT.tune_batch_cg(bt, rhs, T.F32, precond=pre)
-            tuned[name] = {"settings": r["settings"], "cached": r["cached"], "key": r["key"]}
+            tuned[name] = {"settings": r["settings"], "cached": r["cached"], "key": r["key"], "trials": r.get("trials")}
         for _ in range(a.warmup):
             bt.cg(rhs, max_iterations=20, rel_tol=1e-8, precond=pre, refresh=50, graph_iters=10)
         if pre == 1:

@@ -407,20 +407,14 @@ int tbsla_batch_set_wait_limit(tbsla_batch* b, long long ns);
  * iteration runs in FP32: 16-byte loads) or 1 (one row per thread, as for
  * every other batch).  The arithmetic of each row is the same either way. */
 int tbsla_batch_set_rows_per_thread(tbsla_batch* b, int rows);
-/* Persistent engine tuning: rows per work chunk (a multiple of 256; 0 =
- * automatic, about 8 chunks per co-resident CTA within [1024, 4096]).
- * TBSLA_ERR_UNSUPPORTED for a batch on the multi-launch engine. */
-int tbsla_batch_set_chunk_rows(tbsla_batch* b, long rows);
-/* The persistent engine's current chunk rows, rows per thread and work
- * dealing (the set_claim value, -1 for the size-based choice); any pointer
- * may be NULL. */
-int tbsla_batch_tuning(const tbsla_batch* b, long* chunk_rows, int* rows_per_thread, int* claim);
-/* Work dealing of the persistent engine's phases: 1 every CTA claims its
- * next run of chunks from a counter as it finishes one (balanced, an atomic
- * round trip per run), 0 runs dealt round-robin, -1 (default) claimed when
- * every CTA has at least 16 chunks.  Persistent engine only; results agree
+/* Persistent engine tuning: CTAs per SM of the cooperative launch (0,
+ * the default: as many as fit, 3 for the FP32 iteration; at most that).
+ * The work is handed out in warp units whatever the grid, so results agree
  * to the FP64 atomics' summation order. */
-int tbsla_batch_set_claim(tbsla_batch* b, int claim);
+int tbsla_batch_set_ctas_per_sm(tbsla_batch* b, int ctas);
+/* The persistent engine's current rows per thread and CTAs per SM (0: all
+ * that fit); either pointer may be NULL. */
+int tbsla_batch_tuning(const tbsla_batch* b, int* rows_per_thread, int* ctas_per_sm);
 /* The engine of the last tbsla_batch_cg: persistent = 1 when the whole solve
  * was one cooperative launch (every system's entries on at most 8 diagonals,
  * at most 256 systems, a factor, if used, on at most 8 diagonals), 0 for the

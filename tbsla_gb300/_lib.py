@@ -118,9 +118,8 @@ _SIGS = {
     "tbsla_batch_fallbacks": (I, [P, IP, IP]),
     "tbsla_batch_set_wait_limit": (I, [P, C.c_longlong]),
     "tbsla_batch_set_rows_per_thread": (I, [P, I]),
-    "tbsla_batch_set_chunk_rows": (I, [P, L]),
-    "tbsla_batch_set_claim": (I, [P, I]),
-    "tbsla_batch_tuning": (I, [P, C.POINTER(L), IP, IP]),
+    "tbsla_batch_set_ctas_per_sm": (I, [P, I]),
+    "tbsla_batch_tuning": (I, [P, IP, IP]),
     "tbsla_batch_engine": (I, [P, IP, IP]),
     "tbsla_batch_factor_mpnn": (I, [P, P, I]),
     "tbsla_batch_factor_dia": (I, [P, IP, IP, DP]),

@@ -7,8 +7,7 @@ wall clock, the fastest kept):
   sliced-ELL thresholds, column blocks, steps in flight; merge path; row
   blocks), whose choice is cached here;
 * batched CG on the persistent engine (``tune_batch_cg``): rows per thread
-  (4, with 16-byte loads, or 1), rows per work chunk, and whether CTAs claim
-  their runs of chunks from a counter or take them round-robin;
+  (4, with 16-byte loads, or 1) and CTAs per SM of the cooperative launch;
 * batched personalised PageRank with FP32 / BF16 values
   (``tune_pagerank_batched``): X-row gathers in flight per warp (8 or 16)
   and rows per warp (one at a time, or a whole row block walked as one
@@ -146,15 +145,18 @@ def batch_key(batch, precision: int, precond: int) -> str:
 
 def apply_batch_cg(batch, cfg: dict) -> None:
     batch.set_rows_per_thread(cfg["rows_per_thread"])
-    batch.set_chunk_rows(cfg["chunk_rows"])
-    batch.set_claim(cfg.get("claim", -1))
+    batch.set_ctas_per_sm(cfg.get("ctas_per_sm", 0))
 
 
-def tune_batch_cg(batch, rhs, precision: int, precond: int = 1, iters: int = 30, reps: int = 3,
-                  path: str | None = None, force: bool = False) -> dict:
-    """Rows per thread and chunk rows of the persistent CG engine, timed on
-    `iters` iterations of this batch's own solve (rel_tol 0: exactly that
-    many iterations, then the final FP64 residual)."""
+def tune_batch_cg(batch, rhs, precision: int, precond: int = 1, rel_tol: float = 1e-8, max_iterations: int = 20000,
+                  refresh: int = 50, reps: int = 1, path: str | None = None, force: bool = False) -> dict:
+    """Rows per thread and CTAs per SM of the persistent CG engine, each
+    candidate timed on whole solves of this batch to `rel_tol` (after one
+    untimed solve that captures its graph).  Whole solves, because a batch
+    of uneven systems spends much of its time in the tail where few systems
+    are still running, which a few iterations from the start do not show
+    (30-iteration trials picked 2 CTAs per SM for the 64-system batch,
+    whose whole solve then ran 21% slower than with 3)."""
     k = batch_key(batch, precision, precond)
     hit = None if force else lookup(k, path)
     if hit is not None:
@@ -162,19 +164,19 @@ def tune_batch_cg(batch, rhs, precision: int, precond: int = 1, iters: int = 30,
         return dict(hit, cached=True, key=k)
     start = batch.tuning()
     rows_opts = (4, 1) if start["rows_per_thread"] == 4 else (1,)
-    candidates = [{"rows_per_thread": r, "chunk_rows": c, "claim": cl}
-                  for r in rows_opts for c in (1024, 2048, 4096) for cl in (0, 1)]
+    candidates = [{"rows_per_thread": r, "ctas_per_sm": c} for r in rows_opts for c in (0, 2)]
 
     def timer(cfg):
         apply_batch_cg(batch, cfg)
-        run = lambda: batch.cg(rhs, max_iterations=iters, rel_tol=0.0, precond=precond, refresh=50)  # noqa: E731
+        run = lambda: batch.cg(rhs, max_iterations=max_iterations, rel_tol=rel_tol, precond=precond,  # noqa: E731
+                               refresh=refresh)
         run()  # warm-up (graph capture)
         return _median_time(run, reps)
 
     best, trials = pick(candidates, timer)
     apply_batch_cg(batch, best)
-    entry = {"settings": best, "iterations": iters,
-             "trials": [{"settings": c, "ms_per_iteration": t * 1e3 / iters} for c, t in trials]}
+    entry = {"settings": best, "rel_tol": rel_tol, "refresh": refresh,
+             "trials": [{"settings": c, "ms_per_solve": t * 1e3} for c, t in trials]}
     store(k, entry, path)
     return dict(entry, cached=False, key=k)
 

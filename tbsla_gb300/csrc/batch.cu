@@ -92,16 +92,12 @@ struct tbsla_batch {
   bool dia = false;
   bool vec4 = false;              // FP32 iteration, every system's first row and size a multiple of 4
   bool vec4_off = false;          // tuning: one row per thread even where 4 would do
-  int claim = -1;                 // tuning: runs claimed (1) or dealt (0); -1 by the batch's size
+  int ctas_per_sm = 0;            // tuning: CTAs per SM of the persistent launch (0: all that fit)
   int K = 0;                      // diagonal slots of A
   std::vector<int> adelta_h;      // [nsys * kDiaMaxDiag]
   int* adelta = nullptr;
   long* sys_off = nullptr;
   int* row_sys = nullptr;
-  int *dchunks = nullptr, *dchunk_sys = nullptr;  // the persistent engine's work chunks
-  int* dsys_chunk = nullptr;                       // [nsys + 1] first chunk of each system
-  int ndchunks = 0;
-  long chunk_rows = 0;            // rows per work chunk
   void* avals_dia = nullptr;      // [K][n] storage precision
   double* a64_dia = nullptr;      // [K][n]
   float* dinv_f = nullptr;
@@ -136,8 +132,7 @@ struct tbsla_batch {
     void* ps[] = {rowptr, colidx, vals64, blocks, block_sys, chunks, chunk_sys, dinv, b, x, r, z, p, q,
                   scal, status, iters, lrowptr, lcolidx, trowptr, tcolidx, lvals, tvals, rf, tf,
                   ldelta, tdelta, zf, adelta, sys_off, row_sys, a64_dia, dinv_f, fdelta, lvals_dia,
-                  dv, r0, r1, p0, p1, q2, z2, t2, mode_d, fallback_d, relres_d, acc, bar, dchunks, dchunk_sys,
-                  dsys_chunk};
+                  dv, r0, r1, p0, p1, q2, z2, t2, mode_d, fallback_d, relres_d, acc, bar};
     for (void* v : ps)
       if (v) cudaFree(v);
     if (avals_dia && avals_dia != (void*)a64_dia) cudaFree(avals_dia);
@@ -257,45 +252,6 @@ bool dia_deltas(const tbsla_batch* B, const std::vector<int>& rp, const std::vec
   return *K > 0;
 }
 
-// Work chunks of the persistent engine: never across a system; `rows` per
-// chunk (a multiple of 256), or 0: sized so that the batch gives every
-// co-resident CTA about 8 of them (1024 to 4096 rows, i.e. 1 to 4 rows of 4
-// per thread; 3 CTAs of 256 threads per SM).
-cudaError_t dia_chunks(tbsla_batch* B, long rows) {
-  cudaStream_t st = B->stream;
-  const long n = B->n;
-  if (rows <= 0) {
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    rows = n / ((long)sms * 3 * 8);
-    rows = std::min<long>(4096, std::max<long>(1024, (rows + 255) / 256 * 256));
-  }
-  std::vector<int> ch{0}, chs, sc;
-  for (int s = 0; s < B->nsys; s++) {
-    sc.push_back((int)chs.size());
-    for (long r0 = B->off[s]; r0 < B->off[s + 1]; r0 += rows) {
-      ch.push_back((int)std::min<long>(B->off[s + 1], r0 + rows));
-      chs.push_back(s);
-    }
-  }
-  sc.push_back((int)chs.size());
-  if (B->dchunks) cudaFree(B->dchunks);
-  if (B->dchunk_sys) cudaFree(B->dchunk_sys);
-  if (B->dsys_chunk) cudaFree(B->dsys_chunk);
-  B->dchunks = B->dchunk_sys = B->dsys_chunk = nullptr;
-  B->ndchunks = (int)chs.size();
-  B->chunk_rows = rows;
-  cudaError_t e;
-  if ((e = alloc(&B->dchunks, ch.size())) || (e = alloc(&B->dchunk_sys, std::max<size_t>(chs.size(), 1))) ||
-      (e = cudaMemcpyAsync(B->dchunks, ch.data(), ch.size() * 4, cudaMemcpyHostToDevice, st)) ||
-      (e = cudaMemcpyAsync(B->dchunk_sys, chs.data(), chs.size() * 4, cudaMemcpyHostToDevice, st)) ||
-      (e = alloc(&B->dsys_chunk, sc.size())) ||
-      (e = cudaMemcpyAsync(B->dsys_chunk, sc.data(), sc.size() * 4, cudaMemcpyHostToDevice, st)))
-    return e;
-  return cudaStreamSynchronize(st);
-}
-
 // The DIA copy of the batch and the persistent engine's vectors.
 int build_dia(tbsla_batch* B, const std::vector<int>& delta, int K) {
   cudaStream_t st = B->stream;
@@ -326,12 +282,11 @@ int build_dia(tbsla_batch* B, const std::vector<int>& delta, int K) {
   const size_t es = B->prec == TBSLA_F64 ? 8 : 4;
   for (void** v : {&B->dv, &B->r0, &B->r1, &B->p0, &B->p1, &B->q2, &B->z2, &B->t2})
     CK(cudaMalloc(v, std::max<size_t>((size_t)n, 1) * es));
-  CK(dia_chunks(B, 0));
   CK(alloc(&B->mode_d, nsys));
   CK(alloc(&B->fallback_d, nsys));
   CK(alloc(&B->relres_d, nsys));
   CK(alloc(&B->acc, (size_t)12 * nsys));
-  CK(alloc(&B->bar, 128));
+  CK(alloc(&B->bar, 4));
   B->vec4 = B->prec != TBSLA_F64;
   for (int s = 0; s <= nsys; s++) B->vec4 = B->vec4 && B->off[s] % 4 == 0;
   B->adelta_h = delta;
@@ -547,8 +502,13 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   const int ns = B->nsys;
   const long n = B->n;
   const int lprec = precond == 2 ? B->lprec_dia : TBSLA_F32;
-  const int grid = cg_dia_grid(B->prec, lprec);
+  int grid = cg_dia_grid(B->prec, lprec);
   if (grid <= 0) return TBSLA_ERR_CUDA;
+  if (B->ctas_per_sm > 0) {
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, B->device);
+    grid = std::min(grid, B->ctas_per_sm * sms);
+  }
   DiaCg c;
   std::memset(&c, 0, sizeof c);  // padding too: the struct is the graph's cache key
   c.nsys = ns;
@@ -556,10 +516,6 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   c.K = B->K;
   c.KL = precond == 2 ? B->KL : 0;
   c.sys_off = B->sys_off;
-  c.chunks = B->dchunks;
-  c.chunk_sys = B->dchunk_sys;
-  c.sys_chunk = B->dsys_chunk;
-  c.nchunks = B->ndchunks;
   c.adelta = B->adelta;
   c.avals = B->avals_dia;
   c.prec = B->prec;
@@ -590,10 +546,6 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   c.refresh = B->prec != TBSLA_F64 ? refresh : 0;
   c.wait_ns = B->wait_ns;
   c.vec4 = B->vec4 && !B->vec4_off ? 1 : 0;
-  // claimed runs balance the CTAs of a phase at an atomic round trip per run:
-  // worth it when every CTA has many chunks (measured: 32 systems of 128^3,
-  // 36 chunks per CTA, 12% faster; 64 systems of 16^3..96^3, 9 per CTA, 9% slower)
-  c.claim = B->claim >= 0 ? B->claim : (B->ndchunks >= 16 * grid ? 1 : 0);
   std::vector<int> mode(ns, precond);
   CK(cudaMemcpyAsync(B->b, rhs, n * 8, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->x, x, n * 8, cudaMemcpyHostToDevice, s));
@@ -606,7 +558,7 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
     if (precond == 1) e = dia_dinv(B->a64_dia, B->row_sys, B->adelta, B->K, n, B->dinv_f, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B->dv, 0, (size_t)n * es, st);
     if (e == cudaSuccess) e = cudaMemsetAsync(B->acc, 0, (size_t)12 * ns * 8, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(B->bar, 0, 128 * sizeof(unsigned), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(B->bar, 0, 4 * sizeof(unsigned), st);
     if (e == cudaSuccess) e = cg_dia_solve(c, grid, st);
     return e;
   };
@@ -1019,24 +971,16 @@ int tbsla_batch_fallbacks(const tbsla_batch* B, int* fallback, int* precond_used
   return TBSLA_OK;
 }
 
-int tbsla_batch_set_chunk_rows(tbsla_batch* B, long rows) {
-  if (!B || rows < 0 || rows % 256 != 0 || rows > (1L << 20)) return TBSLA_ERR_INVALID_ARG;
-  if (!B->dia) return TBSLA_ERR_UNSUPPORTED;
-  cudaSetDevice(B->device);
-  return st_of(dia_chunks(B, rows));
-}
-
-int tbsla_batch_tuning(const tbsla_batch* B, long* chunk_rows, int* rows_per_thread, int* claim) {
-  if (!B) return TBSLA_ERR_INVALID_ARG;
-  if (chunk_rows) *chunk_rows = B->chunk_rows;
-  if (rows_per_thread) *rows_per_thread = B->vec4 && !B->vec4_off ? 4 : 1;
-  if (claim) *claim = B->claim;
+int tbsla_batch_set_ctas_per_sm(tbsla_batch* B, int ctas) {
+  if (!B || ctas < 0 || ctas > 32) return TBSLA_ERR_INVALID_ARG;
+  B->ctas_per_sm = ctas;
   return TBSLA_OK;
 }
 
-int tbsla_batch_set_claim(tbsla_batch* B, int claim) {
-  if (!B || claim < -1 || claim > 1) return TBSLA_ERR_INVALID_ARG;
-  B->claim = claim;
+int tbsla_batch_tuning(const tbsla_batch* B, int* rows_per_thread, int* ctas_per_sm) {
+  if (!B) return TBSLA_ERR_INVALID_ARG;
+  if (rows_per_thread) *rows_per_thread = B->vec4 && !B->vec4_off ? 4 : 1;
+  if (ctas_per_sm) *ctas_per_sm = B->ctas_per_sm;
   return TBSLA_OK;
 }
 

@@ -181,7 +181,7 @@ __device__ __forceinline__ float dot4(float4 a, float4 b, float acc) {
 // add their rows' terms; when the warp moves to another system (or the phase
 // ends) the warp reduces them and lane 0 adds them to acc[what * ns + sys] in
 // FP64.  No CTA-wide barrier.  Every lane of the warp calls to() / flush()
-// at the same points (the chunk loops are uniform over the CTA).
+// at the same points (a unit belongs to one warp and one system).
 template <class T, int NV>
 struct WarpSums {
   int sys = -1;
@@ -214,36 +214,24 @@ struct WarpSums {
   }
 };
 
-// A phase works on the chunks of the systems it selects (SELECT: the
-// systems in a given state); every CTA computes the same selection from its
-// own copy of the states, so none idles on finished systems.  Only those
-// chunks are handed out, in runs of up to 4 consecutive ones (so a CTA
-// rarely changes system within a phase; fewer when there are too few to
-// give every CTA several runs), either dealt round-robin (c.claim = 0) or
-// claimed from the phase's counter by each CTA as it finishes a run
-// (c.claim = 1: the CTAs end a phase together, at the cost of an atomic
-// round trip per run; a CTA holds one claim ahead).  The run after the
-// current one is prefetched into L2 either way.
-constexpr int kRunMax = 4;
+// A phase works on the rows of the systems it selects (SELECT: the systems
+// in a given state); every CTA computes the same selection from its own copy
+// of the states.  The rows are cut into warp units -- 32 threads x the rows
+// per thread (128 rows with 4 per thread, 32 with 1), never across a system
+// -- and the warps of the grid take the selected units grid-stride: at any
+// moment the whole grid works on one compact window of rows, so each
+// array is read as one front sweeping through memory (many streams at
+// scattered places ran at about 45% of the HBM bandwidth, against 98% for
+// the same loads swept grid-stride), and every warp gets an even share
+// whatever systems have finished.
 #define SELECT(cond)                        \
   select_sys([&](int s_) { return (cond); }); \
-  const int nsel_ = s_nsel;                 \
-  const int runs_ = max(1, min(kRunMax, nsel_ / (4 * (int)gridDim.x)))
-#define FOR_CHUNKS(ch)                                                                           \
-  for (int k0_ = first_run(runs_); k0_ < nsel_; k0_ = after_run(k0_, runs_))                      \
-    for (int k_ = k0_, ke_ = min(k0_ + runs_, nsel_); k_ < ke_; k_++)                         \
-      for (int ch = sel_chunk(k_), once_ = 1; once_; once_ = 0)
-
-// L2 prefetch of rows [r0, r1) of an array by the TMA unit: one bulk
-// prefetch instruction (16-byte aligned start, whole 16-byte units inside
-// the range), issued by one thread; a hint with no completion to wait for.
-template <class E>
-__device__ __forceinline__ void prefetch_rows(const E* a, long r0, long r1) {
-  const uintptr_t lo = (reinterpret_cast<uintptr_t>(a + r0) + 15) & ~(uintptr_t)15;
-  const uintptr_t hi = reinterpret_cast<uintptr_t>(a + r1) & ~(uintptr_t)15;
-  if (hi > lo)
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
-}
+  const int nsel_ = s_nsel
+#define FOR_CHUNKS(ch)                                                                              \
+  for (int ku_ = blockIdx.x * (PNT / 32) + warp_; ku_ < nsel_; ku_ += gridDim.x * (PNT / 32))    \
+    for (int ch_sys = unit_sys(ku_), ch_r0 = unit_r0(ku_, ch_sys),                                 \
+             ch_r1 = (int)min((long)ch_r0 + urows, s_off[ch_sys + 1]), once_ = 1;                 \
+         once_; once_ = 0)
 
 // Three CTAs per SM (80 registers): the phases are bound by the bytes each
 // SM keeps in flight, and 24 warps per SM measured 8% faster than 16 (the
@@ -255,12 +243,14 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       s_prev[kDiaMaxSys], s_rzj[kDiaMaxSys];
   __shared__ int s_st[kDiaMaxSys], s_mode[kDiaMaxSys], s_it[kDiaMaxSys], s_since[kDiaMaxSys], s_fb[kDiaMaxSys];
   __shared__ int s_stop;
-  __shared__ int s_sc[kDiaMaxSys + 1];  // first chunk of each system, then the chunk count
-  __shared__ int s_end[kDiaMaxSys];     // selected chunks of systems 0..s
+  __shared__ long s_off[kDiaMaxSys + 1];  // first row of each system
+  __shared__ int s_su[kDiaMaxSys + 1];    // first warp unit of each system, then the unit count
+  __shared__ int s_end[kDiaMaxSys];       // selected units of systems 0..s
   __shared__ int s_nsel;
-  __shared__ int s_claim[2];  // this CTA's current and next run of the phase
   const int ns = c.nsys;
   const int tid = threadIdx.x;
+  const int lane_ = tid & 31, warp_ = tid >> 5;
+  const int urows = c.vec4 ? 128 : 32;  // rows of a warp unit
   const long n = c.n;
   const V* __restrict__ A = static_cast<const V*>(c.avals);
   const LV* __restrict__ Lv = static_cast<const LV*>(c.lvals);
@@ -278,7 +268,16 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
   const float* __restrict__ dinv = c.dinv;
   const uint64_t pol = policy_evict_first();
 
-  for (int s = tid; s <= ns; s += PNT) s_sc[s] = c.sys_chunk[s];
+  for (int s = tid; s <= ns; s += PNT) s_off[s] = c.sys_off[s];
+  __syncthreads();
+  if (tid == 0) {
+    int u = 0;
+    for (int s = 0; s < ns; s++) {
+      s_su[s] = u;
+      u += (int)((s_off[s + 1] - s_off[s] + urows - 1) / urows);
+    }
+    s_su[ns] = u;
+  }
   for (int s = tid; s < ns; s += PNT) {
     s_st[s] = S_CHECK;
     s_mode[s] = c.mode[s];
@@ -301,7 +300,6 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     if (blockIdx.x == 0) {
       double* a = slot(ph + 1);
       for (int t = tid; t < 4 * ns; t += PNT) a[t] = 0.0;
-      if (tid == 0) c.bar[32 * (1 + (ph + 1) % 3)] = 0u;
     }
   };
   auto any_state = [&](int st, int mode) {
@@ -317,7 +315,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       const int per = (ns + 31) / 32, a0 = tid * per, a1 = min(a0 + per, ns);
       int cnt = 0;
       for (int s = a0; s < a1; s++)
-        if (pred(s)) cnt += s_sc[s + 1] - s_sc[s];
+        if (pred(s)) cnt += s_su[s + 1] - s_su[s];
       int incl = cnt;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
@@ -326,57 +324,26 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       }
       int e = incl - cnt;
       for (int s = a0; s < a1; s++) {
-        if (pred(s)) e += s_sc[s + 1] - s_sc[s];
+        if (pred(s)) e += s_su[s + 1] - s_su[s];
         s_end[s] = e;
       }
       if (tid == 31) s_nsel = incl;
     }
     __syncthreads();
   };
-  // the k-th selected chunk: in the first system whose s_end exceeds k
-  auto sel_chunk = [&](int k) {
+  // the system of the k-th selected unit: the first whose s_end exceeds k
+  auto unit_sys = [&](int k) {
     int lo = 0, hi = ns - 1;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
       if (s_end[mid] > k) hi = mid;
       else lo = mid + 1;
     }
-    return s_sc[lo + 1] - (s_end[lo] - k);
+    return lo;
   };
-  // this CTA's runs of the phase: round-robin, or claimed from the counter
-  // of slot ph % 3 (in a line of its own)
-  const bool claim = c.claim != 0;
-  auto first_run = [&](int runs) {
-    if (!claim) return (int)blockIdx.x * runs;
-    __syncthreads();
-    if (tid == 0) {
-      unsigned* ctr = c.bar + 32 * (1 + ph % 3);
-      s_claim[0] = (int)atomicAdd(ctr, 1u);
-      s_claim[1] = (int)atomicAdd(ctr, 1u);
-    }
-    __syncthreads();
-    return s_claim[0] * runs;
-  };
-  auto after_run = [&](int k0, int runs) {
-    if (!claim) return k0 + (int)gridDim.x * runs;
-    __syncthreads();  // every thread is done with the current run
-    if (tid == 0) {
-      s_claim[0] = s_claim[1];
-      s_claim[1] = (int)atomicAdd(c.bar + 32 * (1 + ph % 3), 1u);
-    }
-    __syncthreads();
-    return s_claim[0] * runs;
-  };
-  // rows [q0, q1) of this CTA's next run after the one at k0 (in the system
-  // of its first chunk), for the L2 prefetch; false when it has none
-  auto next_run = [&](int k0, int runs, int nsel, int& q0, int& q1, int& sn) {
-    const int kn = claim ? s_claim[1] * runs : k0 + (int)gridDim.x * runs;
-    if (kn >= nsel) return false;
-    const int c0 = sel_chunk(kn), c1 = sel_chunk(min(kn + runs, nsel) - 1);
-    sn = c.chunk_sys[c0];
-    q0 = c.chunks[c0];
-    q1 = c.chunk_sys[c1] == sn ? c.chunks[c1 + 1] : (int)c.sys_off[sn + 1];
-    return true;
+  // first row of the k-th selected unit, in system s
+  auto unit_r0 = [&](int k, int s) {
+    return (int)(s_off[s] + (long)(k - (s_end[s] - (s_su[s + 1] - s_su[s]))) * urows);
   };
   auto load_deltas = [&](const int* tab, int s, int kk, int (&dd)[KMAX]) {
 #pragma unroll
@@ -393,12 +360,12 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
         double* acc = slot(ph);
         WarpSums<float, 1> bad;
         FOR_CHUNKS(ch) {
-          const int s = c.chunk_sys[ch];
+          const int s = ch_sys;
           if (s_st[s] != S_CHECK) continue;
-          const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+          const int r0 = ch_r0, r1 = ch_r1;
           const bool chk = init && s_mode[s] == 2;
           if (chk) bad.to(s, acc, ns);
-          for (int i = r0 + tid; i < r1; i += PNT) {
+          for (int i = r0 + lane_; i < r1; i += 32) {
             const double xi = c.x[i] + (double)D[i];
             if (isfinite(xi)) c.x[i] = xi;  // a non-finite correction is dropped
             D[i] = (T)0;
@@ -434,15 +401,15 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
         T* __restrict__ Po = P(g);
         WarpSums<double, 3> part;
         FOR_CHUNKS(ch) {
-          const int s = c.chunk_sys[ch];
+          const int s = ch_sys;
           if (s_st[s] != S_CHECK) continue;
           part.to(s, acc, ns);
-          const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+          const int r0 = ch_r0, r1 = ch_r1;
           const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
           int dd[KMAX];
           load_deltas(c.adelta, s, c.K, dd);
           const bool ident = s_mode[s] == 0;
-          for (int i = r0 + tid; i < r1; i += PNT) {
+          for (int i = r0 + lane_; i < r1; i += 32) {
             double ax = 0;
 #pragma unroll
             for (int k = 0; k < KMAX; k++) {
@@ -509,14 +476,14 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
           const T* __restrict__ Rc = R(g);
           WarpSums<T, 1> part;
           FOR_CHUNKS(ch) {
-            const int s = c.chunk_sys[ch];
+            const int s = ch_sys;
             if (s_st[s] != S_RESTART_F) continue;
             part.to(s, acc, ns);
-            const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+            const int r0 = ch_r0, r1 = ch_r1;
             const long hi = c.sys_off[s + 1];
             int ld[KMAX];
             load_deltas(c.ldelta, s, c.KL, ld);
-            for (int i = r0 + tid; i < r1; i += PNT) {
+            for (int i = r0 + lane_; i < r1; i += 32) {
               T t = (T)0;
 #pragma unroll
               for (int k = 0; k < KMAX; k++) {
@@ -555,13 +522,13 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
           SELECT(s_st[s_] == S_RESTART_F);
           T* __restrict__ Po = P(g);
           FOR_CHUNKS(ch) {
-            const int s = c.chunk_sys[ch];
+            const int s = ch_sys;
             if (s_st[s] != S_RESTART_F) continue;
-            const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+            const int r0 = ch_r0, r1 = ch_r1;
             const long lo = c.sys_off[s];
             int ld[KMAX];
             load_deltas(c.ldelta, s, c.KL, ld);
-            for (int i = r0 + tid; i < r1; i += PNT) {
+            for (int i = r0 + lane_; i < r1; i += 32) {
               T z = (T)0;
 #pragma unroll
               for (int k = 0; k < KMAX; k++) {
@@ -594,19 +561,12 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       double* acc = slot(ph);
       WarpSums<T, 1> part;
       FOR_CHUNKS(ch) {
-        const int s = c.chunk_sys[ch];
+        const int s = ch_sys;
         if (s_st[s] != S_ACTIVE) continue;
         part.to(s, acc, ns);
-        const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+        const int r0 = ch_r0, r1 = ch_r1;
         const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
         const bool fact = s_mode[s] == 2;
-        int q0, q1, sn;
-        if (tid == 0 && k_ == k0_ && next_run(k0_, runs_, nsel_, q0, q1, sn)) {
-          // the next run's streams into L2 while this one runs
-          for (int k = 0; k < c.K; k++) prefetch_rows(A + (size_t)k * n, q0, q1);
-          prefetch_rows(Pold, q0, q1);
-          prefetch_rows(Z, q0, q1);
-        }
         int dd[KMAX];
         load_deltas(c.adelta, s, c.K, dd);
         const T beta = (T)s_beta[s];
@@ -614,7 +574,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
           if (c.vec4) {
             const float* Zf = reinterpret_cast<const float*>(Z);
             const float* Pf = reinterpret_cast<const float*>(Pold);
-            for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+            for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
               float4 a[KMAX];
 #pragma unroll
               for (int k = 0; k < KMAX; k++) a[k] = k < c.K ? ld4_stream(A + (size_t)k * n + i0, pol) : f4zero();
@@ -638,7 +598,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
             continue;
           }
         }
-        for (int i = r0 + tid; i < r1; i += PNT) {
+        for (int i = r0 + lane_; i < r1; i += 32) {
           T a[KMAX];
 #pragma unroll
           for (int k = 0; k < KMAX; k++) a[k] = k < c.K ? val<T, V>(ld_stream(A + (size_t)k * n + i, pol)) : (T)0;
@@ -691,25 +651,12 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       T* __restrict__ Rn = R(g + 1);
       WarpSums<T, 2> part;
       FOR_CHUNKS(ch) {
-        const int s = c.chunk_sys[ch];
+        const int s = ch_sys;
         if (s_st[s] != S_ACTIVE) continue;
         part.to(s, acc, ns);
-        const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+        const int r0 = ch_r0, r1 = ch_r1;
         const T alpha = (T)s_alpha[s];
         const int mode = s_mode[s];
-        int q0, q1, sn;
-        if (tid == 0 && k_ == k0_ && next_run(k0_, runs_, nsel_, q0, q1, sn)) {
-          prefetch_rows(Ro, q0, q1);
-          prefetch_rows(Q, q0, q1);
-          prefetch_rows(D, q0, q1);
-          if (s_mode[sn] == 2) {
-            prefetch_rows(Pold, q0, q1);
-            for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
-          } else {
-            prefetch_rows(Pnew, q0, q1);
-            prefetch_rows(dinv, q0, q1);
-          }
-        }
         if constexpr (sizeof(T) == 4) {
           if (c.vec4) {
             const long lo = c.sys_off[s], hi = c.sys_off[s + 1];
@@ -720,7 +667,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
             if (mode == 2) {
               int ld[KMAX];
               load_deltas(c.ldelta, s, c.KL, ld);
-              for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+              for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
                 st4(Df + i0, fma4s(alpha, ld4(reinterpret_cast<const float*>(Pold) + i0), ld4(Df + i0)));
                 const float4 ri = fma4s(-alpha, ld4(Qf + i0), ld4(Rof + i0));
                 st4(Rnf + i0, ri);
@@ -738,7 +685,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
                 part.v[0] = dot4(t, t, part.v[0]);
               }
             } else {
-              for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+              for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
                 st4(Df + i0, fma4s(alpha, ld4(reinterpret_cast<const float*>(Pnew) + i0), ld4(Df + i0)));
                 const float4 ri = fma4s(-alpha, ld4(Qf + i0), ld4(Rof + i0));
                 st4(Rnf + i0, ri);
@@ -759,7 +706,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
           const long hi = c.sys_off[s + 1];
           int ld[KMAX];
           load_deltas(c.ldelta, s, c.KL, ld);
-          for (int i = r0 + tid; i < r1; i += PNT) {
+          for (int i = r0 + lane_; i < r1; i += 32) {
             D[i] += alpha * Pold[i];
             const T ri = Ro[i] - alpha * Q[i];
             Rn[i] = ri;
@@ -776,7 +723,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
             part.v[0] += t * t;
           }
         } else {
-          for (int i = r0 + tid; i < r1; i += PNT) {
+          for (int i = r0 + lane_; i < r1; i += 32) {
             D[i] += alpha * Pnew[i];
             const T ri = Ro[i] - alpha * Q[i];
             Rn[i] = ri;
@@ -816,24 +763,18 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       clear_ahead();
       SELECT(s_st[s_] == S_ACTIVE && s_mode[s_] == 2);
       FOR_CHUNKS(ch) {
-        const int s = c.chunk_sys[ch];
+        const int s = ch_sys;
         if (s_st[s] != S_ACTIVE || s_mode[s] != 2) continue;
-        const int r0 = c.chunks[ch], r1 = c.chunks[ch + 1];
+        const int r0 = ch_r0, r1 = ch_r1;
         const long lo = c.sys_off[s];
         const T beta = (T)s_beta[s];
-        int q0, q1, sn;
-        if (tid == 0 && k_ == k0_ && next_run(k0_, runs_, nsel_, q0, q1, sn)) {
-          prefetch_rows(Tt, q0, q1);
-          prefetch_rows(Pold, q0, q1);
-          for (int k = 0; k < c.KL; k++) prefetch_rows(Lv + (size_t)k * n, q0, q1);
-        }
         int ld[KMAX];
         load_deltas(c.ldelta, s, c.KL, ld);
         if constexpr (sizeof(T) == 4) {
           if (c.vec4) {
             const long hi = c.sys_off[s + 1];
             const float* Tf = reinterpret_cast<const float*>(Tt);
-            for (long i0 = r0 + 4 * tid; i0 < r1; i0 += 4 * PNT) {
+            for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
               float4 z = f4zero();
 #pragma unroll
               for (int k = 0; k < KMAX; k++)
@@ -843,7 +784,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
             continue;
           }
         }
-        for (int i = r0 + tid; i < r1; i += PNT) {
+        for (int i = r0 + lane_; i < r1; i += 32) {
           T z = (T)0;
 #pragma unroll
           for (int k = 0; k < KMAX; k++) {

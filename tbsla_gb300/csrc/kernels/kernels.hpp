@@ -246,10 +246,6 @@ struct DiaCg {
   long n;
   int K, KL;              // diagonal slots of A and of L (batch-wide, zero-padded)
   const long* sys_off;    // [nsys + 1] first row of each system
-  const int* chunks;      // [nchunks + 1] row bounds of the work chunks (never across systems)
-  const int* chunk_sys;   // [nchunks]
-  const int* sys_chunk;   // [nsys + 1] first chunk of each system (chunks are in system order)
-  int nchunks;
   const int* adelta;      // [nsys * kDiaMaxDiag] col - row of each slot of A (padding: 0, value 0)
   const void* avals;      // [K][n] in `prec` (the iteration's A)
   int prec;
@@ -267,14 +263,12 @@ struct DiaCg {
   int* fallback;          // [nsys] out: DiaFallback
   double* relres;         // [nsys] out: FP64 true relative residual at exit
   double* acc;            // [3][4][nsys] rotating accumulator slots (zeroed before launch)
-  unsigned* bar;          // [128] grid barrier count, generation, error at [0, 3); the work-claim counters
-                          // of the three rotating phase slots at [32], [64], [96] (zeroed before launch)
+  unsigned* bar;          // [4] grid barrier: count, generation, error (zeroed before launch)
   double tol2;
   int max_it;
   int refresh;            // iterations per refinement cycle (narrow storage), 0 = never
   int vec4;               // every system's first row and size a multiple of 4, FP32 iteration:
                           // the hot phases take 4 rows per thread with 16-byte loads
-  int claim;              // 1: CTAs claim runs of chunks from a counter per phase; 0: runs dealt round-robin
   long long wait_ns;      // bound on one grid-wide wait
 };
 // Co-resident CTAs of the persistent kernel for (prec, lprec) on this device.

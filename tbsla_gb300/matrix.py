@@ -503,21 +503,16 @@ class Batch:
         where the layout allows) or 1."""
         check(lib.tbsla_batch_set_rows_per_thread(self._h, int(rows)), "batch_set_rows_per_thread")
 
-    def set_chunk_rows(self, rows: int):
-        """Persistent engine: rows per work chunk (multiple of 256; 0 =
-        automatic)."""
-        check(lib.tbsla_batch_set_chunk_rows(self._h, int(rows)), "batch_set_chunk_rows")
-
-    def set_claim(self, claim: int):
-        """Persistent engine: CTAs claim runs of chunks from a counter (1),
-        runs dealt round-robin (0), or chosen by the batch's size (-1)."""
-        check(lib.tbsla_batch_set_claim(self._h, int(claim)), "batch_set_claim")
+    def set_ctas_per_sm(self, ctas: int):
+        """Persistent engine: CTAs per SM of the cooperative launch (0: as
+        many as fit)."""
+        check(lib.tbsla_batch_set_ctas_per_sm(self._h, int(ctas)), "batch_set_ctas_per_sm")
 
     def tuning(self) -> dict:
         """Current persistent-engine settings."""
-        cr, rpt, cl = C.c_long(), C.c_int(), C.c_int()
-        check(lib.tbsla_batch_tuning(self._h, C.byref(cr), C.byref(rpt), C.byref(cl)), "batch_tuning")
-        return {"chunk_rows": cr.value, "rows_per_thread": rpt.value, "claim": cl.value}
+        rpt, cps = C.c_int(), C.c_int()
+        check(lib.tbsla_batch_tuning(self._h, C.byref(rpt), C.byref(cps)), "batch_tuning")
+        return {"rows_per_thread": rpt.value, "ctas_per_sm": cps.value}
 
     def set_wait_limit(self, ns: int):
         """Bound on one grid-wide wait of the persistent solver (ns)."""

@@ -13,9 +13,9 @@ def test_cache_round_trip(tmp_path):
     k2 = A.key("pagerank_batched", "CSR", 4194304, 67108864, 4096, 2, "nvec32")
     assert k1 == "batch_cg|DIA|17120768|64|884736|f32|precond1"
     assert A.lookup(k1, path) is None  # no file yet
-    A.store(k1, {"settings": {"rows_per_thread": 4, "chunk_rows": 2048}, "iterations": 30}, path)
+    A.store(k1, {"settings": {"rows_per_thread": 4, "ctas_per_sm": 2}, "iterations": 30}, path)
     A.store(k2, {"settings": {"gather": 16}}, path)
-    assert A.lookup(k1, path)["settings"] == {"rows_per_thread": 4, "chunk_rows": 2048}
+    assert A.lookup(k1, path)["settings"] == {"rows_per_thread": 4, "ctas_per_sm": 2}
     assert A.lookup(k2, path)["settings"] == {"gather": 16}
     with open(path) as f:
         on_disk = json.load(f)
