@@ -227,10 +227,18 @@ struct WarpSums {
 #define SELECT(cond)                        \
   select_sys([&](int s_) { return (cond); }); \
   const int nsel_ = s_nsel
-#define FOR_CHUNKS(ch)                                                                              \
-  for (int ku_ = blockIdx.x * (PNT / 32) + warp_; ku_ < nsel_; ku_ += gridDim.x * (PNT / 32))    \
-    for (int ch_sys = unit_sys(ku_), ch_r0 = unit_r0(ku_, ch_sys),                                 \
-             ch_r1 = (int)min((long)ch_r0 + urows, s_off[ch_sys + 1]), once_ = 1;                 \
+// A warp keeps the system of its last unit and that system's range of
+// selected units [uk0_, uk1_): its next unit (a grid's worth of units on)
+// usually lies in the same system, and then needs no search.
+#define FOR_CHUNKS(ch)                                                                          \
+  for (int ku_ = blockIdx.x * (PNT / 32) + warp_, us_ = -1, uk0_ = 0, uk1_ = 0; ku_ < nsel_; \
+       ku_ += gridDim.x * (PNT / 32))                                                           \
+    for (int ch_sys = (ku_ >= uk0_ && ku_ < uk1_)                                               \
+                          ? us_                                                                 \
+                          : (us_ = unit_sys(ku_), uk1_ = s_end[us_],                            \
+                             uk0_ = uk1_ - (s_su[us_ + 1] - s_su[us_]), us_),                   \
+             ch_r0 = (int)(s_off[ch_sys] + (long)(ku_ - uk0_) * urows),                         \
+             ch_r1 = (int)min((long)ch_r0 + urows, s_off[ch_sys + 1]), once_ = 1;              \
          once_; once_ = 0)
 
 // Three CTAs per SM (80 registers): the phases are bound by the bytes each
@@ -340,10 +348,6 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       else lo = mid + 1;
     }
     return lo;
-  };
-  // first row of the k-th selected unit, in system s
-  auto unit_r0 = [&](int k, int s) {
-    return (int)(s_off[s] + (long)(k - (s_end[s] - (s_su[s + 1] - s_su[s]))) * urows);
   };
   auto load_deltas = [&](const int* tab, int s, int kk, int (&dd)[KMAX]) {
 #pragma unroll
