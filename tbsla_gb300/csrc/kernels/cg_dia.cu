@@ -671,11 +671,12 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
             if (mode == 2) {
               int ld[KMAX];
               load_deltas(c.ldelta, s, c.KL, ld);
+              // (d += alpha p is left to phase D, which reads p anyway)
               for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
-                st4(Df + i0, fma4s(alpha, ld4(reinterpret_cast<const float*>(Pold) + i0), ld4(Df + i0)));
+                // every load before the first store (the stores could alias
+                // them as far as the compiler knows, so a store in between
+                // would hold the later loads back a whole memory round trip)
                 const float4 ri = fma4s(-alpha, ld4(Qf + i0), ld4(Rof + i0));
-                st4(Rnf + i0, ri);
-                part.v[1] = dot4(ri, ri, part.v[1]);
                 float4 t = f4zero();
 #pragma unroll
                 for (int k = 0; k < KMAX; k++) {
@@ -685,19 +686,22 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
                     t = fma4(rows4(Lv + (size_t)k * n, i0, sh, lo, hi), rf, t);
                   }
                 }
+                st4(Rnf + i0, ri);
                 st4(reinterpret_cast<float*>(Tt) + i0, t);
+                part.v[1] = dot4(ri, ri, part.v[1]);
                 part.v[0] = dot4(t, t, part.v[0]);
               }
             } else {
               for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
-                st4(Df + i0, fma4s(alpha, ld4(reinterpret_cast<const float*>(Pnew) + i0), ld4(Df + i0)));
+                const float4 pn = ld4(reinterpret_cast<const float*>(Pnew) + i0), dold = ld4(Df + i0);
                 const float4 ri = fma4s(-alpha, ld4(Qf + i0), ld4(Rof + i0));
-                st4(Rnf + i0, ri);
                 float4 zi = ri;
-                if (mode == 1) {
+                if (mode == 1) {  // loaded before the stores, as above
                   const float4 dv = ld4(dinv + i0);
                   zi = make_float4(dv.x * ri.x, dv.y * ri.y, dv.z * ri.z, dv.w * ri.w);
                 }
+                st4(Df + i0, fma4s(alpha, pn, dold));
+                st4(Rnf + i0, ri);
                 st4(reinterpret_cast<float*>(Z) + i0, zi);
                 part.v[0] = dot4(ri, zi, part.v[0]);
                 part.v[1] = dot4(ri, ri, part.v[1]);
@@ -711,10 +715,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
           int ld[KMAX];
           load_deltas(c.ldelta, s, c.KL, ld);
           for (int i = r0 + lane_; i < r1; i += 32) {
-            D[i] += alpha * Pold[i];
             const T ri = Ro[i] - alpha * Q[i];
-            Rn[i] = ri;
-            part.v[1] += ri * ri;
             T t = (T)0;
 #pragma unroll
             for (int k = 0; k < KMAX; k++) {
@@ -723,15 +724,18 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
                 if (j < hi) t += val<T, LV>(Lv[(size_t)k * n + j]) * (Ro[j] - alpha * Q[j]);
               }
             }
+            Rn[i] = ri;  // the stores after every load
             Tt[i] = t;
+            part.v[1] += ri * ri;
             part.v[0] += t * t;
           }
         } else {
           for (int i = r0 + lane_; i < r1; i += 32) {
-            D[i] += alpha * Pnew[i];
+            const T pn = Pnew[i], dold = D[i];
             const T ri = Ro[i] - alpha * Q[i];
-            Rn[i] = ri;
             const T zi = mode == 1 ? (T)dinv[i] * ri : ri;
+            D[i] = dold + alpha * pn;  // the stores after every load
+            Rn[i] = ri;
             Z[i] = zi;
             part.v[0] += ri * zi;
             part.v[1] += ri * ri;
@@ -762,15 +766,20 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
       ph++;
     }
     __syncthreads();
-    if (any_state(S_ACTIVE, 2)) {
-      // D: z = L t, p = z + beta p
+    // factored systems still iterating, or just stopped by phase B' (which
+    // leaves their d += alpha p to this phase)
+    int fact_ = 0;
+    for (int s = tid; s < ns; s += PNT) fact_ |= s_mode[s] == 2 && (s_st[s] == S_ACTIVE || s_st[s] == S_CHECK);
+    if (__syncthreads_or(fact_)) {
+      // D: d += alpha p; z = L t, p = z + beta p (iterating systems)
       clear_ahead();
-      SELECT(s_st[s_] == S_ACTIVE && s_mode[s_] == 2);
+      SELECT(s_mode[s_] == 2 && (s_st[s_] == S_ACTIVE || s_st[s_] == S_CHECK));
       FOR_CHUNKS(ch) {
         const int s = ch_sys;
-        if (s_st[s] != S_ACTIVE || s_mode[s] != 2) continue;
+        const bool act = s_st[s] == S_ACTIVE;
         const int r0 = ch_r0, r1 = ch_r1;
         const long lo = c.sys_off[s];
+        const T alpha = (T)s_alpha[s];
         const T beta = (T)s_beta[s];
         int ld[KMAX];
         load_deltas(c.ldelta, s, c.KL, ld);
@@ -778,27 +787,36 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
           if (c.vec4) {
             const long hi = c.sys_off[s + 1];
             const float* Tf = reinterpret_cast<const float*>(Tt);
+            float* Df = reinterpret_cast<float*>(D);
             for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
+              const float4 po = ld4(reinterpret_cast<const float*>(Pold) + i0), dold = ld4(Df + i0);
               float4 z = f4zero();
+              if (act) {
 #pragma unroll
-              for (int k = 0; k < KMAX; k++)
-                if (k < c.KL) z = fma4(ld4(Lv + (size_t)k * n + i0), rows4(Tf, i0, ld[k], lo, hi), z);
-              st4(reinterpret_cast<float*>(Pnew) + i0, fma4s(beta, ld4(reinterpret_cast<const float*>(Pold) + i0), z));
+                for (int k = 0; k < KMAX; k++)
+                  if (k < c.KL) z = fma4(ld4(Lv + (size_t)k * n + i0), rows4(Tf, i0, ld[k], lo, hi), z);
+              }
+              st4(Df + i0, fma4s(alpha, po, dold));
+              if (act) st4(reinterpret_cast<float*>(Pnew) + i0, fma4s(beta, po, z));
             }
             continue;
           }
         }
         for (int i = r0 + lane_; i < r1; i += 32) {
+          const T po = Pold[i], dold = D[i];
           T z = (T)0;
+          if (act) {
 #pragma unroll
-          for (int k = 0; k < KMAX; k++) {
-            if (k < c.KL) {
-              long j = (long)i + ld[k];
-              j = j < lo ? lo : j;
-              z += val<T, LV>(Lv[(size_t)k * n + i]) * Tt[j];
+            for (int k = 0; k < KMAX; k++) {
+              if (k < c.KL) {
+                long j = (long)i + ld[k];
+                j = j < lo ? lo : j;
+                z += val<T, LV>(Lv[(size_t)k * n + i]) * Tt[j];
+              }
             }
           }
-          Pnew[i] = z + beta * Pold[i];
+          D[i] = dold + alpha * po;
+          if (act) Pnew[i] = z + beta * po;
         }
       }
       if (!grid_sync(c.bar, gen, c.wait_ns, &s_stop)) return;
