@@ -35,9 +35,10 @@
 //   A   q = A p; p.q              (modes 0/1 form p = z + beta p_old on the
 //                                   fly and write it)
 //   B   modes 0/1: alpha; d += alpha p; r -= alpha q; z = M r; r.z, r.r
-//   B'  mode 2: the same r update, and t = L^T r_new formed from r_old and q
-//       at the row's upper neighbours (so no extra pass), r.z = t.t
-//   D   mode 2: z = L t, p = z + beta p
+//   B'  mode 2: r -= alpha q, and t = L^T r_new formed from r_old and q at
+//       the row's upper neighbours (so no extra pass), r.z = t.t, r.r
+//   D   mode 2: d += alpha p (for the systems B' stopped too); z = L t,
+//       p = z + beta p
 // Jacobi costs two barriers per iteration, the factored form three.
 //
 // Per-system scalars are kept in shared memory by every CTA and updated
