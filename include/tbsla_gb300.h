@@ -418,8 +418,15 @@ int tbsla_batch_tuning(const tbsla_batch* b, int* rows_per_thread, int* ctas_per
 /* The engine of the last tbsla_batch_cg: persistent = 1 when the whole solve
  * was one cooperative launch (every system's entries on at most 8 diagonals,
  * at most 256 systems, a factor, if used, on at most 8 diagonals), 0 for the
- * multi-launch engine; graph = 1 when it was replayed from a CUDA graph. */
-int tbsla_batch_engine(const tbsla_batch* b, int* persistent, int* graph);
+ * multi-launch engine; graph = 1 when it was replayed from a CUDA graph;
+ * seven_point = 1 when the persistent kernel ran in its seven-point form
+ * (every system a 7-point stencil whose line and plane sizes are multiples
+ * of 4, FP32 / BF16 storage: the neighbour alignments fixed when compiled).
+ * Any pointer may be NULL. */
+int tbsla_batch_engine(const tbsla_batch* b, int* persistent, int* graph, int* seven_point);
+/* 1 (default): the seven-point form where it applies; 0: always the general
+ * form (the same arithmetic in the same order). */
+int tbsla_batch_set_seven_point(tbsla_batch* b, int on);
 /* Factored preconditioner M^-1 = L L^T for every system of the batch (L:
  * lower-triangular CSR handles, one per system, same sizes), used by
  * tbsla_batch_cg with precond = 2.  Values are stored in `precision`

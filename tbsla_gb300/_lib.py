@@ -120,7 +120,8 @@ _SIGS = {
     "tbsla_batch_set_rows_per_thread": (I, [P, I]),
     "tbsla_batch_set_ctas_per_sm": (I, [P, I]),
     "tbsla_batch_tuning": (I, [P, IP, IP]),
-    "tbsla_batch_engine": (I, [P, IP, IP]),
+    "tbsla_batch_engine": (I, [P, IP, IP, IP]),
+    "tbsla_batch_set_seven_point": (I, [P, I]),
     "tbsla_batch_factor_mpnn": (I, [P, P, I]),
     "tbsla_batch_factor_dia": (I, [P, IP, IP, DP]),
     "tbsla_mpnn_create": (I, [C.POINTER(P), ULL]),

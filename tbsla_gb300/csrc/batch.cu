@@ -92,6 +92,7 @@ struct tbsla_batch {
   bool dia = false;
   bool vec4 = false;              // FP32 iteration, every system's first row and size a multiple of 4
   bool vec4_off = false;          // tuning: one row per thread even where 4 would do
+  bool st7_off = false;           // tuning: the general kernel even for seven-point batches
   int ctas_per_sm = 0;            // tuning: CTAs per SM of the persistent launch (0: all that fit)
   int K = 0;                      // diagonal slots of A
   std::vector<int> adelta_h;      // [nsys * kDiaMaxDiag]
@@ -122,7 +123,7 @@ struct tbsla_batch {
   // last solve
   std::vector<int> fallback_h, mode_h;
   std::vector<int> factor_fb;     // per system: the factor failed the host check (multi-launch engine)
-  int last_engine = 0, last_graph = 0;
+  int last_engine = 0, last_graph = 0, last_st7 = 0;
 
   ~tbsla_batch() {
     cudaSetDevice(device);
@@ -502,7 +503,15 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   const int ns = B->nsys;
   const long n = B->n;
   const int lprec = precond == 2 ? B->lprec_dia : TBSLA_F32;
-  int grid = cg_dia_grid(B->prec, lprec);
+  const bool vec4 = B->vec4 && !B->vec4_off;
+  // the seven-point form of the kernel (neighbour alignments fixed at compile
+  // time) where every system is a 7-point stencil with n, n^2 multiples of 4
+  const bool st7 = vec4 && B->prec != TBSLA_F64 && !B->st7_off &&
+                   B->adelta_h.size() >= (size_t)ns * kDiaMaxDiag &&
+                   (precond != 2 || B->fdelta_h.size() >= (size_t)ns * kDiaMaxDiag) &&
+                   dia_seven_point(B->adelta_h.data(), precond == 2 ? B->fdelta_h.data() : nullptr, ns, B->K,
+                                   precond == 2 ? B->KL : 0);
+  int grid = cg_dia_grid(B->prec, lprec, st7 ? 1 : 0);
   if (grid <= 0) return TBSLA_ERR_CUDA;
   if (B->ctas_per_sm > 0) {
     int sms = 152;
@@ -545,7 +554,8 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   c.max_it = max_iterations;
   c.refresh = B->prec != TBSLA_F64 ? refresh : 0;
   c.wait_ns = B->wait_ns;
-  c.vec4 = B->vec4 && !B->vec4_off ? 1 : 0;
+  c.vec4 = vec4 ? 1 : 0;
+  c.st7 = st7 ? 1 : 0;
   std::vector<int> mode(ns, precond);
   CK(cudaMemcpyAsync(B->b, rhs, n * 8, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(B->x, x, n * 8, cudaMemcpyHostToDevice, s));
@@ -599,6 +609,7 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
   CK(cudaStreamSynchronize(s));
   B->last_engine = 1;
   B->last_graph = B->pgraph ? 1 : 0;
+  B->last_st7 = st7 ? 1 : 0;
   if (err[2]) return TBSLA_ERR_TIMEOUT;
   bool all = true;
   for (int k = 0; k < ns; k++) {
@@ -817,6 +828,7 @@ int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterati
     return dia_solve(B, rhs, x, max_iterations, rel_tol, precond, refresh, iterations, rel_residual);
   B->last_engine = 0;
   B->last_graph = 1;
+  B->last_st7 = 0;
   B->fallback_h.assign(B->nsys, 0);
   B->mode_h.assign(B->nsys, precond);
   if (precond == 2)
@@ -996,10 +1008,17 @@ int tbsla_batch_set_wait_limit(tbsla_batch* B, long long ns) {
   return TBSLA_OK;
 }
 
-int tbsla_batch_engine(const tbsla_batch* B, int* persistent, int* graph) {
+int tbsla_batch_engine(const tbsla_batch* B, int* persistent, int* graph, int* seven_point) {
   if (!B) return TBSLA_ERR_INVALID_ARG;
   if (persistent) *persistent = B->last_engine;
   if (graph) *graph = B->last_graph;
+  if (seven_point) *seven_point = B->last_st7;
+  return TBSLA_OK;
+}
+
+int tbsla_batch_set_seven_point(tbsla_batch* B, int on) {
+  if (!B || (on != 0 && on != 1)) return TBSLA_ERR_INVALID_ARG;
+  B->st7_off = on == 0;
   return TBSLA_OK;
 }
 

@@ -157,9 +157,12 @@ __device__ __forceinline__ float4 ld4_stream(const __nv_bfloat16* p, uint64_t po
                      __uint_as_float(b & 0xffff0000u));
 }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+// The same with the shift's alignment class r = s & 3 given: a constant in
+// the seven-point form of the kernel (the classes of a 7-point stencil whose
+// plane and line sizes are multiples of 4), so each window's loads and lane
+// shuffle are known when the kernel is compiled.
 template <class E>
-__device__ __forceinline__ float4 rows4(const E* v, long i0, long s, long lo, long hi) {
-  const int r = (int)(s & 3);
+__device__ __forceinline__ float4 rows4r(const E* v, long i0, long s, int r, long lo, long hi) {
   const long b = i0 + s - r;
   const float4 v0 = b >= lo && b < hi ? ld4(v + b) : f4zero();
   if (r == 0) return v0;
@@ -168,6 +171,12 @@ __device__ __forceinline__ float4 rows4(const E* v, long i0, long s, long lo, lo
   if (r == 2) return make_float4(v0.z, v0.w, v1.x, v1.y);
   return make_float4(v0.w, v1.x, v1.y, v1.z);
 }
+// Slot classes of the seven-point form: A's deltas ascending (-n^2, -n, -1,
+// 0, +1, +n, +n^2), L's deltas (0, -1, -n, -n^2) and their negations.
+__host__ __device__ constexpr int cls_a(int k) { return k == 2 ? 3 : (k == 4 ? 1 : 0); }
+__host__ __device__ constexpr int cls_l(int k) { return k == 1 ? 3 : 0; }
+__host__ __device__ constexpr int cls_lt(int k) { return k == 1 ? 1 : 0; }
+
 __device__ __forceinline__ float4 fma4(float4 a, float4 b, float4 c) {
   return make_float4(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z), fmaf(a.w, b.w, c.w));
 }
@@ -246,8 +255,11 @@ struct WarpSums {
 // SM keeps in flight, and 24 warps per SM measured 8% faster than 16 (the
 // 128-register form) on the 32 x 128^3 learned batch, 21% on the 64-system
 // batch; 4 CTAs (64 registers) spill in the 4-row paths.
-template <class T, class V, class LV>
+template <class T, class V, class LV, int ST7>
 __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
+  // ST7: every system is a 7-point stencil in the seven-point form (K = 7,
+  // KL = 4, slot classes cls_a / cls_l), checked by the host
+  const int KA = ST7 ? 7 : c.K, KF = ST7 ? 4 : c.KL;
   __shared__ double s_rz[kDiaMaxSys], s_alpha[kDiaMaxSys], s_beta[kDiaMaxSys], s_bb[kDiaMaxSys],
       s_prev[kDiaMaxSys], s_rzj[kDiaMaxSys];
   __shared__ int s_st[kDiaMaxSys], s_mode[kDiaMaxSys], s_it[kDiaMaxSys], s_since[kDiaMaxSys], s_fb[kDiaMaxSys];
@@ -582,18 +594,22 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
             for (long i0 = r0 + 4 * lane_; i0 < r1; i0 += 128) {
               float4 a[KMAX];
 #pragma unroll
-              for (int k = 0; k < KMAX; k++) a[k] = k < c.K ? ld4_stream(A + (size_t)k * n + i0, pol) : f4zero();
+              for (int k = 0; k < KMAX; k++) a[k] = k < KA ? ld4_stream(A + (size_t)k * n + i0, pol) : f4zero();
               float4 q = f4zero(), pi;
               if (fact) {
 #pragma unroll
-                for (int k = 0; k < KMAX; k++)
-                  if (k < c.K) q = fma4(a[k], rows4(Pf, i0, dd[k], lo, hi), q);
+                for (int k = 0; k < KMAX; k++) {
+                  const int r = ST7 ? cls_a(k) : (int)(dd[k] & 3);
+                  if (k < KA) q = fma4(a[k], rows4r(Pf, i0, dd[k], r, lo, hi), q);
+                }
                 pi = ld4(Pf + i0);
               } else {
 #pragma unroll
-                for (int k = 0; k < KMAX; k++)
-                  if (k < c.K)
-                    q = fma4(a[k], fma4s(beta, rows4(Pf, i0, dd[k], lo, hi), rows4(Zf, i0, dd[k], lo, hi)), q);
+                for (int k = 0; k < KMAX; k++) {
+                  const int r = ST7 ? cls_a(k) : (int)(dd[k] & 3);
+                  if (k < KA)
+                    q = fma4(a[k], fma4s(beta, rows4r(Pf, i0, dd[k], r, lo, hi), rows4r(Zf, i0, dd[k], r, lo, hi)), q);
+                }
                 pi = fma4s(beta, ld4(Pf + i0), ld4(Zf + i0));
                 st4(reinterpret_cast<float*>(Pnew) + i0, pi);
               }
@@ -681,10 +697,11 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
                 float4 t = f4zero();
 #pragma unroll
                 for (int k = 0; k < KMAX; k++) {
-                  if (k < c.KL) {
+                  if (k < KF) {
                     const long sh = -(long)ld[k];  // L_{j,i} sits on row j = i - delta
-                    const float4 rf = fma4s(-alpha, rows4(Qf, i0, sh, lo, hi), rows4(Rof, i0, sh, lo, hi));
-                    t = fma4(rows4(Lv + (size_t)k * n, i0, sh, lo, hi), rf, t);
+                    const int r = ST7 ? cls_lt(k) : (int)(sh & 3);
+                    const float4 rf = fma4s(-alpha, rows4r(Qf, i0, sh, r, lo, hi), rows4r(Rof, i0, sh, r, lo, hi));
+                    t = fma4(rows4r(Lv + (size_t)k * n, i0, sh, r, lo, hi), rf, t);
                   }
                 }
                 st4(Rnf + i0, ri);
@@ -794,8 +811,10 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
               float4 z = f4zero();
               if (act) {
 #pragma unroll
-                for (int k = 0; k < KMAX; k++)
-                  if (k < c.KL) z = fma4(ld4(Lv + (size_t)k * n + i0), rows4(Tf, i0, ld[k], lo, hi), z);
+                for (int k = 0; k < KMAX; k++) {
+                  const int r = ST7 ? cls_l(k) : (int)(ld[k] & 3);
+                  if (k < KF) z = fma4(ld4(Lv + (size_t)k * n + i0), rows4r(Tf, i0, ld[k], r, lo, hi), z);
+                }
               }
               st4(Df + i0, fma4s(alpha, po, dold));
               if (act) st4(reinterpret_cast<float*>(Pnew) + i0, fma4s(beta, po, z));
@@ -875,17 +894,25 @@ __global__ void k_dia_dinv(const double* __restrict__ a64, const int* __restrict
 }
 
 template <class T, class V, class LV>
-cudaError_t launch_persistent(const DiaCg& c, int grid, cudaStream_t s) {
-  void* args[] = {const_cast<DiaCg*>(&c)};
-  return cudaLaunchCooperativeKernel((const void*)k_cg_persistent<T, V, LV>, dim3(grid), dim3(PNT), args, 0, s);
+const void* kernel_of(bool st7) {
+  if constexpr (sizeof(T) == 4) {
+    if (st7) return (const void*)k_cg_persistent<T, V, LV, 1>;
+  }
+  return (const void*)k_cg_persistent<T, V, LV, 0>;
 }
 
 template <class T, class V, class LV>
-int resident_grid() {
+cudaError_t launch_persistent(const DiaCg& c, int grid, cudaStream_t s) {
+  void* args[] = {const_cast<DiaCg*>(&c)};
+  return cudaLaunchCooperativeKernel(kernel_of<T, V, LV>(c.st7 != 0), dim3(grid), dim3(PNT), args, 0, s);
+}
+
+template <class T, class V, class LV>
+int resident_grid(bool st7) {
   int dev = 0, sms = 0, per = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cg_persistent<T, V, LV>, PNT, 0) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel_of<T, V, LV>(st7), PNT, 0) != cudaSuccess)
     return 0;
   return sms * per;
 }
@@ -899,16 +926,28 @@ int variant(int prec, int lprec) {
 
 }  // namespace
 
-int cg_dia_grid(int prec, int lprec) {
+int cg_dia_grid(int prec, int lprec, int st7) {
   switch (variant(prec, lprec)) {
-    case 0: return resident_grid<double, double, float>();
-    case 1: return resident_grid<double, double, __nv_bfloat16>();
-    case 2: return resident_grid<float, float, float>();
-    case 3: return resident_grid<float, float, __nv_bfloat16>();
-    case 4: return resident_grid<float, __nv_bfloat16, float>();
-    case 5: return resident_grid<float, __nv_bfloat16, __nv_bfloat16>();
+    case 0: return resident_grid<double, double, float>(false);
+    case 1: return resident_grid<double, double, __nv_bfloat16>(false);
+    case 2: return resident_grid<float, float, float>(st7 != 0);
+    case 3: return resident_grid<float, float, __nv_bfloat16>(st7 != 0);
+    case 4: return resident_grid<float, __nv_bfloat16, float>(st7 != 0);
+    case 5: return resident_grid<float, __nv_bfloat16, __nv_bfloat16>(st7 != 0);
   }
   return 0;
+}
+
+bool dia_seven_point(const int* adelta, const int* ldelta, int nsys, int K, int KL) {
+  if (K != 7 || (ldelta && KL != 4)) return false;
+  for (int s = 0; s < nsys; s++) {
+    for (int k = 0; k < 7; k++)
+      if ((adelta[s * kDiaMaxDiag + k] & 3) != cls_a(k)) return false;
+    if (ldelta)
+      for (int k = 0; k < 4; k++)
+        if ((ldelta[s * kDiaMaxDiag + k] & 3) != cls_l(k)) return false;
+  }
+  return true;
 }
 
 cudaError_t cg_dia_solve(const DiaCg& c, int grid, cudaStream_t s) {

@@ -269,10 +269,17 @@ struct DiaCg {
   int refresh;            // iterations per refinement cycle (narrow storage), 0 = never
   int vec4;               // every system's first row and size a multiple of 4, FP32 iteration:
                           // the hot phases take 4 rows per thread with 16-byte loads
+  int st7;                // with vec4: every system in the seven-point form (dia_seven_point)
   long long wait_ns;      // bound on one grid-wide wait
 };
-// Co-resident CTAs of the persistent kernel for (prec, lprec) on this device.
-int cg_dia_grid(int prec, int lprec);
+// Co-resident CTAs of the persistent kernel for (prec, lprec, seven-point
+// form) on this device.
+int cg_dia_grid(int prec, int lprec, int st7);
+// Host check of the seven-point form: every system has K = 7 slots whose
+// deltas fall in the alignment classes of -n^2, -n, -1, 0, +1, +n, +n^2 with
+// n^2 and n multiples of 4 (ascending slot order), and, with a factor
+// (ldelta not null), KL = 4 slots in the classes of 0, -1, -n, -n^2.
+bool dia_seven_point(const int* adelta, const int* ldelta, int nsys, int K, int KL);
 // The whole batched solve, one cooperative launch of `grid` CTAs.
 cudaError_t cg_dia_solve(const DiaCg& c, int grid, cudaStream_t s);
 // out[k * n + i] = value of row i on slot k (zeroed by the caller).

@@ -521,9 +521,14 @@ class Batch:
     def engine(self) -> dict:
         """Engine of the last cg(): persistent (one cooperative launch) or
         multi-launch, and whether a CUDA graph replayed it."""
-        p, g = C.c_int(), C.c_int()
-        check(lib.tbsla_batch_engine(self._h, C.byref(p), C.byref(g)), "batch_engine")
-        return {"persistent": bool(p.value), "graph": bool(g.value)}
+        p, g, s7 = C.c_int(), C.c_int(), C.c_int()
+        check(lib.tbsla_batch_engine(self._h, C.byref(p), C.byref(g), C.byref(s7)), "batch_engine")
+        return {"persistent": bool(p.value), "graph": bool(g.value), "seven_point": bool(s7.value)}
+
+    def set_seven_point(self, on: bool):
+        """Persistent engine: the seven-point form where it applies (True,
+        default) or always the general form."""
+        check(lib.tbsla_batch_set_seven_point(self._h, int(bool(on))), "batch_set_seven_point")
 
 
 class MPNN:

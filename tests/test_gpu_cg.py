@@ -242,3 +242,37 @@ def test_autotune_batch_cg_and_cache(gpu, tmp_path):
     off = batch.offsets
     for k, m in enumerate(systems):
         assert true_rel_residual(m, x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]) <= TOL
+
+
+def test_seven_point_form_matches_general_form(gpu):
+    """Batches of 7-point stencils whose line and plane sizes are multiples
+    of 4 run the persistent kernel's seven-point form (neighbour alignments
+    fixed when compiled); it does the general form's arithmetic in the same
+    order, so the two agree up to the FP64 atomic dot products' order:
+    iterations within 1% (at least one), every system FP64-verified, for
+    plain, Jacobi and the factored preconditioner (an untrained network's
+    factor on tril(A)).  A batch with a system of line size 10 keeps the
+    general form."""
+    T = gpu
+    sizes = [8, 12, 16, 20]
+    systems = [diffusion(T, s, 740 + i) for i, s in enumerate(sizes)]
+    rhs = np.concatenate([T.fill_uniform(s ** 3, -1.0, 1.0, 750 + i) for i, s in enumerate(sizes)])
+    batch = T.Batch(systems, T.F32)
+    net = T.MPNN(3)
+    batch.factor_mpnn(net, T.BF16)
+    off = batch.offsets
+    for precond in (0, 1, 2):
+        out = []
+        for on in (True, False):
+            batch.set_seven_point(on)
+            x, its, rr, ok = batch.cg(rhs, max_iterations=4000, rel_tol=TOL, precond=precond, refresh=50)
+            assert ok and (rr <= TOL).all()
+            assert batch.engine()["seven_point"] == on, (precond, on)
+            for k, m in enumerate(systems):
+                assert true_rel_residual(m, x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]) <= TOL
+            out.append(its)
+        assert (np.abs(out[0] - out[1]) <= np.maximum(1, out[0] // 100)).all(), (precond, out)
+    mixed = T.Batch([diffusion(T, 10, 760), diffusion(T, 8, 761)], T.F32)
+    rhs2 = np.concatenate([T.fill_uniform(1000, -1.0, 1.0, 762), T.fill_uniform(512, -1.0, 1.0, 763)])
+    x, its, rr, ok = mixed.cg(rhs2, max_iterations=4000, rel_tol=TOL, precond=1)
+    assert ok and not mixed.engine()["seven_point"] and mixed.engine()["persistent"]
