@@ -268,6 +268,7 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
   __shared__ int s_su[kDiaMaxSys + 1];    // first warp unit of each system, then the unit count
   __shared__ int s_end[kDiaMaxSys];       // selected units of systems 0..s
   __shared__ int s_nsel;
+  __shared__ int s_ad[kDiaMaxSys * KMAX], s_ld[kDiaMaxSys * KMAX];
   const int ns = c.nsys;
   const int tid = threadIdx.x;
   const int lane_ = tid & 31, warp_ = tid >> 5;
@@ -290,6 +291,10 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
   const uint64_t pol = policy_evict_first();
 
   for (int s = tid; s <= ns; s += PNT) s_off[s] = c.sys_off[s];
+  for (int t = tid; t < ns * KMAX; t += PNT) {
+    s_ad[t] = c.adelta[t];
+    s_ld[t] = c.ldelta ? c.ldelta[t] : 0;
+  }
   __syncthreads();
   if (tid == 0) {
     int u = 0;
@@ -362,9 +367,12 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
     }
     return lo;
   };
+  // the delta tables, copied to shared memory once (every unit reads its
+  // system's row of one of them)
   auto load_deltas = [&](const int* tab, int s, int kk, int (&dd)[KMAX]) {
+    const int* t = tab == c.adelta ? s_ad : s_ld;
 #pragma unroll
-    for (int k = 0; k < KMAX; k++) dd[k] = k < kk ? tab[s * KMAX + k] : 0;
+    for (int k = 0; k < KMAX; k++) dd[k] = k < kk ? t[s * KMAX + k] : 0;
   };
 
   for (;;) {
