@@ -129,6 +129,13 @@ class Clocks:
             self.t.start()
         except OSError:
             self.proc = None
+            return
+        # nvidia-smi's start-up (NVML initialisation) slowed the host-driven
+        # pageable copies that ran beside it: wait for its first sample (at
+        # most 3 s) so that the timed region sees only its steady sampling
+        t0 = time.time()
+        while not self.lines and self.proc.poll() is None and time.time() - t0 < 3.0:
+            time.sleep(0.01)
 
     def _read(self):
         for line in self.proc.stdout:

@@ -1121,7 +1121,8 @@ int dev_page_rank_batched(tbsla_matrix* m, int nvec, const double* tele, double 
   // FP32 pipe; FP64 values keep FP64 arithmetic
   const bool df = d->prec != TBSLA_F64;
   const int gather = m->pr_gather == 16 ? 16 : 8;
-  const int stream = m->pr_stream;
+  // the row-block stream form keeps X row offsets in 32 bits
+  const int stream = m->pr_stream && (long)I.n_col * nvec <= 0x7fffffffL ? 1 : 0;
   int grid = csr_pagerank_batched_grid(d->prec, gather, stream);
   // the buffers stay with the device copy: repeated solves allocate (and
   // synchronise on frees) nothing

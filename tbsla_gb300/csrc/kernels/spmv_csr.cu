@@ -224,19 +224,30 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int n
 // differs.  Rows of a few entries (most rows of a power-law graph) then
 // share one gather latency instead of paying one each, and a row's
 // epilogue operands (T, X, w) are loaded when the previous row finishes.
+//
+// The kernel is bound by instruction issue and by how many warps hide the
+// gathers, so the per-entry work is kept small: each lane turns its entry
+// of a 32-entry chunk into (X row offset, value) once and leaves it in
+// shared memory, where every lane reads it back with one broadcast load
+// (the offset is 32-bit: the host takes this form only when
+// n_col * nvec < 2^31); a batch of GB whole entries that no row ends inside
+// runs without the per-entry row-end test; and the register cap keeps four
+// CTAs (32 warps) on an SM for GB = 8 (two for GB = 16).
 template <class V, int GB>
-__global__ void __launch_bounds__(NT) k_csr_pagerank_batched_dfs(CsrArgs a, int nvec, const float2* __restrict__ X,
-                                                                float2* __restrict__ Y, const float2* __restrict__ T,
-                                                                const float2* __restrict__ W, PageRankArgs p,
-                                                                Ctl ctl) {
+__global__ void __launch_bounds__(NT, GB <= 8 ? 4 : 2)
+    k_csr_pagerank_batched_dfs(CsrArgs a, int nvec, const float2* __restrict__ X, float2* __restrict__ Y,
+                               const float2* __restrict__ T, const float2* __restrict__ W, PageRankArgs p, Ctl ctl) {
   __shared__ Smem sm;
   __shared__ double s_red[NT / kWarp][3 * kWarp];
+  __shared__ int2 s_ent[NT / kWarp][kWarp];  // per warp: its chunk's (X row offset, value bits)
   if (*(volatile int*)p.done) return;
   constexpr unsigned full = 0xffffffffu;
   const uint64_t pol = policy_evict_first();
   const V* vals = static_cast<const V*>(a.vals);
-  const int lane = threadIdx.x % kWarp;
+  const int warp = threadIdx.x / kWarp, lane = threadIdx.x % kWarp;
   const bool active = lane < nvec;
+  const float2* __restrict__ Xl = X + lane;
+  int2* const ent = s_ent[warp];
   const double scd = active ? p.coef_in[lane] : 0.0;
   const DF sc = df_of(scd), tc = df_of(active ? p.coef_in[kWarp + lane] : 0.0), bsc = df_of(mul_rn(p.beta, scd));
   DF err{0.f, 0.f}, sum{0.f, 0.f}, dsum{0.f, 0.f};
@@ -288,28 +299,51 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_dfs(CsrArgs a, int 
     };
     for (int base = s0; base < e0; base += kWarp) {
       const int j = base + lane;
-      int c = 0;
+      int xo = 0;
       float v = 0.f;
       if (j < e0) {
-        c = ld_stream(a.colidx + j, pol);
+        xo = (ld_stream(a.colidx + j, pol) - a.f_col) * nvec;
         v = as_f32(ld_stream(vals + j, pol));
       }
+      __syncwarp();
+      ent[lane] = make_int2(xo, __float_as_int(v));
+      __syncwarp();
       const int m = min(kWarp, e0 - base);
-      for (int t = 0; t < m; t += GB) {
+      int t = 0;
+      for (; t + GB <= m; t += GB) {
+        DF xv[GB];
+        float vv[GB];
+#pragma unroll
+        for (int u = 0; u < GB; u++) {
+          const int2 ev = ent[t + u];
+          vv[u] = __int_as_float(ev.y);
+          xv[u] = active ? df_ld(Xl + ev.x) : DF{0.f, 0.f};
+        }
+        if (base + t + GB <= row_end) {  // no row ends inside the batch
+#pragma unroll
+          for (int u = 0; u < GB; u++) dot2_step(as, ac, vv[u], xv[u]);
+        } else {
+#pragma unroll
+          for (int u = 0; u < GB; u++) {
+            while (base + t + u >= row_end) finish();  // rows ending before this entry (empty ones too)
+            dot2_step(as, ac, vv[u], xv[u]);
+          }
+        }
+      }
+      if (t < m) {  // the block's last, partial batch (its dead slots neither load nor add)
         DF xv[GB];
         float vv[GB];
 #pragma unroll
         for (int u = 0; u < GB; u++) {
           const bool live = t + u < m;
-          const int ct = __shfl_sync(full, c, (t + u) & (kWarp - 1));
-          const float vu = __shfl_sync(full, v, (t + u) & (kWarp - 1));
-          vv[u] = live ? vu : 0.f;
-          xv[u] = (active && live) ? df_ld(X + (size_t)(ct - a.f_col) * nvec + lane) : DF{0.f, 0.f};
+          const int2 ev = ent[(t + u) & (kWarp - 1)];
+          vv[u] = live ? __int_as_float(ev.y) : 0.f;
+          xv[u] = (active && live) ? df_ld(Xl + ev.x) : DF{0.f, 0.f};
         }
 #pragma unroll
         for (int u = 0; u < GB; u++) {
           if (t + u < m) {
-            while (base + t + u >= row_end) finish();  // rows ending before this entry (empty ones too)
+            while (base + t + u >= row_end) finish();
             dot2_step(as, ac, vv[u], xv[u]);
           }
         }

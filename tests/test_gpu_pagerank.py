@@ -138,6 +138,38 @@ def test_batched_pagerank_gather_width(gpu, tmp_path):
     assert A.tune_pagerank_batched(g, tele, T.F32, path=str(tmp_path / "t.json"))["cached"]
 
 
+def test_batched_pagerank_bf16_partial_warp(gpu):
+    """BF16-valued batched PageRank with 7 vectors (lanes 7-31 of every warp
+    idle): a warp per row and the row-block stream form, each within 1e-10
+    in L1 of the oracle on the bfloat16-rounded values, and within 1e-13 of
+    each other."""
+    T = gpu
+    n = 1 << 13
+    g = graph(T, n, seed=9)
+    g.make_stochastic(np.zeros(n))
+    g.set_precision(T.BF16)
+    rng = np.random.default_rng(5)
+    nvec = 7
+    tele = np.zeros((n, nvec))
+    for k in range(nvec):
+        tele[rng.choice(n, 20 + k, replace=False), k] = 1.0 / (20 + k)
+    out = []
+    for stream in (False, True):
+        g.set_pagerank_stream(stream)
+        X, it, ok = g.page_rank_batched(tele, 0.85, 1e-10, 500)
+        assert ok
+        out.append((X, it))
+    assert out[0][1] == out[1][1]
+    assert np.abs(out[0][0] - out[1][0]).sum(axis=0).max() <= 1e-13
+    a = g.arrays()
+    vb = oracle.bf16_round(a["values"])
+    for k in range(nvec):
+        xr, _, _ = oracle.pagerank(a["rowptr"], a["colidx"], vb, 0.85, 1e-10, out[1][1], stop_early=False,
+                                   teleport=np.ascontiguousarray(tele[:, k]))
+        for X, _ in out:
+            assert np.abs(X[:, k] - xr).sum() <= 1e-10, k
+
+
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_pagerank_fused_epilogue(gpu, prec):
     """With one column block the sliced-ELL kernel runs each step's epilogue
