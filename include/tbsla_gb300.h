@@ -223,7 +223,9 @@ int tbsla_matrix_set_pagerank_gather(tbsla_matrix* m, int gather);
  * whole row block and walks its entries as one stream, `gather` X rows in
  * flight across row boundaries; 0 a warp per row.  The same Y bit for bit
  * (each row sums in entry order either way); the norms' partial sums are
- * added in another order.  No reference counterpart. */
+ * added in another order.  The row-block form keeps X row offsets in 32
+ * bits, so with n_col * nvec >= 2^31 the warp-per-row form runs whatever
+ * this setting.  No reference counterpart. */
 int tbsla_matrix_set_pagerank_stream(tbsla_matrix* m, int stream);
 /* PageRank with the sliced-ELL kernel and one column block: 1 (default)
  * runs each step's epilogue -- the new iterate and its three FP64 sums --
