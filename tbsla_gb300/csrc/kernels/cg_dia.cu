@@ -703,8 +703,18 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
                 // would hold the later loads back a whole memory round trip)
                 const float4 ri = fma4s(-alpha, ld4(Qf + i0), ld4(Rof + i0));
                 float4 t = f4zero();
+                if constexpr (ST7 != 0) {
+                  // L's slots 0 (delta 0) and 1 (rows i0 + 1 .. i0 + 4): the
+                  // new residual of the row itself is ri, and three of the
+                  // four shifted rows are ri's; only row i0 + 4 is formed
+                  // anew (the same operations as the general loop below)
+                  t = fma4(ld4(Lv + i0), ri, t);
+                  const long j = i0 + 4;
+                  const float rn = j < hi ? fmaf(-alpha, Qf[j], Rof[j]) : 0.f;
+                  t = fma4(rows4r(Lv + (size_t)n, i0, 1, 1, lo, hi), make_float4(ri.y, ri.z, ri.w, rn), t);
+                }
 #pragma unroll
-                for (int k = 0; k < KMAX; k++) {
+                for (int k = ST7 ? 2 : 0; k < KMAX; k++) {
                   if (k < KF) {
                     const long sh = -(long)ld[k];  // L_{j,i} sits on row j = i - delta
                     const int r = ST7 ? cls_lt(k) : (int)(sh & 3);
@@ -818,8 +828,17 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
               const float4 po = ld4(reinterpret_cast<const float*>(Pold) + i0), dold = ld4(Df + i0);
               float4 z = f4zero();
               if (act) {
+                if constexpr (ST7 != 0) {
+                  // slot 0 (the rows themselves) and slot 1 (rows i0 - 1 ..
+                  // i0 + 2) from the rows' own vector of t and the one entry
+                  // before it
+                  const float4 t0 = ld4(Tf + i0);
+                  z = fma4(ld4(Lv + i0), t0, z);
+                  const float tm = i0 - 4 >= lo ? Tf[i0 - 1] : 0.f;
+                  z = fma4(ld4(Lv + (size_t)n + i0), make_float4(tm, t0.x, t0.y, t0.z), z);
+                }
 #pragma unroll
-                for (int k = 0; k < KMAX; k++) {
+                for (int k = ST7 ? 2 : 0; k < KMAX; k++) {
                   const int r = ST7 ? cls_l(k) : (int)(ld[k] & 3);
                   if (k < KF) z = fma4(ld4(Lv + (size_t)k * n + i0), rows4r(Tf, i0, ld[k], r, lo, hi), z);
                 }
