@@ -394,8 +394,9 @@ int tbsla_batch_cg(tbsla_batch* b, const double* rhs, double* x, int max_iterati
  * with the preconditioner asked for, 1 when its factor failed the check made
  * before the first iteration (a non-finite value or a diagonal entry <= 0)
  * and it ran Jacobi-PCG instead, 2 when its factored iteration stopped making
- * progress (a refinement cycle that did not lower the FP64 true residual, or
- * r.z not positive and finite) and it continued with Jacobi-PCG;
+ * progress (a refinement cycle that did not lower the FP64 true residual, a
+ * cycle of 25 iterations or more that cut it by less than 10%, or r.z not
+ * positive and finite) and it continued with Jacobi-PCG;
  * precond_used[s] = the preconditioner it ended with (0, 1, 2).  Either
  * pointer may be NULL.  Plain Jacobi-PCG is the fallback of the factored
  * preconditioner: the reference's CG (CG.cpp:32-73) has none. */

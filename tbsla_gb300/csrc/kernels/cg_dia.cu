@@ -28,8 +28,9 @@
 // (stored in FP32 or BF16, applied in T arithmetic).  Mode 2 falls back to
 // Jacobi for the system (fallback code in its status) when its factor holds
 // a non-finite value or a diagonal entry <= 0 (checked before the first
-// iteration), when a refinement cycle does not lower its FP64 true residual,
-// or when r.z stops being positive and finite.
+// iteration), when a refinement cycle does not lower its FP64 true residual
+// (or, over 25 iterations or more, cuts its norm by less than 10%), or when
+// r.z stops being positive and finite.
 //
 // One iteration, all systems at once, grid-wide barriers between phases:
 //   A   q = A p; p.q              (modes 0/1 form p = z + beta p_old on the
@@ -472,7 +473,12 @@ __global__ void __launch_bounds__(PNT, 3) k_cg_persistent(DiaCg c) {
           } else if (s_it[s] >= c.max_it) {
             s_st[s] = S_STOPPED;
           } else {
-            if (s_mode[s] == 2 && !init && !(rrt < s_prev[s])) {  // no progress over a cycle (or NaN)
+            // the factored iteration is given up when a refinement cycle did
+            // not lower the FP64 true residual (or gave NaN), or when a cycle
+            // of 25 iterations or more cut its norm by less than 10%
+            // (squared: to above 0.81 of the last): progress too slow to keep
+            const double keep_below = s_since[s] >= 25 ? 0.81 * s_prev[s] : s_prev[s];
+            if (s_mode[s] == 2 && !init && !(rrt < keep_below)) {
               s_mode[s] = 1;
               s_fb[s] = kFallbackStagnation;
             }
@@ -970,9 +976,14 @@ bool dia_seven_point(const int* adelta, const int* ldelta, int nsys, int K, int 
   for (int s = 0; s < nsys; s++) {
     for (int k = 0; k < 7; k++)
       if ((adelta[s * kDiaMaxDiag + k] & 3) != cls_a(k)) return false;
-    if (ldelta)
+    if (ldelta) {
+      const int* l = ldelta + s * kDiaMaxDiag;
       for (int k = 0; k < 4; k++)
-        if ((ldelta[s * kDiaMaxDiag + k] & 3) != cls_l(k)) return false;
+        if ((l[k] & 3) != cls_l(k)) return false;
+      // phases B' and D take L's slots 0 and 1 from the rows' own vectors:
+      // those two deltas must be exactly 0 and -1, not only of their class
+      if (l[0] != 0 || l[1] != -1) return false;
+    }
   }
   return true;
 }

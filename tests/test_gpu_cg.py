@@ -251,15 +251,18 @@ def test_seven_point_form_matches_general_form(gpu):
     order, so the two agree up to the FP64 atomic dot products' order:
     iterations within 1% (at least one), every system FP64-verified, for
     plain, Jacobi and the factored preconditioner (an untrained network's
-    factor on tril(A)).  A batch with a system of line size 10 keeps the
-    general form."""
+    factor on tril(A), from a network whose head makes every off-diagonal
+    slot of the factor non-zero).  A batch with a system of
+    line size 10 keeps the general form."""
     T = gpu
     sizes = [8, 12, 16, 20]
     systems = [diffusion(T, s, 740 + i) for i, s in enumerate(sizes)]
     rhs = np.concatenate([T.fill_uniform(s ** 3, -1.0, 1.0, 750 + i) for i, s in enumerate(sizes)])
     batch = T.Batch(systems, T.F32)
-    net = T.MPNN(3)
+    net = _neumann_net(T, 3)
     batch.factor_mpnn(net, T.BF16)
+    _, lv = batch.factor_dia()
+    assert np.count_nonzero(lv[1]) > lv.shape[1] // 2  # the -1 slot of L is populated
     off = batch.offsets
     for precond in (0, 1, 2):
         out = []
@@ -276,3 +279,55 @@ def test_seven_point_form_matches_general_form(gpu):
     rhs2 = np.concatenate([T.fill_uniform(1000, -1.0, 1.0, 762), T.fill_uniform(512, -1.0, 1.0, 763)])
     x, its, rr, ok = mixed.cg(rhs2, max_iterations=4000, rel_tol=TOL, precond=1)
     assert ok and not mixed.engine()["seven_point"] and mixed.engine()["persistent"]
+
+
+def _neumann_net(T, seed):
+    """A network whose head gives L = D^-1/2 (I - E_lower / 2) on the
+    pattern of tril(A) (E the scaled off-diagonal entries a_ij s_i s_j):
+    a first-order approximate inverse factor, SPD as M^-1 = L L^T, with
+    every off-diagonal slot of L populated."""
+    import oracle.mpnn as M
+
+    net = T.MPNN(seed)
+    p = M.unpack(net.params().astype(np.float64))
+    p["ce"] = -0.5
+    net.set_params(M.pack(p).astype(np.float32))
+    return net
+
+
+def test_seven_point_form_needs_unit_neighbours(gpu):
+    """With a factor, the seven-point form takes L's delta-0 and delta--1
+    windows from the rows' own vectors, so it needs those exact deltas, not
+    only their alignment classes: a system on the diagonals -64, -8, -5, 0,
+    +5, +8, +64 (the classes of a 7-point stencil of line size 8; L on
+    deltas 0, -5, -8, -64) runs the general form with a factor whose
+    off-diagonal slots are populated; Jacobi, which reads every shift at
+    run time, may take either form.  Both reach the FP64-verified
+    tolerance."""
+    T = gpu
+    n = 512
+    offs = (-64, -8, -5, 0, 5, 8, 64)
+    rows, cols, vals = [], [], []
+    for i in range(n):
+        for d in offs:
+            j = i + d
+            if 0 <= j < n:
+                rows.append(i)
+                cols.append(j)
+                vals.append(6.5 if d == 0 else -1.0)
+    rowptr = np.zeros(n + 1, np.int64)
+    np.add.at(rowptr, np.asarray(rows) + 1, 1)
+    rowptr = np.cumsum(rowptr)
+    a5 = T.MatrixCSR.from_arrays(n, n, rowptr, np.asarray(cols), np.asarray(vals))
+    systems = [a5, diffusion(T, 8, 770)]
+    rhs = np.concatenate([T.fill_uniform(n, -1.0, 1.0, 771), T.fill_uniform(512, -1.0, 1.0, 772)])
+    batch = T.Batch(systems, T.F32)
+    batch.factor_mpnn(_neumann_net(T, 4), T.BF16)
+    off = batch.offsets
+    for precond in (1, 2):
+        x, its, rr, ok = batch.cg(rhs, max_iterations=4000, rel_tol=TOL, precond=precond, refresh=50)
+        assert ok and (rr <= TOL).all()
+        eng = batch.engine()
+        assert eng["persistent"] and (precond == 1 or not eng["seven_point"]), (precond, eng)
+        for k, m in enumerate(systems):
+            assert true_rel_residual(m, x[off[k]:off[k + 1]], rhs[off[k]:off[k + 1]]) <= TOL

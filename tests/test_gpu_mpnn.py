@@ -210,6 +210,39 @@ def test_jacobi_fallback_on_bad_factors(gpu):
             o += k
 
 
+def test_slow_factor_falls_back(gpu):
+    """A factor that keeps lowering the residual, but too slowly, is given up
+    too: with the network head set to L = D^-1/2 (I + 4 E_lower) (E the
+    scaled off-diagonal entries) the factored iteration keeps 0.90-0.99 of
+    the residual norm per 50 iterations on these systems and does not
+    converge in 4,000 iterations (float64 restatement on the host).  The
+    first refinement cycle that cuts the FP64 true residual by less than
+    10% hands each system to Jacobi: all reach the FP64-verified 1e-8, with
+    fallback code 2."""
+    T = gpu
+    systems = [diffusion(T, 12 + 4 * i, 741 + i) for i in range(2)]
+    net = T.MPNN(3)
+    p = M.unpack(net.params().astype(np.float64))
+    p["ce"] = 4.0
+    net.set_params(M.pack(p).astype(np.float32))
+    bt = T.Batch(systems, T.F32)
+    bt.factor_mpnn(net, T.F32)
+    rhs = np.concatenate([T.fill_uniform(len(s.arrays()["rowptr"]) - 1, -1.0, 1.0, 40 + i)
+                          for i, s in enumerate(systems)])
+    x, its, rr, ok = bt.cg(rhs, max_iterations=4000, rel_tol=1e-8, precond=2, refresh=50)
+    assert ok and (rr <= 1e-8).all(), (its, rr)
+    fb, used = bt.fallbacks()
+    assert list(fb) == [2, 2] and list(used) == [1, 1], (fb, used)
+    assert (its < 1000).all(), its
+    o = 0
+    for s in systems:
+        a = s.arrays()
+        k = len(a["rowptr"]) - 1
+        res = rhs[o:o + k] - oracle.csr_ax(a["rowptr"], a["colidx"], a["values"], x[o:o + k])
+        assert np.linalg.norm(res) <= 1.0001e-8 * np.linalg.norm(rhs[o:o + k])
+        o += k
+
+
 def test_device_factor_pipeline_matches_host_factor(gpu):
     """tbsla_batch_factor_mpnn runs the network on the batch's device copy of
     A and writes L into the batch's factor storage with no host round trip.
