@@ -30,6 +30,16 @@ __device__ __forceinline__ DF df_add(DF a, DF b) {
   s = fast_two_sum(s.h, __fadd_rn(s.l, t.h));
   return fast_two_sum(s.h, __fadd_rn(s.l, t.l));
 }
+// a + b for double-float values of the same sign: one two_sum of the high
+// parts, the low parts added to its error, then renormalised (the "sloppy"
+// double-word addition of Dekker 1971; Joldes, Muller & Popescu 2017,
+// Algorithm 5).  Without cancellation its relative error stays within a few
+// units of 2^-48, and in any case its absolute error within a few units of
+// 2^-48 (|a| + |b|); operands that may cancel take df_add.
+__device__ __forceinline__ DF df_add_same_sign(DF a, DF b) {
+  const DF s = two_sum(a.h, b.h);
+  return fast_two_sum(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
 __device__ __forceinline__ DF df_mul(DF a, DF b) {
   const float pr = __fmul_rn(a.h, b.h);
   const float e = __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.l, __fmaf_rn(a.h, b.h, -pr)));

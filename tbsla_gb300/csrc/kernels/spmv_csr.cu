@@ -147,9 +147,12 @@ __device__ __forceinline__ float as_f32(__nv_bfloat16 v) { return __bfloat162flo
 // The batched step in double-float, for FP32 / BF16 values (exact in one
 // float): X, Y, T and the column sums w are stored as float pairs; each
 // lane sums its row's products a_ij X[j, k] in entry order as a compensated
-// dot product (Dot2: about twice FP32 precision), and the epilogue forms the single-vector epilogue's quantities (y = beta s acc +
-// t T, |y - x s|, y, w y) in the same arithmetic.  The CTA and grid
-// reductions run in FP64 (batched_finish).
+// dot product (Dot2: about twice FP32 precision), and the epilogue forms the
+// single-vector epilogue's quantities (y = beta s acc + t T, |y - x s|, y,
+// w y) in the same arithmetic: the difference y - x s, which cancels as the
+// iteration converges, with the full double-float addition, the sums of
+// terms of one sign (y's two terms, the three running sums) with the
+// same-sign one.  The CTA and grid reductions run in FP64 (batched_finish).
 template <class V, int GB>
 __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int nvec, const float2* __restrict__ X,
                                                                float2* __restrict__ Y, const float2* __restrict__ T,
@@ -202,12 +205,12 @@ __global__ void __launch_bounds__(NT) k_csr_pagerank_batched_df(CsrArgs a, int n
       if (active) {
         const DF acc = fast_two_sum(as, ac);
         const size_t o = (size_t)row * nvec + lane;
-        const DF yn = df_add(df_mul(bsc, acc), df_mul(tc, df_ld(T + o)));
+        const DF yn = df_add_same_sign(df_mul(bsc, acc), df_mul(tc, df_ld(T + o)));
         DF dx = df_add(yn, df_neg(df_mul(df_ld(X + o), sc)));
         if (dx.h < 0) dx = df_neg(dx);
-        err = df_add(err, dx);
-        sum = df_add(sum, yn);
-        dsum = df_add(dsum, df_mul(df_ld(W + row), yn));
+        err = df_add_same_sign(err, dx);
+        sum = df_add_same_sign(sum, yn);
+        dsum = df_add_same_sign(dsum, df_mul(df_ld(W + row), yn));
         Y[o] = make_float2(yn.h, yn.l);
       }
     }
@@ -278,12 +281,12 @@ __global__ void __launch_bounds__(NT, GB <= 8 ? 4 : 2)
     auto finish = [&]() {
       if (active) {
         const DF acc = fast_two_sum(as, ac);
-        const DF yn = df_add(df_mul(bsc, acc), df_mul(tc, tn));
+        const DF yn = df_add_same_sign(df_mul(bsc, acc), df_mul(tc, tn));
         DF dx = df_add(yn, df_neg(df_mul(xn, sc)));
         if (dx.h < 0) dx = df_neg(dx);
-        err = df_add(err, dx);
-        sum = df_add(sum, yn);
-        dsum = df_add(dsum, df_mul(wn, yn));
+        err = df_add_same_sign(err, dx);
+        sum = df_add_same_sign(sum, yn);
+        dsum = df_add_same_sign(dsum, df_mul(wn, yn));
         Y[(size_t)row * nvec + lane] = make_float2(yn.h, yn.l);
       }
       as = ac = 0.f;
