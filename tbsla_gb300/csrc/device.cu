@@ -120,7 +120,7 @@ struct DeviceMatrix {
   size_t y_len = 0;
   double* t = nullptr;
   size_t t_len = 0;
-  bool dense_df = false;     // DENSE, FP32 / BF16 values within the double-float range
+  bool dense_df = false;     // DENSE, every value within the double-float range (any precision)
   float* xdf = nullptr;      // DENSE double-float: x split into xh[ln_col], xl[ln_col]
   int* df_flag = nullptr;    // DENSE double-float: x out of range in this call
   double* pr_ctl = nullptr;  // PageRank: coefficients [0, 4) and flags (2 int) at [4]
