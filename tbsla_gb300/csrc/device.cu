@@ -226,8 +226,9 @@ void sort_by_row(const tbsla_matrix* m, long nnz, int rmin, int rmax, std::vecto
 }
 
 // Host <-> device copies of the large arrays go straight from and to the
-// caller's pageable memory: on this host (Grace, C2C link) the driver moves
-// pageable memory at the link's rate, 195 GB/s either way for 1 GiB (5.5 ms),
+// caller's pageable memory: on a Grace host (GB300 on the C2C link) the
+// driver moves pageable memory at the link's rate, measured at 195 GB/s
+// either way for 1 GiB (5.5 ms),
 // the same as from pinned memory, while staging through pinned buffers adds
 // a host memcpy (1 GiB in 76 ms on one core).
 int h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
