@@ -34,3 +34,35 @@ def test_reference_arm_loads_no_library_code():
     out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     assert out.stdout.strip().splitlines()[-1] == "CLEAN"
+
+
+def test_clock_sampler_waits_for_its_first_sample(tmp_path, monkeypatch):
+    """The clock sampler starts nvidia-smi before a timed region and returns
+    only once the first sample is in (the tool's start-up slowed host copies
+    beside it), then parses clocks and throttle reasons; a tool that exits
+    at once does not hold the caller.  A fake nvidia-smi on PATH, no GPU."""
+    import importlib.util
+    import time
+
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text("#!/bin/sh\nsleep 0.4\n"
+                    "while true; do echo '2070, 2070, 900.0, 0x0, Not Active, Not Active, Not Active, Active'; "
+                    "sleep 0.05; done\n")
+    fake.chmod(0o755)
+    monkeypatch.setenv("PATH", f"{tmp_path}{os.pathsep}{os.environ['PATH']}")
+    spec = importlib.util.spec_from_file_location("bench_under_test", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    c = bench.Clocks(0)
+    t0 = time.time()
+    c.start()
+    assert time.time() - t0 >= 0.35 and c.lines
+    d = c.stop()
+    assert d["sm_mhz"] == 2070.0 and d["sm_max_mhz"] == 2070.0 and d["reasons"] == ["sw_power_cap"]
+    assert d["samples"] >= 1
+    fake.write_text("#!/bin/sh\nexit 0\n")
+    c = bench.Clocks(0)
+    t0 = time.time()
+    c.start()
+    assert time.time() - t0 < 2.0
+    assert c.stop()["samples"] == 0
