@@ -10,9 +10,11 @@
  * Conventions
  *  - Every entry point returns an int status: TBSLA_OK (0) or a negative
  *    TBSLA_ERR_* code; tbsla_status_string() names it.  Nothing throws across
- *    the ABI.  Bad input (out-of-range index, non-monotone row pointer,
- *    truncated file, size mismatch) is rejected on the host before any
- *    kernel runs.
+ *    the ABI: a host allocation that fails returns TBSLA_ERR_ALLOC, and a
+ *    matrix whose arrays were being replaced (setters, push_back,
+ *    generators, read) is then left empty, as after tbsla_matrix_create.
+ *    Bad input (out-of-range index, non-monotone row pointer, truncated
+ *    file, size mismatch) is rejected on the host before any kernel runs.
  *  - A handle keeps the reference's host layout (the arrays a reference
  *    Matrix object owns) plus a device copy built on first use (or by
  *    tbsla_matrix_upload); any host-side mutation drops the device copy.

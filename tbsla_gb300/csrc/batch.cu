@@ -26,8 +26,10 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <vector>
 
+#include "api_guard.hpp"
 #include "device.hpp"
 #include "host/parallel.hpp"
 #include "kernels/kernels.hpp"
@@ -624,7 +626,7 @@ int dia_solve(tbsla_batch* B, const double* rhs, double* x, int max_iterations, 
 
 extern "C" {
 
-int tbsla_batch_create(tbsla_batch** out, tbsla_matrix* const* systems, int nsys, int precision) {
+int tbsla_batch_create(tbsla_batch** out, tbsla_matrix* const* systems, int nsys, int precision) try {
   if (!out || !systems || nsys <= 0 || precision < TBSLA_F64 || precision > TBSLA_BF16)
     return TBSLA_ERR_INVALID_ARG;
   for (int s = 0; s < nsys; s++)
@@ -634,24 +636,21 @@ int tbsla_batch_create(tbsla_batch** out, tbsla_matrix* const* systems, int nsys
     cudaGetLastError();
     return TBSLA_ERR_NO_DEVICE;
   }
-  auto* B = new tbsla_batch();
+  std::unique_ptr<tbsla_batch> B(new tbsla_batch());  // freed if the build fails or throws
   cudaGetDevice(&B->device);
   int st = st_of(cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking));
-  if (!st) st = build_batch(B, systems, nsys, precision);
-  if (st) {
-    delete B;
-    return st;
-  }
-  *out = B;
+  if (!st) st = build_batch(B.get(), systems, nsys, precision);
+  if (st) return st;
+  *out = B.release();
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_destroy(tbsla_batch* b) {
+int tbsla_batch_destroy(tbsla_batch* b) try {
   delete b;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int nsys, int precision) {
+int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int nsys, int precision) try {
   using namespace tbsla_impl;
   if (!B || !factors || nsys != B->nsys || precision < TBSLA_F64 || precision > TBSLA_BF16)
     return TBSLA_ERR_INVALID_ARG;
@@ -809,17 +808,17 @@ int tbsla_batch_set_factors(tbsla_batch* B, tbsla_matrix* const* factors, int ns
   cudaFree(tmp);
   if (B->graph_pre == 2) B->graph_pre = -1;  // recapture with the new arrays
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets) {
+int tbsla_batch_rows(const tbsla_batch* b, int* nsys, long* offsets) try {
   if (!b) return TBSLA_ERR_INVALID_ARG;
   if (nsys) *nsys = b->nsys;
   if (offsets) std::copy(b->off.begin(), b->off.end(), offsets);
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
 int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterations, double rel_tol,
-                   int precond, int refresh, int graph_iters, int* iterations, double* rel_residual) {
+                   int precond, int refresh, int graph_iters, int* iterations, double* rel_residual) try {
   if (!B || !rhs || !x || max_iterations < 0 || rel_tol < 0 || precond < 0 || precond > 2 || refresh < 0 ||
       (precond == 2 && !B->rf && !B->dia_factor))
     return TBSLA_ERR_INVALID_ARG;
@@ -910,9 +909,9 @@ int tbsla_batch_cg(tbsla_batch* B, const double* rhs, double* x, int max_iterati
     all &= hs[k] == kDone;
   }
   return all ? TBSLA_OK : TBSLA_ERR_NOT_CONVERGED;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_factor_mpnn(tbsla_batch* B, tbsla_mpnn* net, int precision) {
+int tbsla_batch_factor_mpnn(tbsla_batch* B, tbsla_mpnn* net, int precision) try {
   if (!B || !net || precision < TBSLA_F64 || precision > TBSLA_BF16) return TBSLA_ERR_INVALID_ARG;
   if (!B->dia) return TBSLA_ERR_UNSUPPORTED;
   const int nsys = B->nsys;
@@ -946,9 +945,9 @@ int tbsla_batch_factor_mpnn(tbsla_batch* B, tbsla_mpnn* net, int precision) {
   B->dia_factor = true;
   B->factor_fb.assign(nsys, 0);
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_factor_dia(const tbsla_batch* B, int* slots, int* deltas, double* values) {
+int tbsla_batch_factor_dia(const tbsla_batch* B, int* slots, int* deltas, double* values) try {
   if (!B) return TBSLA_ERR_INVALID_ARG;
   if (!B->dia_factor) return TBSLA_ERR_UNSUPPORTED;
   if (slots) *slots = B->KL;
@@ -972,55 +971,55 @@ int tbsla_batch_factor_dia(const tbsla_batch* B, int* slots, int* deltas, double
     }
   }
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_fallbacks(const tbsla_batch* B, int* fallback, int* precond_used) {
+int tbsla_batch_fallbacks(const tbsla_batch* B, int* fallback, int* precond_used) try {
   if (!B) return TBSLA_ERR_INVALID_ARG;
   for (int k = 0; k < B->nsys; k++) {
     if (fallback) fallback[k] = k < (int)B->fallback_h.size() ? B->fallback_h[k] : 0;
     if (precond_used) precond_used[k] = k < (int)B->mode_h.size() ? B->mode_h[k] : 0;
   }
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_set_ctas_per_sm(tbsla_batch* B, int ctas) {
+int tbsla_batch_set_ctas_per_sm(tbsla_batch* B, int ctas) try {
   if (!B || ctas < 0 || ctas > 32) return TBSLA_ERR_INVALID_ARG;
   B->ctas_per_sm = ctas;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_tuning(const tbsla_batch* B, int* rows_per_thread, int* ctas_per_sm) {
+int tbsla_batch_tuning(const tbsla_batch* B, int* rows_per_thread, int* ctas_per_sm) try {
   if (!B) return TBSLA_ERR_INVALID_ARG;
   if (rows_per_thread) *rows_per_thread = B->vec4 && !B->vec4_off ? 4 : 1;
   if (ctas_per_sm) *ctas_per_sm = B->ctas_per_sm;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_set_rows_per_thread(tbsla_batch* B, int rows) {
+int tbsla_batch_set_rows_per_thread(tbsla_batch* B, int rows) try {
   if (!B || (rows != 1 && rows != 4)) return TBSLA_ERR_INVALID_ARG;
   B->vec4_off = rows == 1;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_set_wait_limit(tbsla_batch* B, long long ns) {
+int tbsla_batch_set_wait_limit(tbsla_batch* B, long long ns) try {
   if (!B || ns < 0) return TBSLA_ERR_INVALID_ARG;
   B->wait_ns = ns;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_engine(const tbsla_batch* B, int* persistent, int* graph, int* seven_point) {
+int tbsla_batch_engine(const tbsla_batch* B, int* persistent, int* graph, int* seven_point) try {
   if (!B) return TBSLA_ERR_INVALID_ARG;
   if (persistent) *persistent = B->last_engine;
   if (graph) *graph = B->last_graph;
   if (seven_point) *seven_point = B->last_st7;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_batch_set_seven_point(tbsla_batch* B, int on) {
+int tbsla_batch_set_seven_point(tbsla_batch* B, int on) try {
   if (!B || (on != 0 && on != 1)) return TBSLA_ERR_INVALID_ARG;
   B->st7_off = on == 0;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
 }  // extern "C"
 

@@ -27,9 +27,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <random>
 #include <vector>
 
+#include "api_guard.hpp"
 #include "device.hpp"
 #include "host/matrix.hpp"
 #include "kernels/common.cuh"
@@ -877,13 +879,13 @@ int mpnn_factor_dia(tbsla_mpnn* net, long n, int K, const double* a64, const int
 
 extern "C" {
 
-int tbsla_mpnn_create(tbsla_mpnn** out, unsigned long long seed) {
+int tbsla_mpnn_create(tbsla_mpnn** out, unsigned long long seed) try {
   if (!out) return TBSLA_ERR_INVALID_ARG;
   *out = nullptr;
   int dev = 0;
   int st = tbsla_impl::dev_ready(&dev);
   if (st) return st;
-  auto* net = new (std::nothrow) tbsla_mpnn();
+  std::unique_ptr<tbsla_mpnn> net(new (std::nothrow) tbsla_mpnn());  // freed on every failure path
   if (!net) return TBSLA_ERR_ALLOC;
   net->device = dev;
   cudaSetDevice(dev);
@@ -892,7 +894,6 @@ int tbsla_mpnn_create(tbsla_mpnn** out, unsigned long long seed) {
       cudaMalloc(&net->grad, NPARAMS * 4) != cudaSuccess || cudaMalloc(&net->mo, NPARAMS * 4) != cudaSuccess ||
       cudaMalloc(&net->ve, NPARAMS * 4) != cudaSuccess || cudaMalloc(&net->dloss, 8) != cudaSuccess) {
     cudaGetLastError();
-    delete net;
     return TBSLA_ERR_ALLOC;
   }
   // He-scaled message layers, zero biases; the head starts at L = D^-1/2
@@ -905,20 +906,17 @@ int tbsla_mpnn_create(tbsla_mpnn** out, unsigned long long seed) {
     for (int k = 0; k < 2 * H * H; k++) th[off_layer(l) + k] = nl(rng);
   th[OFF_BD] = std::log(std::exp(1.f) - 1.f);
   st = net->set(th);
-  if (st) {
-    delete net;
-    return st;
-  }
-  *out = net;
+  if (st) return st;
+  *out = net.release();
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_mpnn_destroy(tbsla_mpnn* net) {
+int tbsla_mpnn_destroy(tbsla_mpnn* net) try {
   delete net;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_mpnn_params(const tbsla_mpnn* net, float* theta, int* nparams) {
+int tbsla_mpnn_params(const tbsla_mpnn* net, float* theta, int* nparams) try {
   if (!net) return TBSLA_ERR_INVALID_ARG;
   if (nparams) *nparams = NPARAMS;
   if (theta) {
@@ -927,16 +925,16 @@ int tbsla_mpnn_params(const tbsla_mpnn* net, float* theta, int* nparams) {
     MCK(cudaStreamSynchronize(net->stream));
   }
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_mpnn_set_params(tbsla_mpnn* net, const float* theta, int nparams) {
+int tbsla_mpnn_set_params(tbsla_mpnn* net, const float* theta, int nparams) try {
   if (!net || !theta || nparams != NPARAMS) return TBSLA_ERR_INVALID_ARG;
   cudaSetDevice(net->device);
   return net->set(std::vector<float>(theta, theta + NPARAMS));
-}
+} TBSLA_API_CATCH
 
 int tbsla_mpnn_loss_grad(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, const double* Z, double* loss,
-                         float* grad) {
+                         float* grad) try {
   if (!net || !A || nprobes < 1 || nprobes > PMAX || !Z) return TBSLA_ERR_INVALID_ARG;
   HostGraph g;
   int st = build_graph(A, &g);
@@ -955,10 +953,10 @@ int tbsla_mpnn_loss_grad(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, co
   MCK(cudaStreamSynchronize(s));
   if (loss) *loss = l;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
 int tbsla_mpnn_train_step(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, unsigned long long seed, float lr,
-                          double* loss) {
+                          double* loss) try {
   if (!net || !A || nprobes < 1 || nprobes > PMAX || !(lr > 0)) return TBSLA_ERR_INVALID_ARG;
   HostGraph g;
   int st = build_graph(A, &g);
@@ -980,9 +978,9 @@ int tbsla_mpnn_train_step(tbsla_mpnn* net, const tbsla_matrix* A, int nprobes, u
   MCK(cudaStreamSynchronize(s));
   if (loss) *loss = l;
   return TBSLA_OK;
-}
+} TBSLA_API_CATCH
 
-int tbsla_mpnn_factor(tbsla_mpnn* net, const tbsla_matrix* A, tbsla_matrix* L) {
+int tbsla_mpnn_factor(tbsla_mpnn* net, const tbsla_matrix* A, tbsla_matrix* L) try {
   if (!net || !A || !L || L->format != TBSLA_CSR) return TBSLA_ERR_INVALID_ARG;
   HostGraph g;
   int st = build_graph(A, &g);
@@ -1000,6 +998,6 @@ int tbsla_mpnn_factor(tbsla_mpnn* net, const tbsla_matrix* A, tbsla_matrix* L) {
   I.nnz = w.nl;
   I.NR = I.NC = 1;
   return tbsla_matrix_set_csr(L, &I, vals.data(), g.lrowptr.data(), g.lcol.data());
-}
+} TBSLA_API_CATCH
 
 }  // extern "C"

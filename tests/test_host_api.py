@@ -265,3 +265,33 @@ def test_oracle_powerlaw_generator_matches_library(n, max_len, local, band, seed
     assert np.array_equal(rp, a["rowptr"]) and np.array_equal(ci, a["colidx"])
     assert np.array_equal(va, a["values"])
     assert np.array_equal(oracle.gen_uniform(n, 0.0, 1.0, seed), T.fill_uniform(n, 0.0, 1.0, seed))
+
+
+def test_failed_host_allocation_returns_status_and_empties_matrix():
+    """No C++ exception crosses the C ABI: a host allocation that cannot be
+    made (here 2^60 entries) returns TBSLA_ERR_ALLOC, and a matrix whose
+    arrays were being replaced is left empty, then takes new arrays as
+    usual.  The source pointers are not read: the allocation fails first."""
+    import ctypes as C
+
+    from tbsla_gb300 import _lib as L
+
+    m = C.c_void_p()
+    L.check(L.lib.tbsla_matrix_create(C.byref(m), L.COO))
+    try:
+        vals = np.ones(3)
+        rows = np.array([0, 1, 2], np.int32)
+        cols = np.array([2, 1, 0], np.int32)
+        ptr = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        big = L.Info(n_row=3, n_col=3, ln_row=3, ln_col=3, nnz=1 << 60, NR=1, NC=1)
+        st = L.lib.tbsla_matrix_set_coo(m, C.byref(big), ptr(vals), ptr(rows), ptr(cols))
+        assert st == L.ERR_ALLOC
+        info = L.Info()
+        L.check(L.lib.tbsla_matrix_info(m, C.byref(info)))
+        assert info.nnz == 0 and info.n_row == 0 and info.NR == 1
+        ok = L.Info(n_row=3, n_col=3, ln_row=3, ln_col=3, nnz=3, NR=1, NC=1)
+        L.check(L.lib.tbsla_matrix_set_coo(m, C.byref(ok), ptr(vals), ptr(rows), ptr(cols)))
+        L.check(L.lib.tbsla_matrix_info(m, C.byref(info)))
+        assert info.nnz == 3
+    finally:
+        L.lib.tbsla_matrix_destroy(m)
